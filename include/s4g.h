@@ -1,0 +1,286 @@
+/*
+ * s4g.h -- C ABI of the GB300 segregated finite-volume solid solver.
+ *
+ * The library replaces, for one mesh region, the outer-corrector loop of
+ * solids4foam's linearGeometryTotalDisplacement and
+ * nonLinearGeometryTotalLagrangian solid models together with the OpenFOAM
+ * finite-volume operators and the PCG/DIC linear solver they call.  Every
+ * entry point is plain C: pointers, sizes and status codes, no exceptions,
+ * no C++ or torch types.  Each declaration names the reference interface it
+ * stands in for (paths relative to the solids4foam source tree).
+ *
+ * Ownership: the caller owns every host array it passes; the library copies
+ * what it needs during the call and never keeps the pointer.  The library
+ * owns all device memory of a context and frees it in the *_destroy calls.
+ * Output arrays are caller-allocated and use the caller's cell order (the
+ * library undoes its internal renumbering).
+ *
+ * Threading: a context is used by one host thread at a time.
+ */
+#ifndef S4G_H
+#define S4G_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define S4G_ABI_VERSION 1
+
+/* Status codes.  Reference convention for errors is FatalError (abort), see
+ * src/solids4FoamModels/solidModels/solidModel/solidModel.C:1735-1742; a
+ * drop-in maps every code but S4G_NOT_CONVERGED to FatalErrorIn, and
+ * S4G_NOT_CONVERGED to the "Max iterations reached within momentum loop"
+ * warning of solidModelTemplates.C:180-185 (the result is still returned). */
+typedef enum s4g_status {
+  S4G_OK = 0,
+  S4G_BAD_ARG = 1,            /* invalid argument or inconsistent mesh */
+  S4G_OOM = 2,                /* device allocation failed */
+  S4G_NOT_CONVERGED = 3,      /* nCorrectors reached; results returned */
+  S4G_NAN_DETECTED = 4,       /* non-finite value in the iteration */
+  S4G_INDEFINITE = 5,         /* PCG found p.Ap <= 0 */
+  S4G_TIMEOUT = 6,            /* a bounded device wait gave up */
+  S4G_CUDA_ERROR = 7,         /* CUDA runtime error */
+  S4G_NO_DEVICE = 8,          /* no CUDA device */
+  S4G_ADMISSION_REJECTED = 9, /* server: footprint can never fit */
+  S4G_PENDING = 10,           /* server: request not finished yet */
+  S4G_CANCELLED = 11,         /* server: request was cancelled */
+  S4G_NOT_BUILT = 12          /* feature not compiled into this library */
+} s4g_status;
+
+/* Human-readable name of a status code (never NULL). */
+const char* s4g_status_str(s4g_status st);
+
+/* ABI version of the loaded library (S4G_ABI_VERSION at build time). */
+int s4g_abi_version(void);
+
+/* Message of the last failing call on this host thread ("" if none). */
+const char* s4g_last_error(void);
+
+/* ------------------------------------------------------------ context -- */
+
+typedef struct s4g_ctx s4g_ctx;
+
+typedef struct s4g_ctx_opts {
+  int device;   /* CUDA device ordinal */
+  int verbose;  /* 1: print the reference's residual table every
+                   infoFrequency correctors */
+} s4g_ctx_opts;
+
+/* Creates a context on one GPU.  Stands in for the per-run state the
+ * reference keeps in the OpenFOAM Time/objectRegistry
+ * (applications/solvers/solids4Foam/solids4Foam.C:36-43). */
+s4g_status s4g_ctx_create(s4g_ctx** out, const s4g_ctx_opts* opts);
+s4g_status s4g_ctx_destroy(s4g_ctx* ctx);
+
+/* --------------------------------------------------------------- mesh -- */
+
+/* An OpenFOAM fvMesh in its primitive form: upper-triangular internal faces
+ * first (owner < neighbour, area vector owner -> neighbour), then boundary
+ * faces grouped by patch, area vectors pointing out of the domain. */
+typedef struct s4g_mesh_desc {
+  int n_cells;
+  int n_faces;            /* internal + boundary */
+  int n_internal_faces;
+  const int* owner;       /* [n_faces] */
+  const int* neighbour;   /* [n_internal_faces] */
+  const double* C;        /* [n_cells][3] cell centres */
+  const double* V;        /* [n_cells] cell volumes */
+  const double* Cf;       /* [n_faces][3] face centres */
+  const double* Sf;       /* [n_faces][3] face area vectors */
+  int n_patches;
+  const int* patch_start; /* [n_patches] first face of each patch */
+  const int* patch_size;  /* [n_patches] */
+} s4g_mesh_desc;
+
+/* Cell numbering used by the DIC preconditioner.  DIC depends on the cell
+ * order exactly as OpenFOAM's does; every choice is an exact DIC of the
+ * renumbered matrix (as after OpenFOAM's renumberMesh). */
+typedef enum s4g_renumber {
+  S4G_RENUMBER_NONE = 0,  /* the caller's numbering */
+  S4G_RENUMBER_RCM = 1,   /* reverse Cuthill-McKee */
+  S4G_RENUMBER_TILED = 2  /* coordinate-bisection parts, part-major order */
+} s4g_renumber;
+
+typedef struct s4g_mesh_opts {
+  s4g_renumber renumber;
+  int part_size;          /* rows per scheduling part (0: default 512) */
+  int ls_boundary_delta;  /* leastSquares boundary d: 0 patch-normal
+                             n(n.(Cf-C)) (OpenFOAM.com/.org fvPatch::delta),
+                             1 full Cf-C (foam-extend) */
+  int dic_subdomains;     /* 0: exact global DIC; 1: DIC restricted to each
+                             part (processor-local DIC of a decomposed run) */
+} s4g_mesh_opts;
+
+typedef struct s4g_mesh s4g_mesh;
+
+typedef struct s4g_mesh_info {
+  int n_cells, n_internal_faces, n_boundary_faces;
+  int n_parts;            /* scheduling parts */
+  int part_depth;         /* longest chain of dependent parts (DIC sweep) */
+  int max_local_levels;   /* deepest in-part level count */
+  int n_levels_global;    /* level count of the whole lower-triangular DAG */
+  long long device_bytes; /* device memory held by this mesh */
+} s4g_mesh_info;
+
+/* Uploads the mesh once: validation, renumbering, cell-to-face CSR in the
+ * solver order, then derived geometry on the device (weights, deltaCoeffs,
+ * nonOrthDeltaCoeffs, nonOrthCorrectionVectors, patch correction vectors,
+ * leastSquares tensors).  Stands in for the lazily built OpenFOAM fvMesh
+ * geometry used by solidModel (solidModel.C:954-1330) and
+ * patchCorrectionVectors.C:24-36. */
+s4g_status s4g_mesh_upload(s4g_ctx* ctx, const s4g_mesh_desc* desc,
+                           const s4g_mesh_opts* opts, s4g_mesh** out);
+/* Host-only planning (no GPU needed): the DIC order and scheduling figures
+ * s4g_mesh_upload would use.  perm_out [n_cells] (may be NULL): perm[i] =
+ * caller cell of solver cell i; a caller can renumber its own mesh with it
+ * (OpenFOAM renumberMesh) to run the identical DIC on the CPU. */
+s4g_status s4g_mesh_plan(const s4g_mesh_desc* desc, const s4g_mesh_opts* opts,
+                         int* perm_out, s4g_mesh_info* info);
+/* perm[i] = caller cell of solver cell i (the DIC order). */
+s4g_status s4g_mesh_get_permutation(const s4g_mesh* mesh, int* perm);
+s4g_status s4g_mesh_get_info(const s4g_mesh* mesh, s4g_mesh_info* info);
+s4g_status s4g_mesh_destroy(s4g_mesh* mesh);
+
+/* ----------------------------------------------------------- material -- */
+
+typedef enum s4g_law_type {
+  S4G_LINEAR_ELASTIC = 0,  /* materialModels/.../linearElastic/linearElastic.C */
+  S4G_NEO_HOOKEAN = 1      /* .../neoHookeanElastic/neoHookeanElastic.C */
+} s4g_law_type;
+
+typedef struct s4g_law {
+  s4g_law_type type;
+  int use_mu_K;     /* 0: E, nu given; 1: mu, K given */
+  double E, nu;
+  double mu, K;
+  double rho;       /* unused by the steady solve; kept for the drop-in */
+} s4g_law;
+
+/* One mechanical law for the whole mesh (mechanicalModel with a single law
+ * forwards to laws[0]: mechanicalModel.C:476-498,571-582). */
+s4g_status s4g_material_set(s4g_mesh* mesh, const s4g_law* law);
+
+/* ---------------------------------------------------------------- BCs -- */
+
+typedef enum s4g_bc_type {
+  S4G_FIXED_DISPLACEMENT = 0, /* fixedDisplacementFvPatchVectorField.C:258-356 */
+  S4G_SOLID_TRACTION = 1      /* solidTractionFvPatchVectorField.C:321-463 */
+} s4g_bc_type;
+
+/* vec3 [patch_size][3]: total displacement (fixedDisplacement) or traction
+ * (solidTraction); NULL means zero.  pressure [patch_size] (solidTraction
+ * only), NULL means zero.  Loads of the nonLinearGeometryTotalLagrangian
+ * model ramp linearly over the load increments, as a tractionSeries /
+ * pressureSeries table from zero would. */
+s4g_status s4g_bc_set(s4g_mesh* mesh, int patch, s4g_bc_type type,
+                      const double* vec3, const double* pressure);
+
+/* ------------------------------------------------------------- solver -- */
+
+typedef enum s4g_precond {
+  S4G_PRECOND_DIC = 0,      /* OpenFOAM DIC / FDIC */
+  S4G_PRECOND_DIAGONAL = 1  /* OpenFOAM diagonal */
+} s4g_precond;
+
+/* fvSolution solvers { "D|DD" { solver PCG; preconditioner; tolerance;
+ * relTol; maxIter; } } */
+typedef struct s4g_lin_solver {
+  s4g_precond preconditioner;
+  double tolerance;
+  double rel_tol;
+  int max_iter;
+} s4g_lin_solver;
+
+/* solidProperties <model>Coeffs (solidModel.C:1138-1243,1307-1323). */
+typedef struct s4g_outer {
+  int n_correctors;        /* nCorrectors */
+  double solution_tol;     /* solutionTolerance */
+  double alternative_tol;  /* alternativeTolerance */
+  double material_tol;     /* materialTolerance */
+  double stab_scale;       /* stabilisation { type RhieChow; scaleFactor; } */
+  int info_frequency;      /* infoFrequency */
+} s4g_outer;
+
+typedef enum s4g_precision {
+  S4G_FP64 = 0,           /* everything in FP64 */
+  S4G_FP32_REFINE = 1     /* PCG/SpMV in FP32 with compensated dots; the
+                             outer correctors refine in FP64 */
+} s4g_precision;
+
+s4g_status s4g_solver_set(s4g_mesh* mesh, const s4g_lin_solver* lin,
+                          const s4g_outer* outer, s4g_precision precision);
+
+/* Fills the reference defaults: PCG+DIC tol 1e-9 relTol 0.1 maxIter 1000;
+ * nCorrectors 10000, solutionTolerance 1e-6, alternativeTolerance 1e-7,
+ * materialTolerance 1e-5, RhieChow 0.1, infoFrequency 100. */
+void s4g_default_controls(s4g_lin_solver* lin, s4g_outer* outer);
+
+/* -------------------------------------------------------------- solve -- */
+
+typedef enum s4g_model {
+  S4G_LIN_GEOM_TOTAL_DISP = 0,   /* linGeomTotalDispSolid.C:111-232 */
+  S4G_NONLIN_GEOM_TOTAL_LAG = 1  /* nonLinGeomTotalLagSolid.C:125-260 */
+} s4g_model;
+
+typedef struct s4g_perf {
+  int n_correctors;           /* outer correctors run (all increments) */
+  int converged;              /* last increment converged */
+  long long total_lin_iters;  /* PCG iterations summed over components */
+  int last_max_lin_iters;     /* cmptMax(nIterations) of the last corrector */
+  double initial_residual;    /* mag(initialResidual) of the last corrector */
+  double rel_residual;        /* relative displacement residual, last */
+  double solve_ms;            /* device time of the solve (CUDA events) */
+  double h2d_ms, d2h_ms;      /* copies inside s4g_solve */
+  long long kernel_launches;  /* kernels launched by the library */
+  int enforce_linear;         /* TL: linear geometry was enforced */
+  int device_status;          /* raw device status word (0 = clean) */
+} s4g_perf;
+
+/* Runs the solid model's evolve() for n_increments load increments (1 for
+ * the linear model) on the device: every corrector, PCG iteration and
+ * convergence test stays on the GPU; only the final fields come back.
+ * D_out [n_cells][3]; sigma_out [n_cells][6] (XX XY XZ YY YZ ZZ); either may
+ * be NULL.  Replaces solidModel::evolve (solidModel.H:759) of the two
+ * models named above, with tractionBoundarySnGrad evaluated on the device. */
+s4g_status s4g_solve(s4g_mesh* mesh, s4g_model model, int n_increments,
+                     double* D_out, double* sigma_out, s4g_perf* perf);
+
+/* Cell gradient of D from the last solve, [n_cells][9] row-major,
+ * grad(D)_ij = dD_j/dx_i (the reference's gradD field). */
+s4g_status s4g_get_gradD(s4g_mesh* mesh, double* gradD_out);
+
+/* -------------------------------------------- operator-level entry points
+ * For kernel-by-kernel parity checks.  Vectors are in the caller's cell
+ * order, k columns stored row-interleaved [n_cells][k], k in 1..3. */
+
+/* Scalar momentum matrix (fvm::laplacian(impKf, D) negated to SPD form),
+ * diag [n_cells] and upper [n_internal_faces] in the caller's face order.
+ * Requires material and BCs. */
+s4g_status s4g_op_matrix(s4g_mesh* mesh, double* diag, double* upper);
+/* y = A x. */
+s4g_status s4g_op_amul(s4g_mesh* mesh, int k, const double* x, double* y);
+/* w = DIC^-1 r (or diagonal). */
+s4g_status s4g_op_precondition(s4g_mesh* mesh, int k, const double* r,
+                               double* w);
+
+/* ---------------------------------------------------- case generation --
+ * Seeded hexahedral box meshes (blockMesh + perturbMeshPoints stand-in,
+ * applications/utilities/perturbMeshPoints/perturbMeshPoints.C:244-330):
+ * patches xmin, xmax, ymin, ymax, zmin, zmax; interior vertices jittered by
+ * up to jitter*h per axis.  Host-only helpers of the standalone driver. */
+s4g_status s4g_box_mesh_sizes(int nx, int ny, int nz, int* n_cells,
+                              int* n_faces, int* n_internal_faces,
+                              int* n_points);
+s4g_status s4g_box_mesh_build(int nx, int ny, int nz, double lx, double ly,
+                              double lz, double jitter, uint64_t seed,
+                              int* owner, int* neighbour, double* C, double* V,
+                              double* Cf, double* Sf, int* patch_start,
+                              int* patch_size, double* points);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* S4G_H */

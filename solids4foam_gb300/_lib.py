@@ -1,0 +1,145 @@
+"""ctypes binding of libs4g.so (the C ABI declared in include/s4g.h).
+
+The library is built in-tree by solids4foam_gb300/build.py.  Loading fails
+loudly when it is missing: there is no CPU fallback for the solver.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libs4g.so")
+
+# s4g_status
+OK, BAD_ARG, OOM, NOT_CONVERGED, NAN_DETECTED, INDEFINITE, TIMEOUT, CUDA_ERROR, NO_DEVICE, \
+    ADMISSION_REJECTED, PENDING, CANCELLED, NOT_BUILT = range(13)
+# enums
+RENUMBER_NONE, RENUMBER_RCM, RENUMBER_TILED = 0, 1, 2
+LINEAR_ELASTIC, NEO_HOOKEAN = 0, 1
+FIXED_DISPLACEMENT, SOLID_TRACTION = 0, 1
+PRECOND_DIC, PRECOND_DIAGONAL = 0, 1
+FP64, FP32_REFINE = 0, 1
+LIN_GEOM_TOTAL_DISP, NONLIN_GEOM_TOTAL_LAG = 0, 1
+
+
+class CtxOpts(ct.Structure):
+    _fields_ = [("device", ct.c_int), ("verbose", ct.c_int)]
+
+
+class MeshDesc(ct.Structure):
+    _fields_ = [
+        ("n_cells", ct.c_int), ("n_faces", ct.c_int), ("n_internal_faces", ct.c_int),
+        ("owner", ct.c_void_p), ("neighbour", ct.c_void_p),
+        ("C", ct.c_void_p), ("V", ct.c_void_p), ("Cf", ct.c_void_p), ("Sf", ct.c_void_p),
+        ("n_patches", ct.c_int), ("patch_start", ct.c_void_p), ("patch_size", ct.c_void_p),
+    ]
+
+
+class MeshOpts(ct.Structure):
+    _fields_ = [("renumber", ct.c_int), ("part_size", ct.c_int),
+                ("ls_boundary_delta", ct.c_int), ("dic_subdomains", ct.c_int)]
+
+
+class MeshInfo(ct.Structure):
+    _fields_ = [("n_cells", ct.c_int), ("n_internal_faces", ct.c_int),
+                ("n_boundary_faces", ct.c_int), ("n_parts", ct.c_int),
+                ("part_depth", ct.c_int), ("max_local_levels", ct.c_int),
+                ("n_levels_global", ct.c_int), ("device_bytes", ct.c_longlong)]
+
+
+class Law(ct.Structure):
+    _fields_ = [("type", ct.c_int), ("use_mu_K", ct.c_int), ("E", ct.c_double),
+                ("nu", ct.c_double), ("mu", ct.c_double), ("K", ct.c_double),
+                ("rho", ct.c_double)]
+
+
+class LinSolver(ct.Structure):
+    _fields_ = [("preconditioner", ct.c_int), ("tolerance", ct.c_double),
+                ("rel_tol", ct.c_double), ("max_iter", ct.c_int)]
+
+
+class Outer(ct.Structure):
+    _fields_ = [("n_correctors", ct.c_int), ("solution_tol", ct.c_double),
+                ("alternative_tol", ct.c_double), ("material_tol", ct.c_double),
+                ("stab_scale", ct.c_double), ("info_frequency", ct.c_int)]
+
+
+class Perf(ct.Structure):
+    _fields_ = [
+        ("n_correctors", ct.c_int), ("converged", ct.c_int),
+        ("total_lin_iters", ct.c_longlong), ("last_max_lin_iters", ct.c_int),
+        ("initial_residual", ct.c_double), ("rel_residual", ct.c_double),
+        ("solve_ms", ct.c_double), ("h2d_ms", ct.c_double), ("d2h_ms", ct.c_double),
+        ("kernel_launches", ct.c_longlong), ("enforce_linear", ct.c_int),
+        ("device_status", ct.c_int),
+    ]
+
+    def as_dict(self):
+        return {f[0]: getattr(self, f[0]) for f in self._fields_}
+
+
+# every symbol declared in include/s4g.h, with its ctypes signature
+_SIGS = {
+    "s4g_status_str": (ct.c_char_p, [ct.c_int]),
+    "s4g_abi_version": (ct.c_int, []),
+    "s4g_last_error": (ct.c_char_p, []),
+    "s4g_ctx_create": (ct.c_int, [ct.POINTER(ct.c_void_p), ct.POINTER(CtxOpts)]),
+    "s4g_ctx_destroy": (ct.c_int, [ct.c_void_p]),
+    "s4g_mesh_upload": (ct.c_int, [ct.c_void_p, ct.POINTER(MeshDesc), ct.POINTER(MeshOpts),
+                                   ct.POINTER(ct.c_void_p)]),
+    "s4g_mesh_plan": (ct.c_int, [ct.POINTER(MeshDesc), ct.POINTER(MeshOpts), ct.c_void_p,
+                                 ct.POINTER(MeshInfo)]),
+    "s4g_mesh_get_permutation": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "s4g_mesh_get_info": (ct.c_int, [ct.c_void_p, ct.POINTER(MeshInfo)]),
+    "s4g_mesh_destroy": (ct.c_int, [ct.c_void_p]),
+    "s4g_material_set": (ct.c_int, [ct.c_void_p, ct.POINTER(Law)]),
+    "s4g_bc_set": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p]),
+    "s4g_solver_set": (ct.c_int, [ct.c_void_p, ct.POINTER(LinSolver), ct.POINTER(Outer), ct.c_int]),
+    "s4g_default_controls": (None, [ct.POINTER(LinSolver), ct.POINTER(Outer)]),
+    "s4g_solve": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
+                             ct.POINTER(Perf)]),
+    "s4g_get_gradD": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "s4g_op_matrix": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "s4g_op_amul": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p]),
+    "s4g_op_precondition": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p]),
+    "s4g_box_mesh_sizes": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int] + [ct.POINTER(ct.c_int)] * 4),
+    "s4g_box_mesh_build": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_double, ct.c_double,
+                                      ct.c_double, ct.c_double, ct.c_uint64] + [ct.c_void_p] * 9),
+}
+
+_lib = None
+
+
+class S4GError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        msg = lib().s4g_last_error().decode(errors="replace")
+        name = lib().s4g_status_str(status).decode()
+        super().__init__(f"{where}: {name} ({msg})")
+
+
+def lib():
+    """Loads libs4g.so; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; "
+                f"g.build()\"` (or solids4foam_gb300/build.py); the solver has no CPU fallback")
+        _lib = ct.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(_lib, name)
+            fn.restype = res
+            fn.argtypes = args
+    return _lib
+
+
+def check(status: int, where: str, allow=(OK,)):
+    if status not in allow:
+        raise S4GError(status, where)
+    return status
+
+
+def declared_symbols():
+    return list(_SIGS)

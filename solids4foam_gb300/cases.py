@@ -1,0 +1,88 @@
+"""Seeded box meshes and the benchmark cases of the segregated solid solve.
+
+Meshes come from the library's host-side generator (s4g_box_mesh_build): a
+structured hex box in OpenFOAM polyMesh conventions with interior vertices
+jittered by up to `jitter` cell sizes per axis.  Patches are, in order,
+xmin, xmax, ymin, ymax, zmin, zmax.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+
+from . import _lib
+
+PATCHES = ("xmin", "xmax", "ymin", "ymax", "zmin", "zmax")
+
+
+def box_mesh(nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=1, points=False):
+    L = _lib.lib()
+    nc, nf, ni, npt = ct.c_int(), ct.c_int(), ct.c_int(), ct.c_int()
+    _lib.check(L.s4g_box_mesh_sizes(nx, ny, nz, ct.byref(nc), ct.byref(nf), ct.byref(ni),
+                                    ct.byref(npt)), "s4g_box_mesh_sizes")
+    nc, nf, ni, npt = nc.value, nf.value, ni.value, npt.value
+    m = dict(owner=np.zeros(nf, np.int32), neighbour=np.zeros(ni, np.int32),
+             C=np.zeros((nc, 3)), V=np.zeros(nc), Cf=np.zeros((nf, 3)), Sf=np.zeros((nf, 3)),
+             patch_start=np.zeros(6, np.int32), patch_size=np.zeros(6, np.int32))
+    pts = np.zeros((npt, 3)) if points else None
+    ptrs = [m[k].ctypes.data for k in ("owner", "neighbour", "C", "V", "Cf", "Sf",
+                                       "patch_start", "patch_size")]
+    _lib.check(L.s4g_box_mesh_build(nx, ny, nz, lx, ly, lz, jitter, seed, *ptrs,
+                                    None if pts is None else pts.ctypes.data),
+               "s4g_box_mesh_build")
+    m["shape"] = (nx, ny, nz)
+    m["patch_names"] = PATCHES
+    if points:
+        m["points"] = pts
+    return m
+
+
+def patch_faces(mesh, name):
+    p = PATCHES.index(name)
+    s, n = int(mesh["patch_start"][p]), int(mesh["patch_size"][p])
+    return p, s, n
+
+
+def cantilever_case():
+    """80x8x8 cantilever, 2.0 x 0.2 x 0.2 m, E = 200 GPa, nu = 0.3; x=0
+    fixed, end traction (0, -1 MPa, 0), other faces traction-free; PCG+DIC
+    tol 1e-9 relTol 0.1; outer tolerance 1e-6, 2000 correctors."""
+    mesh = box_mesh(80, 8, 8, 2.0, 0.2, 0.2, 0.0, 1)
+    n_end = int(mesh["patch_size"][1])
+    bcs = {
+        "xmin": ("fixedDisplacement", None, None),
+        "xmax": ("solidTraction", np.tile([0.0, -1e6, 0.0], (n_end, 1)), None),
+    }
+    return dict(mesh=mesh, bcs=bcs, law=dict(type="linearElastic", E=200e9, nu=0.3),
+                solver=dict(tolerance=1e-9, relTol=0.1, maxIter=1000),
+                outer=dict(nCorrectors=2000, solutionTolerance=1e-6))
+
+
+def cube_case(n=128, seed=1, jitter=0.2):
+    """Unit cube n^3 with interior vertices jittered +-0.2 h (seeded),
+    E = 70 GPa, nu = 0.33; bottom (z=0) fixed, top uniform pressure 10 MPa,
+    sides traction-free; PCG+DIC tol 1e-9 relTol 0.1; outer 1e-6, 2000."""
+    mesh = box_mesh(n, n, n, 1.0, 1.0, 1.0, jitter, seed)
+    n_top = int(mesh["patch_size"][5])
+    bcs = {
+        "zmin": ("fixedDisplacement", None, None),
+        "zmax": ("solidTraction", None, np.full(n_top, 10e6)),
+    }
+    return dict(mesh=mesh, bcs=bcs, law=dict(type="linearElastic", E=70e9, nu=0.33),
+                solver=dict(tolerance=1e-9, relTol=0.1, maxIter=1000),
+                outer=dict(nCorrectors=2000, solutionTolerance=1e-6))
+
+
+def oracle_bcs(mesh, bcs):
+    """The same boundary conditions as (type, value, pressure) per patch for
+    the CPU oracle: 0 fixedDisplacement, 1 solidTraction; unnamed patches are
+    traction-free."""
+    out = []
+    for name in PATCHES:
+        if name in bcs:
+            t, v, p = bcs[name]
+            out.append((0 if t == "fixedDisplacement" else 1, v, p))
+        else:
+            out.append((1, None, None))
+    return out

@@ -1,0 +1,814 @@
+// Host side of the GB300 solid solver: device memory, once-per-mesh upload,
+// the solve orchestration and the C ABI (include/s4g.h).
+//
+// The solve mirrors linGeomTotalDispSolid::evolve (linGeomTotalDispSolid.C:
+// 111-232) and nonLinGeomTotalLagSolid::evolve (nonLinGeomTotalLagSolid.C:
+// 125-260): per corrector the right-hand side, the three component PCG solves
+// and the post-solve pass run on the device; the loop conditions (PCG
+// convergence, converged()) are decided on the device and only read back by
+// the host between launch batches.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "s4g_internal.hpp"
+
+namespace s4g {
+
+thread_local std::string gLastError;
+
+static s4g_status setErr(s4g_status st, const std::string& msg) {
+  gLastError = msg;
+  return st;
+}
+
+#define S4G_CUDA(call)                                                              \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) {                                                        \
+      return setErr(e_ == cudaErrorMemoryAllocation ? S4G_OOM : S4G_CUDA_ERROR,     \
+                    std::string(#call) + ": " + cudaGetErrorString(e_));            \
+    }                                                                               \
+  } while (0)
+
+struct Ctx {
+  int device = 0;
+  int verbose = 0;
+  int numSMs = 0;
+  cudaStream_t stream = nullptr;
+};
+
+struct Engine {
+  Ctx* ctx = nullptr;
+  HostPrep hp;
+  std::vector<void*> allocs;
+  size_t bytes = 0;
+  MeshView mv{};
+  GeomOutputs geo{};
+  // boundary condition host mirror (storage boundary order)
+  int nPatches = 0;
+  std::vector<int> patchStart, patchSize;
+  std::vector<int> patchType;
+  std::vector<double> bvalH, bpressH;
+  std::vector<int> btypeH;
+  bool bcDirty = true;
+  // device arrays not in MeshView
+  int* dBtype = nullptr;
+  double* dBval = nullptr;
+  double* dBpress = nullptr;
+  int* dC2s = nullptr;
+  double* dVal = nullptr;
+  double* dDiag = nullptr;
+  double* dRD = nullptr;
+  FieldPtrs f{};
+  PcgPtrs pc{};
+  DevState* dState = nullptr;
+  DevState* hState = nullptr;  // pinned
+  double* dPartials = nullptr;
+  double* dOut = nullptr;
+  bool tlAllocated = false;
+  // material / controls
+  bool materialSet = false;
+  s4g_law law{};
+  double mu = 0, K = 0, lambda = 0, impK = 0;
+  s4g_lin_solver lin{};
+  s4g_outer outer{};
+  s4g_precision precision = S4G_FP64;
+  bool matrixValid = false;
+  int matrixPrecond = -1;
+  int sweepGrid = 1;
+  int lastModel = -1;
+  long long launches = 0;
+
+  ~Engine() {
+    for (void* p : allocs) cudaFree(p);
+    if (hState) cudaFreeHost(hState);
+  }
+
+  template <class T>
+  s4g_status alloc(T** p, size_t n) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) return setErr(S4G_OOM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    allocs.push_back(*p);
+    bytes += n * sizeof(T);
+    return S4G_OK;
+  }
+  template <class T>
+  s4g_status upload(T** p, const std::vector<T>& h) {
+    s4g_status st = alloc(p, h.size());
+    if (st != S4G_OK) return st;
+    if (!h.empty()) S4G_CUDA(cudaMemcpyAsync(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return S4G_OK;
+  }
+#define S4G_TRY(x)                      \
+  do {                                  \
+    s4g_status st_ = (x);               \
+    if (st_ != S4G_OK) return st_;      \
+  } while (0)
+
+  s4g_status uploadMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o) {
+    std::string err;
+    s4g_status st = prepareMesh(d, o, hp, err);
+    if (st != S4G_OK) return setErr(st, err);
+    const int nC = hp.nC, nI = hp.nI, nB = hp.nB;
+    cudaStream_t s = ctx->stream;
+    int *dRow, *dCol, *dFidx, *dFown, *dFnei, *dBrow, *dPartStart, *dLvlOff, *dLvlStart, *dUpPtr,
+        *dUpIdx, *dDnPtr, *dDnIdx, *dS2c, *dFcaller, *dBcaller, *dBcell;
+    S4G_TRY(upload(&dRow, hp.rowptr));
+    S4G_TRY(upload(&dCol, hp.col));
+    S4G_TRY(upload(&dFidx, hp.fidx));
+    S4G_TRY(upload(&dFown, hp.fown));
+    S4G_TRY(upload(&dFnei, hp.fnei));
+    S4G_TRY(upload(&dBrow, hp.browptr));
+    S4G_TRY(upload(&dPartStart, hp.partStart));
+    S4G_TRY(upload(&dLvlOff, hp.lvlOff));
+    S4G_TRY(upload(&dLvlStart, hp.lvlStart));
+    S4G_TRY(upload(&dUpPtr, hp.upPtr));
+    S4G_TRY(upload(&dUpIdx, hp.upIdx));
+    S4G_TRY(upload(&dDnPtr, hp.dnPtr));
+    S4G_TRY(upload(&dDnIdx, hp.dnIdx));
+    S4G_TRY(upload(&dS2c, hp.s2c));
+    S4G_TRY(upload(&dC2s, hp.c2s));
+    S4G_TRY(upload(&dFcaller, hp.fcaller));
+    S4G_TRY(upload(&dBcaller, hp.bcaller));
+    S4G_TRY(upload(&dBcell, hp.bcell));
+    char* dFflip;
+    S4G_TRY(upload(&dFflip, hp.fflip));
+    // caller geometry, consumed by the geometry kernels
+    const int nF = d->n_faces;
+    double *dCc, *dCfc, *dSfc;
+    S4G_TRY(alloc(&dCc, 3 * (size_t)nC));
+    S4G_TRY(alloc(&dCfc, 3 * (size_t)nF));
+    S4G_TRY(alloc(&dSfc, 3 * (size_t)nF));
+    S4G_CUDA(cudaMemcpyAsync(dCc, d->C, sizeof(double) * 3 * nC, cudaMemcpyHostToDevice, s));
+    S4G_CUDA(cudaMemcpyAsync(dCfc, d->Cf, sizeof(double) * 3 * (size_t)nF, cudaMemcpyHostToDevice, s));
+    S4G_CUDA(cudaMemcpyAsync(dSfc, d->Sf, sizeof(double) * 3 * (size_t)nF, cudaMemcpyHostToDevice, s));
+    S4G_TRY(alloc(&geo.C, 3 * (size_t)nC));
+    S4G_TRY(alloc(&geo.invDd, 6 * (size_t)nC));
+    S4G_TRY(alloc(&geo.fS, 3 * (size_t)nI));
+    S4G_TRY(alloc(&geo.fmagS, nI));
+    S4G_TRY(alloc(&geo.fw, nI));
+    S4G_TRY(alloc(&geo.fdelta, nI));
+    S4G_TRY(alloc(&geo.bS, 3 * (size_t)nB));
+    S4G_TRY(alloc(&geo.bmagS, nB));
+    S4G_TRY(alloc(&geo.bn, 3 * (size_t)nB));
+    S4G_TRY(alloc(&geo.bk, 3 * (size_t)nB));
+    S4G_TRY(alloc(&geo.bdelta, nB));
+    S4G_TRY(alloc(&geo.bls, 3 * (size_t)nB));
+    S4G_TRY(alloc(&dBtype, nB));
+    S4G_TRY(alloc(&dBval, 3 * (size_t)nB));
+    S4G_TRY(alloc(&dBpress, nB));
+
+    mv.nC = nC; mv.nI = nI; mv.nB = nB; mv.nParts = hp.nParts;
+    mv.subdomains = (o && o->dic_subdomains) ? 1 : 0;
+    mv.rowptr = dRow; mv.col = dCol; mv.fidx = dFidx; mv.fown = dFown; mv.fnei = dFnei;
+    mv.fS = geo.fS; mv.fmagS = geo.fmagS; mv.fw = geo.fw; mv.fdelta = geo.fdelta;
+    mv.C = geo.C; mv.invDd = geo.invDd;
+    mv.browptr = dBrow; mv.btype = dBtype;
+    mv.bS = geo.bS; mv.bmagS = geo.bmagS; mv.bn = geo.bn; mv.bk = geo.bk;
+    mv.bdelta = geo.bdelta; mv.bls = geo.bls; mv.bval = dBval; mv.bpress = dBpress;
+    mv.partStart = dPartStart; mv.lvlOff = dLvlOff; mv.lvlStart = dLvlStart;
+    mv.upPtr = dUpPtr; mv.upIdx = dUpIdx; mv.dnPtr = dDnPtr; mv.dnIdx = dDnIdx;
+    {
+      int *dHfp, *dHfi, *dHbp, *dHbi, *dSlot;
+      S4G_TRY(upload(&dHfp, hp.haloFPtr));
+      S4G_TRY(upload(&dHfi, hp.haloFIdx));
+      S4G_TRY(upload(&dHbp, hp.haloBPtr));
+      S4G_TRY(upload(&dHbi, hp.haloBIdx));
+      S4G_TRY(upload(&dSlot, hp.slot));
+      mv.haloFPtr = dHfp; mv.haloFIdx = dHfi; mv.haloBPtr = dHbp; mv.haloBIdx = dHbi;
+      mv.slot = dSlot;
+      mv.maxRows = hp.maxRows; mv.maxHalo = hp.maxHalo; mv.maxEntries = hp.maxEntries;
+    }
+
+    GeomInputs gi{dCc, dCfc, dSfc, dS2c, dFcaller, dFflip, dBcaller, dBcell,
+                  o ? o->ls_boundary_delta : 0};
+    launchGeometry(mv, gi, geo, s);
+    launches += 5;
+    S4G_CUDA(cudaGetLastError());
+
+    // boundary condition mirror: default traction-free on every patch
+    nPatches = d->n_patches;
+    patchStart.assign(d->patch_start, d->patch_start + nPatches);
+    patchSize.assign(d->patch_size, d->patch_size + nPatches);
+    patchType.assign(nPatches, S4G_SOLID_TRACTION);
+    bvalH.assign(3 * (size_t)nB, 0.0);
+    bpressH.assign(nB, 0.0);
+    btypeH.assign(nB, 1);
+    bcDirty = true;
+
+    // fields and solver work arrays
+    S4G_TRY(alloc(&dVal, 2 * (size_t)nI));
+    S4G_TRY(alloc(&dDiag, nC));
+    S4G_TRY(alloc(&dRD, nC));
+    for (int k = 0; k < 2; ++k) S4G_TRY(alloc(&f.D[k], 3 * (size_t)nC));
+    S4G_TRY(alloc(&f.D0, 3 * (size_t)nC));
+    S4G_TRY(alloc(&f.D0b, 3 * (size_t)nB));
+    S4G_TRY(alloc(&f.G, 9 * (size_t)nC));
+    S4G_TRY(alloc(&f.sig, 6 * (size_t)nC));
+    S4G_TRY(alloc(&f.Gb, 9 * (size_t)nB));
+    S4G_TRY(alloc(&f.sigb, 6 * (size_t)nB));
+    S4G_TRY(alloc(&f.g, 3 * (size_t)nB));
+    S4G_TRY(alloc(&pc.x, 3 * (size_t)nC));
+    S4G_TRY(alloc(&pc.r, 3 * (size_t)nC));
+    S4G_TRY(alloc(&pc.w, 3 * (size_t)nC));
+    S4G_TRY(alloc(&pc.p[0], 3 * (size_t)nC));
+    S4G_TRY(alloc(&pc.p[1], 3 * (size_t)nC));
+    S4G_TRY(alloc(&pc.q, 3 * (size_t)nC));
+    S4G_TRY(alloc(&pc.flags[0], hp.nParts));
+    S4G_TRY(alloc(&pc.flags[1], hp.nParts));
+    pc.val = dVal; pc.diag = dDiag; pc.rD = dRD;
+    S4G_TRY(alloc(&dState, 1));
+    S4G_CUDA(cudaMallocHost((void**)&hState, sizeof(DevState)));
+    const size_t rowBlocks = (nC + kRowBlock - 1) / kRowBlock;
+    S4G_TRY(alloc(&dPartials, std::max(8 * rowBlocks, 4 * (size_t)hp.nParts)));
+    S4G_TRY(alloc(&dOut, 9 * (size_t)nC));
+    S4G_CUDA(cudaMemsetAsync(dState, 0, sizeof(DevState), s));
+
+    int maxSmem = 0;
+    S4G_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    if (sweepSmemBytes(mv) + 1024 > (size_t)maxSmem)
+      return setErr(S4G_BAD_ARG, "a DIC scheduling part does not fit in shared memory; use a smaller part_size");
+    int perSM = 0;
+    S4G_CUDA(sweepPrepare(mv, &perSM));
+    if (perSM < 1) return setErr(S4G_BAD_ARG, "DIC sweep kernel cannot be resident; use a smaller part_size");
+    sweepGrid = std::max(1, std::min(hp.nParts, perSM * ctx->numSMs));
+    S4G_CUDA(cudaStreamSynchronize(s));
+    // caller geometry is no longer needed
+    for (double* p : {dCc, dCfc, dSfc}) {
+      cudaFree(p);
+      allocs.erase(std::find(allocs.begin(), allocs.end(), (void*)p));
+    }
+    bytes -= sizeof(double) * 3 * ((size_t)nC + 2 * (size_t)nF);
+    return S4G_OK;
+  }
+
+  s4g_status allocTL() {
+    if (tlAllocated) return S4G_OK;
+    const size_t nC = hp.nC, nB = hp.nB;
+    S4G_TRY(alloc(&f.GD, 9 * nC)); S4G_TRY(alloc(&f.GD0, 9 * nC));
+    S4G_TRY(alloc(&f.GDb, 9 * nB)); S4G_TRY(alloc(&f.GD0b, 9 * nB));
+    S4G_TRY(alloc(&f.Finv, 9 * nC)); S4G_TRY(alloc(&f.Finvb, 9 * nB));
+    S4G_TRY(alloc(&f.J, nC)); S4G_TRY(alloc(&f.Jb, nB));
+    S4G_TRY(alloc(&f.FL, 9 * nC)); S4G_TRY(alloc(&f.FL0, 9 * nC));
+    S4G_TRY(alloc(&f.FLb, 9 * nB)); S4G_TRY(alloc(&f.FL0b, 9 * nB));
+    S4G_TRY(alloc(&f.sig0, 6 * nC)); S4G_TRY(alloc(&f.sig0b, 6 * nB));
+    tlAllocated = true;
+    return S4G_OK;
+  }
+
+  s4g_status setMaterial(const s4g_law* l) {
+    if (!l || (l->type != S4G_LINEAR_ELASTIC && l->type != S4G_NEO_HOOKEAN))
+      return setErr(S4G_BAD_ARG, "unknown law");
+    double E = l->E, nu = l->nu;
+    if (l->use_mu_K) {
+      if (!(l->mu > 0) || !(l->K > 0)) return setErr(S4G_BAD_ARG, "mu and K must be positive");
+      mu = l->mu; K = l->K;
+      E = 9.0 * K * mu / (3.0 * K + mu);
+      nu = (3.0 * K - 2.0 * mu) / (2.0 * (3.0 * K + mu));
+    } else {
+      // linearElastic.C:126-133: nu must lie in [-1, 0.5]
+      if (!(E > 0) || !(nu >= -1.0 && nu < 0.5)) return setErr(S4G_BAD_ARG, "need E > 0 and -1 <= nu < 0.5");
+      mu = E / (2.0 * (1.0 + nu));
+      K = (nu * E / ((1.0 + nu) * (1.0 - 2.0 * nu))) + (2.0 / 3.0) * mu;
+    }
+    lambda = nu * E / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    if (l->type == S4G_LINEAR_ELASTIC) {
+      K = E / (3.0 * (1.0 - 2.0 * nu));  // linearElastic.C:118-123
+      impK = 2.0 * mu + lambda;          // linearElastic.C:204-245
+    } else {
+      impK = (4.0 / 3.0) * mu + K;       // neoHookeanElastic.C:101-119
+    }
+    law = *l;
+    materialSet = true;
+    matrixValid = false;
+    return S4G_OK;
+  }
+
+  s4g_status setBC(int patch, s4g_bc_type type, const double* vec3, const double* pressure) {
+    if (patch < 0 || patch >= nPatches) return setErr(S4G_BAD_ARG, "patch index out of range");
+    if (type != S4G_FIXED_DISPLACEMENT && type != S4G_SOLID_TRACTION) return setErr(S4G_BAD_ARG, "unknown BC type");
+    const int nI = hp.nI;
+    const int ps = patchStart[patch], sz = patchSize[patch];
+    for (int i = 0; i < sz; ++i) {
+      if (vec3) for (int k = 0; k < 3; ++k) if (!std::isfinite(vec3[3 * i + k])) return setErr(S4G_BAD_ARG, "non-finite BC value");
+      if (pressure && !std::isfinite(pressure[i])) return setErr(S4G_BAD_ARG, "non-finite pressure");
+    }
+    if (patchType[patch] != type) matrixValid = false;
+    patchType[patch] = type;
+    // storage positions of this patch's faces
+    for (int k = 0; k < hp.nB; ++k) {
+      int b = hp.bcaller[k];
+      int i = b + nI - ps;
+      if (i < 0 || i >= sz) continue;
+      btypeH[k] = (int)type;
+      for (int j = 0; j < 3; ++j) bvalH[3 * (size_t)k + j] = vec3 ? vec3[3 * i + j] : 0.0;
+      bpressH[k] = (type == S4G_SOLID_TRACTION && pressure) ? pressure[i] : 0.0;
+    }
+    bcDirty = true;
+    return S4G_OK;
+  }
+
+  s4g_status syncBC() {
+    if (!bcDirty) return S4G_OK;
+    cudaStream_t s = ctx->stream;
+    S4G_CUDA(cudaMemcpyAsync(dBtype, btypeH.data(), sizeof(int) * hp.nB, cudaMemcpyHostToDevice, s));
+    S4G_CUDA(cudaMemcpyAsync(dBval, bvalH.data(), sizeof(double) * 3 * hp.nB, cudaMemcpyHostToDevice, s));
+    S4G_CUDA(cudaMemcpyAsync(dBpress, bpressH.data(), sizeof(double) * hp.nB, cudaMemcpyHostToDevice, s));
+    bcDirty = false;
+    return S4G_OK;
+  }
+
+  Controls controls(int tl) const {
+    Controls c{};
+    c.law = law.type == S4G_NEO_HOOKEAN ? 1 : 0;
+    c.tl = tl;
+    c.mu = mu; c.K = K; c.lambda = lambda; c.impK = impK; c.rImpK = 1.0 / impK;
+    c.gamma = impK;
+    c.gammaS = outer.stab_scale * impK;
+    c.loadFactor = 1.0;
+    c.tol = lin.tolerance; c.relTol = lin.rel_tol; c.maxIter = lin.max_iter;
+    c.nCorr = outer.n_correctors;
+    c.solTol = outer.solution_tol; c.altTol = outer.alternative_tol; c.matTol = outer.material_tol;
+    c.precond = lin.preconditioner == S4G_PRECOND_DIC ? 0 : 1;
+    return c;
+  }
+
+  s4g_status resetSweepState() {
+    cudaStream_t s = ctx->stream;
+    S4G_CUDA(cudaMemsetAsync(pc.flags[0], 0, sizeof(unsigned) * hp.nParts, s));
+    S4G_CUDA(cudaMemsetAsync(pc.flags[1], 0, sizeof(unsigned) * hp.nParts, s));
+    S4G_CUDA(cudaMemsetAsync(dState, 0, sizeof(DevState), s));
+    DevState init{};
+    init.epoch[0] = 1; init.epoch[1] = 1;
+    S4G_CUDA(cudaMemcpyAsync(&dState->epoch, &init.epoch, sizeof(init.epoch), cudaMemcpyHostToDevice, s));
+    return S4G_OK;
+  }
+
+  // Matrix and preconditioner (constant across correctors: impKf is fixed at
+  // construction, linGeomTotalDispSolid.C:72, and the mesh is static).
+  s4g_status ensureMatrix() {
+    if (!materialSet) return setErr(S4G_BAD_ARG, "material not set");
+    S4G_TRY(syncBC());
+    const int pre = lin.preconditioner == S4G_PRECOND_DIC ? 0 : 1;
+    if (matrixValid && matrixPrecond == pre) return S4G_OK;
+    cudaStream_t s = ctx->stream;
+    launchMatrix(mv, impK, dVal, dDiag, s);
+    launches++;
+    if (pre == 0) {
+      S4G_TRY(resetSweepState());
+      S4G_CUDA(cudaMemcpyAsync(dRD, dDiag, sizeof(double) * hp.nC, cudaMemcpyDeviceToDevice, s));
+      launchDicFactor(mv, pc, dState, sweepGrid, s);
+      launches += 2;
+    } else {
+      // diagonalPreconditioner: rD = 1/diag
+      S4G_CUDA(cudaMemcpyAsync(dRD, dDiag, sizeof(double) * hp.nC, cudaMemcpyDeviceToDevice, s));
+      launchReciprocal(hp.nC, dRD, s);
+      launches++;
+    }
+    S4G_CUDA(cudaGetLastError());
+    S4G_CUDA(cudaStreamSynchronize(s));
+    S4G_TRY(readState());
+    if (hState->status & kErrTimeout) return setErr(S4G_TIMEOUT, "DIC factor sweep wait gave up");
+    matrixValid = true;
+    matrixPrecond = pre;
+    return S4G_OK;
+  }
+
+  s4g_status readState() {
+    S4G_CUDA(cudaMemcpyAsync(hState, dState, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+    S4G_CUDA(cudaStreamSynchronize(ctx->stream));
+    return S4G_OK;
+  }
+
+  s4g_status initFields(int tl) {
+    cudaStream_t s = ctx->stream;
+    const size_t nC = hp.nC, nB = hp.nB;
+    auto z = [&](double* p, size_t n) { return cudaMemsetAsync(p, 0, n * sizeof(double), s); };
+    S4G_CUDA(z(f.D[0], 3 * nC)); S4G_CUDA(z(f.D[1], 3 * nC)); S4G_CUDA(z(f.D0, 3 * nC));
+    S4G_CUDA(z(f.D0b, 3 * nB)); S4G_CUDA(z(f.G, 9 * nC)); S4G_CUDA(z(f.sig, 6 * nC));
+    S4G_CUDA(z(f.Gb, 9 * nB)); S4G_CUDA(z(f.sigb, 6 * nB)); S4G_CUDA(z(f.g, 3 * nB));
+    S4G_CUDA(z(pc.x, 3 * nC)); S4G_CUDA(z(pc.r, 3 * nC)); S4G_CUDA(z(pc.w, 3 * nC));
+    S4G_CUDA(z(pc.p[0], 3 * nC)); S4G_CUDA(z(pc.p[1], 3 * nC)); S4G_CUDA(z(pc.q, 3 * nC));
+    if (tl) {
+      S4G_CUDA(z(f.GD, 9 * nC)); S4G_CUDA(z(f.GD0, 9 * nC)); S4G_CUDA(z(f.GDb, 9 * nB));
+      S4G_CUDA(z(f.GD0b, 9 * nB)); S4G_CUDA(z(f.sig0, 6 * nC)); S4G_CUDA(z(f.sig0b, 6 * nB));
+      // F = I, F^-1 = I, J = 1 (nonLinGeomTotalLagSolid.C:57-93)
+      std::vector<double> I9(9 * std::max(nC, nB), 0.0), one(std::max(nC, nB), 1.0);
+      for (size_t i = 0; i < std::max(nC, nB); ++i) { I9[9 * i] = 1; I9[9 * i + 4] = 1; I9[9 * i + 8] = 1; }
+      for (double* p : {f.Finv, f.FL, f.FL0}) S4G_CUDA(cudaMemcpyAsync(p, I9.data(), 9 * nC * sizeof(double), cudaMemcpyHostToDevice, s));
+      for (double* p : {f.Finvb, f.FLb, f.FL0b}) S4G_CUDA(cudaMemcpyAsync(p, I9.data(), 9 * nB * sizeof(double), cudaMemcpyHostToDevice, s));
+      S4G_CUDA(cudaMemcpyAsync(f.J, one.data(), nC * sizeof(double), cudaMemcpyHostToDevice, s));
+      S4G_CUDA(cudaMemcpyAsync(f.Jb, one.data(), nB * sizeof(double), cudaMemcpyHostToDevice, s));
+      S4G_CUDA(cudaStreamSynchronize(s));
+    }
+    return S4G_OK;
+  }
+
+  // PCG loop of one corrector: launch batches, read the device decision.
+  s4g_status pcgLoop(const Controls& c) {
+    int chunk = 2;
+    for (int guard = 0; guard < 1000000; ++guard) {
+      for (int i = 0; i < chunk; ++i)
+        launchPcgIteration(mv, c, pc, dState, dPartials, sweepGrid, ctx->stream, &launches);
+      S4G_CUDA(cudaGetLastError());
+      S4G_TRY(readState());
+      if (!hState->pcgContinue || (hState->status & (kErrTimeout | kErrNaN))) return S4G_OK;
+      chunk = std::min(chunk * 2, 16);
+    }
+    return setErr(S4G_TIMEOUT, "PCG loop did not end");
+  }
+
+  // One evolve(): correctors until converged() or nCorrectors.
+  s4g_status correctorLoop(Controls& c, int tl) {
+    cudaStream_t s = ctx->stream;
+    for (;;) {
+      launchRhs(mv, c, f, pc.x, pc.r, dState, dPartials, s);
+      launches++;
+      S4G_TRY(readState());
+      if (hState->pcgContinue) S4G_TRY(pcgLoop(c));
+      launchPost(mv, c, f, pc.x, dState, dPartials, 1, s);
+      launches += tl ? 2 : 1;
+      S4G_CUDA(cudaGetLastError());
+      S4G_TRY(readState());
+      if (ctx->verbose && outer.info_frequency > 0 &&
+          ((hState->iCorr - 1) % outer.info_frequency == 0 || hState->converged))
+        std::printf("    %d, %g, %g, 0, %d\n", hState->iCorr - 1, hState->initResMag, hState->relRes,
+                    hState->lastMaxIters);
+      if (hState->status & (kErrTimeout | kErrNaN)) return S4G_OK;
+      if (!hState->outerContinue) return S4G_OK;
+    }
+  }
+
+  s4g_status solve(s4g_model model, int nInc, double* Dout, double* sigOut, s4g_perf* perf) {
+    if (model != S4G_LIN_GEOM_TOTAL_DISP && model != S4G_NONLIN_GEOM_TOTAL_LAG)
+      return setErr(S4G_BAD_ARG, "unknown model");
+    if (!materialSet) return setErr(S4G_BAD_ARG, "material not set");
+    const int tl = model == S4G_NONLIN_GEOM_TOTAL_LAG;
+    if (tl && law.type != S4G_NEO_HOOKEAN) return setErr(S4G_BAD_ARG, "the TL model needs a neoHookeanElastic law");
+    if (!tl && law.type != S4G_LINEAR_ELASTIC) return setErr(S4G_BAD_ARG, "the linear-geometry model needs a linearElastic law");
+    if (precision != S4G_FP64) return setErr(S4G_NOT_BUILT, "FP32 refinement path not built yet");
+    if (tl) S4G_TRY(allocTL());
+    if (!tl) nInc = 1;
+    if (nInc < 1) return setErr(S4G_BAD_ARG, "n_increments must be >= 1");
+    cudaStream_t s = ctx->stream;
+    const long long launches0 = launches;
+    S4G_TRY(ensureMatrix());
+    cudaEvent_t e0, e1;
+    S4G_CUDA(cudaEventCreate(&e0));
+    S4G_CUDA(cudaEventCreate(&e1));
+    S4G_TRY(initFields(tl));
+    S4G_TRY(resetSweepState());
+    S4G_CUDA(cudaEventRecord(e0, s));
+    Controls c = controls(tl);
+    int nCorrTotal = 0;
+    if (!tl) {
+      launchTractionInit(mv, c, f, s);
+      launchPost(mv, c, f, pc.x, dState, dPartials, 0, s);
+      launches += 2;
+      S4G_TRY(correctorLoop(c, 0));
+      nCorrTotal = hState->nCorrDone;
+    } else {
+      for (int n = 1; n <= nInc; ++n) {
+        c.loadFactor = (double)n / nInc;
+        // evolve(): enforceLinear = false; iCorr restarts
+        int zero = 0;
+        S4G_CUDA(cudaMemcpyAsync(&dState->enforceLinear, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+        S4G_CUDA(cudaMemcpyAsync(&dState->iCorr, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+        launchTractionInit(mv, c, f, s);
+        launches++;
+        S4G_TRY(correctorLoop(c, 1));
+        launchTlShift(mv, c, f, dState, s);
+        launches += 2;
+        if (hState->status & (kErrTimeout | kErrNaN)) break;
+      }
+      S4G_TRY(readState());
+      nCorrTotal = hState->nCorrDone;
+    }
+    S4G_CUDA(cudaEventRecord(e1, s));
+    S4G_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // outputs in caller order
+    auto t0 = std::chrono::steady_clock::now();
+    if (Dout) {
+      const double* src = tl ? f.D0 : f.D[hState->dcur];
+      launchGather(hp.nC, 3, dC2s, src, dOut, s);
+      S4G_CUDA(cudaMemcpyAsync(Dout, dOut, sizeof(double) * 3 * hp.nC, cudaMemcpyDeviceToHost, s));
+    }
+    if (sigOut) {
+      launchGather(hp.nC, 6, dC2s, f.sig, dOut + 3 * (size_t)hp.nC, s);
+      S4G_CUDA(cudaMemcpyAsync(sigOut, dOut + 3 * (size_t)hp.nC, sizeof(double) * 6 * hp.nC, cudaMemcpyDeviceToHost, s));
+    }
+    S4G_CUDA(cudaStreamSynchronize(s));
+    auto t1 = std::chrono::steady_clock::now();
+    lastModel = model;
+    if (perf) {
+      std::memset(perf, 0, sizeof(*perf));
+      perf->n_correctors = nCorrTotal;
+      perf->converged = hState->converged;
+      perf->total_lin_iters = hState->totalLinIters;
+      perf->last_max_lin_iters = hState->lastMaxIters;
+      perf->initial_residual = hState->initResMag;
+      perf->rel_residual = hState->relRes;
+      perf->solve_ms = ms;
+      perf->d2h_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+      perf->kernel_launches = launches - launches0;
+      perf->enforce_linear = hState->enforceLinear;
+      perf->device_status = (int)hState->status;
+    }
+    if (hState->status & kErrTimeout) return setErr(S4G_TIMEOUT, "a bounded device wait gave up");
+    if (hState->status & kErrNaN) return setErr(S4G_NAN_DETECTED, "non-finite value in the iteration");
+    if (hState->status & kErrIndefinite) return setErr(S4G_INDEFINITE, "PCG met p.Ap <= 0");
+    if (!hState->converged) return S4G_NOT_CONVERGED;
+    return S4G_OK;
+  }
+
+  // ---------------------------------------------------------- operators ---
+  s4g_status opMatrix(double* diag, double* upper) {
+    S4G_TRY(ensureMatrix());
+    std::vector<double> v(2 * (size_t)hp.nI), dg(hp.nC);
+    S4G_CUDA(cudaMemcpy(v.data(), dVal, sizeof(double) * v.size(), cudaMemcpyDeviceToHost));
+    S4G_CUDA(cudaMemcpy(dg.data(), dDiag, sizeof(double) * dg.size(), cudaMemcpyDeviceToHost));
+    for (int s = 0; s < hp.nC; ++s) {
+      if (diag) diag[hp.s2c[s]] = dg[s];
+      for (int e = hp.rowptr[s]; e < hp.rowptr[s + 1]; ++e)
+        if (hp.fidx[e] >= 0 && upper) upper[hp.fcaller[hp.fidx[e]]] = v[e];
+    }
+    return S4G_OK;
+  }
+
+  s4g_status toStorage(int k, const double* in, std::vector<double>& out) {
+    out.assign(3 * (size_t)hp.nC, 0.0);
+    for (int s = 0; s < hp.nC; ++s)
+      for (int j = 0; j < k; ++j) out[3 * (size_t)s + j] = in[(size_t)hp.s2c[s] * k + j];
+    return S4G_OK;
+  }
+  void fromStorage(int k, const std::vector<double>& in, double* out) {
+    for (int s = 0; s < hp.nC; ++s)
+      for (int j = 0; j < k; ++j) out[(size_t)hp.s2c[s] * k + j] = in[3 * (size_t)s + j];
+  }
+
+  s4g_status opAmul(int k, const double* x, double* y) {
+    if (k < 1 || k > 3 || !x || !y) return setErr(S4G_BAD_ARG, "k must be 1..3");
+    S4G_TRY(ensureMatrix());
+    std::vector<double> hx, hy(3 * (size_t)hp.nC);
+    toStorage(k, x, hx);
+    S4G_CUDA(cudaMemcpy(pc.w, hx.data(), sizeof(double) * hx.size(), cudaMemcpyHostToDevice));
+    launchAmul(mv, dVal, dDiag, pc.w, pc.q, ctx->stream);
+    launches++;
+    S4G_CUDA(cudaGetLastError());
+    S4G_CUDA(cudaMemcpy(hy.data(), pc.q, sizeof(double) * hy.size(), cudaMemcpyDeviceToHost));
+    fromStorage(k, hy, y);
+    return S4G_OK;
+  }
+
+  s4g_status opPrecondition(int k, const double* r, double* w) {
+    if (k < 1 || k > 3 || !r || !w) return setErr(S4G_BAD_ARG, "k must be 1..3");
+    S4G_TRY(ensureMatrix());
+    std::vector<double> hr, hw(3 * (size_t)hp.nC);
+    toStorage(k, r, hr);
+    S4G_CUDA(cudaMemcpy(pc.r, hr.data(), sizeof(double) * hr.size(), cudaMemcpyHostToDevice));
+    S4G_TRY(resetSweepState());
+    DevState init{};
+    init.pcgContinue = 1;
+    S4G_CUDA(cudaMemcpyAsync(&dState->pcgContinue, &init.pcgContinue, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    Controls c = controls(0);
+    launchPrecondOnly(mv, c, pc, dState, dPartials, sweepGrid, ctx->stream);
+    launches += 2;
+    S4G_CUDA(cudaGetLastError());
+    S4G_CUDA(cudaStreamSynchronize(ctx->stream));
+    S4G_TRY(readState());
+    if (hState->status & kErrTimeout) return setErr(S4G_TIMEOUT, "sweep wait gave up");
+    S4G_CUDA(cudaMemcpy(hw.data(), pc.w, sizeof(double) * hw.size(), cudaMemcpyDeviceToHost));
+    fromStorage(k, hw, w);
+    return S4G_OK;
+  }
+
+  s4g_status getGradD(double* out) {
+    if (lastModel < 0) return setErr(S4G_BAD_ARG, "no solve has run");
+    const double* src = lastModel == S4G_NONLIN_GEOM_TOTAL_LAG ? f.GD : f.G;
+    launchGather(hp.nC, 9, dC2s, src, dOut, ctx->stream);
+    S4G_CUDA(cudaMemcpyAsync(out, dOut, sizeof(double) * 9 * hp.nC, cudaMemcpyDeviceToHost, ctx->stream));
+    S4G_CUDA(cudaStreamSynchronize(ctx->stream));
+    return S4G_OK;
+  }
+};
+
+}  // namespace s4g
+
+// ------------------------------------------------------------------ C ABI ---
+
+struct s4g_ctx { s4g::Ctx c; };
+struct s4g_mesh { s4g::Engine e; };
+
+using s4g::setErr;
+
+extern "C" {
+
+const char* s4g_status_str(s4g_status st) {
+  switch (st) {
+    case S4G_OK: return "OK";
+    case S4G_BAD_ARG: return "BAD_ARG";
+    case S4G_OOM: return "OOM";
+    case S4G_NOT_CONVERGED: return "NOT_CONVERGED";
+    case S4G_NAN_DETECTED: return "NAN_DETECTED";
+    case S4G_INDEFINITE: return "INDEFINITE";
+    case S4G_TIMEOUT: return "TIMEOUT";
+    case S4G_CUDA_ERROR: return "CUDA_ERROR";
+    case S4G_NO_DEVICE: return "NO_DEVICE";
+    case S4G_ADMISSION_REJECTED: return "ADMISSION_REJECTED";
+    case S4G_PENDING: return "PENDING";
+    case S4G_CANCELLED: return "CANCELLED";
+    case S4G_NOT_BUILT: return "NOT_BUILT";
+  }
+  return "UNKNOWN";
+}
+
+int s4g_abi_version(void) { return S4G_ABI_VERSION; }
+
+const char* s4g_last_error(void) { return s4g::gLastError.c_str(); }
+
+s4g_status s4g_ctx_create(s4g_ctx** out, const s4g_ctx_opts* opts) {
+  if (!out) return setErr(S4G_BAD_ARG, "null output");
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) return setErr(S4G_NO_DEVICE, "no CUDA device");
+  int dev = opts ? opts->device : 0;
+  if (dev < 0 || dev >= n) return setErr(S4G_BAD_ARG, "device ordinal out of range");
+  std::unique_ptr<s4g_ctx> c(new s4g_ctx());
+  c->c.device = dev;
+  c->c.verbose = opts ? opts->verbose : 0;
+  if (cudaSetDevice(dev) != cudaSuccess) return setErr(S4G_CUDA_ERROR, "cudaSetDevice failed");
+  cudaDeviceGetAttribute(&c->c.numSMs, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking) != cudaSuccess)
+    return setErr(S4G_CUDA_ERROR, "cudaStreamCreate failed");
+  *out = c.release();
+  return S4G_OK;
+}
+
+s4g_status s4g_ctx_destroy(s4g_ctx* ctx) {
+  if (!ctx) return S4G_BAD_ARG;
+  cudaSetDevice(ctx->c.device);
+  if (ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
+  delete ctx;
+  return S4G_OK;
+}
+
+s4g_status s4g_mesh_upload(s4g_ctx* ctx, const s4g_mesh_desc* desc, const s4g_mesh_opts* opts,
+                           s4g_mesh** out) {
+  if (!ctx || !desc || !out) return setErr(S4G_BAD_ARG, "null argument");
+  *out = nullptr;
+  cudaSetDevice(ctx->c.device);
+  std::unique_ptr<s4g_mesh> m(new s4g_mesh());
+  m->e.ctx = &ctx->c;
+  s4g_lin_solver lin;
+  s4g_outer outer;
+  s4g_default_controls(&lin, &outer);
+  m->e.lin = lin;
+  m->e.outer = outer;
+  s4g_status st = m->e.uploadMesh(desc, opts);
+  if (st != S4G_OK) return st;
+  *out = m.release();
+  return S4G_OK;
+}
+
+s4g_status s4g_mesh_get_permutation(const s4g_mesh* mesh, int* perm) {
+  if (!mesh || !perm) return setErr(S4G_BAD_ARG, "null argument");
+  const s4g::HostPrep& hp = mesh->e.hp;
+  // solver rank r -> caller cell
+  for (int s = 0; s < hp.nC; ++s) perm[hp.solverRank[s]] = hp.s2c[s];
+  return S4G_OK;
+}
+
+s4g_status s4g_mesh_plan(const s4g_mesh_desc* desc, const s4g_mesh_opts* opts, int* perm_out,
+                         s4g_mesh_info* info) {
+  if (!desc) return setErr(S4G_BAD_ARG, "null mesh");
+  s4g::HostPrep hp;
+  std::string err;
+  s4g_status st = s4g::prepareMesh(desc, opts, hp, err);
+  if (st != S4G_OK) return setErr(st, err);
+  if (perm_out)
+    for (int s = 0; s < hp.nC; ++s) perm_out[hp.solverRank[s]] = hp.s2c[s];
+  if (info) {
+    std::memset(info, 0, sizeof(*info));
+    info->n_cells = hp.nC;
+    info->n_internal_faces = hp.nI;
+    info->n_boundary_faces = hp.nB;
+    info->n_parts = hp.nParts;
+    info->part_depth = hp.partDepth;
+    info->max_local_levels = hp.maxLocalLevels;
+    info->n_levels_global = hp.globalLevels;
+  }
+  return S4G_OK;
+}
+
+s4g_status s4g_mesh_get_info(const s4g_mesh* mesh, s4g_mesh_info* info) {
+  if (!mesh || !info) return setErr(S4G_BAD_ARG, "null argument");
+  const s4g::HostPrep& hp = mesh->e.hp;
+  info->n_cells = hp.nC;
+  info->n_internal_faces = hp.nI;
+  info->n_boundary_faces = hp.nB;
+  info->n_parts = hp.nParts;
+  info->part_depth = hp.partDepth;
+  info->max_local_levels = hp.maxLocalLevels;
+  info->n_levels_global = hp.globalLevels;
+  info->device_bytes = (long long)mesh->e.bytes;
+  return S4G_OK;
+}
+
+s4g_status s4g_mesh_destroy(s4g_mesh* mesh) {
+  if (!mesh) return S4G_BAD_ARG;
+  cudaSetDevice(mesh->e.ctx->device);
+  cudaStreamSynchronize(mesh->e.ctx->stream);
+  delete mesh;
+  return S4G_OK;
+}
+
+s4g_status s4g_material_set(s4g_mesh* mesh, const s4g_law* law) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  return mesh->e.setMaterial(law);
+}
+
+s4g_status s4g_bc_set(s4g_mesh* mesh, int patch, s4g_bc_type type, const double* vec3,
+                      const double* pressure) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  return mesh->e.setBC(patch, type, vec3, pressure);
+}
+
+void s4g_default_controls(s4g_lin_solver* lin, s4g_outer* outer) {
+  if (lin) {
+    lin->preconditioner = S4G_PRECOND_DIC;
+    lin->tolerance = 1e-9;
+    lin->rel_tol = 0.1;
+    lin->max_iter = 1000;
+  }
+  if (outer) {
+    outer->n_correctors = 10000;
+    outer->solution_tol = 1e-6;
+    outer->alternative_tol = 1e-7;
+    outer->material_tol = 1e-5;
+    outer->stab_scale = 0.1;
+    outer->info_frequency = 100;
+  }
+}
+
+s4g_status s4g_solver_set(s4g_mesh* mesh, const s4g_lin_solver* lin, const s4g_outer* outer,
+                          s4g_precision precision) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  if (lin) {
+    if (lin->max_iter < 0 || !(lin->tolerance >= 0) || !(lin->rel_tol >= 0) ||
+        (lin->preconditioner != S4G_PRECOND_DIC && lin->preconditioner != S4G_PRECOND_DIAGONAL))
+      return setErr(S4G_BAD_ARG, "invalid linear solver controls");
+    mesh->e.lin = *lin;
+  }
+  if (outer) {
+    if (outer->n_correctors < 1 || !(outer->stab_scale >= 0))
+      return setErr(S4G_BAD_ARG, "invalid outer controls");
+    mesh->e.outer = *outer;
+  }
+  if (precision != S4G_FP64 && precision != S4G_FP32_REFINE) return setErr(S4G_BAD_ARG, "unknown precision");
+  mesh->e.precision = precision;
+  return S4G_OK;
+}
+
+s4g_status s4g_solve(s4g_mesh* mesh, s4g_model model, int n_increments, double* D_out,
+                     double* sigma_out, s4g_perf* perf) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  cudaSetDevice(mesh->e.ctx->device);
+  return mesh->e.solve(model, n_increments, D_out, sigma_out, perf);
+}
+
+s4g_status s4g_get_gradD(s4g_mesh* mesh, double* gradD_out) {
+  if (!mesh || !gradD_out) return setErr(S4G_BAD_ARG, "null argument");
+  return mesh->e.getGradD(gradD_out);
+}
+
+s4g_status s4g_op_matrix(s4g_mesh* mesh, double* diag, double* upper) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  return mesh->e.opMatrix(diag, upper);
+}
+
+s4g_status s4g_op_amul(s4g_mesh* mesh, int k, const double* x, double* y) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  return mesh->e.opAmul(k, x, y);
+}
+
+s4g_status s4g_op_precondition(s4g_mesh* mesh, int k, const double* r, double* w) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  return mesh->e.opPrecondition(k, r, w);
+}
+
+}  // extern "C"

@@ -1,0 +1,542 @@
+// Finite-volume kernels of the segregated solid solve: once-per-mesh geometry
+// and matrix, the post-solve pass (gradient, law, boundary conditions,
+// convergence reductions) and the right-hand-side pass (divergence of stress,
+// Rhie-Chow stabilisation, boundary terms).
+//
+// Reference arithmetic (paths relative to the solids4foam tree):
+//   outer loop     solidModels/linGeomTotalDispSolid/linGeomTotalDispSolid.C:135-208
+//   TL loop        solidModels/nonLinGeomTotalLagSolid/nonLinGeomTotalLagSolid.C:145-240
+//   traction BC    solidModels/fvPatchFields/solidTraction/solidTractionFvPatchVectorField.C:321-463
+//                  + tractionBoundarySnGrad linGeomTotalDispSolid.C:235-271,
+//                    nonLinGeomTotalLagSolid.C:263-325
+//   fixed disp BC  .../fixedDisplacement/fixedDisplacementFvPatchVectorField.C:258-356
+//   correction k   numerics/patchCorrectionVectors/patchCorrectionVectors.C:24-36
+//   Rhie-Chow      solidModels/solidModel/momentumStabilisation/momentumStabilisation.C:79-217
+//   laws           linearElastic.C:318-339 (+ mechanicalLaw.C:983-1001),
+//                  neoHookeanElastic.C:275-303 (+ mechanicalLaw.C:1095-1159)
+//   converged()    solidModels/solidModel/solidModelTemplates.C:26-188
+// OpenFOAM operators (leastSquares gradient, Gauss linear corrected laplacian,
+// Gauss linear divergence, linear interpolation) follow the published
+// finite-volume formulation.
+//
+// The momentum system of one corrector is  M D_new = M D_old + R(D_old):
+// the implicit (fvm) and explicit (fvc) laplacians of the reference cancel
+// except for M (D_new - D_old), so the PCG solves M x = R for the correction
+// x = D_new - D_old.  Each face flux is evaluated in the owner orientation by
+// both cells that share it, so owner and neighbour contributions are exact
+// negatives of each other; there are no atomics and sums run in a fixed order.
+
+#include "kernels.cuh"
+
+namespace s4g {
+namespace {
+
+__device__ __forceinline__ S6 hooke(const Controls& c, const T9& g) {
+  S6 eps = symmT(g);
+  return addI((2.0 * c.mu) * devS(eps), c.K * trS(eps));
+}
+
+__device__ __forceinline__ S6 neoHookean(const Controls& c, const T9& F) {
+  double J = detT(F);
+  T9 b = dotTT(F, transposeT(F));
+  S6 bEbar = pow(J, -2.0 / 3.0) * symmT(b);
+  S6 sdev = c.mu * devS(bEbar);
+  double sigmaHyd = 0.5 * c.K * (pow(J, 2.0) - 1.0);
+  return (1.0 / J) * addI(sdev, sigmaHyd);
+}
+
+// ------------------------------------------------------------- geometry ---
+
+__global__ void kGeomCells(MeshView mv, GeomInputs in, GeomOutputs out) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= mv.nC) return;
+  int c = in.s2c[s];
+  stV(out.C, s, ldV(in.Cc, c));
+}
+
+__global__ void kGeomFaces(MeshView mv, GeomInputs in, GeomOutputs out) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= mv.nI) return;
+  int f = in.fcaller[k];
+  V3 S = ldV(in.Sfc, f);
+  if (in.fflip[k]) S = -1.0 * S;
+  V3 Cf = ldV(in.Cfc, f);
+  V3 Co = ldV(out.C, mv.fown[k]), Cn = ldV(out.C, mv.fnei[k]);
+  double magS = mag(S);
+  V3 n = (1.0 / magS) * S;
+  // surfaceInterpolation::makeWeights
+  double sfdOwn = fabs(dot(S, Cf - Co));
+  double sfdNei = fabs(dot(S, Cn - Cf));
+  double w = sfdNei / (sfdOwn + sfdNei);
+  V3 d = Cn - Co;
+  // stabilised non-orthogonal deltaCoeffs 1/max(n.d, 0.05|d|)
+  double delta = 1.0 / fmax(dot(n, d), 0.05 * mag(d));
+  stV(out.fS, k, S);
+  out.fmagS[k] = magS;
+  out.fw[k] = w;
+  out.fdelta[k] = delta;
+}
+
+// Boundary geometry that does not need the least-squares tensor.
+__global__ void kGeomBFaces1(MeshView mv, GeomInputs in, GeomOutputs out, double* bd) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= mv.nB) return;
+  int f = mv.nI + in.bcaller[k];
+  V3 S = ldV(in.Sfc, f);
+  V3 Cf = ldV(in.Cfc, f);
+  V3 Cp = ldV(out.C, in.bcell[k]);
+  double magS = mag(S);
+  V3 n = (1.0 / magS) * S;
+  V3 dfull = Cf - Cp;
+  V3 dn = dot(n, dfull) * n;             // fvPatch::delta(): patch-normal
+  stV(out.bS, k, S);
+  out.bmagS[k] = magS;
+  stV(out.bn, k, n);
+  out.bdelta[k] = 1.0 / mag(dn);
+  stV(out.bk, k, dfull - dot(n, dfull) * n);  // (I - n n) & (Cf - C)
+  stV(bd, k, in.lsBoundaryDelta ? dfull : dn);
+}
+
+// leastSquaresVectors: dd = sum d d^T/|d|^2 over the cell's faces, inverted.
+__global__ void kGeomLs(MeshView mv, GeomOutputs out, const double* bd) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= mv.nC) return;
+  V3 Cs = ldV(out.C, s);
+  S6 acc = {0, 0, 0, 0, 0, 0};
+  for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) {
+    V3 d = ldV(out.C, mv.col[e]) - Cs;
+    double r = 1.0 / magSqr(d);
+    S6 wdd = {r * d.x * d.x, r * d.x * d.y, r * d.x * d.z, r * d.y * d.y, r * d.y * d.z, r * d.z * d.z};
+    acc = acc + wdd;
+  }
+  for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
+    V3 d = ldV(bd, b);
+    double r = 1.0 / magSqr(d);
+    S6 wdd = {r * d.x * d.x, r * d.x * d.y, r * d.x * d.z, r * d.y * d.y, r * d.y * d.z, r * d.z * d.z};
+    acc = acc + wdd;
+  }
+  S6 inv = invS(acc);
+  stS(out.invDd, s, inv);
+  for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
+    V3 d = ldV(bd, b);
+    stV(out.bls, b, (1.0 / magSqr(d)) * dotVS(d, inv));
+  }
+}
+
+__global__ void kMatrix(MeshView mv, double gamma, double* val, double* diag) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= mv.nC) return;
+  double d = 0;
+  for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) {
+    int fk = mv.fidx[e];
+    int f = fk >= 0 ? fk : ~fk;
+    double upper = mv.fdelta[f] * (gamma * mv.fmagS[f]);
+    d -= upper;
+    val[e] = -upper;
+  }
+  for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b)
+    if (mv.btype[b] == 0) d += gamma * mv.bmagS[b] * (-mv.bdelta[b]);
+  diag[s] = -d;
+}
+
+// ---------------------------------------------------------- traction BC ---
+
+__device__ __forceinline__ V3 tractionSnGrad(const MeshView& mv, const Controls& c, int b,
+                                             const S6& sb, const T9& Gb, const T9* Finvb,
+                                             int enforceLinear) {
+  V3 t = c.loadFactor * ldV(mv.bval, b);
+  double p = c.loadFactor * mv.bpress[b];
+  V3 n = ldV(mv.bn, b);
+  if (!c.tl) {
+    T9 a = fromS(sb) - c.impK * Gb;
+    return c.rImpK * ((t - p * n) - dotVT(n, a));
+  }
+  if (enforceLinear || !Finvb)
+    return c.rImpK * ((t - p * n) - dotVS(n, sb) + c.impK * dotVT(n, Gb));
+  V3 nc = dotVT(n, *Finvb);
+  nc = (1.0 / mag(nc)) * nc;
+  return c.rImpK * ((t - p * nc) - dotVS(nc, sb) + c.impK * dotVT(n, Gb));
+}
+
+__global__ void kTractionInit(MeshView mv, Controls c, FieldPtrs f) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= mv.nB || mv.btype[b] != 1) return;
+  T9 Fi;
+  const T9* pF = nullptr;
+  if (c.tl) { Fi = ldT(f.Finvb, b); pF = &Fi; }
+  stV(f.g, b, tractionSnGrad(mv, c, b, ldS(f.sigb, b), ldT(f.Gb, b), pF, 0));
+}
+
+// Boundary value of the solved field on face b of cell s (correctBoundaryConditions).
+__device__ __forceinline__ V3 boundaryValue(const MeshView& mv, const Controls& c,
+                                            const FieldPtrs& f, int b, V3 Up, const T9& Gold) {
+  if (mv.btype[b] == 1)
+    return Up + dotVT(ldV(mv.bk, b), Gold) + (1.0 / mv.bdelta[b]) * ldV(f.g, b);
+  V3 v = c.loadFactor * ldV(mv.bval, b);
+  if (c.tl) v = v - ldV(f.D0b, b);
+  return v;
+}
+
+// --------------------------------------------------------- post-solve pass ---
+// mode 0 (constructor): gradient only, from the current field.
+// mode 1 (corrector): apply the correction x, gradient, law, boundary, g.
+// For the TL model the law needs the global J check first, so mode 1 stops
+// after the kinematics (F, F^-1, J) and kPostLawTL finishes the pass.
+
+__global__ void __launch_bounds__(kRowBlock)
+kPost(MeshView mv, Controls c, FieldPtrs f, const double* __restrict__ x, DevState* st,
+      double* partials, int mode) {
+  __shared__ double smem[32 * 6];
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int dc = st->dcur;
+  const double* Uold = f.D[dc];
+  double* Unew = f.D[dc ^ 1];
+  const bool apply = (mode == 1);
+  double red[6] = {0, 0, 0, 0, 0, 0};  // max|x|, max|U-D0|, max|U|, sum U
+  double mx[3] = {0, 0, 0};
+  double minJ = 1e300, maxJ = -1e300;
+  if (s < mv.nC) {
+    V3 Up = ldV(Uold, s);
+    if (apply) Up = Up + ldV(x, s);
+    const bool hasB = mv.browptr[s + 1] > mv.browptr[s];
+    T9 Gold = hasB ? ldT(f.G, s) : zeroT();
+    // leastSquares gradient (cell-centric; owner-oriented d and dU)
+    const S6 inv = ldS(mv.invDd, s);
+    const V3 Cs = ldV(mv.C, s);
+    T9 acc = zeroT();
+    for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) {
+      const int nb = mv.col[e];
+      V3 Un = ldV(Uold, nb);
+      if (apply) Un = Un + ldV(x, nb);
+      const V3 Cn = ldV(mv.C, nb);
+      if (mv.fidx[e] >= 0) {
+        V3 d = Cn - Cs;
+        double r = 1.0 / magSqr(d);
+        acc = acc + outer(r * dotVS(d, inv), Un - Up);
+      } else {
+        V3 d = Cs - Cn;
+        double r = 1.0 / magSqr(d);
+        acc = acc - outer(-r * dotVS(d, inv), Up - Un);
+      }
+    }
+    for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
+      V3 Ub = boundaryValue(mv, c, f, b, Up, Gold);
+      acc = acc + outer(ldV(mv.bls, b), Ub - Up);
+    }
+    const T9 G = acc;
+    stT(f.G, s, G);
+    // boundary gradient: Gb = G + n (snGrad - n.G)
+    for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
+      V3 n = ldV(mv.bn, b);
+      V3 sg;
+      if (mv.btype[b] == 1) {
+        sg = ldV(f.g, b);
+      } else {
+        V3 Ub = boundaryValue(mv, c, f, b, Up, Gold);
+        sg = mv.bdelta[b] * (Ub - (Up + dotVT(ldV(mv.bk, b), Gold)));
+      }
+      T9 Gb = G + outer(n, sg - dotVT(n, G));
+      stT(f.Gb, b, Gb);
+      if (!c.tl) {
+        S6 sb = mode == 1 ? hooke(c, Gb) : ldS(f.sigb, b);
+        if (mode == 1) stS(f.sigb, b, sb);
+        if (mv.btype[b] == 1) stV(f.g, b, tractionSnGrad(mv, c, b, sb, Gb, nullptr, 0));
+      }
+    }
+    if (!c.tl) {
+      if (mode == 1) stS(f.sig, s, hooke(c, G));
+    } else if (mode == 1) {
+      // TL kinematics: gradD = gradD.oldTime + gradDD; F = I + gradD^T
+      T9 GD = ldT(f.GD0, s) + G;
+      stT(f.GD, s, GD);
+      T9 F = transposeT(GD);
+      F.xx += 1.0; F.yy += 1.0; F.zz += 1.0;
+      stT(f.Finv, s, invT(F));
+      double J = detT(F);
+      f.J[s] = J;
+      minJ = fmin(minJ, J); maxJ = fmax(maxJ, J);
+      for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
+        T9 GDb = ldT(f.GD0b, b) + ldT(f.Gb, b);
+        stT(f.GDb, b, GDb);
+        T9 Fb = transposeT(GDb);
+        Fb.xx += 1.0; Fb.yy += 1.0; Fb.zz += 1.0;
+        stT(f.Finvb, b, invT(Fb));
+        double Jb = detT(Fb);
+        f.Jb[b] = Jb;
+        minJ = fmin(minJ, Jb); maxJ = fmax(maxJ, Jb);
+      }
+    }
+    if (apply) {
+      stV(Unew, s, Up);
+      V3 xs = ldV(x, s);
+      mx[0] = mag(xs);
+      mx[1] = c.tl ? mag(Up) : mag(Up - ldV(f.D0, s));
+      mx[2] = mag(Up);
+      red[0] = Up.x; red[1] = Up.y; red[2] = Up.z;
+      if (!(isfinite(Up.x) && isfinite(Up.y) && isfinite(Up.z))) atomicOr(&st->status, kErrNaN);
+    }
+  }
+  if (mode == 0) return;
+  double sums[3] = {red[0], red[1], red[2]};
+  blockSum<3>(sums, smem);
+  double mxs[5] = {mx[0], mx[1], mx[2], -minJ, maxJ};
+  blockMax<5>(mxs, smem);
+  if (threadIdx.x == 0) {
+    double* p = partials + 8 * (size_t)blockIdx.x;
+    p[0] = sums[0]; p[1] = sums[1]; p[2] = sums[2];
+    p[3] = mxs[0]; p[4] = mxs[1]; p[5] = mxs[2]; p[6] = mxs[3]; p[7] = mxs[4];
+  }
+  if (!lastBlockDone(&st->counter[0], gridDim.x)) return;
+  double S[3], M[5];
+  reducePartials<3>(partials, 8, gridDim.x, S, smem);
+  reducePartialsMax<5>(partials + 3, 8, gridDim.x, M, smem);
+  if (threadIdx.x != 0) return;
+  st->counter[0] = 0;
+  st->dcur = dc ^ 1;
+  // converged(): relative displacement residual
+  double denom = M[1];
+  if (denom < 1e-15) denom = fmax(M[2], 1e-15);
+  double relRes = M[0] / denom;
+  double r2 = 0;
+  int maxIt = 0;
+  for (int k = 0; k < 3; ++k) {
+    r2 += st->initRes[k] * st->initRes[k];
+    maxIt = max(maxIt, st->nIter[k]);
+    st->totalLinIters += st->nIter[k];
+  }
+  double initResMag = sqrt(r2);
+  st->relRes = relRes;
+  st->initResMag = initResMag;
+  st->lastMaxIters = maxIt;
+  for (int k = 0; k < 3; ++k) st->xbar[k] = S[k] / mv.nC;
+  if (c.tl) {
+    st->minJ = -M[3]; st->maxJ = M[4];
+    if (!st->enforceLinear && (st->minJ < 0.01 || st->maxJ > 100)) st->enforceLinear = 1;
+  }
+  const int iCorr = st->iCorr;
+  const double materialResidual = 0.0;
+  bool conv = false;
+  if (iCorr > 1 && materialResidual < c.matTol) {
+    if (initResMag < c.solTol && relRes < c.solTol) conv = true;
+    else if (relRes < c.altTol) conv = true;
+    else if (initResMag < c.altTol) conv = true;
+  }
+  st->converged = conv ? 1 : 0;
+  st->nCorrDone += 1;
+  st->iCorr = iCorr + 1;
+  st->outerContinue = (!conv && iCorr + 1 < c.nCorr) ? 1 : 0;
+  if (st->status & kErrNaN) st->outerContinue = 0;
+}
+
+// TL second half: law (with the enforceLinear decision of this corrector),
+// boundary stress and the next traction snGrad.
+__global__ void __launch_bounds__(kRowBlock)
+kPostLawTL(MeshView mv, Controls c, FieldPtrs f, const DevState* st) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= mv.nC) return;
+  const int el = st->enforceLinear;
+  T9 G = ldT(f.G, s);
+  T9 FL = ldT(f.FL0, s) + transposeT(G);
+  stT(f.FL, s, FL);
+  S6 sg;
+  if (el) {
+    S6 s0 = ldS(f.sig0, s);
+    sg = addI(s0 + (2.0 * c.mu) * devS(symmT(G)), c.K * trT(G));
+  } else {
+    sg = neoHookean(c, FL);
+  }
+  stS(f.sig, s, sg);
+  for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
+    T9 Gb = ldT(f.Gb, b);
+    T9 FLb = ldT(f.FL0b, b) + transposeT(Gb);
+    stT(f.FLb, b, FLb);
+    S6 sb;
+    if (el) sb = addI(ldS(f.sig0b, b) + (2.0 * c.mu) * devS(symmT(Gb)), c.K * trT(Gb));
+    else sb = neoHookean(c, FLb);
+    stS(f.sigb, b, sb);
+    if (mv.btype[b] == 1) {
+      T9 Fi = ldT(f.Finvb, b);
+      stV(f.g, b, tractionSnGrad(mv, c, b, sb, Gb, &Fi, el));
+    }
+  }
+}
+
+// --------------------------------------------------------------- RHS pass ---
+
+__global__ void __launch_bounds__(kRowBlock)
+kRhs(MeshView mv, Controls c, FieldPtrs f, double* __restrict__ x, double* __restrict__ r,
+     DevState* st, double* partials) {
+  __shared__ double smem[32 * 6];
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const double* U = f.D[st->dcur];
+  double part[6] = {0, 0, 0, 0, 0, 0};  // normFactor (3), sum|R| (3)
+  const int el = c.tl ? st->enforceLinear : 1;
+  if (s < mv.nC) {
+    const V3 Us = ldV(U, s);
+    const V3 Cs = ldV(mv.C, s);
+    const T9 Gs = ldT(f.G, s);
+    const S6 Ss = ldS(f.sig, s);
+    T9 Ts;
+    if (!el) Ts = f.J[s] * dotTT(ldT(f.Finv, s), fromS(Ss));
+    V3 R = {0, 0, 0}, MD = {0, 0, 0};
+    double sumA = 0;
+    for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) {
+      const int nb = mv.col[e];
+      const int fk = mv.fidx[e];
+      const bool own = fk >= 0;
+      const int fi = own ? fk : ~fk;
+      const V3 Un = ldV(U, nb);
+      const V3 Cn = ldV(mv.C, nb);
+      const T9 Gn = ldT(f.G, nb);
+      const S6 Sn = ldS(f.sig, nb);
+      const double w = mv.fw[fi];
+      const V3 S = ldV(mv.fS, fi);
+      const double cm = mv.fmagS[fi] * mv.fdelta[fi];
+      // owner-oriented quantities
+      const V3 dU = own ? Un - Us : Us - Un;
+      const V3 d = own ? Cn - Cs : Cs - Cn;
+      const T9 Gf = own ? w * Gs + (1.0 - w) * Gn : w * Gn + (1.0 - w) * Gs;
+      V3 sigFlux;
+      if (el) {
+        const S6 sf = own ? w * Ss + (1.0 - w) * Sn : w * Sn + (1.0 - w) * Ss;
+        sigFlux = dotVS(S, sf);
+      } else {
+        const T9 Tn = f.J[nb] * dotTT(ldT(f.Finv, nb), fromS(Sn));
+        const T9 Tf = own ? w * Ts + (1.0 - w) * Tn : w * Tn + (1.0 - w) * Ts;
+        sigFlux = dotVT(S, Tf);
+      }
+      // Rhie-Chow: gammaS |S| delta (dU - d.grad_f)
+      const V3 flux = sigFlux + (c.gammaS * cm) * (dU - dotVT(d, Gf));
+      const V3 mflux = (c.gamma * cm) * dU;
+      if (own) { R = R + flux; MD = MD - mflux; }
+      else { R = R - flux; MD = MD + mflux; }
+    }
+    for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
+      const V3 S = ldV(mv.bS, b);
+      const S6 sb = ldS(f.sigb, b);
+      if (el) {
+        R = R + dotVS(S, sb);
+      } else {
+        T9 tb = f.Jb[b] * dotTT(ldT(f.Finvb, b), fromS(sb));
+        R = R + dotVT(S, tb);
+      }
+      if (mv.btype[b] == 0) {
+        double a = c.gamma * mv.bmagS[b] * mv.bdelta[b];
+        MD = MD + a * Us;
+        sumA += a;
+      }
+    }
+    stV(r, s, R);
+    stV(x, s, V3{0, 0, 0});
+    const double xb[3] = {st->xbar[0], st->xbar[1], st->xbar[2]};
+    const double md[3] = {MD.x, MD.y, MD.z}, rr[3] = {R.x, R.y, R.z};
+    for (int k = 0; k < 3; ++k) {
+      double t = sumA * xb[k];
+      part[k] = fabs(md[k] - t) + fabs(md[k] + rr[k] - t);
+      part[3 + k] = fabs(rr[k]);
+    }
+  }
+  blockSum<6>(part, smem);
+  if (threadIdx.x == 0) {
+    double* p = partials + 8 * (size_t)blockIdx.x;
+    for (int k = 0; k < 6; ++k) p[k] = part[k];
+  }
+  if (!lastBlockDone(&st->counter[1], gridDim.x)) return;
+  double S[6];
+  reducePartials<6>(partials, 8, gridDim.x, S, smem);
+  if (threadIdx.x != 0) return;
+  st->counter[1] = 0;
+  int any = 0;
+  for (int k = 0; k < 3; ++k) {
+    double nf = S[k] + 1e-20;
+    st->normFactor[k] = nf;
+    st->initRes[k] = S[3 + k] / nf;
+    st->finalRes[k] = st->initRes[k];
+    st->nIter[k] = 0;
+    st->active[k] = (st->initRes[k] < c.tol) ? 0 : 1;
+    st->wArA[k] = 1e20;
+    any |= st->active[k];
+  }
+  st->pcgContinue = (any && c.maxIter > 0) ? 1 : 0;
+}
+
+__global__ void kGather(int n, int width, const int* c2s, const double* in, double* out) {
+  long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
+  if (i >= (long)n * width) return;
+  int c = (int)(i / width), k = (int)(i % width);
+  out[i] = in[(long)c2s[c] * width + k];
+}
+
+// New load increment: D.oldTime = D, gradD.oldTime = gradD, F.oldTime = F,
+// sigma.oldTime = sigma (OpenFOAM stores old-time values when time advances).
+__global__ void kTlShift(MeshView mv, FieldPtrs f, const DevState* st) {
+  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s < mv.nC) {
+    const double* U = f.D[st->dcur];
+    stV(f.D0, s, ldV(f.D0, s) + ldV(U, s));
+    stT(f.GD0, s, ldT(f.GD, s));
+    stT(f.FL0, s, ldT(f.FL, s));
+    stS(f.sig0, s, ldS(f.sig, s));
+  }
+}
+
+__global__ void kTlShiftB(MeshView mv, Controls c, FieldPtrs f) {
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= mv.nB) return;
+  // Only fixedDisplacement faces read D.oldTime on the boundary; at the end of
+  // an increment their total displacement is the prescribed value.
+  if (mv.btype[b] == 0) stV(f.D0b, b, c.loadFactor * ldV(mv.bval, b));
+  stT(f.GD0b, b, ldT(f.GDb, b));
+  stT(f.FL0b, b, ldT(f.FLb, b));
+  stS(f.sig0b, b, ldS(f.sigb, b));
+}
+
+}  // namespace
+
+void launchGeometry(const MeshView& mv, const GeomInputs& in, const GeomOutputs& out,
+                    cudaStream_t s) {
+  const int B = kRowBlock;
+  kGeomCells<<<(mv.nC + B - 1) / B, B, 0, s>>>(mv, in, out);
+  if (mv.nI > 0) kGeomFaces<<<(mv.nI + B - 1) / B, B, 0, s>>>(mv, in, out);
+  double* bd = nullptr;
+  cudaMallocAsync(&bd, sizeof(double) * 3 * (size_t)(mv.nB > 0 ? mv.nB : 1), s);
+  if (mv.nB > 0) kGeomBFaces1<<<(mv.nB + B - 1) / B, B, 0, s>>>(mv, in, out, bd);
+  kGeomLs<<<(mv.nC + B - 1) / B, B, 0, s>>>(mv, out, bd);
+  cudaFreeAsync(bd, s);
+}
+
+void launchMatrix(const MeshView& mv, double gamma, double* val, double* diag, cudaStream_t s) {
+  kMatrix<<<(mv.nC + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, gamma, val, diag);
+}
+
+void launchTractionInit(const MeshView& mv, const Controls& c, const FieldPtrs& f,
+                        cudaStream_t s) {
+  if (mv.nB == 0) return;
+  kTractionInit<<<(mv.nB + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, c, f);
+}
+
+void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const double* x,
+                DevState* st, double* partials, int mode, cudaStream_t s) {
+  const int grid = (mv.nC + kRowBlock - 1) / kRowBlock;
+  kPost<<<grid, kRowBlock, 0, s>>>(mv, c, f, x, st, partials, mode);
+  if (c.tl && mode == 1) kPostLawTL<<<grid, kRowBlock, 0, s>>>(mv, c, f, st);
+}
+
+void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, double* x, double* r,
+               DevState* st, double* partials, cudaStream_t s) {
+  const int grid = (mv.nC + kRowBlock - 1) / kRowBlock;
+  kRhs<<<grid, kRowBlock, 0, s>>>(mv, c, f, x, r, st, partials);
+}
+
+void launchGather(int n, int width, const int* c2s, const double* in, double* out, cudaStream_t s) {
+  long tot = (long)n * width;
+  kGather<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, width, c2s, in, out);
+}
+
+void launchTlShift(const MeshView& mv, const Controls& c, const FieldPtrs& f, DevState* st,
+                   cudaStream_t s) {
+  kTlShift<<<(mv.nC + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, f, st);
+  if (mv.nB > 0) kTlShiftB<<<(mv.nB + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, c, f);
+}
+
+}  // namespace s4g

@@ -1,0 +1,222 @@
+"""Host-side mirror of the reference's solidModel / mechanicalLaw interface.
+
+A ``SolidModel`` is built from the same vocabulary as a solids4foam case:
+the ``solidModel`` type name of constant/solidProperties
+(``linearGeometryTotalDisplacement`` or ``nonLinearGeometryTotalLagrangian``),
+a ``mechanical`` law entry of constant/mechanicalProperties
+(``linearElastic`` with E/nu, ``neoHookeanElastic`` with E/nu or mu/K), the
+``0/D`` patch types ``fixedDisplacement`` / ``solidTraction`` (with traction
+and pressure), the ``solvers { "D|DD" {...} }`` entry of system/fvSolution and
+the ``<model>Coeffs`` keys of solidProperties.  ``evolve()`` runs the model's
+outer-corrector loop on the GPU through the C ABI (include/s4g.h), as
+solidModel::evolve does in the reference (solidModel.H:759).
+
+Errors raise S4GError, the counterpart of the reference's FatalError; a run
+that reaches nCorrectors without converging returns its result and sets
+``perf["converged"] = 0`` (the reference prints "Max iterations reached").
+"""
+from __future__ import annotations
+
+import ctypes as ct
+
+import numpy as np
+
+from . import _lib
+from .cases import PATCHES
+
+MODELS = {
+    "linearGeometryTotalDisplacement": _lib.LIN_GEOM_TOTAL_DISP,
+    "nonLinearGeometryTotalLagrangian": _lib.NONLIN_GEOM_TOTAL_LAG,
+}
+PRECONDITIONERS = {"DIC": _lib.PRECOND_DIC, "FDIC": _lib.PRECOND_DIC,
+                   "diagonal": _lib.PRECOND_DIAGONAL}
+RENUMBER = {"none": _lib.RENUMBER_NONE, "RCM": _lib.RENUMBER_RCM, "tiled": _lib.RENUMBER_TILED}
+
+
+class Context:
+    """One GPU (s4g_ctx)."""
+
+    def __init__(self, device: int = 0, verbose: bool = False):
+        self.L = _lib.lib()
+        h = ct.c_void_p()
+        opts = _lib.CtxOpts(device, 1 if verbose else 0)
+        _lib.check(self.L.s4g_ctx_create(ct.byref(h), ct.byref(opts)), "s4g_ctx_create")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.L.s4g_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def _desc(mesh, keep):
+    arrs = {}
+    for k, dt in (("owner", np.int32), ("neighbour", np.int32), ("C", np.float64),
+                  ("V", np.float64), ("Cf", np.float64), ("Sf", np.float64),
+                  ("patch_start", np.int32), ("patch_size", np.int32)):
+        arrs[k] = np.ascontiguousarray(mesh[k], dtype=dt)
+    keep.append(arrs)
+    d = _lib.MeshDesc()
+    d.n_cells = arrs["V"].shape[0]
+    d.n_faces = arrs["owner"].shape[0]
+    d.n_internal_faces = arrs["neighbour"].shape[0]
+    d.n_patches = arrs["patch_start"].shape[0]
+    for k, a in arrs.items():
+        setattr(d, k, a.ctypes.data)
+    return d
+
+
+class SolidModel:
+    """GPU drop-in for one solid region's outer-corrector loop."""
+
+    def __init__(self, ctx: Context, mesh, law: dict, bcs: dict, model: str =
+                 "linearGeometryTotalDisplacement", solver: dict | None = None,
+                 outer: dict | None = None, precision: str = "FP64", renumber: str = "tiled",
+                 part_size: int = 512, ls_boundary_delta: int = 0, dic_subdomains: bool = False):
+        if model not in MODELS:
+            raise ValueError(f"unknown solidModel {model!r}; valid: {list(MODELS)}")
+        self.ctx = ctx
+        self.L = ctx.L
+        self.model = model
+        self.mesh = mesh
+        self.n_cells = int(np.asarray(mesh["V"]).shape[0])
+        keep = []
+        d = _desc(mesh, keep)
+        opts = _lib.MeshOpts(RENUMBER[renumber], part_size, ls_boundary_delta,
+                             1 if dic_subdomains else 0)
+        h = ct.c_void_p()
+        _lib.check(self.L.s4g_mesh_upload(ctx.h, ct.byref(d), ct.byref(opts), ct.byref(h)),
+                   "s4g_mesh_upload")
+        self.h = h
+        self.set_law(law)
+        names = list(mesh.get("patch_names", PATCHES))
+        for name, spec in bcs.items():
+            self.set_bc(names.index(name), *spec)
+        self.set_controls(solver or {}, outer or {}, precision)
+
+    def close(self):
+        if self.h:
+            self.L.s4g_mesh_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- constant/mechanicalProperties
+    def set_law(self, law: dict):
+        t = law.get("type", "linearElastic")
+        if t not in ("linearElastic", "neoHookeanElastic"):
+            raise ValueError(f"unknown mechanical law {t!r}")
+        use_muK = "mu" in law and "K" in law
+        lw = _lib.Law(_lib.LINEAR_ELASTIC if t == "linearElastic" else _lib.NEO_HOOKEAN,
+                      1 if use_muK else 0, float(law.get("E", 0.0)), float(law.get("nu", 0.0)),
+                      float(law.get("mu", 0.0)), float(law.get("K", 0.0)),
+                      float(law.get("rho", 1000.0)))
+        _lib.check(self.L.s4g_material_set(self.h, ct.byref(lw)), "s4g_material_set")
+
+    # -- 0/D boundaryField
+    def set_bc(self, patch: int, bc_type: str, value=None, pressure=None):
+        t = {"fixedDisplacement": _lib.FIXED_DISPLACEMENT,
+             "solidTraction": _lib.SOLID_TRACTION,
+             "solidTractionFree": _lib.SOLID_TRACTION}[bc_type]
+        size = int(self.mesh["patch_size"][patch])
+        v = None if value is None else np.ascontiguousarray(
+            np.broadcast_to(np.asarray(value, dtype=np.float64), (size, 3)))
+        p = None if pressure is None else np.ascontiguousarray(
+            np.broadcast_to(np.asarray(pressure, dtype=np.float64), (size,)))
+        _lib.check(self.L.s4g_bc_set(self.h, patch, t, None if v is None else v.ctypes.data,
+                                     None if p is None else p.ctypes.data), "s4g_bc_set")
+
+    # -- system/fvSolution and solidProperties <model>Coeffs
+    def set_controls(self, solver: dict, outer: dict, precision: str = "FP64"):
+        lin, out = _lib.LinSolver(), _lib.Outer()
+        self.L.s4g_default_controls(ct.byref(lin), ct.byref(out))
+        if "preconditioner" in solver:
+            lin.preconditioner = PRECONDITIONERS[solver["preconditioner"]]
+        lin.tolerance = solver.get("tolerance", lin.tolerance)
+        lin.rel_tol = solver.get("relTol", lin.rel_tol)
+        lin.max_iter = solver.get("maxIter", lin.max_iter)
+        out.n_correctors = outer.get("nCorrectors", out.n_correctors)
+        out.solution_tol = outer.get("solutionTolerance", out.solution_tol)
+        out.alternative_tol = outer.get("alternativeTolerance", out.alternative_tol)
+        out.material_tol = outer.get("materialTolerance", out.material_tol)
+        out.info_frequency = outer.get("infoFrequency", out.info_frequency)
+        stab = outer.get("stabilisation", {"type": "RhieChow", "scaleFactor": 0.1})
+        if stab.get("type", "RhieChow") != "RhieChow":
+            raise ValueError("only RhieChow stabilisation is built")
+        out.stab_scale = stab.get("scaleFactor", 0.1)
+        prec = {"FP64": _lib.FP64, "FP32_REFINE": _lib.FP32_REFINE}[precision]
+        _lib.check(self.L.s4g_solver_set(self.h, ct.byref(lin), ct.byref(out), prec),
+                   "s4g_solver_set")
+
+    def evolve(self, n_increments: int = 1):
+        """Runs the outer-corrector loop; returns (D [n,3], sigma [n,6], perf)."""
+        D = np.zeros((self.n_cells, 3))
+        sig = np.zeros((self.n_cells, 6))
+        perf = _lib.Perf()
+        st = self.L.s4g_solve(self.h, MODELS[self.model], int(n_increments), D.ctypes.data,
+                              sig.ctypes.data, ct.byref(perf))
+        _lib.check(st, "s4g_solve", allow=(_lib.OK, _lib.NOT_CONVERGED))
+        return D, sig, perf.as_dict()
+
+    def gradD(self):
+        G = np.zeros((self.n_cells, 9))
+        _lib.check(self.L.s4g_get_gradD(self.h, G.ctypes.data), "s4g_get_gradD")
+        return G
+
+    def permutation(self):
+        perm = np.zeros(self.n_cells, np.int32)
+        _lib.check(self.L.s4g_mesh_get_permutation(self.h, perm.ctypes.data),
+                   "s4g_mesh_get_permutation")
+        return perm
+
+    def info(self):
+        inf = _lib.MeshInfo()
+        _lib.check(self.L.s4g_mesh_get_info(self.h, ct.byref(inf)), "s4g_mesh_get_info")
+        return {f[0]: getattr(inf, f[0]) for f in inf._fields_}
+
+    # operator-level access (parity tests)
+    def op_matrix(self):
+        diag = np.zeros(self.n_cells)
+        upper = np.zeros(int(np.asarray(self.mesh["neighbour"]).shape[0]))
+        _lib.check(self.L.s4g_op_matrix(self.h, diag.ctypes.data, upper.ctypes.data),
+                   "s4g_op_matrix")
+        return diag, upper
+
+    def op_amul(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        k = 1 if x.ndim == 1 else x.shape[1]
+        y = np.zeros_like(x)
+        _lib.check(self.L.s4g_op_amul(self.h, k, x.ctypes.data, y.ctypes.data), "s4g_op_amul")
+        return y
+
+    def op_precondition(self, r):
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        k = 1 if r.ndim == 1 else r.shape[1]
+        w = np.zeros_like(r)
+        _lib.check(self.L.s4g_op_precondition(self.h, k, r.ctypes.data, w.ctypes.data),
+                   "s4g_op_precondition")
+        return w
+
+
+def plan(mesh, renumber: str = "tiled", part_size: int = 512, dic_subdomains: bool = False):
+    """Host-only DIC order and scheduling figures (no GPU): (perm, info)."""
+    L = _lib.lib()
+    keep = []
+    d = _desc(mesh, keep)
+    opts = _lib.MeshOpts(RENUMBER[renumber], part_size, 0, 1 if dic_subdomains else 0)
+    n = d.n_cells
+    perm = np.zeros(n, np.int32)
+    inf = _lib.MeshInfo()
+    _lib.check(L.s4g_mesh_plan(ct.byref(d), ct.byref(opts), perm.ctypes.data, ct.byref(inf)),
+               "s4g_mesh_plan")
+    return perm, {f[0]: getattr(inf, f[0]) for f in inf._fields_}
