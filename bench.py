@@ -1,0 +1,354 @@
+#!/usr/bin/env python
+"""Benchmark of the segregated finite-volume solid solve on GB300.
+
+One step is one full solve of the plain-FP64 benchmark case: the 128^3
+jittered unit cube (2,097,152 hex cells, interior vertices jittered +-0.2 h,
+seed 1), linear elastic E = 70 GPa, nu = 0.33, bottom fixed, top pressure
+10 MPa, sides traction-free, linearGeometryTotalDisplacement with PCG+DIC
+(tol 1e-9, relTol 0.1) and outer tolerance 1e-6 / 2000 correctors -- run to
+convergence through the library's public API.  Inputs are synthetic
+(generated from the seed), the working set (about 1.7 GB) is far larger than
+L2, so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+                  [--precision FP64|FP32_REFINE] [--n 128] [--dic exact|decomposed]
+
+--impl reference times the CPU FP64 oracle (the restatement of the
+reference's solve; the reference itself needs an OpenFOAM installation that
+is not available) on all host cores over a bounded sample of correctors of
+the same case and reports the same metric, scaled to a full solve.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("solves/s + p50/p99 latency (FP32+refine batched vs plain FP64), 1 GB300, "
+          "err≤1e-6")
+# Correctors the 128^3 benchmark case takes to converge (solutionTolerance
+# 1e-6), measured with the GPU path; the CPU sample is scaled to a full solve
+# with it when the GPU run is not in the same process.
+FULL_SOLVE_CORRECTORS_128 = None
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_bytes(kind, n_cells, n_faces, n_bfaces, v):
+    """Minimal DRAM bytes of one launch of a kernel kind (k = 3 columns,
+    v = value bytes, 4-byte indices); the formulas follow the solve's
+    scope table: SpMV nnz(v+i) + 4(N+1) + 2Nvk; one DIC sweep
+    nnz_L(v+i) + 4(N+1) + Nv + 2Nvk (+ Nvk for the backward w.r sums)."""
+    N, F, B, k = n_cells, n_faces, n_bfaces, 3
+    nnz_l = F
+    if kind == "sweep_fwd":
+        return nnz_l * (v + 4) + 4 * (N + 1) + N * v + 2 * N * v * k
+    if kind == "sweep_bwd":
+        return nnz_l * (v + 4) + 4 * (N + 1) + N * v + 3 * N * v * k
+    if kind == "spmv":
+        return 2 * F * (v + 4) + N * v + 4 * (N + 1) + 2 * N * v * k
+    if kind == "update":
+        return 5 * N * v * k          # read x, p, q, r; write x, r (x, r in place)
+    if kind == "p_update":
+        return 3 * N * v * k
+    if kind == "rhs":                  # FP64 fields: D, grad, sigma, face data, r, x
+        return N * 8 * (3 + 9 + 6 + 3) + F * 8 * 6 + 2 * F * 8 + N * v * 6 + B * 8 * 10
+    if kind == "post":
+        return N * 8 * (3 + 3 + 6 + 9 + 6) + 2 * F * 4 + N * v * 3 + B * 8 * 30
+    return None
+
+
+def load_traffic(workload):
+    """Per-launch DRAM traffic from the committed ncu summary, if it covers
+    this workload: lines '<kind> <bytes_per_launch> <workload>'."""
+    path = os.path.join(ROOT, "profiles", "kernel_traffic.txt")
+    out = {}
+    try:
+        with open(path) as f:
+            for ln in f:
+                parts = ln.split()
+                if len(parts) >= 3 and not ln.startswith("#") and parts[2] == workload:
+                    out[parts[0]] = float(parts[1])
+    except OSError:
+        pass
+    return out
+
+
+def build_case(n):
+    from solids4foam_gb300.cases import cube_case
+    return cube_case(n)
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as td
+        td.init_process_group("gloo")
+        dist = td
+    return world, rank, local, dist
+
+
+def barrier(dist):
+    if dist:
+        dist.barrier()
+
+
+def allmax(dist, x):
+    if not dist:
+        return x
+    import torch
+    t = torch.tensor([float(x)])
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(case, n_correctors_full, sample_s=20.0, threads=None):
+    """Times the CPU oracle on the first correctors of the case with all host
+    threads; returns (solves/s scaled to a full solve, details)."""
+    from oracle import pyoracle
+    from solids4foam_gb300.cases import oracle_bcs
+    threads = threads or os.cpu_count() or 1
+    bcs = oracle_bcs(case["mesh"], case["bcs"])
+    law = case["law"]
+    # first a 1-corrector probe to size the sample
+    _, _, _, p1 = pyoracle.solve(case["mesh"], bcs, E=law["E"], nu=law["nu"], n_threads=threads,
+                                 max_correctors_run=1, n_correctors=2000)
+    per = max(p1["seconds"], 1e-3)
+    m = max(2, min(400, int(sample_s / per)))
+    _, _, _, pm = pyoracle.solve(case["mesh"], bcs, E=law["E"], nu=law["nu"], n_threads=threads,
+                                 max_correctors_run=m, n_correctors=2000)
+    per_corr = pm["seconds"] / pm["n_correctors"]
+    full = n_correctors_full or pm["n_correctors"]
+    est = per_corr * full
+    return 1.0 / est, {
+        "cores": threads,
+        "sample": (f"first {pm['n_correctors']} correctors of the same case "
+                   f"({pm['seconds']:.1f} s, {pm['total_lin_iters']} PCG iterations, "
+                   f"DIC restricted to {threads} thread subdomains), scaled to {full} correctors"),
+        "seconds_per_corrector": per_corr,
+    }
+
+
+def run_reference(args):
+    world, rank, local, dist = dist_init()
+    if rank != 0:
+        return
+    case = build_case(args.n)
+    full = args.full_correctors or FULL_SOLVE_CORRECTORS_128
+    vals = []
+    info = None
+    for i in range(args.warmup + args.steps):
+        v, info = cpu_sample(case, full, sample_s=args.cpu_sample_s)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"cube{args.n}_jittered_linear_elastic_pcg_dic",
+                   "cells": args.n ** 3, "model": "linearGeometryTotalDisplacement",
+                   "note": "CPU FP64 oracle (restatement of the reference solve); the "
+                           "reference itself needs OpenFOAM, which is not installed"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": info["cores"],
+                         "kind": "port", "sample": info["sample"]},
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args):
+    import solids4foam_gb300 as sg
+    world, rank, local, dist = dist_init()
+    case = build_case(args.n)
+    mesh = case["mesh"]
+    ctx = sg.Context(local, profile=True)
+    kw = dict(solver=case["solver"], outer=case["outer"], precision=args.precision,
+              dic_subdomains=(args.dic == "decomposed"))
+    model = sg.SolidModel(ctx, mesh, case["law"], case["bcs"], **kw)
+    for _ in range(args.warmup):
+        model.evolve()
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(dist)
+    perfs = []
+    for _ in range(args.steps):
+        D, sig, perf = model.evolve()
+        perfs.append(perf)
+    barrier(dist)
+    clocks = sampler.stop()
+    ms = [p["solve_ms"] for p in perfs]
+    ms_step = allmax(dist, statistics.mean(ms))
+    value = world * 1000.0 / ms_step
+
+    # end to end through the C ABI with host buffers: upload, solve, download
+    e2e_ms = []
+    h2d = sum(np.asarray(mesh[k]).nbytes for k in ("owner", "neighbour", "C", "V", "Cf", "Sf",
+                                                     "patch_start", "patch_size"))
+    h2d += sum(np.asarray(v).nbytes for _, v, p in case["bcs"].values() if v is not None)
+    h2d += sum(np.asarray(p).nbytes for _, v, p in case["bcs"].values() if p is not None)
+    d2h = mesh["V"].shape[0] * 8 * (3 + 6)
+    for _ in range(args.e2e_steps):
+        barrier(dist)
+        t0 = time.perf_counter()
+        m2 = sg.SolidModel(ctx, mesh, case["law"], case["bcs"], **kw)
+        m2.evolve()
+        m2.close()
+        e2e_ms.append(1000.0 * (time.perf_counter() - t0))
+    e2e_step = allmax(dist, statistics.mean(e2e_ms)) if e2e_ms else None
+
+    # roofline of the dominant kernel (CUDA events on the library's stream)
+    v = 8 if args.precision == "FP64" else 4
+    nC, nI = mesh["V"].shape[0], mesh["neighbour"].shape[0]
+    nB = mesh["owner"].shape[0] - nI
+    tot_ms = {k: sum(p["kernel_ms"][k] for p in perfs) for k in perfs[0]["kernel_ms"]}
+    tot_n = {k: sum(p["kernel_launches_by"][k] for p in perfs) for k in perfs[0]["kernel_ms"]}
+    dom = max(tot_ms, key=lambda k: tot_ms[k])
+    peak, peak_kind = peaks()
+    avg_ms = tot_ms[dom] / max(1, tot_n[dom])
+    ab = algorithmic_bytes(dom, nC, nI, nB, v)
+    achieved = ab / (avg_ms * 1e-3) / 1e9 if ab else None
+    workload = f"cube{args.n}_{args.precision.lower()}_{args.dic}"
+    traffic = load_traffic(workload).get(dom)
+    kernels = {k: {"launches": tot_n[k], "ms_total": round(tot_ms[k], 3),
+                   "share": round(tot_ms[k] / max(1e-9, sum(tot_ms.values())), 4),
+                   "avg_us": round(1000 * tot_ms[k] / max(1, tot_n[k]), 2),
+                   "gbs": (round(algorithmic_bytes(k, nC, nI, nB, v) /
+                                 (tot_ms[k] / max(1, tot_n[k]) * 1e-3) / 1e9, 1)
+                           if tot_n[k] and algorithmic_bytes(k, nC, nI, nB, v) else None)}
+               for k in tot_ms if tot_n[k]}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cv, info = cpu_sample(case, perfs[0]["n_correctors"], sample_s=args.cpu_sample_s)
+        cpu = {"value": cv, "unit": "solves/s", "cores": info["cores"], "kind": "port",
+               "sample": info["sample"]}
+    if rank != 0:
+        return
+    p0 = perfs[0]
+    line = {
+        "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "FP64" else "f32+f64",
+        "data": "synthetic",
+        "config": {"workload": workload, "cells": nC, "internal_faces": nI,
+                   "model": "linearGeometryTotalDisplacement", "law": "linearElastic",
+                   "solver": "PCG+DIC tol 1e-9 relTol 0.1", "outer": "solutionTolerance 1e-6, "
+                   "nCorrectors 2000", "precision": args.precision, "dic": args.dic,
+                   "parallelism": f"replicas{world}",
+                   "l2": "working set ~1.7 GB >> 129 MB L2 (no flush needed)",
+                   "n_correctors": p0["n_correctors"], "converged": p0["converged"],
+                   "pcg_iterations": p0["total_lin_iters"]},
+        "e2e": {"value": (world * 1000.0 / e2e_step) if e2e_step else None, "unit": "solves/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(sum(p["kernel_launches"] for p in perfs)),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes_per_launch": ab, "avg_launch_us": avg_ms * 1000},
+        "kernels": kernels,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="FP64", choices=["FP64", "FP32_REFINE"])
+    ap.add_argument("--dic", default="exact", choices=["exact", "decomposed"])
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--cpu-sample-s", type=float, default=20.0)
+    ap.add_argument("--full-correctors", type=int, default=0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

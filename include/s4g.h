@@ -66,7 +66,22 @@ typedef struct s4g_ctx_opts {
   int device;   /* CUDA device ordinal */
   int verbose;  /* 1: print the reference's residual table every
                    infoFrequency correctors */
+  int profile;  /* 1: time every kernel kind with CUDA events on the
+                   library's stream (s4g_perf.kernel_ms / kernel_launches_by) */
 } s4g_ctx_opts;
+
+/* Kernel kinds of the per-kernel timers. */
+enum {
+  S4G_K_RHS = 0,       /* right-hand side: div(sigma), Rhie-Chow, BC terms */
+  S4G_K_POST = 1,      /* post-solve: gradient, law, boundary, convergence */
+  S4G_K_SWEEP_FWD = 2, /* DIC forward substitution */
+  S4G_K_SWEEP_BWD = 3, /* DIC backward substitution */
+  S4G_K_DIAG = 4,      /* diagonal preconditioner */
+  S4G_K_PUPDATE = 5,   /* p = w + beta p */
+  S4G_K_SPMV = 6,      /* q = A p */
+  S4G_K_UPDATE = 7,    /* x, r update and residual */
+  S4G_K_KINDS = 8
+};
 
 /* Creates a context on one GPU.  Stands in for the per-run state the
  * reference keeps in the OpenFOAM Time/objectRegistry
@@ -140,6 +155,10 @@ s4g_status s4g_mesh_plan(const s4g_mesh_desc* desc, const s4g_mesh_opts* opts,
                          int* perm_out, s4g_mesh_info* info);
 /* perm[i] = caller cell of solver cell i (the DIC order). */
 s4g_status s4g_mesh_get_permutation(const s4g_mesh* mesh, int* perm);
+/* part_of_cell [n_cells] (caller order): the scheduling part of each cell;
+ * with dic_subdomains these are the DIC subdomains (the counterpart of a
+ * decomposePar cell decomposition). */
+s4g_status s4g_mesh_get_parts(const s4g_mesh* mesh, int* part_of_cell);
 s4g_status s4g_mesh_get_info(const s4g_mesh* mesh, s4g_mesh_info* info);
 s4g_status s4g_mesh_destroy(s4g_mesh* mesh);
 
@@ -236,6 +255,10 @@ typedef struct s4g_perf {
   long long kernel_launches;  /* kernels launched by the library */
   int enforce_linear;         /* TL: linear geometry was enforced */
   int device_status;          /* raw device status word (0 = clean) */
+  /* per kernel kind (S4G_K_*), only with s4g_ctx_opts.profile: summed
+   * CUDA-event time and number of launches that did work */
+  double kernel_ms[S4G_K_KINDS];
+  long long kernel_launches_by[S4G_K_KINDS];
 } s4g_perf;
 
 /* Runs the solid model's evolve() for n_increments load increments (1 for

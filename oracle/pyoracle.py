@@ -54,6 +54,7 @@ class Settings(ct.Structure):
         ("material_tol", ct.c_double), ("stab_scale", ct.c_double),
         ("ls_boundary_delta", ct.c_int), ("n_increments", ct.c_int),
         ("n_threads", ct.c_int), ("max_correctors_run", ct.c_int),
+        ("dic_domain", ct.c_void_p),
     ]
 
 
@@ -139,10 +140,15 @@ def default_settings(**kw) -> Settings:
     return s
 
 
-def solve(mesh, bcs, settings: Settings | None = None, perm=None, **kw):
-    """Full oracle solve.  Returns (D [n,3], sigma [n,6], gradD [n,9], perf dict)."""
+def solve(mesh, bcs, settings: Settings | None = None, perm=None, dic_domain=None, **kw):
+    """Full oracle solve.  Returns (D [n,3], sigma [n,6], gradD [n,9], perf dict).
+    dic_domain (optional, caller cell order): DIC restricted to subdomains."""
     s = settings if settings is not None else default_settings(**kw)
     keep = []
+    if dic_domain is not None:
+        dd = np.ascontiguousarray(dic_domain, dtype=np.int32)
+        keep.append(dd)
+        s.dic_domain = dd.ctypes.data
     d = _desc(mesh, keep)
     b = _bcs(bcs, mesh, keep)
     n = d.n_cells

@@ -174,6 +174,7 @@ struct Mesh {
 
   // cell -> internal faces (increasing face index), cell -> boundary faces
   std::vector<int> cfStart, cfFace, cbStart, cbFace;
+  std::vector<int> newOfCaller;  // caller cell -> solver cell
 
   bool build(const orc_mesh_desc* d, const int* perm, int lsBoundaryDelta);
 };
@@ -192,6 +193,7 @@ bool Mesh::build(const orc_mesh_desc* d, const int* perm, int lsBoundaryDelta) {
   } else {
     std::iota(newOf.begin(), newOf.end(), 0);
   }
+  newOfCaller = newOf;
   C.resize(nC); V.resize(nC);
   for (int c = 0; c < nC; ++c) {
     C[newOf[c]] = getV(d->C, c);
@@ -324,17 +326,19 @@ void amul(const Mesh& m, const Ldu& A, const double* x, double* y, int nt) {
   }
 }
 
-// DIC preconditioner (OpenFOAM DICPreconditioner semantics).  With nt > 1
-// the factor and the sweeps ignore faces that couple different thread
-// subdomains (processor-local DIC, as in a decomposed run).
+// DIC preconditioner (OpenFOAM DICPreconditioner semantics).  The factor and
+// the sweeps ignore faces that couple different subdomains (processor-local
+// DIC, as in a decomposed run): the thread subdomains with nt > 1, or the
+// caller's cell-to-subdomain map when one is given.
 struct Dic {
   std::vector<double> rD;
   std::vector<int> dom;  // subdomain of each cell
   int nd = 1;
-  void build(const Mesh& m, const Ldu& A, int nt) {
+  void build(const Mesh& m, const Ldu& A, int nt, const std::vector<int>* domain = nullptr) {
     nd = std::max(1, nt);
     dom.resize(m.nC);
     for (int c = 0; c < m.nC; ++c) dom[c] = (int)((long long)c * nd / m.nC);
+    if (domain) dom = *domain;
     rD = A.diag;
     // calcReciprocalD: rD[u] -= upper^2/rD[l] over faces in order
     for (int u = 0; u < m.nC; ++u)
@@ -347,14 +351,14 @@ struct Dic {
     for (int c = 0; c < m.nC; ++c) rD[c] = 1.0 / rD[c];
   }
   void apply(const Mesh& m, const Ldu& A, const double* r, double* wv) const {
-    auto sweep = [&](int d, int c0, int c1) {
+    auto sweep = [&](int, int c0, int c1) {
       for (int u = c0; u < c1; ++u) {
         double v = rD[u] * r[u];
         for (int e = m.cfStart[u]; e < m.cfStart[u + 1]; ++e) {
           int f = m.cfFace[e];
           if (m.nei[f] != u) continue;
           int l = m.own[f];
-          if (dom[l] != d) continue;
+          if (dom[l] != dom[u]) continue;
           v -= rD[u] * A.upper[f] * wv[l];
         }
         wv[u] = v;
@@ -365,7 +369,7 @@ struct Dic {
           int f = m.cfFace[e];
           if (m.own[f] != l) continue;
           int u = m.nei[f];
-          if (dom[u] != d) continue;
+          if (dom[u] != dom[l]) continue;
           v -= rD[l] * A.upper[f] * wv[u];
         }
         wv[l] = v;
@@ -529,7 +533,15 @@ struct Solver {
       sig0 = sig; sig0b = sigb;
     }
     assembleMatrix();
-    if (s.preconditioner == ORC_DIC) dic.build(m, A, nt);
+    if (s.preconditioner == ORC_DIC) {
+      if (s.dic_domain) {
+        std::vector<int> dom(m.nC);
+        for (int c = 0; c < m.nC; ++c) dom[m.newOfCaller[c]] = s.dic_domain[c];
+        dic.build(m, A, 1, &dom);
+      } else {
+        dic.build(m, A, nt);
+      }
+    }
   }
 
   int patchType(int b) const { return bcs[m.patchOfB[b]].type; }

@@ -65,6 +65,8 @@ typedef struct {
   int n_increments;       /* load increments (time steps), loads ramp linearly */
   int n_threads;          /* >1: OpenMP, DIC restricted to thread subdomains */
   int max_correctors_run; /* >0: stop after this many correctors (timing samples) */
+  const int* dic_domain;  /* optional [n_cells] subdomain of each cell (caller
+                             order): DIC restricted to each subdomain */
 } orc_settings;
 
 typedef struct {

@@ -24,7 +24,11 @@ LIN_GEOM_TOTAL_DISP, NONLIN_GEOM_TOTAL_LAG = 0, 1
 
 
 class CtxOpts(ct.Structure):
-    _fields_ = [("device", ct.c_int), ("verbose", ct.c_int)]
+    _fields_ = [("device", ct.c_int), ("verbose", ct.c_int), ("profile", ct.c_int)]
+
+
+# kernel kinds of the per-kernel timers (S4G_K_*)
+KERNEL_KINDS = ("rhs", "post", "sweep_fwd", "sweep_bwd", "diag", "p_update", "spmv", "update")
 
 
 class MeshDesc(ct.Structure):
@@ -73,10 +77,14 @@ class Perf(ct.Structure):
         ("solve_ms", ct.c_double), ("h2d_ms", ct.c_double), ("d2h_ms", ct.c_double),
         ("kernel_launches", ct.c_longlong), ("enforce_linear", ct.c_int),
         ("device_status", ct.c_int),
+        ("kernel_ms", ct.c_double * 8), ("kernel_launches_by", ct.c_longlong * 8),
     ]
 
     def as_dict(self):
-        return {f[0]: getattr(self, f[0]) for f in self._fields_}
+        d = {f[0]: getattr(self, f[0]) for f in self._fields_[:-2]}
+        d["kernel_ms"] = dict(zip(KERNEL_KINDS, list(self.kernel_ms)))
+        d["kernel_launches_by"] = dict(zip(KERNEL_KINDS, list(self.kernel_launches_by)))
+        return d
 
 
 # every symbol declared in include/s4g.h, with its ctypes signature
@@ -91,6 +99,7 @@ _SIGS = {
     "s4g_mesh_plan": (ct.c_int, [ct.POINTER(MeshDesc), ct.POINTER(MeshOpts), ct.c_void_p,
                                  ct.POINTER(MeshInfo)]),
     "s4g_mesh_get_permutation": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "s4g_mesh_get_parts": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "s4g_mesh_get_info": (ct.c_int, [ct.c_void_p, ct.POINTER(MeshInfo)]),
     "s4g_mesh_destroy": (ct.c_int, [ct.c_void_p]),
     "s4g_material_set": (ct.c_int, [ct.c_void_p, ct.POINTER(Law)]),

@@ -32,7 +32,8 @@ struct MeshView {
   // shared-memory staging of the sweeps (see HostPrep)
   const int* haloFPtr; const int* haloFIdx; const int* haloBPtr; const int* haloBIdx;
   const int* slot;
-  int maxRows, maxHalo, maxEntries;
+  const int* lowCnt;   // lower entries per row
+  int maxRows, maxHalo, maxEntries, maxLevels;
 };
 
 // Material and solver constants of a solve.
@@ -85,6 +86,12 @@ __device__ __forceinline__ unsigned ldAcquire(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ unsigned ldRelaxed(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void fenceAcqRel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ void stRelease(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -95,6 +102,15 @@ struct T9 { double xx, xy, xz, yx, yy, yz, zx, zy, zz; };
 struct S6 { double xx, xy, xz, yy, yz, zz; };
 
 __device__ __forceinline__ V3 ldV(const double* a, long i) { return {a[3 * i], a[3 * i + 1], a[3 * i + 2]}; }
+// vectors of the PCG value type (double or float) as FP64
+template <typename T>
+__device__ __forceinline__ V3 ldVT(const T* a, long i) {
+  return {(double)a[3 * i], (double)a[3 * i + 1], (double)a[3 * i + 2]};
+}
+template <typename T>
+__device__ __forceinline__ void stVT(T* a, long i, V3 v) {
+  a[3 * i] = (T)v.x; a[3 * i + 1] = (T)v.y; a[3 * i + 2] = (T)v.z;
+}
 __device__ __forceinline__ void stV(double* a, long i, V3 v) { a[3 * i] = v.x; a[3 * i + 1] = v.y; a[3 * i + 2] = v.z; }
 __device__ __forceinline__ T9 ldT(const double* a, long i) {
   const double* p = a + 9 * i;

@@ -43,8 +43,59 @@ static s4g_status setErr(s4g_status st, const std::string& msg) {
 struct Ctx {
   int device = 0;
   int verbose = 0;
+  int profile = 0;
   int numSMs = 0;
   cudaStream_t stream = nullptr;
+};
+
+// CUDA-event timer of each kernel kind on the library's stream.  Events are
+// resolved after the host waits on the stream anyway (between launch batches).
+struct EventTimer : LaunchTimer {
+  struct Pending { int kind; cudaEvent_t a, b; };
+  std::vector<cudaEvent_t> pool;
+  std::vector<Pending> pending;
+  cudaEvent_t open = nullptr;
+  double ms[S4G_K_KINDS] = {};
+  long long count[S4G_K_KINDS] = {};
+  ~EventTimer() {
+    for (auto& p : pending) { cudaEventDestroy(p.a); cudaEventDestroy(p.b); }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+  cudaEvent_t get() {
+    if (pool.empty()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      return e;
+    }
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  void before(int, cudaStream_t s) override {
+    open = get();
+    cudaEventRecord(open, s);
+  }
+  void after(int kind, cudaStream_t s) override {
+    cudaEvent_t b = get();
+    cudaEventRecord(b, s);
+    pending.push_back({kind, open, b});
+  }
+  void resolve() {
+    for (auto& p : pending) {
+      float t = 0;
+      if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) {
+        ms[p.kind] += t;
+        count[p.kind] += 1;
+      }
+      pool.push_back(p.a);
+      pool.push_back(p.b);
+    }
+    pending.clear();
+  }
+  void reset() {
+    resolve();
+    for (int k = 0; k < S4G_K_KINDS; ++k) { ms[k] = 0; count[k] = 0; }
+  }
 };
 
 struct Engine {
@@ -69,8 +120,13 @@ struct Engine {
   double* dVal = nullptr;
   double* dDiag = nullptr;
   double* dRD = nullptr;
+  double* dRDa = nullptr;
   FieldPtrs f{};
-  PcgPtrs pc{};
+  PcgPtrs<double> pc{};    // plain FP64 inner solve
+  PcgPtrs<float> pc32{};   // FP32 inner solve of the mixed-precision path
+  bool fp32Allocated = false;
+  bool fp32Valid = false;  // FP32 copies match the FP64 matrix/factor
+  int sweepGrid32 = 1;
   DevState* dState = nullptr;
   DevState* hState = nullptr;  // pinned
   double* dPartials = nullptr;
@@ -88,6 +144,8 @@ struct Engine {
   int sweepGrid = 1;
   int lastModel = -1;
   long long launches = 0;
+  EventTimer timer;
+  LaunchTimer* tm() { return ctx->profile ? &timer : nullptr; }
 
   ~Engine() {
     for (void* p : allocs) cudaFree(p);
@@ -180,7 +238,9 @@ struct Engine {
     mv.partStart = dPartStart; mv.lvlOff = dLvlOff; mv.lvlStart = dLvlStart;
     mv.upPtr = dUpPtr; mv.upIdx = dUpIdx; mv.dnPtr = dDnPtr; mv.dnIdx = dDnIdx;
     {
-      int *dHfp, *dHfi, *dHbp, *dHbi, *dSlot;
+      int *dHfp, *dHfi, *dHbp, *dHbi, *dSlot, *dLow;
+      S4G_TRY(upload(&dLow, hp.lowCnt));
+      mv.lowCnt = dLow;
       S4G_TRY(upload(&dHfp, hp.haloFPtr));
       S4G_TRY(upload(&dHfi, hp.haloFIdx));
       S4G_TRY(upload(&dHbp, hp.haloBPtr));
@@ -189,6 +249,7 @@ struct Engine {
       mv.haloFPtr = dHfp; mv.haloFIdx = dHfi; mv.haloBPtr = dHbp; mv.haloBIdx = dHbi;
       mv.slot = dSlot;
       mv.maxRows = hp.maxRows; mv.maxHalo = hp.maxHalo; mv.maxEntries = hp.maxEntries;
+      mv.maxLevels = hp.maxLocalLevels;
     }
 
     GeomInputs gi{dCc, dCfc, dSfc, dS2c, dFcaller, dFflip, dBcaller, dBcell,
@@ -211,6 +272,7 @@ struct Engine {
     S4G_TRY(alloc(&dVal, 2 * (size_t)nI));
     S4G_TRY(alloc(&dDiag, nC));
     S4G_TRY(alloc(&dRD, nC));
+    S4G_TRY(alloc(&dRDa, 2 * (size_t)nI));
     for (int k = 0; k < 2; ++k) S4G_TRY(alloc(&f.D[k], 3 * (size_t)nC));
     S4G_TRY(alloc(&f.D0, 3 * (size_t)nC));
     S4G_TRY(alloc(&f.D0b, 3 * (size_t)nB));
@@ -222,12 +284,11 @@ struct Engine {
     S4G_TRY(alloc(&pc.x, 3 * (size_t)nC));
     S4G_TRY(alloc(&pc.r, 3 * (size_t)nC));
     S4G_TRY(alloc(&pc.w, 3 * (size_t)nC));
-    S4G_TRY(alloc(&pc.p[0], 3 * (size_t)nC));
-    S4G_TRY(alloc(&pc.p[1], 3 * (size_t)nC));
+    S4G_TRY(alloc(&pc.p, 3 * (size_t)nC));
     S4G_TRY(alloc(&pc.q, 3 * (size_t)nC));
     S4G_TRY(alloc(&pc.flags[0], hp.nParts));
     S4G_TRY(alloc(&pc.flags[1], hp.nParts));
-    pc.val = dVal; pc.diag = dDiag; pc.rD = dRD;
+    pc.val = dVal; pc.diag = dDiag; pc.rD = dRD; pc.rDa = dRDa;
     S4G_TRY(alloc(&dState, 1));
     S4G_CUDA(cudaMallocHost((void**)&hState, sizeof(DevState)));
     const size_t rowBlocks = (nC + kRowBlock - 1) / kRowBlock;
@@ -237,12 +298,14 @@ struct Engine {
 
     int maxSmem = 0;
     S4G_CUDA(cudaDeviceGetAttribute(&maxSmem, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-    if (sweepSmemBytes(mv) + 1024 > (size_t)maxSmem)
+    if (sweepSmemBytes<double>(mv) + 1024 > (size_t)maxSmem)
       return setErr(S4G_BAD_ARG, "a DIC scheduling part does not fit in shared memory; use a smaller part_size");
     int perSM = 0;
-    S4G_CUDA(sweepPrepare(mv, &perSM));
+    S4G_CUDA(sweepPrepare<double>(mv, &perSM));
     if (perSM < 1) return setErr(S4G_BAD_ARG, "DIC sweep kernel cannot be resident; use a smaller part_size");
     sweepGrid = std::max(1, std::min(hp.nParts, perSM * ctx->numSMs));
+    S4G_CUDA(sweepPrepare<float>(mv, &perSM));
+    sweepGrid32 = std::max(1, std::min(hp.nParts, std::max(1, perSM) * ctx->numSMs));
     S4G_CUDA(cudaStreamSynchronize(s));
     // caller geometry is no longer needed
     for (double* p : {dCc, dCfc, dSfc}) {
@@ -368,12 +431,10 @@ struct Engine {
     if (pre == 0) {
       S4G_TRY(resetSweepState());
       S4G_CUDA(cudaMemcpyAsync(dRD, dDiag, sizeof(double) * hp.nC, cudaMemcpyDeviceToDevice, s));
-      launchDicFactor(mv, pc, dState, sweepGrid, s);
+      launchDicFactor(mv, dVal, dDiag, dRD, dRDa, pc.flags[0], dState, sweepGrid, s);
       launches += 2;
     } else {
-      // diagonalPreconditioner: rD = 1/diag
-      S4G_CUDA(cudaMemcpyAsync(dRD, dDiag, sizeof(double) * hp.nC, cudaMemcpyDeviceToDevice, s));
-      launchReciprocal(hp.nC, dRD, s);
+      launchReciprocal(hp.nC, dDiag, dRD, s);  // diagonalPreconditioner: rD = 1/diag
       launches++;
     }
     S4G_CUDA(cudaGetLastError());
@@ -382,12 +443,39 @@ struct Engine {
     if (hState->status & kErrTimeout) return setErr(S4G_TIMEOUT, "DIC factor sweep wait gave up");
     matrixValid = true;
     matrixPrecond = pre;
+    fp32Valid = false;
+    return S4G_OK;
+  }
+
+  // FP32 copies of the matrix, factor and work vectors (mixed precision).
+  s4g_status ensureFp32() {
+    const size_t nC = hp.nC, nE = 2 * (size_t)hp.nI;
+    if (!fp32Allocated) {
+      float *val, *diag, *rD, *rDa;
+      S4G_TRY(alloc(&val, nE)); S4G_TRY(alloc(&diag, nC)); S4G_TRY(alloc(&rD, nC)); S4G_TRY(alloc(&rDa, nE));
+      pc32.val = val; pc32.diag = diag; pc32.rD = rD; pc32.rDa = rDa;
+      S4G_TRY(alloc(&pc32.x, 3 * nC)); S4G_TRY(alloc(&pc32.r, 3 * nC)); S4G_TRY(alloc(&pc32.w, 3 * nC));
+      S4G_TRY(alloc(&pc32.p, 3 * nC)); S4G_TRY(alloc(&pc32.q, 3 * nC));
+      pc32.flags[0] = pc.flags[0]; pc32.flags[1] = pc.flags[1];
+      fp32Allocated = true;
+    }
+    if (!fp32Valid) {
+      cudaStream_t s = ctx->stream;
+      launchToFloat(nE, dVal, const_cast<float*>(pc32.val), s);
+      launchToFloat(nC, dDiag, const_cast<float*>(pc32.diag), s);
+      launchToFloat(nC, dRD, const_cast<float*>(pc32.rD), s);
+      launchToFloat(nE, dRDa, const_cast<float*>(pc32.rDa), s);
+      launches += 4;
+      S4G_CUDA(cudaGetLastError());
+      fp32Valid = true;
+    }
     return S4G_OK;
   }
 
   s4g_status readState() {
     S4G_CUDA(cudaMemcpyAsync(hState, dState, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
     S4G_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (ctx->profile) timer.resolve();
     return S4G_OK;
   }
 
@@ -399,7 +487,10 @@ struct Engine {
     S4G_CUDA(z(f.D0b, 3 * nB)); S4G_CUDA(z(f.G, 9 * nC)); S4G_CUDA(z(f.sig, 6 * nC));
     S4G_CUDA(z(f.Gb, 9 * nB)); S4G_CUDA(z(f.sigb, 6 * nB)); S4G_CUDA(z(f.g, 3 * nB));
     S4G_CUDA(z(pc.x, 3 * nC)); S4G_CUDA(z(pc.r, 3 * nC)); S4G_CUDA(z(pc.w, 3 * nC));
-    S4G_CUDA(z(pc.p[0], 3 * nC)); S4G_CUDA(z(pc.p[1], 3 * nC)); S4G_CUDA(z(pc.q, 3 * nC));
+    S4G_CUDA(z(pc.p, 3 * nC)); S4G_CUDA(z(pc.q, 3 * nC));
+    if (fp32Allocated)
+      for (float* p : {pc32.x, pc32.r, pc32.w, pc32.p, pc32.q})
+        S4G_CUDA(cudaMemsetAsync(p, 0, 3 * nC * sizeof(float), s));
     if (tl) {
       S4G_CUDA(z(f.GD, 9 * nC)); S4G_CUDA(z(f.GD0, 9 * nC)); S4G_CUDA(z(f.GDb, 9 * nB));
       S4G_CUDA(z(f.GD0b, 9 * nB)); S4G_CUDA(z(f.sig0, 6 * nC)); S4G_CUDA(z(f.sig0b, 6 * nB));
@@ -416,28 +507,33 @@ struct Engine {
   }
 
   // PCG loop of one corrector: launch batches, read the device decision.
-  s4g_status pcgLoop(const Controls& c) {
-    int chunk = 2;
+  template <typename T>
+  s4g_status pcgLoop(const Controls& c, const PcgPtrs<T>& p, int grid) {
+    // profiling steps one iteration at a time, so no timed launch is idle
+    int chunk = ctx->profile ? 1 : 2;
     for (int guard = 0; guard < 1000000; ++guard) {
       for (int i = 0; i < chunk; ++i)
-        launchPcgIteration(mv, c, pc, dState, dPartials, sweepGrid, ctx->stream, &launches);
+        launchPcgIteration<T>(mv, c, p, dState, dPartials, grid, ctx->stream, &launches, tm());
       S4G_CUDA(cudaGetLastError());
       S4G_TRY(readState());
       if (!hState->pcgContinue || (hState->status & (kErrTimeout | kErrNaN))) return S4G_OK;
-      chunk = std::min(chunk * 2, 16);
+      if (!ctx->profile) chunk = std::min(chunk * 2, 16);
     }
     return setErr(S4G_TIMEOUT, "PCG loop did not end");
   }
 
-  // One evolve(): correctors until converged() or nCorrectors.
-  s4g_status correctorLoop(Controls& c, int tl) {
+  // One evolve(): correctors until converged() or nCorrectors.  The inner
+  // PCG runs in T; the right-hand side, the correction of D and every
+  // convergence test stay in FP64.
+  template <typename T>
+  s4g_status correctorLoop(Controls& c, int tl, const PcgPtrs<T>& p, int grid) {
     cudaStream_t s = ctx->stream;
     for (;;) {
-      launchRhs(mv, c, f, pc.x, pc.r, dState, dPartials, s);
+      launchRhs<T>(mv, c, f, p.x, p.r, dState, dPartials, s, tm());
       launches++;
       S4G_TRY(readState());
-      if (hState->pcgContinue) S4G_TRY(pcgLoop(c));
-      launchPost(mv, c, f, pc.x, dState, dPartials, 1, s);
+      if (hState->pcgContinue) S4G_TRY(pcgLoop<T>(c, p, grid));
+      launchPost<T>(mv, c, f, p.x, dState, dPartials, 1, s, tm());
       launches += tl ? 2 : 1;
       S4G_CUDA(cudaGetLastError());
       S4G_TRY(readState());
@@ -457,26 +553,32 @@ struct Engine {
     const int tl = model == S4G_NONLIN_GEOM_TOTAL_LAG;
     if (tl && law.type != S4G_NEO_HOOKEAN) return setErr(S4G_BAD_ARG, "the TL model needs a neoHookeanElastic law");
     if (!tl && law.type != S4G_LINEAR_ELASTIC) return setErr(S4G_BAD_ARG, "the linear-geometry model needs a linearElastic law");
-    if (precision != S4G_FP64) return setErr(S4G_NOT_BUILT, "FP32 refinement path not built yet");
     if (tl) S4G_TRY(allocTL());
     if (!tl) nInc = 1;
     if (nInc < 1) return setErr(S4G_BAD_ARG, "n_increments must be >= 1");
     cudaStream_t s = ctx->stream;
     const long long launches0 = launches;
     S4G_TRY(ensureMatrix());
+    const bool mixed = precision == S4G_FP32_REFINE;
+    if (mixed) S4G_TRY(ensureFp32());
     cudaEvent_t e0, e1;
     S4G_CUDA(cudaEventCreate(&e0));
     S4G_CUDA(cudaEventCreate(&e1));
     S4G_TRY(initFields(tl));
     S4G_TRY(resetSweepState());
+    timer.reset();
     S4G_CUDA(cudaEventRecord(e0, s));
     Controls c = controls(tl);
     int nCorrTotal = 0;
+    auto loop = [&](int isTl) -> s4g_status {
+      return mixed ? correctorLoop<float>(c, isTl, pc32, sweepGrid32)
+                   : correctorLoop<double>(c, isTl, pc, sweepGrid);
+    };
     if (!tl) {
       launchTractionInit(mv, c, f, s);
-      launchPost(mv, c, f, pc.x, dState, dPartials, 0, s);
+      launchPost<double>(mv, c, f, pc.x, dState, dPartials, 0, s);
       launches += 2;
-      S4G_TRY(correctorLoop(c, 0));
+      S4G_TRY(loop(0));
       nCorrTotal = hState->nCorrDone;
     } else {
       for (int n = 1; n <= nInc; ++n) {
@@ -487,7 +589,7 @@ struct Engine {
         S4G_CUDA(cudaMemcpyAsync(&dState->iCorr, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
         launchTractionInit(mv, c, f, s);
         launches++;
-        S4G_TRY(correctorLoop(c, 1));
+        S4G_TRY(loop(1));
         launchTlShift(mv, c, f, dState, s);
         launches += 2;
         if (hState->status & (kErrTimeout | kErrNaN)) break;
@@ -528,6 +630,11 @@ struct Engine {
       perf->kernel_launches = launches - launches0;
       perf->enforce_linear = hState->enforceLinear;
       perf->device_status = (int)hState->status;
+      timer.resolve();
+      for (int k = 0; k < S4G_K_KINDS; ++k) {
+        perf->kernel_ms[k] = timer.ms[k];
+        perf->kernel_launches_by[k] = timer.count[k];
+      }
     }
     if (hState->status & kErrTimeout) return setErr(S4G_TIMEOUT, "a bounded device wait gave up");
     if (hState->status & kErrNaN) return setErr(S4G_NAN_DETECTED, "non-finite value in the iteration");
@@ -537,11 +644,19 @@ struct Engine {
   }
 
   // ---------------------------------------------------------- operators ---
+  // All copies go through the library's stream (non-blocking: it does not
+  // order against the legacy default stream), then wait for it.
+  s4g_status copySync(void* dst, const void* src, size_t bytes, cudaMemcpyKind kind) {
+    S4G_CUDA(cudaMemcpyAsync(dst, src, bytes, kind, ctx->stream));
+    S4G_CUDA(cudaStreamSynchronize(ctx->stream));
+    return S4G_OK;
+  }
+
   s4g_status opMatrix(double* diag, double* upper) {
     S4G_TRY(ensureMatrix());
     std::vector<double> v(2 * (size_t)hp.nI), dg(hp.nC);
-    S4G_CUDA(cudaMemcpy(v.data(), dVal, sizeof(double) * v.size(), cudaMemcpyDeviceToHost));
-    S4G_CUDA(cudaMemcpy(dg.data(), dDiag, sizeof(double) * dg.size(), cudaMemcpyDeviceToHost));
+    S4G_TRY(copySync(v.data(), dVal, sizeof(double) * v.size(), cudaMemcpyDeviceToHost));
+    S4G_TRY(copySync(dg.data(), dDiag, sizeof(double) * dg.size(), cudaMemcpyDeviceToHost));
     for (int s = 0; s < hp.nC; ++s) {
       if (diag) diag[hp.s2c[s]] = dg[s];
       for (int e = hp.rowptr[s]; e < hp.rowptr[s + 1]; ++e)
@@ -566,11 +681,11 @@ struct Engine {
     S4G_TRY(ensureMatrix());
     std::vector<double> hx, hy(3 * (size_t)hp.nC);
     toStorage(k, x, hx);
-    S4G_CUDA(cudaMemcpy(pc.w, hx.data(), sizeof(double) * hx.size(), cudaMemcpyHostToDevice));
-    launchAmul(mv, dVal, dDiag, pc.w, pc.q, ctx->stream);
+    S4G_TRY(copySync(pc.w, hx.data(), sizeof(double) * hx.size(), cudaMemcpyHostToDevice));
+    launchAmul<double>(mv, (const double*)dVal, dDiag, pc.w, pc.q, ctx->stream);
     launches++;
     S4G_CUDA(cudaGetLastError());
-    S4G_CUDA(cudaMemcpy(hy.data(), pc.q, sizeof(double) * hy.size(), cudaMemcpyDeviceToHost));
+    S4G_TRY(copySync(hy.data(), pc.q, sizeof(double) * hy.size(), cudaMemcpyDeviceToHost));
     fromStorage(k, hy, y);
     return S4G_OK;
   }
@@ -580,19 +695,19 @@ struct Engine {
     S4G_TRY(ensureMatrix());
     std::vector<double> hr, hw(3 * (size_t)hp.nC);
     toStorage(k, r, hr);
-    S4G_CUDA(cudaMemcpy(pc.r, hr.data(), sizeof(double) * hr.size(), cudaMemcpyHostToDevice));
+    S4G_TRY(copySync(pc.r, hr.data(), sizeof(double) * hr.size(), cudaMemcpyHostToDevice));
     S4G_TRY(resetSweepState());
     DevState init{};
     init.pcgContinue = 1;
     S4G_CUDA(cudaMemcpyAsync(&dState->pcgContinue, &init.pcgContinue, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     Controls c = controls(0);
-    launchPrecondOnly(mv, c, pc, dState, dPartials, sweepGrid, ctx->stream);
+    launchPrecondOnly<double>(mv, c, pc, dState, dPartials, sweepGrid, ctx->stream);
     launches += 2;
     S4G_CUDA(cudaGetLastError());
     S4G_CUDA(cudaStreamSynchronize(ctx->stream));
     S4G_TRY(readState());
     if (hState->status & kErrTimeout) return setErr(S4G_TIMEOUT, "sweep wait gave up");
-    S4G_CUDA(cudaMemcpy(hw.data(), pc.w, sizeof(double) * hw.size(), cudaMemcpyDeviceToHost));
+    S4G_TRY(copySync(hw.data(), pc.w, sizeof(double) * hw.size(), cudaMemcpyDeviceToHost));
     fromStorage(k, hw, w);
     return S4G_OK;
   }
@@ -611,8 +726,16 @@ struct Engine {
 
 // ------------------------------------------------------------------ C ABI ---
 
-struct s4g_ctx { s4g::Ctx c; };
-struct s4g_mesh { s4g::Engine e; };
+struct s4g_mesh;
+// A context owns its meshes: destroying it frees the meshes still alive.
+struct s4g_ctx {
+  s4g::Ctx c;
+  std::vector<s4g_mesh*> meshes;
+};
+struct s4g_mesh {
+  s4g::Engine e;
+  s4g_ctx* owner = nullptr;
+};
 
 using s4g::setErr;
 
@@ -651,6 +774,7 @@ s4g_status s4g_ctx_create(s4g_ctx** out, const s4g_ctx_opts* opts) {
   std::unique_ptr<s4g_ctx> c(new s4g_ctx());
   c->c.device = dev;
   c->c.verbose = opts ? opts->verbose : 0;
+  c->c.profile = opts ? opts->profile : 0;
   if (cudaSetDevice(dev) != cudaSuccess) return setErr(S4G_CUDA_ERROR, "cudaSetDevice failed");
   cudaDeviceGetAttribute(&c->c.numSMs, cudaDevAttrMultiProcessorCount, dev);
   if (cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -662,6 +786,9 @@ s4g_status s4g_ctx_create(s4g_ctx** out, const s4g_ctx_opts* opts) {
 s4g_status s4g_ctx_destroy(s4g_ctx* ctx) {
   if (!ctx) return S4G_BAD_ARG;
   cudaSetDevice(ctx->c.device);
+  if (ctx->c.stream) cudaStreamSynchronize(ctx->c.stream);
+  for (s4g_mesh* m : ctx->meshes) delete m;
+  ctx->meshes.clear();
   if (ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
   delete ctx;
   return S4G_OK;
@@ -681,6 +808,8 @@ s4g_status s4g_mesh_upload(s4g_ctx* ctx, const s4g_mesh_desc* desc, const s4g_me
   m->e.outer = outer;
   s4g_status st = m->e.uploadMesh(desc, opts);
   if (st != S4G_OK) return st;
+  m->owner = ctx;
+  ctx->meshes.push_back(m.get());
   *out = m.release();
   return S4G_OK;
 }
@@ -690,6 +819,14 @@ s4g_status s4g_mesh_get_permutation(const s4g_mesh* mesh, int* perm) {
   const s4g::HostPrep& hp = mesh->e.hp;
   // solver rank r -> caller cell
   for (int s = 0; s < hp.nC; ++s) perm[hp.solverRank[s]] = hp.s2c[s];
+  return S4G_OK;
+}
+
+s4g_status s4g_mesh_get_parts(const s4g_mesh* mesh, int* part_of_cell) {
+  if (!mesh || !part_of_cell) return setErr(S4G_BAD_ARG, "null argument");
+  const s4g::HostPrep& hp = mesh->e.hp;
+  for (int p = 0; p < hp.nParts; ++p)
+    for (int s = hp.partStart[p]; s < hp.partStart[p + 1]; ++s) part_of_cell[hp.s2c[s]] = p;
   return S4G_OK;
 }
 
@@ -733,6 +870,10 @@ s4g_status s4g_mesh_destroy(s4g_mesh* mesh) {
   if (!mesh) return S4G_BAD_ARG;
   cudaSetDevice(mesh->e.ctx->device);
   cudaStreamSynchronize(mesh->e.ctx->stream);
+  if (mesh->owner) {
+    auto& v = mesh->owner->meshes;
+    v.erase(std::remove(v.begin(), v.end(), mesh), v.end());
+  }
   delete mesh;
   return S4G_OK;
 }

@@ -2,8 +2,22 @@
 #pragma once
 
 #include "device_common.cuh"
+#include "s4g.h"
 
 namespace s4g {
+
+// Optional per-kernel timing: before/after bracket one launch of a kernel
+// kind (S4G_K_* of s4g.h) on the launch stream.
+struct LaunchTimer {
+  virtual void before(int kind, cudaStream_t s) = 0;
+  virtual void after(int kind, cudaStream_t s) = 0;
+  virtual ~LaunchTimer() {}
+};
+struct TimeScope {
+  LaunchTimer* t; int k; cudaStream_t s;
+  TimeScope(LaunchTimer* t_, int k_, cudaStream_t s_) : t(t_), k(k_), s(s_) { if (t) t->before(k, s); }
+  ~TimeScope() { if (t) t->after(k, s); }
+};
 
 // ---- once per mesh (kernels_fv.cu) -----------------------------------------
 struct GeomInputs {
@@ -47,12 +61,15 @@ void launchTractionInit(const MeshView& mv, const Controls& c, const FieldPtrs& 
 // Post-solve pass: D += x, boundary values, leastSquares gradient, law,
 // boundary gradient/stress, next traction snGrad, convergence reductions.
 // mode 0: constructor pass (no correction, no stress); 1: corrector.
-void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const double* x,
-                DevState* st, double* partials, int mode, cudaStream_t s);
-// RHS pass: R = div(sigma) + RhieChow + boundary terms, M*D_old for the
-// residual normalisation; zeroes x, sets r = R.
-void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, double* x,
-               double* r, DevState* st, double* partials, cudaStream_t s);
+template <typename T>
+void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const T* x,
+                DevState* st, double* partials, int mode, cudaStream_t s,
+                LaunchTimer* tm = nullptr);
+// RHS pass (FP64): R = div(sigma) + RhieChow + boundary terms, M*D_old for the
+// residual normalisation; zeroes x, sets r = R rounded to the PCG type.
+template <typename T>
+void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, T* x, T* r,
+               DevState* st, double* partials, cudaStream_t s, LaunchTimer* tm = nullptr);
 // out[c] = in[c2s[c]] for rows of `width` doubles.
 void launchGather(int n, int width, const int* c2s, const double* in, double* out, cudaStream_t s);
 // TL: new time step -- old-time fields take the converged values.
@@ -60,26 +77,41 @@ void launchTlShift(const MeshView& mv, const Controls& c, const FieldPtrs& f, De
                    cudaStream_t s);
 
 // ---- PCG (kernels_pcg.cu) ----------------------------------------------------
+// PCG arrays in the value type T of the inner solve: double (plain FP64) or
+// float (FP32 inner solve of the mixed-precision path).
+template <typename T>
 struct PcgPtrs {
-  const double* val; const double* diag; double* rD;
-  double* x; double* r; double* w; double* p[2]; double* q;
+  const T* val; const T* diag; const T* rD;
+  const T* rDa;        // rD[row] * val[e] per CSR entry (FDIC coefficients)
+  T* x; T* r; T* w; T* p; T* q;
   unsigned* flags[2];  // per-part sweep flags (forward, backward)
 };
-// DIC factor: rD = 1/pivots by a scheduled forward sweep.
-void launchDicFactor(const MeshView& mv, const PcgPtrs& p, DevState* st, int grid, cudaStream_t s);
+
+// DIC factor in FP64: rD64 = 1/pivots by a scheduled forward sweep
+// (flags[0] of the FP64 set), then rDa64 = rD64[row]*val64[e].
+void launchDicFactor(const MeshView& mv, const double* val, const double* diag, double* rD,
+                     double* rDa, unsigned* flags, DevState* st, int grid, cudaStream_t s);
+// Diagonal preconditioner coefficients: rD = 1/diag, rDa unused.
+void launchReciprocal(int n, const double* diag, double* rD, cudaStream_t s);
+// FP32 copies of the FP64 matrix and factor for the mixed-precision path.
+void launchToFloat(size_t n, const double* in, float* out, cudaStream_t s);
+
 // One PCG iteration for the three components (skips when converged).
-void launchPcgIteration(const MeshView& mv, const Controls& c, const PcgPtrs& p, DevState* st,
-                        double* partials, int sweepGrid, cudaStream_t s, long long* launches);
-// Shared memory of the staged sweeps, threads per sweep block, and the
-// per-kernel attribute set-up (returns resident sweep blocks per SM).
+template <typename T>
+void launchPcgIteration(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
+                        double* partials, int sweepGrid, cudaStream_t s, long long* launches,
+                        LaunchTimer* tm = nullptr);
+// Shared memory of the staged sweeps and the per-kernel attribute set-up
+// (returns resident sweep blocks per SM).
+template <typename T>
 size_t sweepSmemBytes(const MeshView& mv);
-int sweepBlockThreads();
+template <typename T>
 cudaError_t sweepPrepare(const MeshView& mv, int* blocksPerSM);
-void launchReciprocal(int n, double* rD, cudaStream_t s);
 // Operator checks.
-void launchAmul(const MeshView& mv, const double* val, const double* diag, const double* x,
-                double* y, cudaStream_t s);
-void launchPrecondOnly(const MeshView& mv, const Controls& c, const PcgPtrs& p, DevState* st,
+template <typename T>
+void launchAmul(const MeshView& mv, const T* val, const T* diag, const T* x, T* y, cudaStream_t s);
+template <typename T>
+void launchPrecondOnly(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                        double* partials, int sweepGrid, cudaStream_t s);
 
 }  // namespace s4g

@@ -183,8 +183,9 @@ __device__ __forceinline__ V3 boundaryValue(const MeshView& mv, const Controls& 
 // For the TL model the law needs the global J check first, so mode 1 stops
 // after the kinematics (F, F^-1, J) and kPostLawTL finishes the pass.
 
+template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
-kPost(MeshView mv, Controls c, FieldPtrs f, const double* __restrict__ x, DevState* st,
+kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* st,
       double* partials, int mode) {
   __shared__ double smem[32 * 6];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -197,7 +198,7 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const double* __restrict__ x, DevSta
   double minJ = 1e300, maxJ = -1e300;
   if (s < mv.nC) {
     V3 Up = ldV(Uold, s);
-    if (apply) Up = Up + ldV(x, s);
+    if (apply) Up = Up + ldVT(x, s);
     const bool hasB = mv.browptr[s + 1] > mv.browptr[s];
     T9 Gold = hasB ? ldT(f.G, s) : zeroT();
     // leastSquares gradient (cell-centric; owner-oriented d and dU)
@@ -207,7 +208,7 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const double* __restrict__ x, DevSta
     for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) {
       const int nb = mv.col[e];
       V3 Un = ldV(Uold, nb);
-      if (apply) Un = Un + ldV(x, nb);
+      if (apply) Un = Un + ldVT(x, nb);
       const V3 Cn = ldV(mv.C, nb);
       if (mv.fidx[e] >= 0) {
         V3 d = Cn - Cs;
@@ -268,7 +269,7 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const double* __restrict__ x, DevSta
     }
     if (apply) {
       stV(Unew, s, Up);
-      V3 xs = ldV(x, s);
+      V3 xs = ldVT(x, s);
       mx[0] = mag(xs);
       mx[1] = c.tl ? mag(Up) : mag(Up - ldV(f.D0, s));
       mx[2] = mag(Up);
@@ -363,8 +364,9 @@ kPostLawTL(MeshView mv, Controls c, FieldPtrs f, const DevState* st) {
 
 // --------------------------------------------------------------- RHS pass ---
 
+template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
-kRhs(MeshView mv, Controls c, FieldPtrs f, double* __restrict__ x, double* __restrict__ r,
+kRhs(MeshView mv, Controls c, FieldPtrs f, T* __restrict__ x, T* __restrict__ r,
      DevState* st, double* partials) {
   __shared__ double smem[32 * 6];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -426,8 +428,8 @@ kRhs(MeshView mv, Controls c, FieldPtrs f, double* __restrict__ x, double* __res
         sumA += a;
       }
     }
-    stV(r, s, R);
-    stV(x, s, V3{0, 0, 0});
+    stVT(r, s, R);
+    stVT(x, s, V3{0, 0, 0});
     const double xb[3] = {st->xbar[0], st->xbar[1], st->xbar[2]};
     const double md[3] = {MD.x, MD.y, MD.z}, rr[3] = {R.x, R.y, R.z};
     for (int k = 0; k < 3; ++k) {
@@ -515,18 +517,31 @@ void launchTractionInit(const MeshView& mv, const Controls& c, const FieldPtrs& 
   kTractionInit<<<(mv.nB + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, c, f);
 }
 
-void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const double* x,
-                DevState* st, double* partials, int mode, cudaStream_t s) {
+template <typename T>
+void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const T* x,
+                DevState* st, double* partials, int mode, cudaStream_t s, LaunchTimer* tm) {
   const int grid = (mv.nC + kRowBlock - 1) / kRowBlock;
-  kPost<<<grid, kRowBlock, 0, s>>>(mv, c, f, x, st, partials, mode);
+  TimeScope ts(tm, S4G_K_POST, s);
+  kPost<T><<<grid, kRowBlock, 0, s>>>(mv, c, f, x, st, partials, mode);
   if (c.tl && mode == 1) kPostLawTL<<<grid, kRowBlock, 0, s>>>(mv, c, f, st);
 }
 
-void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, double* x, double* r,
-               DevState* st, double* partials, cudaStream_t s) {
+template <typename T>
+void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, T* x, T* r,
+               DevState* st, double* partials, cudaStream_t s, LaunchTimer* tm) {
   const int grid = (mv.nC + kRowBlock - 1) / kRowBlock;
-  kRhs<<<grid, kRowBlock, 0, s>>>(mv, c, f, x, r, st, partials);
+  TimeScope ts(tm, S4G_K_RHS, s);
+  kRhs<T><<<grid, kRowBlock, 0, s>>>(mv, c, f, x, r, st, partials);
 }
+
+template void launchPost<double>(const MeshView&, const Controls&, const FieldPtrs&, const double*,
+                                 DevState*, double*, int, cudaStream_t, LaunchTimer*);
+template void launchPost<float>(const MeshView&, const Controls&, const FieldPtrs&, const float*,
+                                DevState*, double*, int, cudaStream_t, LaunchTimer*);
+template void launchRhs<double>(const MeshView&, const Controls&, const FieldPtrs&, double*, double*,
+                                DevState*, double*, cudaStream_t, LaunchTimer*);
+template void launchRhs<float>(const MeshView&, const Controls&, const FieldPtrs&, float*, float*,
+                               DevState*, double*, cudaStream_t, LaunchTimer*);
 
 void launchGather(int n, int width, const int* c2s, const double* in, double* out, cudaStream_t s) {
   long tot = (long)n * width;

@@ -7,6 +7,10 @@
 // residual normalised by OpenFOAM's normFactor, stopping at tolerance,
 // relTol*initialResidual or maxIter.  The three components share the matrix,
 // so every kernel streams the matrix once for all three right-hand sides.
+// The value type T is double for the plain FP64 path and float for the inner
+// solve of the mixed-precision path; dot products and residual sums of the
+// float path are compensated (Neumaier two-sum per thread, FP64 across
+// threads).
 //
 // DIC sweeps.  The incomplete-Cholesky (zero fill) forward and backward
 // substitutions are sequential in the DIC cell order.  Rows are stored in a
@@ -15,24 +19,61 @@
 // persistent grid takes parts from a ticket counter in topological order
 // (forward) or reverse topological order (backward), waits -- with an
 // iteration limit -- for the parts it depends on to publish an epoch flag,
-// stages the part (its rows, its matrix entries and the remote values it
+// stages the part (its rows, its matrix coefficients and the remote values it
 // reads) in shared memory, walks its levels with __syncthreads between them,
 // writes the part back and publishes its own flag.  Every part a CTA waits
 // for was taken earlier by a running CTA, so the scheme cannot deadlock.
 // Values written by other CTAs in the same sweep are read with ld.global.cg
-// (L2), never from a possibly stale L1 line.
+// (L2), never from a possibly stale L1 line.  The coefficients rD_row*a_e are
+// precomputed once per matrix, as OpenFOAM's FDIC does (bit-identical to DIC).
 
 #include "kernels.cuh"
 
 namespace s4g {
 namespace {
 
-constexpr int kSweepSmBlock = 256;
+constexpr int kSweepSmBlock = 64;
 
+// Asynchronous global->shared copies (LDGSTS): a part's static data is put in
+// flight at once and waited for with one hardware wait.
+template <int BYTES>
+__device__ __forceinline__ void cpAsync(void* sm, const void* gm) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(sm);
+  if (BYTES == 8) asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gm) : "memory");
+  else asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gm) : "memory");
+}
+template <typename T>
+__device__ __forceinline__ void cpAsyncT(T* sm, const T* gm) { cpAsync<sizeof(T)>(sm, gm); }
+__device__ __forceinline__ void cpAsyncWaitAll() {
+  asm volatile("cp.async.commit_group;\ncp.async.wait_all;" ::: "memory");
+}
+
+// Sum of T values: plain for double; Neumaier-compensated for float.
+template <typename T> struct Acc;
+template <> struct Acc<double> {
+  double s = 0;
+  __device__ __forceinline__ void add(double x) { s += x; }
+  __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct Acc<float> {
+  float s = 0, c = 0;
+  __device__ __forceinline__ void add(float x) {
+    const float t = s + x;
+    c += (fabsf(s) >= fabsf(x)) ? (s - t) + x : (x - t) + s;
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
+// Poll with relaxed loads (an acquire load per poll would also invalidate the
+// SM's L1 each time), then one acquire fence once the flag is seen.
 __device__ __forceinline__ void waitPart(const unsigned* flag, unsigned epoch, unsigned* status) {
   for (int it = 0; it < kSpinLimit; ++it) {
-    if (ldAcquire(flag) == epoch) return;
-    if ((it & 63) == 63) __nanosleep(32);
+    if (ldRelaxed(flag) == epoch) {
+      fenceAcqRel();
+      return;
+    }
+    if (it > 4096) __nanosleep(64);
   }
   atomicOr(status, kErrTimeout);
 }
@@ -59,9 +100,11 @@ __device__ __forceinline__ void sweepEpilogue(DevState* st, int dir, unsigned ep
 }
 
 // DIC factor (calcReciprocalD): pivot_u = diag_u - sum upper^2/pivot_l,
-// once per matrix, scheduled like the forward sweep but reading global memory.
+// once per matrix in FP64, scheduled like the forward sweep but reading
+// global memory.
 __global__ void __launch_bounds__(kSweepBlock)
-kSweepFactor(MeshView mv, PcgPtrs p, DevState* st) {
+kSweepFactor(MeshView mv, const double* val, const double* diag, double* rD, unsigned* flags,
+             DevState* st) {
   __shared__ int sPart;
   const unsigned epoch = st->epoch[0];
   for (;;) {
@@ -70,47 +113,128 @@ kSweepFactor(MeshView mv, PcgPtrs p, DevState* st) {
     const int pLo = mv.partStart[part];
     if (!mv.subdomains)
       for (int i = mv.upPtr[part] + threadIdx.x; i < mv.upPtr[part + 1]; i += blockDim.x)
-        waitPart(p.flags[0] + mv.upIdx[i], epoch, &st->status);
+        waitPart(flags + mv.upIdx[i], epoch, &st->status);
     __syncthreads();
     for (int lvl = mv.lvlOff[part]; lvl < mv.lvlOff[part + 1]; ++lvl) {
       for (int row = mv.lvlStart[lvl] + threadIdx.x; row < mv.lvlStart[lvl + 1]; row += blockDim.x) {
-        double dv = p.diag[row];
+        double dv = diag[row];
         for (int e = mv.rowptr[row]; e < mv.rowptr[row + 1]; ++e) {
           const int cl = mv.col[e];
           if (cl >= row) break;
           if (mv.subdomains && cl < pLo) continue;
-          const double a = p.val[e];
-          dv -= a * a / __ldcg(p.rD + cl);
+          const double a = val[e];
+          dv -= a * a / __ldcg(rD + cl);
         }
-        __stcg(p.rD + row, dv);
+        __stcg(rD + row, dv);
       }
       __threadfence();
       __syncthreads();
     }
     if (threadIdx.x == 0) {
       __threadfence();
-      stRelease(p.flags[0] + part, epoch);
+      stRelease(flags + part, epoch);
     }
   }
   sweepEpilogue(st, 0, epoch);
 }
 
+// rD = 1/pivot; rDa[e] = rD[row]*val[e] (FDIC coefficients)
+__global__ void kFactorFinish(MeshView mv, const double* val, double* rD, double* rDa) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= mv.nC) return;
+  const double r = 1.0 / rD[s];
+  rD[s] = r;
+  for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) rDa[e] = r * val[e];
+}
+
+__global__ void kReciprocal(int n, const double* diag, double* rD) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) rD[i] = 1.0 / diag[i];
+}
+
+__global__ void kToFloat(size_t n, const double* in, float* out) {
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (float)in[i];
+}
+
+// One thread's row of a level, read ahead of the level's barrier: start
+// value (forward: rD r; backward: the forward result), the coefficients and
+// shared-memory slots of the entries the sweep uses, in sweep order.
+constexpr int kPreEntries = 4;
+template <typename T>
+struct RowPre {
+  int i, n;
+  T v0, v1, v2, r0, r1, r2;
+  T a[kPreEntries];
+  int sl[kPreEntries];
+};
+
+template <int DIR, typename T>
+__device__ __forceinline__ void preRow(RowPre<T>& pr, int lvl, const int* lvS, const int* rpS,
+                                       const int* loS, const int* sS, const T* aS, const T* dS,
+                                       const T* rS, const T* wS, int pLo, int e0) {
+  const int r0 = lvS[lvl] - pLo, r1 = lvS[lvl + 1] - pLo;
+  const int i = r0 + threadIdx.x;
+  if (i >= r1) { pr.i = -1; return; }
+  pr.i = i;
+  const int j0 = rpS[i] - e0, j1 = rpS[i + 1] - e0, nl = loS[i];
+  if (DIR == 0) {
+    const T rd = dS[i];
+    pr.v0 = rd * rS[3 * i]; pr.v1 = rd * rS[3 * i + 1]; pr.v2 = rd * rS[3 * i + 2];
+    pr.n = nl;
+#pragma unroll
+    for (int q = 0; q < kPreEntries; ++q)
+      if (q < nl) { pr.sl[q] = sS[j0 + q]; pr.a[q] = aS[j0 + q]; }
+  } else {
+    pr.v0 = wS[3 * i]; pr.v1 = wS[3 * i + 1]; pr.v2 = wS[3 * i + 2];
+    pr.r0 = rS[3 * i]; pr.r1 = rS[3 * i + 1]; pr.r2 = rS[3 * i + 2];
+    pr.n = (j1 - j0) - nl;
+#pragma unroll
+    for (int q = 0; q < kPreEntries; ++q)
+      if (q < pr.n) { pr.sl[q] = ~sS[j1 - 1 - q]; pr.a[q] = aS[j1 - 1 - q]; }
+  }
+}
+
+// The same row update reading everything from shared memory (rows with more
+// entries than kPreEntries, and rows beyond a thread's first of a level).
+template <int DIR, typename T>
+__device__ __forceinline__ void sweepRowGeneric(int i, T& v0, T& v1, T& v2, const int* rpS,
+                                                const int* loS, const int* sS, const T* aS,
+                                                const T* wS, int e0) {
+  const int j0 = rpS[i] - e0, j1 = rpS[i + 1] - e0, nl = loS[i];
+  if (DIR == 0) {
+    for (int j = j0; j < j0 + nl; ++j) {
+      const int sl = sS[j];
+      const T a = aS[j];
+      v0 -= a * wS[3 * sl]; v1 -= a * wS[3 * sl + 1]; v2 -= a * wS[3 * sl + 2];
+    }
+  } else {
+    for (int j = j1 - 1; j >= j0 + nl; --j) {
+      const int su = ~sS[j];
+      const T a = aS[j];
+      v0 -= a * wS[3 * su]; v1 -= a * wS[3 * su + 1]; v2 -= a * wS[3 * su + 2];
+    }
+  }
+}
+
 // Preconditioner sweep with the part staged in shared memory.
 //   DIR 0 (forward):  w_u = rD_u r_u - sum_{l<u} (rD_u a_ul) w_l
 //   DIR 1 (backward): w_l = w_l - sum_{u>l} (rD_l a_lu) w_u, plus w.r sums
-// (OpenFOAM DICPreconditioner::precondition, face order per row.)
-template <int DIR>
-__global__ void __launch_bounds__(kSweepSmBlock)
-kSweepSm(MeshView mv, PcgPtrs p, DevState* st, double* partials) {
+// (OpenFOAM DIC/FDIC precondition, face order per row.)  NT threads per part.
+template <int DIR, int NT, typename T>
+__global__ void __launch_bounds__(NT, 1)
+kSweepSm(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   if (!st->pcgContinue) return;
-  extern __shared__ double smem[];
+  extern __shared__ __align__(16) unsigned char smraw[];
   const int P = mv.maxRows, H = mv.maxHalo, EM = mv.maxEntries;
-  double* wS = smem;                       // (P + H + 1) * 3
-  double* rS = wS + 3 * (P + H + 1);       // P * 3
-  double* dS = rS + 3 * P;                 // P
-  double* vS = dS + P;                     // EM
-  int* sS = (int*)(vS + EM);               // EM
+  T* wS = (T*)smraw;                       // (P + H + 1) * 3
+  T* rS = wS + 3 * (P + H + 1);            // P * 3
+  T* dS = rS + 3 * P;                      // P
+  T* aS = dS + P;                          // EM: rD_row * a_e
+  int* sS = (int*)(aS + EM);               // EM
   int* rpS = sS + EM;                      // P + 1
+  int* lvS = rpS + P + 1;                  // maxLevels + 1: the part's level offsets
+  int* loS = lvS + mv.maxLevels + 1;       // P: lower entries per row
   __shared__ int sPart;
   __shared__ int sLast;
   __shared__ double red[32 * 3];
@@ -123,89 +247,107 @@ kSweepSm(MeshView mv, PcgPtrs p, DevState* st, double* partials) {
     const int pLo = mv.partStart[part], pHi = mv.partStart[part + 1];
     const int nR = pHi - pLo;
     const int e0 = mv.rowptr[pLo], nE = mv.rowptr[pHi] - e0;
-    // stage what does not depend on other parts while waiting
-    for (int i = threadIdx.x; i < nR; i += blockDim.x) {
-      const int row = pLo + i;
-      dS[i] = p.rD[row];
-      rS[3 * i] = p.r[3 * row]; rS[3 * i + 1] = p.r[3 * row + 1]; rS[3 * i + 2] = p.r[3 * row + 2];
-      rpS[i] = mv.rowptr[row] - e0;
-      if (DIR == 1) {
-        wS[3 * i] = __ldcg(p.w + 3 * row);
-        wS[3 * i + 1] = __ldcg(p.w + 3 * row + 1);
-        wS[3 * i + 2] = __ldcg(p.w + 3 * row + 2);
-      }
+    // stage what does not depend on other parts while waiting (the forward
+    // results the backward sweep starts from were written by the previous
+    // kernel, so they may go through L1)
+    for (int j = threadIdx.x; j < nE; j += NT) {
+      cpAsyncT(aS + j, p.rDa + e0 + j);
+      cpAsync<4>(sS + j, mv.slot + e0 + j);
     }
-    for (int j = threadIdx.x; j < nE; j += blockDim.x) {
-      vS[j] = p.val[e0 + j];
-      sS[j] = mv.slot[e0 + j];
+    for (int i = threadIdx.x; i < nR; i += NT) {
+      cpAsyncT(dS + i, p.rD + pLo + i);
+      cpAsync<4>(rpS + i, mv.rowptr + pLo + i);
+      cpAsync<4>(loS + i, mv.lowCnt + pLo + i);
     }
-    if (threadIdx.x == 0) rpS[nR] = nE;
-    if (threadIdx.x < 3) wS[3 * (P + H) + threadIdx.x] = 0.0;  // zero slot
+    for (int k = threadIdx.x; k < 3 * nR; k += NT) {
+      cpAsyncT(rS + k, p.r + 3 * (size_t)pLo + k);
+      if (DIR == 1) cpAsyncT(wS + k, p.w + 3 * (size_t)pLo + k);
+    }
+    const int l0 = mv.lvlOff[part], nL = mv.lvlOff[part + 1] - l0;
+    for (int k = threadIdx.x; k <= nL; k += NT) cpAsync<4>(lvS + k, mv.lvlStart + l0 + k);
+    if (threadIdx.x < 3) wS[3 * (P + H) + threadIdx.x] = T(0);  // zero slot
     // wait for the parts this one reads
     if (!mv.subdomains) {
       const int* dep = DIR == 0 ? mv.upIdx : mv.dnIdx;
       const int d0 = DIR == 0 ? mv.upPtr[part] : mv.dnPtr[part];
       const int d1 = DIR == 0 ? mv.upPtr[part + 1] : mv.dnPtr[part + 1];
-      for (int i = d0 + threadIdx.x; i < d1; i += blockDim.x) waitPart(flags + dep[i], epoch, &st->status);
+      for (int i = d0 + threadIdx.x; i < d1; i += NT) waitPart(flags + dep[i], epoch, &st->status);
     }
     __syncthreads();
     {
       const int* hIdx = DIR == 0 ? mv.haloFIdx : mv.haloBIdx;
       const int h0 = DIR == 0 ? mv.haloFPtr[part] : mv.haloBPtr[part];
       const int h1 = DIR == 0 ? mv.haloFPtr[part + 1] : mv.haloBPtr[part + 1];
-      for (int h = h0 + threadIdx.x; h < h1; h += blockDim.x) {
+      for (int h = h0 + threadIdx.x; h < h1; h += NT) {
         const int row = hIdx[h];
-        double* dst = wS + 3 * (P + h - h0);
-        dst[0] = __ldcg(p.w + 3 * row);
-        dst[1] = __ldcg(p.w + 3 * row + 1);
-        dst[2] = __ldcg(p.w + 3 * row + 2);
+        const T a0 = __ldcg(p.w + 3 * row), a1 = __ldcg(p.w + 3 * row + 1),
+                a2 = __ldcg(p.w + 3 * row + 2);
+        T* dst = wS + 3 * (P + h - h0);
+        dst[0] = a0; dst[1] = a1; dst[2] = a2;
       }
     }
+    if (threadIdx.x == 0) rpS[nR] = e0 + nE;  // rpS holds absolute CSR offsets
+    cpAsyncWaitAll();
     __syncthreads();
-    const int l0 = mv.lvlOff[part], l1 = mv.lvlOff[part + 1];
-    double dot[3] = {0, 0, 0};
-    for (int li = 0; li < l1 - l0; ++li) {
-      const int lvl = DIR == 0 ? l0 + li : l1 - 1 - li;
-      const int r0 = mv.lvlStart[lvl] - pLo, r1 = mv.lvlStart[lvl + 1] - pLo;
-      for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-        const double rd = dS[i];
-        const int j0 = rpS[i], j1 = rpS[i + 1];
-        double v0, v1, v2;
+    Acc<T> dot0, dot1, dot2;
+    // Software pipeline over levels: each thread's first row of the next
+    // level has its static data (start value, coefficients, slots) read
+    // before the barrier that ends the current level, so after the barrier
+    // only the neighbour loads and the multiply-add chain remain.
+    RowPre<T> cur, nxt;
+    preRow<DIR>(cur, DIR == 0 ? 0 : nL - 1, lvS, rpS, loS, sS, aS, dS, rS, wS, pLo, e0);
+    for (int li = 0; li < nL; ++li) {
+      const int lvl = DIR == 0 ? li : nL - 1 - li;
+      if (li + 1 < nL) preRow<DIR>(nxt, DIR == 0 ? li + 1 : nL - 2 - li, lvS, rpS, loS, sS, aS, dS, rS, wS, pLo, e0);
+      if (cur.i >= 0) {
+        T v0 = cur.v0, v1 = cur.v1, v2 = cur.v2;
+        if (cur.n <= kPreEntries) {
+#pragma unroll
+          for (int q = 0; q < kPreEntries; ++q)
+            if (q < cur.n) {
+              const int sl = cur.sl[q];
+              const T a = cur.a[q];
+              v0 -= a * wS[3 * sl]; v1 -= a * wS[3 * sl + 1]; v2 -= a * wS[3 * sl + 2];
+            }
+        } else {
+          sweepRowGeneric<DIR>(cur.i, v0, v1, v2, rpS, loS, sS, aS, wS, e0);
+        }
+        if (DIR == 1) { dot0.add(v0 * cur.r0); dot1.add(v1 * cur.r1); dot2.add(v2 * cur.r2); }
+        wS[3 * cur.i] = v0; wS[3 * cur.i + 1] = v1; wS[3 * cur.i + 2] = v2;
+      }
+      // rows beyond the first NT of a wide level
+      const int r0 = lvS[lvl] - pLo, r1 = lvS[lvl + 1] - pLo;
+      for (int i = r0 + threadIdx.x + NT; i < r1; i += NT) {
+        T v0, v1, v2;
         if (DIR == 0) {
+          const T rd = dS[i];
           v0 = rd * rS[3 * i]; v1 = rd * rS[3 * i + 1]; v2 = rd * rS[3 * i + 2];
-          for (int j = j0; j < j1; ++j) {
-            const int sl = sS[j];
-            if (sl < 0) break;
-            const double tt = rd * vS[j];
-            v0 -= tt * wS[3 * sl]; v1 -= tt * wS[3 * sl + 1]; v2 -= tt * wS[3 * sl + 2];
-          }
         } else {
           v0 = wS[3 * i]; v1 = wS[3 * i + 1]; v2 = wS[3 * i + 2];
-          for (int j = j1 - 1; j >= j0; --j) {
-            const int sl = sS[j];
-            if (sl >= 0) break;
-            const int su = ~sl;
-            const double tt = rd * vS[j];
-            v0 -= tt * wS[3 * su]; v1 -= tt * wS[3 * su + 1]; v2 -= tt * wS[3 * su + 2];
-          }
-          dot[0] += v0 * rS[3 * i]; dot[1] += v1 * rS[3 * i + 1]; dot[2] += v2 * rS[3 * i + 2];
         }
+        sweepRowGeneric<DIR>(i, v0, v1, v2, rpS, loS, sS, aS, wS, e0);
+        if (DIR == 1) { dot0.add(v0 * rS[3 * i]); dot1.add(v1 * rS[3 * i + 1]); dot2.add(v2 * rS[3 * i + 2]); }
         wS[3 * i] = v0; wS[3 * i + 1] = v1; wS[3 * i + 2] = v2;
       }
+      cur = nxt;
       __syncthreads();
     }
-    // write the part back and publish it
-    for (int k = threadIdx.x; k < 3 * nR; k += blockDim.x) __stcg(p.w + 3 * (size_t)pLo + k, wS[k]);
+    // write the part back and publish it: barrier, then one gpu-scope fence
+    // and a release store by thread 0 (the cooperative-groups grid pattern)
+    for (int k = threadIdx.x; k < 3 * nR; k += NT) __stcg(p.w + 3 * (size_t)pLo + k, wS[k]);
     if (DIR == 1) {
-      blockSum<3>(dot, red);
+      double d3[3] = {dot0.value(), dot1.value(), dot2.value()};
+      blockSum<3>(d3, red);
       if (threadIdx.x == 0) {
         double* q = partials + 4 * (size_t)part;
-        q[0] = dot[0]; q[1] = dot[1]; q[2] = dot[2];
+        q[0] = d3[0]; q[1] = d3[1]; q[2] = d3[2];
       }
     }
-    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) stRelease(flags + part, epoch);
+    if (threadIdx.x == 0) {
+      __threadfence();
+      stRelease(flags + part, epoch);
+    }
     if (DIR == 1) {
       // the CTA completing the last part reduces the w.r products
       if (threadIdx.x == 0) sLast = (atomicAdd(&st->partsDone[1], 1u) == (unsigned)mv.nParts - 1);
@@ -227,24 +369,20 @@ kSweepSm(MeshView mv, PcgPtrs p, DevState* st, double* partials) {
   sweepEpilogue(st, DIR, epoch);
 }
 
-__global__ void kReciprocal(int n, double* rD) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) rD[i] = 1.0 / rD[i];
-}
-
 // diagonal preconditioner: w = rD r, with the w.r sums
+template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
-kDiagPrecond(MeshView mv, PcgPtrs p, DevState* st, double* partials) {
+kDiagPrecond(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   if (!st->pcgContinue) return;
   __shared__ double smem[32 * 3];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   double acc[3] = {0, 0, 0};
   if (s < mv.nC) {
-    const double rd = p.rD[s];
+    const T rd = p.rD[s];
     for (int k = 0; k < 3; ++k) {
-      double v = rd * p.r[3 * s + k];
+      const T v = rd * p.r[3 * s + k];
       p.w[3 * s + k] = v;
-      acc[k] = v * p.r[3 * s + k];
+      acc[k] = (double)(v * p.r[3 * s + k]);
     }
   }
   blockSum<3>(acc, smem);
@@ -264,39 +402,42 @@ kDiagPrecond(MeshView mv, PcgPtrs p, DevState* st, double* partials) {
     }
 }
 
-// p = w + beta p (first iteration: p = w), q = A p, and the p.q products.
-// Neighbour values of p are rebuilt from w and the previous p buffer, so one
-// kernel both updates the search direction and multiplies by A.
+// p = w (first iteration) or p = w + beta p
+template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
-kSpmvP(MeshView mv, PcgPtrs p, DevState* st, double* partials) {
+kPUpdate(MeshView mv, PcgPtrs<T> p, const DevState* st) {
+  if (!st->pcgContinue) return;
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= mv.nC) return;
+  for (int k = 0; k < 3; ++k) {
+    if (!st->active[k]) continue;
+    const T wv = p.w[3 * s + k];
+    p.p[3 * s + k] = st->nIter[k] == 0 ? wv : wv + (T)st->beta[k] * p.p[3 * s + k];
+  }
+}
+
+// q = A p and the p.q products.
+template <typename T>
+__global__ void __launch_bounds__(kRowBlock)
+kSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   if (!st->pcgContinue) return;
   __shared__ double smem[32 * 3];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const int par = st->pcgIter & 1;
-  const double* __restrict__ pold = p.p[par];
-  double* __restrict__ pnew = p.p[par ^ 1];
-  const double b0 = st->beta[0], b1 = st->beta[1], b2 = st->beta[2];
-  const bool f0 = st->nIter[0] == 0, f1 = st->nIter[1] == 0, f2 = st->nIter[2] == 0;
   double acc[3] = {0, 0, 0};
   if (s < mv.nC) {
-    const double dg = p.diag[s];
-    const double w0 = p.w[3 * s], w1 = p.w[3 * s + 1], w2 = p.w[3 * s + 2];
-    const double p0 = f0 ? w0 : w0 + b0 * pold[3 * s];
-    const double p1 = f1 ? w1 : w1 + b1 * pold[3 * s + 1];
-    const double p2 = f2 ? w2 : w2 + b2 * pold[3 * s + 2];
-    double y0 = dg * p0, y1 = dg * p1, y2 = dg * p2;
+    const T dg = p.diag[s];
+    const T p0 = p.p[3 * s], p1 = p.p[3 * s + 1], p2 = p.p[3 * s + 2];
+    T y0 = dg * p0, y1 = dg * p1, y2 = dg * p2;
     const int e1 = mv.rowptr[s + 1];
     for (int e = mv.rowptr[s]; e < e1; ++e) {
       const int cl = mv.col[e];
-      const double a = p.val[e];
-      const double n0 = p.w[3 * cl], n1 = p.w[3 * cl + 1], n2 = p.w[3 * cl + 2];
-      y0 += a * (f0 ? n0 : n0 + b0 * pold[3 * cl]);
-      y1 += a * (f1 ? n1 : n1 + b1 * pold[3 * cl + 1]);
-      y2 += a * (f2 ? n2 : n2 + b2 * pold[3 * cl + 2]);
+      const T a = p.val[e];
+      y0 += a * p.p[3 * cl]; y1 += a * p.p[3 * cl + 1]; y2 += a * p.p[3 * cl + 2];
     }
-    pnew[3 * s] = p0; pnew[3 * s + 1] = p1; pnew[3 * s + 2] = p2;
     p.q[3 * s] = y0; p.q[3 * s + 1] = y1; p.q[3 * s + 2] = y2;
-    acc[0] = y0 * p0; acc[1] = y1 * p1; acc[2] = y2 * p2;
+    Acc<T> a0, a1, a2;
+    a0.add(y0 * p0); a1.add(y1 * p1); a2.add(y2 * p2);
+    acc[0] = a0.value(); acc[1] = a1.value(); acc[2] = a2.value();
   }
   blockSum<3>(acc, smem);
   if (threadIdx.x == 0) {
@@ -321,22 +462,24 @@ kSpmvP(MeshView mv, PcgPtrs p, DevState* st, double* partials) {
 }
 
 // x += alpha p, r -= alpha q, residual sums and the convergence test.
+template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
-kUpdate(MeshView mv, Controls c, PcgPtrs p, DevState* st, double* partials) {
+kUpdate(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partials) {
   if (!st->pcgContinue) return;
   __shared__ double smem[32 * 3];
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const int par = st->pcgIter & 1;
-  const double* pnew = p.p[par ^ 1];
-  const bool a0 = st->active[0], a1 = st->active[1], a2 = st->active[2];
-  const double al0 = st->alpha[0], al1 = st->alpha[1], al2 = st->alpha[2];
   double acc[3] = {0, 0, 0};
   if (s < mv.nC) {
-    double r0 = p.r[3 * s], r1 = p.r[3 * s + 1], r2 = p.r[3 * s + 2];
-    if (a0) { p.x[3 * s] += al0 * pnew[3 * s]; r0 -= al0 * p.q[3 * s]; p.r[3 * s] = r0; }
-    if (a1) { p.x[3 * s + 1] += al1 * pnew[3 * s + 1]; r1 -= al1 * p.q[3 * s + 1]; p.r[3 * s + 1] = r1; }
-    if (a2) { p.x[3 * s + 2] += al2 * pnew[3 * s + 2]; r2 -= al2 * p.q[3 * s + 2]; p.r[3 * s + 2] = r2; }
-    acc[0] = fabs(r0); acc[1] = fabs(r1); acc[2] = fabs(r2);
+    for (int k = 0; k < 3; ++k) {
+      T rv = p.r[3 * s + k];
+      if (st->active[k]) {
+        const T al = (T)st->alpha[k];
+        p.x[3 * s + k] += al * p.p[3 * s + k];
+        rv -= al * p.q[3 * s + k];
+        p.r[3 * s + k] = rv;
+      }
+      acc[k] = (double)fabs(rv);
+    }
   }
   blockSum<3>(acc, smem);
   if (threadIdx.x == 0) {
@@ -363,11 +506,12 @@ kUpdate(MeshView mv, Controls c, PcgPtrs p, DevState* st, double* partials) {
   st->pcgContinue = any;
 }
 
+template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
-kAmul(MeshView mv, const double* val, const double* diag, const double* x, double* y) {
+kAmul(MeshView mv, const T* val, const T* diag, const T* x, T* y) {
   const int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= mv.nC) return;
-  double acc[3];
+  T acc[3];
   for (int k = 0; k < 3; ++k) acc[k] = diag[s] * x[3 * s + k];
   for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) {
     const int cl = mv.col[e];
@@ -378,64 +522,106 @@ kAmul(MeshView mv, const double* val, const double* diag, const double* x, doubl
 
 int rowGrid(const MeshView& mv) { return (mv.nC + kRowBlock - 1) / kRowBlock; }
 
-void launchSweeps(const MeshView& mv, const PcgPtrs& p, DevState* st, double* partials,
-                  int sweepGrid, cudaStream_t s) {
-  const size_t sm = sweepSmemBytes(mv);
-  kSweepSm<0><<<sweepGrid, kSweepSmBlock, sm, s>>>(mv, p, st, partials);
-  kSweepSm<1><<<sweepGrid, kSweepSmBlock, sm, s>>>(mv, p, st, partials);
+template <typename T>
+void launchSweeps(const MeshView& mv, const PcgPtrs<T>& p, DevState* st, double* partials,
+                  int sweepGrid, cudaStream_t s, LaunchTimer* tm) {
+  const size_t sm = sweepSmemBytes<T>(mv);
+  {
+    TimeScope ts(tm, S4G_K_SWEEP_FWD, s);
+    kSweepSm<0, kSweepSmBlock, T><<<sweepGrid, kSweepSmBlock, sm, s>>>(mv, p, st, partials);
+  }
+  {
+    TimeScope ts(tm, S4G_K_SWEEP_BWD, s);
+    kSweepSm<1, kSweepSmBlock, T><<<sweepGrid, kSweepSmBlock, sm, s>>>(mv, p, st, partials);
+  }
 }
 
 }  // namespace
 
+template <typename T>
 size_t sweepSmemBytes(const MeshView& mv) {
   const size_t P = mv.maxRows, H = mv.maxHalo, EM = mv.maxEntries;
-  return sizeof(double) * (3 * (P + H + 1) + 3 * P + P + EM) + sizeof(int) * (EM + P + 1);
+  return sizeof(T) * (3 * (P + H + 1) + 3 * P + P + EM) +
+         sizeof(int) * (EM + P + 1 + mv.maxLevels + 1 + P);
 }
 
-int sweepBlockThreads() { return kSweepSmBlock; }
-
+template <typename T>
 cudaError_t sweepPrepare(const MeshView& mv, int* blocksPerSM) {
-  const int sm = (int)sweepSmemBytes(mv);
-  cudaError_t e = cudaFuncSetAttribute(kSweepSm<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  const int sm = (int)sweepSmemBytes<T>(mv);
+  cudaError_t e = cudaFuncSetAttribute(kSweepSm<0, kSweepSmBlock, T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(kSweepSm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  e = cudaFuncSetAttribute(kSweepSm<1, kSweepSmBlock, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kSweepSm<0>, kSweepSmBlock, sm);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kSweepSm<0, kSweepSmBlock, T>,
+                                                       kSweepSmBlock, sm);
 }
 
-void launchDicFactor(const MeshView& mv, const PcgPtrs& p, DevState* st, int grid, cudaStream_t s) {
-  kSweepFactor<<<grid, kSweepBlock, 0, s>>>(mv, p, st);
-  kReciprocal<<<(mv.nC + 255) / 256, 256, 0, s>>>(mv.nC, p.rD);
+void launchDicFactor(const MeshView& mv, const double* val, const double* diag, double* rD,
+                     double* rDa, unsigned* flags, DevState* st, int grid, cudaStream_t s) {
+  kSweepFactor<<<grid, kSweepBlock, 0, s>>>(mv, val, diag, rD, flags, st);
+  kFactorFinish<<<rowGrid(mv), kRowBlock, 0, s>>>(mv, val, rD, rDa);
 }
 
-void launchPcgIteration(const MeshView& mv, const Controls& c, const PcgPtrs& p, DevState* st,
-                        double* partials, int sweepGrid, cudaStream_t s, long long* launches) {
+void launchReciprocal(int n, const double* diag, double* rD, cudaStream_t s) {
+  kReciprocal<<<(n + 255) / 256, 256, 0, s>>>(n, diag, rD);
+}
+
+void launchToFloat(size_t n, const double* in, float* out, cudaStream_t s) {
+  if (n) kToFloat<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, in, out);
+}
+
+template <typename T>
+void launchPcgIteration(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
+                        double* partials, int sweepGrid, cudaStream_t s, long long* launches,
+                        LaunchTimer* tm) {
   const int g = rowGrid(mv);
   if (c.precond == 0) {
-    launchSweeps(mv, p, st, partials, sweepGrid, s);
+    launchSweeps(mv, p, st, partials, sweepGrid, s, tm);
     *launches += 2;
   } else {
-    kDiagPrecond<<<g, kRowBlock, 0, s>>>(mv, p, st, partials);
+    TimeScope ts(tm, S4G_K_DIAG, s);
+    kDiagPrecond<T><<<g, kRowBlock, 0, s>>>(mv, p, st, partials);
     *launches += 1;
   }
-  kSpmvP<<<g, kRowBlock, 0, s>>>(mv, p, st, partials);
-  kUpdate<<<g, kRowBlock, 0, s>>>(mv, c, p, st, partials);
-  *launches += 2;
+  {
+    TimeScope ts(tm, S4G_K_PUPDATE, s);
+    kPUpdate<T><<<g, kRowBlock, 0, s>>>(mv, p, st);
+  }
+  {
+    TimeScope ts(tm, S4G_K_SPMV, s);
+    kSpmv<T><<<g, kRowBlock, 0, s>>>(mv, p, st, partials);
+  }
+  {
+    TimeScope ts(tm, S4G_K_UPDATE, s);
+    kUpdate<T><<<g, kRowBlock, 0, s>>>(mv, c, p, st, partials);
+  }
+  *launches += 3;
 }
 
-void launchReciprocal(int n, double* rD, cudaStream_t s) {
-  kReciprocal<<<(n + 255) / 256, 256, 0, s>>>(n, rD);
+template <typename T>
+void launchAmul(const MeshView& mv, const T* val, const T* diag, const T* x, T* y, cudaStream_t s) {
+  kAmul<T><<<rowGrid(mv), kRowBlock, 0, s>>>(mv, val, diag, x, y);
 }
 
-void launchAmul(const MeshView& mv, const double* val, const double* diag, const double* x,
-                double* y, cudaStream_t s) {
-  kAmul<<<rowGrid(mv), kRowBlock, 0, s>>>(mv, val, diag, x, y);
-}
-
-void launchPrecondOnly(const MeshView& mv, const Controls& c, const PcgPtrs& p, DevState* st,
+template <typename T>
+void launchPrecondOnly(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                        double* partials, int sweepGrid, cudaStream_t s) {
-  if (c.precond == 0) launchSweeps(mv, p, st, partials, sweepGrid, s);
-  else kDiagPrecond<<<rowGrid(mv), kRowBlock, 0, s>>>(mv, p, st, partials);
+  if (c.precond == 0) launchSweeps(mv, p, st, partials, sweepGrid, s, nullptr);
+  else kDiagPrecond<T><<<rowGrid(mv), kRowBlock, 0, s>>>(mv, p, st, partials);
 }
+
+#define S4G_INSTANTIATE(T)                                                                        \
+  template size_t sweepSmemBytes<T>(const MeshView&);                                              \
+  template cudaError_t sweepPrepare<T>(const MeshView&, int*);                                     \
+  template void launchPcgIteration<T>(const MeshView&, const Controls&, const PcgPtrs<T>&,         \
+                                      DevState*, double*, int, cudaStream_t, long long*,           \
+                                      LaunchTimer*);                                               \
+  template void launchAmul<T>(const MeshView&, const T*, const T*, const T*, T*, cudaStream_t);    \
+  template void launchPrecondOnly<T>(const MeshView&, const Controls&, const PcgPtrs<T>&,          \
+                                     DevState*, double*, int, cudaStream_t);
+S4G_INSTANTIATE(double)
+S4G_INSTANTIATE(float)
+#undef S4G_INSTANTIATE
 
 }  // namespace s4g

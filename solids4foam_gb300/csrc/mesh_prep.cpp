@@ -412,6 +412,10 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
   }
 
   // ---- 8. shared-memory staging tables of the sweeps
+  hp.lowCnt.assign(nC, 0);
+  for (int s = 0; s < nC; ++s)
+    for (int k = hp.rowptr[s]; k < hp.rowptr[s + 1]; ++k)
+      if (hp.col[k] < s) hp.lowCnt[s]++;
   hp.maxRows = 0; hp.maxHalo = 0; hp.maxEntries = 0;
   for (int p = 0; p < hp.nParts; ++p) {
     hp.maxRows = std::max(hp.maxRows, hp.partStart[p + 1] - hp.partStart[p]);

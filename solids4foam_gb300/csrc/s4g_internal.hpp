@@ -42,6 +42,7 @@ struct HostPrep {
   // column: local row index, maxRows + halo index, or the zero slot for an
   // entry a subdomain DIC ignores.  Lower entries >= 0, upper entries ~slot.
   std::vector<int> haloFPtr, haloFIdx, haloBPtr, haloBIdx, slot;
+  std::vector<int> lowCnt;  // per row: number of lower entries (they come first)
   int maxRows = 0, maxHalo = 0, maxEntries = 0;
 };
 

@@ -18,6 +18,7 @@ that reaches nCorrectors without converging returns its result and sets
 from __future__ import annotations
 
 import ctypes as ct
+import weakref
 
 import numpy as np
 
@@ -36,15 +37,20 @@ RENUMBER = {"none": _lib.RENUMBER_NONE, "RCM": _lib.RENUMBER_RCM, "tiled": _lib.
 class Context:
     """One GPU (s4g_ctx)."""
 
-    def __init__(self, device: int = 0, verbose: bool = False):
+    def __init__(self, device: int = 0, verbose: bool = False, profile: bool = False):
         self.L = _lib.lib()
         h = ct.c_void_p()
-        opts = _lib.CtxOpts(device, 1 if verbose else 0)
+        opts = _lib.CtxOpts(device, 1 if verbose else 0, 1 if profile else 0)
         _lib.check(self.L.s4g_ctx_create(ct.byref(h), ct.byref(opts)), "s4g_ctx_create")
         self.h = h
+        self.models = weakref.WeakSet()
 
     def close(self):
+        """Destroys the context; the library frees meshes still alive, and
+        the Python models of those meshes are marked closed first."""
         if self.h:
+            for m in list(self.models):
+                m.h = None
             self.L.s4g_ctx_destroy(self.h)
             self.h = None
 
@@ -94,6 +100,7 @@ class SolidModel:
         _lib.check(self.L.s4g_mesh_upload(ctx.h, ct.byref(d), ct.byref(opts), ct.byref(h)),
                    "s4g_mesh_upload")
         self.h = h
+        ctx.models.add(self)
         self.set_law(law)
         names = list(mesh.get("patch_names", PATCHES))
         for name, spec in bcs.items():
@@ -101,9 +108,9 @@ class SolidModel:
         self.set_controls(solver or {}, outer or {}, precision)
 
     def close(self):
-        if self.h:
+        if self.h and self.ctx.h:
             self.L.s4g_mesh_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -178,6 +185,12 @@ class SolidModel:
         _lib.check(self.L.s4g_mesh_get_permutation(self.h, perm.ctypes.data),
                    "s4g_mesh_get_permutation")
         return perm
+
+    def parts(self):
+        """Scheduling part (DIC subdomain with dic_subdomains) of each cell."""
+        part = np.zeros(self.n_cells, np.int32)
+        _lib.check(self.L.s4g_mesh_get_parts(self.h, part.ctypes.data), "s4g_mesh_get_parts")
+        return part
 
     def info(self):
         inf = _lib.MeshInfo()

@@ -1,0 +1,37 @@
+"""GPU parity of the processor-local (decomposed) DIC: the DIC restricted to
+the library's scheduling parts, against the oracle given the same cell
+decomposition -- what a decomposed OpenFOAM run with one processor per part
+computes."""
+import numpy as np
+import pytest
+
+import solids4foam_gb300 as sg
+from solids4foam_gb300.cases import oracle_bcs
+from oracle import pyoracle
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("precision", ["FP64", "FP32_REFINE"])
+def test_decomposed_dic_matches_oracle(ctx, precision):
+    m = sg.box_mesh(12, 12, 12, 1.0, 1.0, 1.0, 0.2, 9)
+    bcs = {"zmin": ("fixedDisplacement", None, None),
+           "zmax": ("solidTraction", None, np.full(int(m["patch_size"][5]), 1e7))}
+    model = sg.SolidModel(ctx, m, dict(type="linearElastic", E=70e9, nu=0.33), bcs,
+                          outer=dict(nCorrectors=2000), precision=precision, part_size=128,
+                          dic_subdomains=True)
+    D, sig, perf = model.evolve()
+    perm, parts = model.permutation(), model.parts()
+    assert len(set(parts.tolist())) == model.info()["n_parts"] > 1
+    Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=perm, dic_domain=parts, E=70e9,
+                                   nu=0.33, n_correctors=2000)
+    assert perf["converged"] == 1 and po["converged"] == 1
+    assert rel(D, Do) < 1e-6 and rel(sig, so) < 1e-5
+    if precision == "FP64":
+        assert perf["total_lin_iters"] == po["total_lin_iters"]
+        assert rel(D, Do) < 1e-12
+    model.close()

@@ -1,0 +1,134 @@
+"""CPU tests of the C ABI library: it loads, exports every declared symbol,
+and its host-side logic (mesh generation, validation, DIC ordering and
+scheduling) is correct.  No compute call needs a GPU here."""
+import ctypes as ct
+import os
+import re
+
+import numpy as np
+import pytest
+
+import solids4foam_gb300 as sg
+from solids4foam_gb300 import _lib
+from solids4foam_gb300.solid_model import _desc, plan
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    txt = open(os.path.join(ROOT, "include", "s4g.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(s4g_[A-Za-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(built):
+    L = _lib.lib()
+    names = _declared()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(_lib.declared_symbols())
+    assert L.s4g_abi_version() == 1
+    assert L.s4g_status_str(_lib.NOT_CONVERGED) == b"NOT_CONVERGED"
+
+
+def test_box_mesh_geometry(built):
+    m = sg.box_mesh(7, 5, 4, 1.4, 1.0, 0.8, 0.2, 3)
+    nC = m["V"].shape[0]
+    assert np.isclose(m["V"].sum(), 1.4 * 1.0 * 0.8, rtol=1e-12)
+    # closed cells: outward areas sum to zero
+    acc = np.zeros((nC, 3))
+    ni = m["neighbour"].shape[0]
+    np.add.at(acc, m["owner"], m["Sf"])
+    np.add.at(acc, m["neighbour"], -m["Sf"][:ni])
+    assert np.abs(acc).max() < 1e-14
+    # upper-triangular face order
+    own = m["owner"][:ni]
+    assert np.all(own < m["neighbour"])
+    key = own.astype(np.int64) * nC + m["neighbour"]
+    assert np.all(np.diff(key) > 0)
+    # boundary patches planar and outward
+    for k, (ax, side) in enumerate([(0, 0), (0, 1), (1, 0), (1, 1), (2, 0), (2, 1)]):
+        s, n = m["patch_start"][k], m["patch_size"][k]
+        nrm = m["Sf"][s:s + n] / np.linalg.norm(m["Sf"][s:s + n], axis=1)[:, None]
+        assert np.allclose(nrm[:, ax], 1.0 if side else -1.0)
+    # jitter is seeded and stays inside +-0.2 h
+    m2 = sg.box_mesh(7, 5, 4, 1.4, 1.0, 0.8, 0.2, 3)
+    assert np.array_equal(m["C"], m2["C"])
+    m3 = sg.box_mesh(7, 5, 4, 1.4, 1.0, 0.8, 0.2, 4)
+    assert not np.array_equal(m["C"], m3["C"])
+
+
+@pytest.mark.parametrize("renumber", ["none", "RCM", "tiled"])
+@pytest.mark.parametrize("shape", [(8, 8, 8), (20, 3, 5), (1, 1, 40)])
+def test_plan_is_a_permutation_with_topological_parts(built, renumber, shape):
+    m = sg.box_mesh(*shape, 1.0, 1.0, 1.0, 0.1, 1)
+    n = m["V"].shape[0]
+    perm, info = plan(m, renumber, part_size=64)
+    assert sorted(perm.tolist()) == list(range(n))
+    assert info["n_cells"] == n
+    assert 1 <= info["part_depth"] <= info["n_parts"]
+    assert info["n_levels_global"] >= 1
+    if renumber == "none":
+        assert np.array_equal(perm, np.arange(n))
+
+
+def test_tiled_order_has_shallow_part_dag(built):
+    m = sg.box_mesh(32, 32, 32, 1.0, 1.0, 1.0, 0.2, 1)
+    _, tiled = plan(m, "tiled", part_size=512)
+    _, natural = plan(m, "none", part_size=512)
+    assert tiled["part_depth"] <= 10
+    assert natural["part_depth"] > 5 * tiled["part_depth"]
+
+
+def test_rcm_reduces_bandwidth(built):
+    m = sg.box_mesh(12, 12, 12, 1.0, 1.0, 1.0, 0.0, 1)
+    rng = np.random.default_rng(2)
+    shuffle = rng.permutation(m["V"].shape[0])
+    from oracle.pyoracle import renumber_mesh
+    ms = renumber_mesh(m, shuffle)
+    perm, _ = plan(ms, "RCM")
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(perm.shape[0])
+    bw_rcm = np.abs(inv[ms["owner"][:ms["neighbour"].shape[0]]] - inv[ms["neighbour"]]).max()
+    bw_shuffled = np.abs(ms["owner"][:ms["neighbour"].shape[0]] - ms["neighbour"]).max()
+    assert bw_rcm < bw_shuffled / 4
+
+
+def test_invalid_meshes_are_rejected(built):
+    L = _lib.lib()
+    m = sg.box_mesh(3, 3, 3, 1.0, 1.0, 1.0, 0.0, 1)
+    bad = dict(m)
+    bad["neighbour"] = m["neighbour"].copy()
+    bad["neighbour"][0] = 999
+    keep = []
+    d = _desc(bad, keep)
+    assert L.s4g_mesh_plan(ct.byref(d), None, None, None) == _lib.BAD_ARG
+    assert b"neighbour" in L.s4g_last_error()
+    bad = dict(m)
+    bad["V"] = m["V"].copy()
+    bad["V"][3] = -1.0
+    d = _desc(bad, keep)
+    assert L.s4g_mesh_plan(ct.byref(d), None, None, None) == _lib.BAD_ARG
+    bad = dict(m)
+    bad["C"] = m["C"].copy()
+    bad["C"][0, 0] = np.nan
+    d = _desc(bad, keep)
+    assert L.s4g_mesh_plan(ct.byref(d), None, None, None) == _lib.BAD_ARG
+    bad = dict(m)
+    bad["patch_size"] = m["patch_size"].copy()
+    bad["patch_size"][2] += 1
+    d = _desc(bad, keep)
+    assert L.s4g_mesh_plan(ct.byref(d), None, None, None) == _lib.BAD_ARG
+    # box generator refuses inverting jitter and bad sizes
+    assert L.s4g_box_mesh_build(2, 2, 2, 1.0, 1.0, 1.0, 0.7, 1, *([None] * 9)) == _lib.BAD_ARG
+
+
+def test_no_device_is_reported_without_gpu(built):
+    """Without a GPU the context refuses to start: no CPU fallback."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(sg.S4GError) as e:
+        sg.Context(0)
+    assert e.value.status == _lib.NO_DEVICE

@@ -1,0 +1,169 @@
+"""CPU tests of the FP64 oracle: the reference's known answers and the
+properties its discretisation must have (no GPU needed)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+import solids4foam_gb300 as sg
+from solids4foam_gb300.cases import oracle_bcs
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+@pytest.fixture(scope="module")
+def patch():
+    with open(os.path.join(HERE, "golden", "patch_test.json")) as f:
+        return json.load(f)
+
+
+def _linear_field(p, X):
+    a = np.asarray(p["a"])
+    b = np.asarray(p["b"])
+    return a + X @ b.T
+
+
+def _patch_bcs(mesh, p):
+    bcs = []
+    for k in range(6):
+        s, n = int(mesh["patch_start"][k]), int(mesh["patch_size"][k])
+        bcs.append((0, _linear_field(p, mesh["Cf"][s:s + n]), None))
+    return bcs
+
+
+def _strain(G):
+    G = G.reshape(-1, 3, 3)
+    return 0.5 * (G + G.transpose(0, 2, 1))
+
+
+@pytest.mark.parametrize("jitter,lsdelta", [(0.0, 0), (0.25, 1)])
+def test_patch_test_constant_strain(patch, jitter, lsdelta):
+    """patchTest: a linear displacement on every boundary gives the constant
+    strain of the reference's README (exx 2e-6, eyy 6e-6, exy 4e-6), to
+    round-off, on a distorted mesh once the least-squares boundary vectors
+    are consistent (full Cf - C), and on an orthogonal mesh with either."""
+    m = sg.box_mesh(6, 5, 4, 1.0, 0.9, 0.8, jitter, 3)
+    D, sig, G, perf = pyoracle.solve(m, _patch_bcs(m, patch), E=patch["E"], nu=patch["nu"],
+                                     n_correctors=400, solution_tol=1e-13,
+                                     alternative_tol=1e-14, tolerance=1e-15, rel_tol=0.0,
+                                     ls_boundary_delta=lsdelta)
+    eps = _strain(G)
+    exp = patch["expected_strain"]
+    for (i, j), key in {(0, 0): "xx", (1, 1): "yy", (0, 1): "xy", (2, 2): "zz"}.items():
+        np.testing.assert_allclose(eps[:, i, j], exp[key], atol=1e-15, rtol=1e-8)
+    np.testing.assert_allclose(D, _linear_field(patch, m["C"]), atol=1e-15, rtol=1e-8)
+    # stresses constant too
+    assert np.ptp(sig, axis=0).max() < 1e-6 * np.abs(sig).max()
+
+
+def test_patch_test_normal_delta_distorted_is_close(patch):
+    """With OpenFOAM.com/.org patch-normal boundary deltas the leastSquares
+    gradient is not exact next to distorted boundaries (the reference README
+    warns about this); the error stays small."""
+    m = sg.box_mesh(6, 5, 4, 1.0, 0.9, 0.8, 0.25, 3)
+    D, sig, G, perf = pyoracle.solve(m, _patch_bcs(m, patch), E=patch["E"], nu=patch["nu"],
+                                     n_correctors=300, solution_tol=1e-12,
+                                     alternative_tol=1e-13, tolerance=1e-15, rel_tol=0.0)
+    eps = _strain(G)
+    assert abs(eps[:, 0, 0].mean() - 2e-6) < 0.05 * 2e-6
+
+
+def test_matrix_symmetric_positive(patch):
+    m = sg.box_mesh(5, 4, 3, 1.0, 1.0, 1.0, 0.2, 5)
+    bcs = [(0, None, None)] + [(1, None, None)] * 5
+    diag, upper = pyoracle.matrix(m, bcs, 1.0)
+    n = diag.shape[0]
+    A = np.diag(diag)
+    own, nei = m["owner"][:upper.shape[0]], m["neighbour"]
+    A[own, nei] = upper
+    A[nei, own] = upper
+    assert np.allclose(A, A.T)
+    assert np.linalg.eigvalsh(A).min() > 0
+    # rows of cells away from fixed patches sum to zero (negSumDiag)
+    fixed_cells = set(m["owner"][m["patch_start"][0]:m["patch_start"][0] + m["patch_size"][0]])
+    interior = [c for c in range(n) if c not in fixed_cells]
+    assert np.abs(A[interior].sum(1)).max() < 1e-12 * diag.max()
+    # DIC is the exact solve for a 1-row system and a contraction otherwise
+    x = np.random.default_rng(1).standard_normal(n)
+    w = pyoracle.dic(m, diag, upper, A @ x)
+    assert np.linalg.norm(w - x) < np.linalg.norm(x)
+
+
+def test_renumbered_oracle_equals_permuted_mesh():
+    """Running with perm equals running on the renumbered mesh, bit for bit."""
+    m = sg.box_mesh(5, 4, 4, 1.0, 1.0, 1.0, 0.2, 9)
+    bcs = oracle_bcs(m, {"zmin": ("fixedDisplacement", None, None),
+                         "zmax": ("solidTraction", None, np.full(int(m["patch_size"][5]), 1e6))})
+    perm = np.random.default_rng(0).permutation(m["V"].shape[0]).astype(np.int32)
+    D1, s1, _, p1 = pyoracle.solve(m, bcs, perm=perm, E=70e9, nu=0.33, n_correctors=30)
+    mr = pyoracle.renumber_mesh(m, perm)
+    D2, s2, _, p2 = pyoracle.solve(mr, bcs, E=70e9, nu=0.33, n_correctors=30)
+    assert np.array_equal(D1[perm], D2)
+    assert np.array_equal(s1[perm], s2)
+
+
+def test_cantilever_tip_deflection_trend():
+    """Tip deflection of a cantilever under end shear approaches the
+    Euler-Bernoulli + Timoshenko estimate as the mesh is refined
+    (cantileverAnalyticalSolution is the reference's own check)."""
+    E, nu, L, h, P = 200e9, 0.3, 2.0, 0.2, 1e6 * 0.2 * 0.2
+    I = h ** 4 / 12
+    G = E / (2 * (1 + nu))
+    exact = P * L ** 3 / (3 * E * I) + P * L / (5.0 / 6.0 * G * h * h)
+    tips = []
+    for nx, ny in ((20, 2), (40, 4)):
+        m = sg.box_mesh(nx, ny, ny, L, h, h, 0.0, 1)
+        ps = m["patch_size"]
+        bcs = [(0, None, None), (1, np.tile([0, -1e6, 0], (int(ps[1]), 1)), None)] + [(1, None, None)] * 4
+        D, _, _, perf = pyoracle.solve(m, bcs, E=E, nu=nu, n_correctors=30000,
+                                       solution_tol=1e-6)
+        tips.append(-D[np.argmax(m["C"][:, 0] - 1e-9 * m["C"][:, 1]), 1])
+    assert abs(tips[1] - exact) < abs(tips[0] - exact)
+    assert abs(tips[1] - exact) / exact < 0.15
+
+
+def test_fixed_point_residual_small():
+    """At convergence D_new = D_old, so fvm and fvc laplacians cancel and
+    the correction of one more corrector is tiny."""
+    m = sg.box_mesh(6, 6, 6, 1.0, 1.0, 1.0, 0.2, 4)
+    bcs = oracle_bcs(m, {"zmin": ("fixedDisplacement", None, None),
+                         "zmax": ("solidTraction", None, np.full(int(m["patch_size"][5]), 1e7))})
+    D1, _, _, p1 = pyoracle.solve(m, bcs, E=70e9, nu=0.33, n_correctors=5000,
+                                  solution_tol=1e-10, alternative_tol=1e-11)
+    assert p1["converged"] == 1
+    D2, _, _, _ = pyoracle.solve(m, bcs, E=70e9, nu=0.33, n_correctors=p1["n_correctors"] + 5,
+                                 solution_tol=0, alternative_tol=0)
+    assert np.linalg.norm(D2 - D1) / np.linalg.norm(D1) < 1e-8
+
+
+def test_oracle_regression_fixture():
+    """The oracle still reproduces its committed outputs."""
+    g = np.load(os.path.join(HERE, "golden", "oracle_small.npz"))
+    m = sg.box_mesh(6, 5, 4, 1.2, 1.0, 0.8, 0.2, 11)
+    ps = m["patch_size"]
+    bcs = {"zmin": ("fixedDisplacement", None, None),
+           "zmax": ("solidTraction", np.tile([1e5, 0.0, -2e5], (int(ps[5]), 1)),
+                    np.full(int(ps[5]), 3e5))}
+    D, sig, G, perf = pyoracle.solve(m, oracle_bcs(m, bcs), E=70e9, nu=0.33, n_correctors=50)
+    np.testing.assert_allclose(D, g["lin_D"], rtol=1e-12, atol=1e-22)
+    np.testing.assert_allclose(sig, g["lin_sigma"], rtol=1e-10, atol=1e-6)
+    assert perf["total_lin_iters"] == int(g["lin_iters"])
+
+
+def test_tl_small_strain_matches_linear():
+    """Total Lagrangian neo-Hookean under a tiny load reduces to linear
+    elasticity with the same mu, K."""
+    m = sg.box_mesh(5, 4, 4, 1.0, 0.8, 0.8, 0.15, 12)
+    ps = m["patch_size"]
+    t = np.tile([0.0, 1e2, 0.0], (int(ps[5]), 1))
+    bcs = [(1, None, None)] * 4 + [(0, None, None), (1, t, None)]
+    mu, K = 1e6, 2e7
+    E = 9 * K * mu / (3 * K + mu)
+    nu = (3 * K - 2 * mu) / (2 * (3 * K + mu))
+    Dl, _, _, _ = pyoracle.solve(m, bcs, E=E, nu=nu, n_correctors=3000, solution_tol=1e-10,
+                                 alternative_tol=1e-11)
+    Dn, _, _, _ = pyoracle.solve(m, bcs, model=1, law=1, use_mu_K=1, mu=mu, K=K,
+                                 n_correctors=3000, solution_tol=1e-10, alternative_tol=1e-11)
+    assert np.linalg.norm(Dn - Dl) / np.linalg.norm(Dl) < 1e-3
