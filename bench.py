@@ -1,17 +1,20 @@
 #!/usr/bin/env python
 """Benchmark of the segregated finite-volume solid solve on GB300.
 
-One step is one full solve of the plain-FP64 benchmark case: the 128^3
-jittered unit cube (2,097,152 hex cells, interior vertices jittered +-0.2 h,
+One step is one full solve of the benchmark case: the 128^3 jittered unit cube (2,097,152 hex cells, interior vertices jittered +-0.2 h,
 seed 1), linear elastic E = 70 GPa, nu = 0.33, bottom fixed, top pressure
 10 MPa, sides traction-free, linearGeometryTotalDisplacement with PCG+DIC
 (tol 1e-9, relTol 0.1) and outer tolerance 1e-6 / 2000 correctors -- run to
-convergence through the library's public API.  Inputs are synthetic
+convergence through the library's public API.  By default the inner solves
+run in FP32 with FP64 refinement and the DIC factor is processor-local over
+the library's cell parts (the preconditioner of a decomposed run); one plain
+FP64 solve of the same case is timed beside it.  Inputs are synthetic
 (generated from the seed), the working set (about 1.7 GB) is far larger than
 L2, so no L2 flush is needed between steps.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
-                  [--precision FP64|FP32_REFINE] [--n 128] [--dic exact|decomposed]
+                  [--precision FP32_REFINE|FP64] [--n 128] [--dic decomposed|exact]
+                  [--no-fp64] [--no-cpu] [--e2e-steps 1]
 
 --impl reference times the CPU FP64 oracle (the restatement of the
 reference's solve; the reference itself needs an OpenFOAM installation that
@@ -39,7 +42,7 @@ METRIC = ("solves/s + p50/p99 latency (FP32+refine batched vs plain FP64), 1 GB3
 # Correctors the 128^3 benchmark case takes to converge (solutionTolerance
 # 1e-6), measured with the GPU path; the CPU sample is scaled to a full solve
 # with it when the GPU run is not in the same process.
-FULL_SOLVE_CORRECTORS_128 = None
+FULL_SOLVE_CORRECTORS_128 = 799
 
 
 def peaks():
@@ -181,7 +184,7 @@ def cpu_sample(case, n_correctors_full, sample_s=20.0, threads=None):
     threads; returns (solves/s scaled to a full solve, details)."""
     from oracle import pyoracle
     from solids4foam_gb300.cases import oracle_bcs
-    threads = threads or os.cpu_count() or 1
+    threads = threads or len(os.sched_getaffinity(0)) or 1
     bcs = oracle_bcs(case["mesh"], case["bcs"])
     law = case["law"]
     # first a 1-corrector probe to size the sample
@@ -294,6 +297,20 @@ def run_gb300(args):
                            if tot_n[k] and algorithmic_bytes(k, nC, nI, nB, v) else None)}
                for k in tot_ms if tot_n[k]}
 
+    # plain FP64 solve of the same case, for the FP32+refine comparison
+    fp64 = None
+    if args.precision != "FP64" and not args.no_fp64:
+        kw64 = dict(kw, precision="FP64")
+        m64 = sg.SolidModel(ctx, mesh, case["law"], case["bcs"], **kw64)
+        D64, s64, p64 = m64.evolve()
+        m64.close()
+        relD = float(np.linalg.norm(D - D64) / np.linalg.norm(D64))
+        relS = float(np.linalg.norm(sig - s64) / np.linalg.norm(s64))
+        fp64 = {"solves_per_s": 1000.0 / p64["solve_ms"], "ms_per_solve": p64["solve_ms"],
+                "n_correctors": p64["n_correctors"], "pcg_iterations": p64["total_lin_iters"],
+                "speedup_of_fp32_refine": p64["solve_ms"] / ms_step,
+                "rel_l2_D_fp32_vs_fp64": relD, "rel_l2_sigma_fp32_vs_fp64": relS}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cv, info = cpu_sample(case, perfs[0]["n_correctors"], sample_s=args.cpu_sample_s)
@@ -312,6 +329,7 @@ def run_gb300(args):
                    "model": "linearGeometryTotalDisplacement", "law": "linearElastic",
                    "solver": "PCG+DIC tol 1e-9 relTol 0.1", "outer": "solutionTolerance 1e-6, "
                    "nCorrectors 2000", "precision": args.precision, "dic": args.dic,
+                   "dic_subdomains": model.info()["n_parts"] if args.dic == "decomposed" else 1,
                    "parallelism": f"replicas{world}",
                    "l2": "working set ~1.7 GB >> 129 MB L2 (no flush needed)",
                    "n_correctors": p0["n_correctors"], "converged": p0["converged"],
@@ -324,6 +342,7 @@ def run_gb300(args):
                      "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": ab, "avg_launch_us": avg_ms * 1000},
         "kernels": kernels,
+        "plain_fp64": fp64,
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
@@ -336,8 +355,10 @@ def main():
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--precision", default="FP64", choices=["FP64", "FP32_REFINE"])
-    ap.add_argument("--dic", default="exact", choices=["exact", "decomposed"])
+    ap.add_argument("--precision", default="FP32_REFINE", choices=["FP64", "FP32_REFINE"])
+    ap.add_argument("--dic", default="decomposed", choices=["exact", "decomposed"])
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the plain-FP64 comparison solve")
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)

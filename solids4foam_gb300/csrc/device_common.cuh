@@ -34,6 +34,7 @@ struct MeshView {
   const int* slot;
   const int* lowCnt;   // lower entries per row
   int maxRows, maxHalo, maxEntries, maxLevels;
+  int rowGrid;         // blocks of the grid-stride row kernels
 };
 
 // Material and solver constants of a solve.
@@ -281,15 +282,23 @@ __device__ __forceinline__ void reducePartialsMax(const double* partials, int st
   blockMax<N>(out, smem);
 }
 
-// Every thread publishes its writes, then one thread takes a ticket; true in
-// all threads of the block that arrived last.
+// Thread 0 has written the block's partial record; it publishes it with one
+// gpu-scope fence and takes a ticket.  True in all threads of the block that
+// arrived last (which then reads every block's record).
 __device__ __forceinline__ bool lastBlockDone(unsigned* counter, unsigned total) {
   __shared__ int amLast;
-  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) amLast = (atomicAdd(counter, 1u) == total - 1);
+  if (threadIdx.x == 0) {
+    __threadfence();
+    amLast = (atomicAdd(counter, 1u) == total - 1);
+  }
   __syncthreads();
+  if (amLast) __threadfence();
   return amLast != 0;
 }
+
+// Grid of the row kernels: a few resident blocks per SM, rows in a
+// grid-stride loop, so the per-launch finalize reads few partial records.
+constexpr int kRowBlocksPerSM = 4;
 
 }  // namespace s4g

@@ -51,10 +51,11 @@ struct Ctx {
 // CUDA-event timer of each kernel kind on the library's stream.  Events are
 // resolved after the host waits on the stream anyway (between launch batches).
 struct EventTimer : LaunchTimer {
-  struct Pending { int kind; cudaEvent_t a, b; };
+  struct Pending { int kind; int tag; cudaEvent_t a, b; };
   std::vector<cudaEvent_t> pool;
   std::vector<Pending> pending;
   cudaEvent_t open = nullptr;
+  int tag = -1;  // PCG iteration index of the launches being recorded (-1: not PCG)
   double ms[S4G_K_KINDS] = {};
   long long count[S4G_K_KINDS] = {};
   ~EventTimer() {
@@ -78,12 +79,14 @@ struct EventTimer : LaunchTimer {
   void after(int kind, cudaStream_t s) override {
     cudaEvent_t b = get();
     cudaEventRecord(b, s);
-    pending.push_back({kind, open, b});
+    pending.push_back({kind, tag, open, b});
   }
-  void resolve() {
+  // Launches of PCG iterations at or past keepBelow ran as no-ops (the
+  // device had already stopped the loop) and are not counted.
+  void resolve(int keepBelow = 1 << 30) {
     for (auto& p : pending) {
       float t = 0;
-      if (cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) {
+      if (p.tag < keepBelow && cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) {
         ms[p.kind] += t;
         count[p.kind] += 1;
       }
@@ -229,6 +232,8 @@ struct Engine {
 
     mv.nC = nC; mv.nI = nI; mv.nB = nB; mv.nParts = hp.nParts;
     mv.subdomains = (o && o->dic_subdomains) ? 1 : 0;
+    mv.rowGrid = std::max(1, std::min((nC + kRowBlock - 1) / kRowBlock,
+                                      ctx->numSMs * kRowBlocksPerSM));
     mv.rowptr = dRow; mv.col = dCol; mv.fidx = dFidx; mv.fown = dFown; mv.fnei = dFnei;
     mv.fS = geo.fS; mv.fmagS = geo.fmagS; mv.fw = geo.fw; mv.fdelta = geo.fdelta;
     mv.C = geo.C; mv.invDd = geo.invDd;
@@ -472,10 +477,10 @@ struct Engine {
     return S4G_OK;
   }
 
-  s4g_status readState() {
+  s4g_status readState(int pcgBase = -1) {
     S4G_CUDA(cudaMemcpyAsync(hState, dState, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
     S4G_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (ctx->profile) timer.resolve();
+    if (ctx->profile) timer.resolve(pcgBase >= 0 ? hState->pcgIter - pcgBase : 1 << 30);
     return S4G_OK;
   }
 
@@ -509,15 +514,20 @@ struct Engine {
   // PCG loop of one corrector: launch batches, read the device decision.
   template <typename T>
   s4g_status pcgLoop(const Controls& c, const PcgPtrs<T>& p, int grid) {
-    // profiling steps one iteration at a time, so no timed launch is idle
-    int chunk = ctx->profile ? 1 : 2;
+    // Iterations are launched in growing batches; the launches after the
+    // device's stop decision return at once.
+    int chunk = 2, launched = 0;
+    const int base = hState->pcgIter;
     for (int guard = 0; guard < 1000000; ++guard) {
-      for (int i = 0; i < chunk; ++i)
+      for (int i = 0; i < chunk; ++i) {
+        timer.tag = launched++;
         launchPcgIteration<T>(mv, c, p, dState, dPartials, grid, ctx->stream, &launches, tm());
+      }
+      timer.tag = -1;
       S4G_CUDA(cudaGetLastError());
-      S4G_TRY(readState());
+      S4G_TRY(readState(base));
       if (!hState->pcgContinue || (hState->status & (kErrTimeout | kErrNaN))) return S4G_OK;
-      if (!ctx->profile) chunk = std::min(chunk * 2, 16);
+      chunk = std::min(chunk * 2, 16);
     }
     return setErr(S4G_TIMEOUT, "PCG loop did not end");
   }

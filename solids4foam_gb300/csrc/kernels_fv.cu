@@ -188,15 +188,14 @@ __global__ void __launch_bounds__(kRowBlock)
 kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* st,
       double* partials, int mode) {
   __shared__ double smem[32 * 6];
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
   const int dc = st->dcur;
   const double* Uold = f.D[dc];
   double* Unew = f.D[dc ^ 1];
   const bool apply = (mode == 1);
-  double red[6] = {0, 0, 0, 0, 0, 0};  // max|x|, max|U-D0|, max|U|, sum U
-  double mx[3] = {0, 0, 0};
+  double red[6] = {0, 0, 0, 0, 0, 0};  // sum U
+  double mx[3] = {0, 0, 0};            // max|x|, max|U-D0|, max|U|
   double minJ = 1e300, maxJ = -1e300;
-  if (s < mv.nC) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x) {
     V3 Up = ldV(Uold, s);
     if (apply) Up = Up + ldVT(x, s);
     const bool hasB = mv.browptr[s + 1] > mv.browptr[s];
@@ -270,10 +269,10 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
     if (apply) {
       stV(Unew, s, Up);
       V3 xs = ldVT(x, s);
-      mx[0] = mag(xs);
-      mx[1] = c.tl ? mag(Up) : mag(Up - ldV(f.D0, s));
-      mx[2] = mag(Up);
-      red[0] = Up.x; red[1] = Up.y; red[2] = Up.z;
+      mx[0] = fmax(mx[0], mag(xs));
+      mx[1] = fmax(mx[1], c.tl ? mag(Up) : mag(Up - ldV(f.D0, s)));
+      mx[2] = fmax(mx[2], mag(Up));
+      red[0] += Up.x; red[1] += Up.y; red[2] += Up.z;
       if (!(isfinite(Up.x) && isfinite(Up.y) && isfinite(Up.z))) atomicOr(&st->status, kErrNaN);
     }
   }
@@ -369,11 +368,10 @@ __global__ void __launch_bounds__(kRowBlock)
 kRhs(MeshView mv, Controls c, FieldPtrs f, T* __restrict__ x, T* __restrict__ r,
      DevState* st, double* partials) {
   __shared__ double smem[32 * 6];
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
   const double* U = f.D[st->dcur];
   double part[6] = {0, 0, 0, 0, 0, 0};  // normFactor (3), sum|R| (3)
   const int el = c.tl ? st->enforceLinear : 1;
-  if (s < mv.nC) {
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x) {
     const V3 Us = ldV(U, s);
     const V3 Cs = ldV(mv.C, s);
     const T9 Gs = ldT(f.G, s);
@@ -434,8 +432,8 @@ kRhs(MeshView mv, Controls c, FieldPtrs f, T* __restrict__ x, T* __restrict__ r,
     const double md[3] = {MD.x, MD.y, MD.z}, rr[3] = {R.x, R.y, R.z};
     for (int k = 0; k < 3; ++k) {
       double t = sumA * xb[k];
-      part[k] = fabs(md[k] - t) + fabs(md[k] + rr[k] - t);
-      part[3 + k] = fabs(rr[k]);
+      part[k] += fabs(md[k] - t) + fabs(md[k] + rr[k] - t);
+      part[3 + k] += fabs(rr[k]);
     }
   }
   blockSum<6>(part, smem);
@@ -522,16 +520,15 @@ void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const
                 DevState* st, double* partials, int mode, cudaStream_t s, LaunchTimer* tm) {
   const int grid = (mv.nC + kRowBlock - 1) / kRowBlock;
   TimeScope ts(tm, S4G_K_POST, s);
-  kPost<T><<<grid, kRowBlock, 0, s>>>(mv, c, f, x, st, partials, mode);
+  kPost<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, c, f, x, st, partials, mode);
   if (c.tl && mode == 1) kPostLawTL<<<grid, kRowBlock, 0, s>>>(mv, c, f, st);
 }
 
 template <typename T>
 void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, T* x, T* r,
                DevState* st, double* partials, cudaStream_t s, LaunchTimer* tm) {
-  const int grid = (mv.nC + kRowBlock - 1) / kRowBlock;
   TimeScope ts(tm, S4G_K_RHS, s);
-  kRhs<T><<<grid, kRowBlock, 0, s>>>(mv, c, f, x, r, st, partials);
+  kRhs<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, c, f, x, r, st, partials);
 }
 
 template void launchPost<double>(const MeshView&, const Controls&, const FieldPtrs&, const double*,

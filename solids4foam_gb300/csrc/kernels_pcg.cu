@@ -369,22 +369,26 @@ kSweepSm(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   sweepEpilogue(st, DIR, epoch);
 }
 
+// Row kernels: grid-stride loops over a few resident blocks per SM; the
+// block that finishes last reduces the per-block records in a fixed order.
+#define S4G_ROWS(s) for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; \
+                         s += gridDim.x * blockDim.x)
+
 // diagonal preconditioner: w = rD r, with the w.r sums
 template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
 kDiagPrecond(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   if (!st->pcgContinue) return;
   __shared__ double smem[32 * 3];
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[3] = {0, 0, 0};
-  if (s < mv.nC) {
+  Acc<T> a0, a1, a2;
+  S4G_ROWS(s) {
     const T rd = p.rD[s];
-    for (int k = 0; k < 3; ++k) {
-      const T v = rd * p.r[3 * s + k];
-      p.w[3 * s + k] = v;
-      acc[k] = (double)(v * p.r[3 * s + k]);
-    }
+    const T r0 = p.r[3 * s], r1 = p.r[3 * s + 1], r2 = p.r[3 * s + 2];
+    const T w0 = rd * r0, w1 = rd * r1, w2 = rd * r2;
+    p.w[3 * s] = w0; p.w[3 * s + 1] = w1; p.w[3 * s + 2] = w2;
+    a0.add(w0 * r0); a1.add(w1 * r1); a2.add(w2 * r2);
   }
+  double acc[3] = {a0.value(), a1.value(), a2.value()};
   blockSum<3>(acc, smem);
   if (threadIdx.x == 0) {
     double* q = partials + 4 * (size_t)blockIdx.x;
@@ -407,12 +411,18 @@ template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
 kPUpdate(MeshView mv, PcgPtrs<T> p, const DevState* st) {
   if (!st->pcgContinue) return;
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= mv.nC) return;
+  bool act[3], first[3];
+  T b[3];
   for (int k = 0; k < 3; ++k) {
-    if (!st->active[k]) continue;
-    const T wv = p.w[3 * s + k];
-    p.p[3 * s + k] = st->nIter[k] == 0 ? wv : wv + (T)st->beta[k] * p.p[3 * s + k];
+    act[k] = st->active[k] != 0; first[k] = st->nIter[k] == 0; b[k] = (T)st->beta[k];
+  }
+  S4G_ROWS(s) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      if (!act[k]) continue;
+      const T wv = p.w[3 * s + k];
+      p.p[3 * s + k] = first[k] ? wv : wv + b[k] * p.p[3 * s + k];
+    }
   }
 }
 
@@ -422,9 +432,8 @@ __global__ void __launch_bounds__(kRowBlock)
 kSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   if (!st->pcgContinue) return;
   __shared__ double smem[32 * 3];
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[3] = {0, 0, 0};
-  if (s < mv.nC) {
+  Acc<T> a0, a1, a2;
+  S4G_ROWS(s) {
     const T dg = p.diag[s];
     const T p0 = p.p[3 * s], p1 = p.p[3 * s + 1], p2 = p.p[3 * s + 2];
     T y0 = dg * p0, y1 = dg * p1, y2 = dg * p2;
@@ -435,10 +444,9 @@ kSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
       y0 += a * p.p[3 * cl]; y1 += a * p.p[3 * cl + 1]; y2 += a * p.p[3 * cl + 2];
     }
     p.q[3 * s] = y0; p.q[3 * s + 1] = y1; p.q[3 * s + 2] = y2;
-    Acc<T> a0, a1, a2;
     a0.add(y0 * p0); a1.add(y1 * p1); a2.add(y2 * p2);
-    acc[0] = a0.value(); acc[1] = a1.value(); acc[2] = a2.value();
   }
+  double acc[3] = {a0.value(), a1.value(), a2.value()};
   blockSum<3>(acc, smem);
   if (threadIdx.x == 0) {
     double* q = partials + 4 * (size_t)blockIdx.x;
@@ -467,20 +475,23 @@ __global__ void __launch_bounds__(kRowBlock)
 kUpdate(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partials) {
   if (!st->pcgContinue) return;
   __shared__ double smem[32 * 3];
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[3] = {0, 0, 0};
-  if (s < mv.nC) {
+  bool act[3];
+  T al[3];
+  for (int k = 0; k < 3; ++k) { act[k] = st->active[k] != 0; al[k] = (T)st->alpha[k]; }
+  Acc<T> acc3[3];
+  S4G_ROWS(s) {
+#pragma unroll
     for (int k = 0; k < 3; ++k) {
       T rv = p.r[3 * s + k];
-      if (st->active[k]) {
-        const T al = (T)st->alpha[k];
-        p.x[3 * s + k] += al * p.p[3 * s + k];
-        rv -= al * p.q[3 * s + k];
+      if (act[k]) {
+        p.x[3 * s + k] += al[k] * p.p[3 * s + k];
+        rv -= al[k] * p.q[3 * s + k];
         p.r[3 * s + k] = rv;
       }
-      acc[k] = (double)fabs(rv);
+      acc3[k].add(fabs(rv));
     }
   }
+  double acc[3] = {acc3[0].value(), acc3[1].value(), acc3[2].value()};
   blockSum<3>(acc, smem);
   if (threadIdx.x == 0) {
     double* q = partials + 4 * (size_t)blockIdx.x;
@@ -520,7 +531,7 @@ kAmul(MeshView mv, const T* val, const T* diag, const T* x, T* y) {
   for (int k = 0; k < 3; ++k) y[3 * s + k] = acc[k];
 }
 
-int rowGrid(const MeshView& mv) { return (mv.nC + kRowBlock - 1) / kRowBlock; }
+int rowGrid(const MeshView& mv) { return mv.rowGrid; }
 
 template <typename T>
 void launchSweeps(const MeshView& mv, const PcgPtrs<T>& p, DevState* st, double* partials,
@@ -560,7 +571,7 @@ cudaError_t sweepPrepare(const MeshView& mv, int* blocksPerSM) {
 void launchDicFactor(const MeshView& mv, const double* val, const double* diag, double* rD,
                      double* rDa, unsigned* flags, DevState* st, int grid, cudaStream_t s) {
   kSweepFactor<<<grid, kSweepBlock, 0, s>>>(mv, val, diag, rD, flags, st);
-  kFactorFinish<<<rowGrid(mv), kRowBlock, 0, s>>>(mv, val, rD, rDa);
+  kFactorFinish<<<(mv.nC + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, val, rD, rDa);
 }
 
 void launchReciprocal(int n, const double* diag, double* rD, cudaStream_t s) {
@@ -601,7 +612,7 @@ void launchPcgIteration(const MeshView& mv, const Controls& c, const PcgPtrs<T>&
 
 template <typename T>
 void launchAmul(const MeshView& mv, const T* val, const T* diag, const T* x, T* y, cudaStream_t s) {
-  kAmul<T><<<rowGrid(mv), kRowBlock, 0, s>>>(mv, val, diag, x, y);
+  kAmul<T><<<(mv.nC + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, val, diag, x, y);
 }
 
 template <typename T>
