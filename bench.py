@@ -108,13 +108,21 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_bytes(kind, n_cells, n_faces, n_bfaces, v):
+def algorithmic_bytes(kind, n_cells, n_faces, n_bfaces, v, n_loc=0):
     """Minimal DRAM bytes of one launch of a kernel kind (k = 3 columns,
     v = value bytes, 4-byte indices); the formulas follow the solve's
     scope table: SpMV nnz(v+i) + 4(N+1) + 2Nvk; one DIC sweep
-    nnz_L(v+i) + 4(N+1) + Nv + 2Nvk (+ Nvk for the backward w.r sums)."""
+    nnz_L(v+i) + 4(N+1) + Nv + 2Nvk (+ Nvk for the backward w.r sums).
+    Fused processor-local iteration: loc_precond reads r, q, p, x and
+    writes r, x, w (7Nvk) plus rD (Nv), the in-part table (n_loc entries of
+    v + 2 bytes) and 4 bytes of row metadata per row; loc_spmv reads w and
+    p_old, writes p_new and q (4Nvk), plus the matrix nnz(v+i) + Nv + 4(N+1)."""
     N, F, B, k = n_cells, n_faces, n_bfaces, 3
     nnz_l = F
+    if kind == "loc_precond":
+        return 7 * N * v * k + N * v + n_loc * (v + 2) + 4 * N
+    if kind == "loc_spmv":
+        return 4 * N * v * k + 2 * F * (v + 4) + N * v + 4 * (N + 1)
     if kind == "sweep_fwd":
         return nnz_l * (v + 4) + 4 * (N + 1) + N * v + 2 * N * v * k
     if kind == "sweep_bwd":
@@ -285,16 +293,17 @@ def run_gb300(args):
     dom = max(tot_ms, key=lambda k: tot_ms[k])
     peak, peak_kind = peaks()
     avg_ms = tot_ms[dom] / max(1, tot_n[dom])
-    ab = algorithmic_bytes(dom, nC, nI, nB, v)
+    n_loc = model.info()["n_local_entries"]
+    ab = algorithmic_bytes(dom, nC, nI, nB, v, n_loc)
     achieved = ab / (avg_ms * 1e-3) / 1e9 if ab else None
     workload = f"cube{args.n}_{args.precision.lower()}_{args.dic}"
     traffic = load_traffic(workload).get(dom)
     kernels = {k: {"launches": tot_n[k], "ms_total": round(tot_ms[k], 3),
                    "share": round(tot_ms[k] / max(1e-9, sum(tot_ms.values())), 4),
                    "avg_us": round(1000 * tot_ms[k] / max(1, tot_n[k]), 2),
-                   "gbs": (round(algorithmic_bytes(k, nC, nI, nB, v) /
+                   "gbs": (round(algorithmic_bytes(k, nC, nI, nB, v, n_loc) /
                                  (tot_ms[k] / max(1, tot_n[k]) * 1e-3) / 1e9, 1)
-                           if tot_n[k] and algorithmic_bytes(k, nC, nI, nB, v) else None)}
+                           if tot_n[k] and algorithmic_bytes(k, nC, nI, nB, v, n_loc) else None)}
                for k in tot_ms if tot_n[k]}
 
     # plain FP64 solve of the same case, for the FP32+refine comparison

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define S4G_ABI_VERSION 1
+#define S4G_ABI_VERSION 2
 
 /* Status codes.  Reference convention for errors is FatalError (abort), see
  * src/solids4FoamModels/solidModels/solidModel/solidModel.C:1735-1742; a
@@ -80,7 +80,9 @@ enum {
   S4G_K_PUPDATE = 5,   /* p = w + beta p */
   S4G_K_SPMV = 6,      /* q = A p */
   S4G_K_UPDATE = 7,    /* x, r update and residual */
-  S4G_K_KINDS = 8
+  S4G_K_LOC_PRECOND = 8, /* fused x, r update + processor-local DIC (both sweeps) */
+  S4G_K_LOC_SPMV = 9,  /* fused p = w + beta p and q = A p */
+  S4G_K_KINDS = 10
 };
 
 /* Creates a context on one GPU.  Stands in for the per-run state the
@@ -137,6 +139,8 @@ typedef struct s4g_mesh_info {
   int max_local_levels;   /* deepest in-part level count */
   int n_levels_global;    /* level count of the whole lower-triangular DAG */
   long long device_bytes; /* device memory held by this mesh */
+  long long n_local_entries; /* processor-local DIC table entries (with padding);
+                                0 unless dic_subdomains */
 } s4g_mesh_info;
 
 /* Uploads the mesh once: validation, renumbering, cell-to-face CSR in the

@@ -18,7 +18,9 @@
 //                       .../fixedDisplacement/fixedDisplacementFvPatchVectorField.C:258-356;
 //                       numerics/patchCorrectionVectors/patchCorrectionVectors.C:24-36
 // OpenFOAM operators (third-party, not in the tree; written from the published
-// finite-volume formulation; conventions listed in oracle/CONVENTIONS.md):
+// finite-volume formulation, with the conventions: linear weights
+// |S.(C_N-C_f)|/(|S.(C_f-C_P)|+|S.(C_N-C_f)|), deltaCoeffs 1/max(n.d, 0.05|d|),
+// boundary deltaCoeffs 1/(n.(C_f-C_P)), RhieChow gamma = 0 on boundary faces):
 // fvm/fvc::laplacian Gauss linear corrected, fvc::div Gauss linear,
 // leastSquares gradient with boundary snGrad correction, linear interpolation,
 // PCG with DIC and OpenFOAM's residual normalisation.

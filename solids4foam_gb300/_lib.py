@@ -28,7 +28,8 @@ class CtxOpts(ct.Structure):
 
 
 # kernel kinds of the per-kernel timers (S4G_K_*)
-KERNEL_KINDS = ("rhs", "post", "sweep_fwd", "sweep_bwd", "diag", "p_update", "spmv", "update")
+KERNEL_KINDS = ("rhs", "post", "sweep_fwd", "sweep_bwd", "diag", "p_update", "spmv", "update",
+                "loc_precond", "loc_spmv")
 
 
 class MeshDesc(ct.Structure):
@@ -49,7 +50,8 @@ class MeshInfo(ct.Structure):
     _fields_ = [("n_cells", ct.c_int), ("n_internal_faces", ct.c_int),
                 ("n_boundary_faces", ct.c_int), ("n_parts", ct.c_int),
                 ("part_depth", ct.c_int), ("max_local_levels", ct.c_int),
-                ("n_levels_global", ct.c_int), ("device_bytes", ct.c_longlong)]
+                ("n_levels_global", ct.c_int), ("device_bytes", ct.c_longlong),
+                ("n_local_entries", ct.c_longlong)]
 
 
 class Law(ct.Structure):

@@ -35,6 +35,10 @@ struct MeshView {
   const int* lowCnt;   // lower entries per row
   int maxRows, maxHalo, maxEntries, maxLevels;
   int rowGrid;         // blocks of the grid-stride row kernels
+  // processor-local DIC tables (see HostPrep)
+  const int* locEntStart; const int* locSrc; const uint16_t* locIdx;
+  const int* locMetaStart; const uint32_t* locMeta;
+  int maxLocEntries, maxLocMeta;
 };
 
 // Material and solver constants of a solve.
@@ -73,6 +77,10 @@ struct DevState {
   int nIter[3];
   double normFactor[3], initRes[3], finalRes[3];
   double wArA[3], wApA[3], alpha[3], beta[3];
+  // fused (processor-local DIC) iteration: an update x += alpha p,
+  // r -= alpha q is pending per component; which p buffer is the newest
+  int pending[3];
+  int pbuf;
   // error bits
   unsigned status;
   // last-block counters (one per kernel kind)

@@ -130,6 +130,10 @@ struct Engine {
   bool fp32Allocated = false;
   bool fp32Valid = false;  // FP32 copies match the FP64 matrix/factor
   int sweepGrid32 = 1;
+  // processor-local DIC path (subdomain runs with DIC)
+  int nLoc = 0;
+  int* dLocSrc = nullptr;
+  int localGrid = 1, localGrid32 = 1;
   DevState* dState = nullptr;
   DevState* hState = nullptr;  // pinned
   double* dPartials = nullptr;
@@ -297,7 +301,7 @@ struct Engine {
     S4G_TRY(alloc(&dState, 1));
     S4G_CUDA(cudaMallocHost((void**)&hState, sizeof(DevState)));
     const size_t rowBlocks = (nC + kRowBlock - 1) / kRowBlock;
-    S4G_TRY(alloc(&dPartials, std::max(8 * rowBlocks, 4 * (size_t)hp.nParts)));
+    S4G_TRY(alloc(&dPartials, std::max(8 * rowBlocks, 8 * (size_t)hp.nParts)));
     S4G_TRY(alloc(&dOut, 9 * (size_t)nC));
     S4G_CUDA(cudaMemsetAsync(dState, 0, sizeof(DevState), s));
 
@@ -311,6 +315,30 @@ struct Engine {
     sweepGrid = std::max(1, std::min(hp.nParts, perSM * ctx->numSMs));
     S4G_CUDA(sweepPrepare<float>(mv, &perSM));
     sweepGrid32 = std::max(1, std::min(hp.nParts, std::max(1, perSM) * ctx->numSMs));
+    if (mv.subdomains) {
+      nLoc = (int)hp.locSrc.size();
+      int *dEs, *dMs;
+      uint16_t* dIdx;
+      uint32_t* dMeta;
+      S4G_TRY(upload(&dLocSrc, hp.locSrc));
+      S4G_TRY(upload(&dEs, hp.locEntStart));
+      S4G_TRY(upload(&dMs, hp.locMetaStart));
+      S4G_TRY(upload(&dIdx, hp.locIdx));
+      S4G_TRY(upload(&dMeta, hp.locMeta));
+      mv.locSrc = dLocSrc; mv.locEntStart = dEs; mv.locMetaStart = dMs;
+      mv.locIdx = dIdx; mv.locMeta = dMeta;
+      mv.maxLocEntries = hp.maxLocEntries; mv.maxLocMeta = hp.maxLocMeta;
+      if (localSmemBytes<double>(mv) + 2048 > (size_t)maxSmem)
+        return setErr(S4G_BAD_ARG, "a DIC part does not fit in shared memory; use a smaller part_size");
+      S4G_CUDA(localPrepare<double>(mv, &perSM));
+      localGrid = std::max(1, std::min(hp.nParts, std::max(1, perSM) * ctx->numSMs));
+      S4G_CUDA(localPrepare<float>(mv, &perSM));
+      localGrid32 = std::max(1, std::min(hp.nParts, std::max(1, perSM) * ctx->numSMs));
+      S4G_TRY(alloc(&pc.p2, 3 * (size_t)nC));
+      double* lc;
+      S4G_TRY(alloc(&lc, (size_t)nLoc));
+      pc.lcoef = lc;
+    }
     S4G_CUDA(cudaStreamSynchronize(s));
     // caller geometry is no longer needed
     for (double* p : {dCc, dCfc, dSfc}) {
@@ -438,6 +466,10 @@ struct Engine {
       S4G_CUDA(cudaMemcpyAsync(dRD, dDiag, sizeof(double) * hp.nC, cudaMemcpyDeviceToDevice, s));
       launchDicFactor(mv, dVal, dDiag, dRD, dRDa, pc.flags[0], dState, sweepGrid, s);
       launches += 2;
+      if (mv.subdomains) {
+        launchLocalGather<double>(nLoc, dLocSrc, dRDa, const_cast<double*>(pc.lcoef), s);
+        launches++;
+      }
     } else {
       launchReciprocal(hp.nC, dDiag, dRD, s);  // diagonalPreconditioner: rD = 1/diag
       launches++;
@@ -462,6 +494,12 @@ struct Engine {
       S4G_TRY(alloc(&pc32.x, 3 * nC)); S4G_TRY(alloc(&pc32.r, 3 * nC)); S4G_TRY(alloc(&pc32.w, 3 * nC));
       S4G_TRY(alloc(&pc32.p, 3 * nC)); S4G_TRY(alloc(&pc32.q, 3 * nC));
       pc32.flags[0] = pc.flags[0]; pc32.flags[1] = pc.flags[1];
+      if (mv.subdomains) {
+        float* lc;
+        S4G_TRY(alloc(&pc32.p2, 3 * nC));
+        S4G_TRY(alloc(&lc, (size_t)nLoc));
+        pc32.lcoef = lc;
+      }
       fp32Allocated = true;
     }
     if (!fp32Valid) {
@@ -471,6 +509,10 @@ struct Engine {
       launchToFloat(nC, dRD, const_cast<float*>(pc32.rD), s);
       launchToFloat(nE, dRDa, const_cast<float*>(pc32.rDa), s);
       launches += 4;
+      if (mv.subdomains) {
+        launchLocalGather<float>(nLoc, dLocSrc, dRDa, const_cast<float*>(pc32.lcoef), s);
+        launches++;
+      }
       S4G_CUDA(cudaGetLastError());
       fp32Valid = true;
     }
@@ -521,7 +563,10 @@ struct Engine {
     for (int guard = 0; guard < 1000000; ++guard) {
       for (int i = 0; i < chunk; ++i) {
         timer.tag = launched++;
-        launchPcgIteration<T>(mv, c, p, dState, dPartials, grid, ctx->stream, &launches, tm());
+        if (mv.subdomains && c.precond == 0)
+          launchLocalIteration<T>(mv, c, p, dState, dPartials, grid, ctx->stream, &launches, tm());
+        else
+          launchPcgIteration<T>(mv, c, p, dState, dPartials, grid, ctx->stream, &launches, tm());
       }
       timer.tag = -1;
       S4G_CUDA(cudaGetLastError());
@@ -581,8 +626,9 @@ struct Engine {
     Controls c = controls(tl);
     int nCorrTotal = 0;
     auto loop = [&](int isTl) -> s4g_status {
-      return mixed ? correctorLoop<float>(c, isTl, pc32, sweepGrid32)
-                   : correctorLoop<double>(c, isTl, pc, sweepGrid);
+      const bool local = mv.subdomains && c.precond == 0;
+      return mixed ? correctorLoop<float>(c, isTl, pc32, local ? localGrid32 : sweepGrid32)
+                   : correctorLoop<double>(c, isTl, pc, local ? localGrid : sweepGrid);
     };
     if (!tl) {
       launchTractionInit(mv, c, f, s);
@@ -858,6 +904,7 @@ s4g_status s4g_mesh_plan(const s4g_mesh_desc* desc, const s4g_mesh_opts* opts, i
     info->part_depth = hp.partDepth;
     info->max_local_levels = hp.maxLocalLevels;
     info->n_levels_global = hp.globalLevels;
+    info->n_local_entries = (long long)hp.locSrc.size();
   }
   return S4G_OK;
 }
@@ -873,6 +920,7 @@ s4g_status s4g_mesh_get_info(const s4g_mesh* mesh, s4g_mesh_info* info) {
   info->max_local_levels = hp.maxLocalLevels;
   info->n_levels_global = hp.globalLevels;
   info->device_bytes = (long long)mesh->e.bytes;
+  info->n_local_entries = (long long)hp.locSrc.size();
   return S4G_OK;
 }
 

@@ -85,6 +85,8 @@ struct PcgPtrs {
   const T* rDa;        // rD[row] * val[e] per CSR entry (FDIC coefficients)
   T* x; T* r; T* w; T* p; T* q;
   unsigned* flags[2];  // per-part sweep flags (forward, backward)
+  T* p2;               // second p buffer of the fused iteration
+  const T* lcoef;      // in-part FDIC coefficients (processor-local DIC tables)
 };
 
 // DIC factor in FP64: rD64 = 1/pivots by a scheduled forward sweep
@@ -113,5 +115,22 @@ void launchAmul(const MeshView& mv, const T* val, const T* diag, const T* x, T* 
 template <typename T>
 void launchPrecondOnly(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                        double* partials, int sweepGrid, cudaStream_t s);
+
+// ---- processor-local DIC PCG (kernels_local.cu) -----------------------------
+// Gathers the n in-part FDIC coefficients of the local tables from rDa (FP64):
+// lcoef[i] = rDa[src[i]], 0 where src[i] < 0 (padding).
+template <typename T>
+void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaStream_t s);
+// One fused PCG iteration (two kernels): [x, r update of the previous
+// iteration + residual test + processor-local DIC + w.r] and
+// [p = w + beta p, q = A p, p.q].
+template <typename T>
+void launchLocalIteration(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p,
+                          DevState* st, double* partials, int grid, cudaStream_t s,
+                          long long* launches, LaunchTimer* tm = nullptr);
+template <typename T>
+size_t localSmemBytes(const MeshView& mv);
+template <typename T>
+cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM);
 
 }  // namespace s4g

@@ -453,6 +453,7 @@ kRhs(MeshView mv, Controls c, FieldPtrs f, T* __restrict__ x, T* __restrict__ r,
     st->initRes[k] = S[3 + k] / nf;
     st->finalRes[k] = st->initRes[k];
     st->nIter[k] = 0;
+    st->pending[k] = 0;
     st->active[k] = (st->initRes[k] < c.tol) ? 0 : 1;
     st->wArA[k] = 1e20;
     any |= st->active[k];

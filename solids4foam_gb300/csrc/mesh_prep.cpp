@@ -465,6 +465,41 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
         }
     }
   }
+
+  // ---- 9. compact in-part tables of the processor-local DIC
+  hp.locEntStart.assign(1, 0); hp.locMetaStart.assign(1, 0);
+  hp.locSrc.clear(); hp.locIdx.clear(); hp.locMeta.clear();
+  hp.maxLocEntries = 0; hp.maxLocMeta = 0;
+  if (subdomains) {
+    for (int p = 0; p < hp.nParts; ++p) {
+      const int lo = hp.partStart[p], hi = hp.partStart[p + 1];
+      const size_t e0 = hp.locSrc.size();
+      if (hi - lo > 65535) { err = "part too large for the local DIC tables"; return S4G_BAD_ARG; }
+      for (int s = lo; s < hi; ++s) {
+        const int off = (int)(hp.locSrc.size() - e0);
+        int nl = 0, nu = 0;
+        for (int k = hp.rowptr[s]; k < hp.rowptr[s + 1]; ++k) {
+          const int c = hp.col[k];
+          if (c < s && c >= lo) { hp.locSrc.push_back(k); hp.locIdx.push_back((uint16_t)(c - lo)); ++nl; }
+        }
+        for (int k = hp.rowptr[s + 1] - 1; k >= hp.rowptr[s]; --k) {
+          const int c = hp.col[k];
+          if (c > s && c < hi) { hp.locSrc.push_back(k); hp.locIdx.push_back((uint16_t)(c - lo)); ++nu; }
+        }
+        if (off > 65535 || nl > 255 || nu > 255) {
+          err = "part too large for the local DIC tables; use a smaller part_size";
+          return S4G_BAD_ARG;
+        }
+        hp.locMeta.push_back((uint32_t)off | ((uint32_t)nl << 16) | ((uint32_t)nu << 24));
+      }
+      while ((hp.locSrc.size() - e0) % 8) { hp.locSrc.push_back(-1); hp.locIdx.push_back(0); }
+      while (hp.locMeta.size() % 4) hp.locMeta.push_back(0);
+      hp.locEntStart.push_back((int)hp.locSrc.size());
+      hp.locMetaStart.push_back((int)hp.locMeta.size());
+      hp.maxLocEntries = std::max(hp.maxLocEntries, hp.locEntStart[p + 1] - hp.locEntStart[p]);
+      hp.maxLocMeta = std::max(hp.maxLocMeta, hp.locMetaStart[p + 1] - hp.locMetaStart[p]);
+    }
+  }
   return S4G_OK;
 }
 

@@ -44,6 +44,18 @@ struct HostPrep {
   std::vector<int> haloFPtr, haloFIdx, haloBPtr, haloBIdx, slot;
   std::vector<int> lowCnt;  // per row: number of lower entries (they come first)
   int maxRows = 0, maxHalo = 0, maxEntries = 0;
+
+  // Processor-local DIC (subdomain runs only): per part, the in-part
+  // entries of each row, lower entries in CSR order then upper entries in
+  // reverse CSR order, as (CSR entry, local row) pairs.  Each part's range
+  // is padded to a multiple of 8 entries (padding: locSrc -1, locIdx 0) so
+  // that it can be staged with 16-byte copies.  locMeta per row, padded to a
+  // multiple of 4 per part: entry offset within the part (bits 0-15), lower
+  // count (16-23), upper count (24-31).
+  std::vector<int> locEntStart, locSrc, locMetaStart;
+  std::vector<uint16_t> locIdx;
+  std::vector<uint32_t> locMeta;
+  int maxLocEntries = 0, maxLocMeta = 0;
 };
 
 // Builds the preparation.  Returns S4G_OK or S4G_BAD_ARG with `err` set.

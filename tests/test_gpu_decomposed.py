@@ -37,3 +37,41 @@ def test_decomposed_dic_matches_oracle(ctx, precision):
         assert abs(perf["n_correctors"] - po["n_correctors"]) <= 1
         assert abs(perf["total_lin_iters"] - po["total_lin_iters"]) <= 0.005 * po["total_lin_iters"]
     model.close()
+
+
+def test_decomposed_tl_neo_hookean_matches_oracle(ctx):
+    """The fused processor-local iteration inside the total Lagrangian loop
+    (3 load increments), against the oracle with the same decomposition."""
+    m = sg.box_mesh(8, 6, 6, 1.0, 0.8, 0.8, 0.15, 12)
+    ps = m["patch_size"]
+    bcs = {"zmin": ("fixedDisplacement", None, None),
+           "zmax": ("solidTraction", np.tile([0.0, 2e5, 0.0], (int(ps[5]), 1)), None)}
+    law = dict(type="neoHookeanElastic", mu=1e6, K=2e7)
+    model = sg.SolidModel(ctx, m, law, bcs, model="nonLinearGeometryTotalLagrangian",
+                          outer=dict(nCorrectors=40), part_size=64, dic_subdomains=True)
+    D, sig, perf = model.evolve(n_increments=3)
+    Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=model.permutation(),
+                                   dic_domain=model.parts(), model=1, law=1, use_mu_K=1,
+                                   mu=1e6, K=2e7, n_correctors=40, n_increments=3)
+    assert abs(perf["n_correctors"] - po["n_correctors"]) <= 1
+    assert rel(D, Do) < 1e-6 and rel(sig, so) < 1e-5
+    model.close()
+
+
+def test_decomposed_ragged_parts(ctx):
+    """Small ragged parts (the smallest part size) and an uneven split still
+    match the oracle."""
+    m = sg.box_mesh(7, 5, 3, 1.0, 0.8, 0.6, 0.1, 4)
+    bcs = {"xmin": ("fixedDisplacement", None, None),
+           "xmax": ("solidTraction", np.tile([0.0, -1e5, 0.0], (int(m["patch_size"][1]), 1)), None)}
+    law = dict(type="linearElastic", E=1e9, nu=0.3)
+    for part in (32, 48):
+        model = sg.SolidModel(ctx, m, law, bcs, outer=dict(nCorrectors=3000), part_size=part,
+                              dic_subdomains=True)
+        D, sig, perf = model.evolve()
+        Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=model.permutation(),
+                                       dic_domain=model.parts(), E=1e9, nu=0.3,
+                                       n_correctors=3000)
+        assert perf["converged"] == 1 and po["converged"] == 1
+        assert rel(D, Do) < 1e-6 and rel(sig, so) < 1e-5
+        model.close()
