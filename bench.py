@@ -195,13 +195,9 @@ def cpu_sample(case, n_correctors_full, sample_s=20.0, threads=None):
     threads = threads or len(os.sched_getaffinity(0)) or 1
     bcs = oracle_bcs(case["mesh"], case["bcs"])
     law = case["law"]
-    # first a 1-corrector probe to size the sample
-    _, _, _, p1 = pyoracle.solve(case["mesh"], bcs, E=law["E"], nu=law["nu"], n_threads=threads,
-                                 max_correctors_run=1, n_correctors=2000)
-    per = max(p1["seconds"], 1e-3)
-    m = max(2, min(400, int(sample_s / per)))
+    # the oracle stops after the corrector that passes sample_s of wall time
     _, _, _, pm = pyoracle.solve(case["mesh"], bcs, E=law["E"], nu=law["nu"], n_threads=threads,
-                                 max_correctors_run=m, n_correctors=2000)
+                                 max_seconds=sample_s, n_correctors=2000)
     per_corr = pm["seconds"] / pm["n_correctors"]
     full = n_correctors_full or pm["n_correctors"]
     est = per_corr * full

@@ -831,6 +831,12 @@ struct Solver {
       }
       perf.n_correctors++;
       if (--correctorsLeft == 0) break;
+      if (s.max_seconds > 0 &&
+          std::chrono::duration<double>(std::chrono::steady_clock::now() - tStart).count() >
+              s.max_seconds) {
+        correctorsLeft = 0;
+        break;
+      }
     } while (!conv && ++iCorr < s.n_correctors);
     perf.initial_residual = initResMag;
     perf.rel_residual = relRes;
@@ -838,7 +844,10 @@ struct Solver {
     return conv;
   }
 
+  std::chrono::steady_clock::time_point tStart;
+
   void run() {
+    tStart = std::chrono::steady_clock::now();
     int left = s.max_correctors_run > 0 ? s.max_correctors_run : -1;
     if (!tl) {
       // Constructor: D.correctBoundaryConditions(); grad(D)
@@ -895,6 +904,8 @@ void orc_default_settings(orc_settings* s) {
   s->n_increments = 1;
   s->n_threads = 1;
   s->max_correctors_run = 0;
+  s->dic_domain = nullptr;
+  s->max_seconds = 0;
 }
 
 int orc_solve(const orc_mesh_desc* md, const orc_bc* bcs, const orc_settings* s,

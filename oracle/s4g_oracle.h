@@ -67,6 +67,8 @@ typedef struct {
   int max_correctors_run; /* >0: stop after this many correctors (timing samples) */
   const int* dic_domain;  /* optional [n_cells] subdomain of each cell (caller
                              order): DIC restricted to each subdomain */
+  double max_seconds;     /* >0: stop after the corrector that passes this wall
+                             time (bounded timing samples) */
 } orc_settings;
 
 typedef struct {

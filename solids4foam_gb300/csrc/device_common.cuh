@@ -26,6 +26,7 @@ struct MeshView {
   const int* browptr; const int* btype;                    // boundary faces by cell
   const double* bS; const double* bmagS; const double* bn; const double* bk;
   const double* bdelta; const double* bls;
+  const double* lsv;                                       // [2 nI][3] per CSR entry
   const double* bval; const double* bpress;                // BC data [nB][3], [nB]
   const int* partStart; const int* lvlOff; const int* lvlStart;
   const int* upPtr; const int* upIdx; const int* dnPtr; const int* dnIdx;

@@ -230,6 +230,7 @@ struct Engine {
     S4G_TRY(alloc(&geo.bk, 3 * (size_t)nB));
     S4G_TRY(alloc(&geo.bdelta, nB));
     S4G_TRY(alloc(&geo.bls, 3 * (size_t)nB));
+    S4G_TRY(alloc(&geo.lsv, 6 * (size_t)nI));
     S4G_TRY(alloc(&dBtype, nB));
     S4G_TRY(alloc(&dBval, 3 * (size_t)nB));
     S4G_TRY(alloc(&dBpress, nB));
@@ -244,6 +245,7 @@ struct Engine {
     mv.browptr = dBrow; mv.btype = dBtype;
     mv.bS = geo.bS; mv.bmagS = geo.bmagS; mv.bn = geo.bn; mv.bk = geo.bk;
     mv.bdelta = geo.bdelta; mv.bls = geo.bls; mv.bval = dBval; mv.bpress = dBpress;
+    mv.lsv = geo.lsv;
     mv.partStart = dPartStart; mv.lvlOff = dLvlOff; mv.lvlStart = dLvlStart;
     mv.upPtr = dUpPtr; mv.upIdx = dUpIdx; mv.dnPtr = dDnPtr; mv.dnIdx = dDnIdx;
     {
@@ -290,6 +292,7 @@ struct Engine {
     S4G_TRY(alloc(&f.Gb, 9 * (size_t)nB));
     S4G_TRY(alloc(&f.sigb, 6 * (size_t)nB));
     S4G_TRY(alloc(&f.g, 3 * (size_t)nB));
+    S4G_TRY(alloc(&f.flux, 6 * (size_t)nI));
     S4G_TRY(alloc(&pc.x, 3 * (size_t)nC));
     S4G_TRY(alloc(&pc.r, 3 * (size_t)nC));
     S4G_TRY(alloc(&pc.w, 3 * (size_t)nC));

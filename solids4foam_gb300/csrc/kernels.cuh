@@ -30,6 +30,7 @@ struct GeomOutputs {
   double* C; double* invDd;
   double* fS; double* fmagS; double* fw; double* fdelta;
   double* bS; double* bmagS; double* bn; double* bk; double* bdelta; double* bls;
+  double* lsv;  // [2 nI][3] leastSquares vector of each CSR entry
 };
 void launchGeometry(const MeshView& mv, const GeomInputs& in, const GeomOutputs& out,
                     cudaStream_t s);
@@ -53,6 +54,7 @@ struct FieldPtrs {
   double* Finv; double* Finvb; double* J; double* Jb;
   double* FL; double* FL0; double* FLb; double* FL0b;    // law's F and F.oldTime
   double* sig0; double* sig0b;                           // sigma.oldTime
+  double* flux;  // [nI][6] per internal face: owner-oriented flux of R and gamma|S|delta dU
 };
 
 // g = tractionBoundarySnGrad with the current sigma_b / grad_b (constructor).

@@ -117,6 +117,21 @@ __global__ void kGeomLs(MeshView mv, GeomOutputs out, const double* bd) {
   }
   S6 inv = invS(acc);
   stS(out.invDd, s, inv);
+  // per CSR entry, oriented so that grad += lsv (x) (U_nb - U_P) on both sides
+  for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) {
+    const V3 Cn = ldV(out.C, mv.col[e]);
+    V3 v;
+    if (mv.fidx[e] >= 0) {
+      const V3 d = Cn - Cs;
+      const double r = 1.0 / magSqr(d);
+      v = r * dotVS(d, inv);
+    } else {
+      const V3 d = Cs - Cn;
+      const double r = 1.0 / magSqr(d);
+      v = -r * dotVS(d, inv);
+    }
+    stV(out.lsv, e, v);
+  }
   for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
     V3 d = ldV(bd, b);
     stV(out.bls, b, (1.0 / magSqr(d)) * dotVS(d, inv));
@@ -178,6 +193,17 @@ __device__ __forceinline__ V3 boundaryValue(const MeshView& mv, const Controls& 
 }
 
 // --------------------------------------------------------- post-solve pass ---
+// D_new = D + x (the correction of the corrector; x in the PCG type).
+template <typename T>
+__global__ void __launch_bounds__(kRowBlock)
+kApplyX(MeshView mv, FieldPtrs f, const T* __restrict__ x, const DevState* st) {
+  const int dc = st->dcur;
+  const double* Uold = f.D[dc];
+  double* Unew = f.D[dc ^ 1];
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x)
+    stV(Unew, s, ldV(Uold, s) + ldVT(x, s));
+}
+
 // mode 0 (constructor): gradient only, from the current field.
 // mode 1 (corrector): apply the correction x, gradient, law, boundary, g.
 // For the TL model the law needs the global J check first, so mode 1 stops
@@ -189,36 +215,20 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
       double* partials, int mode) {
   __shared__ double smem[32 * 6];
   const int dc = st->dcur;
-  const double* Uold = f.D[dc];
-  double* Unew = f.D[dc ^ 1];
   const bool apply = (mode == 1);
+  // the corrected field D + x, written by kApplyX (mode 1), or D (mode 0)
+  const double* U = f.D[apply ? dc ^ 1 : dc];
   double red[6] = {0, 0, 0, 0, 0, 0};  // sum U
   double mx[3] = {0, 0, 0};            // max|x|, max|U-D0|, max|U|
   double minJ = 1e300, maxJ = -1e300;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x) {
-    V3 Up = ldV(Uold, s);
-    if (apply) Up = Up + ldVT(x, s);
+    const V3 Up = ldV(U, s);
     const bool hasB = mv.browptr[s + 1] > mv.browptr[s];
     T9 Gold = hasB ? ldT(f.G, s) : zeroT();
-    // leastSquares gradient (cell-centric; owner-oriented d and dU)
-    const S6 inv = ldS(mv.invDd, s);
-    const V3 Cs = ldV(mv.C, s);
+    // leastSquares gradient with the precomputed vectors of the cell's faces
     T9 acc = zeroT();
-    for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) {
-      const int nb = mv.col[e];
-      V3 Un = ldV(Uold, nb);
-      if (apply) Un = Un + ldVT(x, nb);
-      const V3 Cn = ldV(mv.C, nb);
-      if (mv.fidx[e] >= 0) {
-        V3 d = Cn - Cs;
-        double r = 1.0 / magSqr(d);
-        acc = acc + outer(r * dotVS(d, inv), Un - Up);
-      } else {
-        V3 d = Cs - Cn;
-        double r = 1.0 / magSqr(d);
-        acc = acc - outer(-r * dotVS(d, inv), Up - Un);
-      }
-    }
+    for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e)
+      acc = acc + outer(ldV(mv.lsv, e), ldV(U, mv.col[e]) - Up);
     for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
       V3 Ub = boundaryValue(mv, c, f, b, Up, Gold);
       acc = acc + outer(ldV(mv.bls, b), Ub - Up);
@@ -267,11 +277,11 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
       }
     }
     if (apply) {
-      stV(Unew, s, Up);
+      // maxima of squared magnitudes; the square root is taken once at the end
       V3 xs = ldVT(x, s);
-      mx[0] = fmax(mx[0], mag(xs));
-      mx[1] = fmax(mx[1], c.tl ? mag(Up) : mag(Up - ldV(f.D0, s)));
-      mx[2] = fmax(mx[2], mag(Up));
+      mx[0] = fmax(mx[0], magSqr(xs));
+      mx[1] = fmax(mx[1], c.tl ? magSqr(Up) : magSqr(Up - ldV(f.D0, s)));
+      mx[2] = fmax(mx[2], magSqr(Up));
       red[0] += Up.x; red[1] += Up.y; red[2] += Up.z;
       if (!(isfinite(Up.x) && isfinite(Up.y) && isfinite(Up.z))) atomicOr(&st->status, kErrNaN);
     }
@@ -291,6 +301,7 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
   reducePartials<3>(partials, 8, gridDim.x, S, smem);
   reducePartialsMax<5>(partials + 3, 8, gridDim.x, M, smem);
   if (threadIdx.x != 0) return;
+  for (int k = 0; k < 3; ++k) M[k] = sqrt(M[k]);
   st->counter[0] = 0;
   st->dcur = dc ^ 1;
   // converged(): relative displacement residual
@@ -362,6 +373,39 @@ kPostLawTL(MeshView mv, Controls c, FieldPtrs f, const DevState* st) {
 }
 
 // --------------------------------------------------------------- RHS pass ---
+// Face pass: for every internal face, in owner orientation (storage owner =
+// lower row), the flux of R -- S.sigma_f + RhieChow -- and the
+// gamma |S| delta (D_N - D_P) term of M D.  Each face is evaluated once; the
+// cell pass adds it to the owner and subtracts it from the neighbour.
+__global__ void __launch_bounds__(kRowBlock)
+kRhsFace(MeshView mv, Controls c, FieldPtrs f, const DevState* st) {
+  const double* U = f.D[st->dcur];
+  const int el = c.tl ? st->enforceLinear : 1;
+  for (int fi = blockIdx.x * blockDim.x + threadIdx.x; fi < mv.nI; fi += gridDim.x * blockDim.x) {
+    const int o = mv.fown[fi], n = mv.fnei[fi];
+    const double w = mv.fw[fi];
+    const V3 S = ldV(mv.fS, fi);
+    const double cm = mv.fmagS[fi] * mv.fdelta[fi];
+    const V3 dU = ldV(U, n) - ldV(U, o);
+    const V3 d = ldV(mv.C, n) - ldV(mv.C, o);
+    const T9 Gf = w * ldT(f.G, o) + (1.0 - w) * ldT(f.G, n);
+    const S6 So = ldS(f.sig, o), Sn = ldS(f.sig, n);
+    V3 sigFlux;
+    if (el) {
+      sigFlux = dotVS(S, w * So + (1.0 - w) * Sn);
+    } else {
+      const T9 To = f.J[o] * dotTT(ldT(f.Finv, o), fromS(So));
+      const T9 Tn = f.J[n] * dotTT(ldT(f.Finv, n), fromS(Sn));
+      sigFlux = dotVT(S, w * To + (1.0 - w) * Tn);
+    }
+    // Rhie-Chow: gammaS |S| delta (dU - d.grad_f)
+    const V3 flux = sigFlux + (c.gammaS * cm) * (dU - dotVT(d, Gf));
+    const V3 mflux = (c.gamma * cm) * dU;
+    double* q = f.flux + 6 * (size_t)fi;
+    q[0] = flux.x; q[1] = flux.y; q[2] = flux.z;
+    q[3] = mflux.x; q[4] = mflux.y; q[5] = mflux.z;
+  }
+}
 
 template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
@@ -373,41 +417,13 @@ kRhs(MeshView mv, Controls c, FieldPtrs f, T* __restrict__ x, T* __restrict__ r,
   const int el = c.tl ? st->enforceLinear : 1;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x) {
     const V3 Us = ldV(U, s);
-    const V3 Cs = ldV(mv.C, s);
-    const T9 Gs = ldT(f.G, s);
-    const S6 Ss = ldS(f.sig, s);
-    T9 Ts;
-    if (!el) Ts = f.J[s] * dotTT(ldT(f.Finv, s), fromS(Ss));
     V3 R = {0, 0, 0}, MD = {0, 0, 0};
     double sumA = 0;
     for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) {
-      const int nb = mv.col[e];
       const int fk = mv.fidx[e];
       const bool own = fk >= 0;
-      const int fi = own ? fk : ~fk;
-      const V3 Un = ldV(U, nb);
-      const V3 Cn = ldV(mv.C, nb);
-      const T9 Gn = ldT(f.G, nb);
-      const S6 Sn = ldS(f.sig, nb);
-      const double w = mv.fw[fi];
-      const V3 S = ldV(mv.fS, fi);
-      const double cm = mv.fmagS[fi] * mv.fdelta[fi];
-      // owner-oriented quantities
-      const V3 dU = own ? Un - Us : Us - Un;
-      const V3 d = own ? Cn - Cs : Cs - Cn;
-      const T9 Gf = own ? w * Gs + (1.0 - w) * Gn : w * Gn + (1.0 - w) * Gs;
-      V3 sigFlux;
-      if (el) {
-        const S6 sf = own ? w * Ss + (1.0 - w) * Sn : w * Sn + (1.0 - w) * Ss;
-        sigFlux = dotVS(S, sf);
-      } else {
-        const T9 Tn = f.J[nb] * dotTT(ldT(f.Finv, nb), fromS(Sn));
-        const T9 Tf = own ? w * Ts + (1.0 - w) * Tn : w * Tn + (1.0 - w) * Ts;
-        sigFlux = dotVT(S, Tf);
-      }
-      // Rhie-Chow: gammaS |S| delta (dU - d.grad_f)
-      const V3 flux = sigFlux + (c.gammaS * cm) * (dU - dotVT(d, Gf));
-      const V3 mflux = (c.gamma * cm) * dU;
+      const double* q = f.flux + 6 * (size_t)(own ? fk : ~fk);
+      const V3 flux = {q[0], q[1], q[2]}, mflux = {q[3], q[4], q[5]};
       if (own) { R = R + flux; MD = MD - mflux; }
       else { R = R - flux; MD = MD + mflux; }
     }
@@ -521,6 +537,7 @@ void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const
                 DevState* st, double* partials, int mode, cudaStream_t s, LaunchTimer* tm) {
   const int grid = (mv.nC + kRowBlock - 1) / kRowBlock;
   TimeScope ts(tm, S4G_K_POST, s);
+  if (mode == 1) kApplyX<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, f, x, st);
   kPost<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, c, f, x, st, partials, mode);
   if (c.tl && mode == 1) kPostLawTL<<<grid, kRowBlock, 0, s>>>(mv, c, f, st);
 }
@@ -529,6 +546,7 @@ template <typename T>
 void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, T* x, T* r,
                DevState* st, double* partials, cudaStream_t s, LaunchTimer* tm) {
   TimeScope ts(tm, S4G_K_RHS, s);
+  if (mv.nI > 0) kRhsFace<<<mv.rowGrid, kRowBlock, 0, s>>>(mv, c, f, st);
   kRhs<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, c, f, x, r, st, partials);
 }
 
