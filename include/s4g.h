@@ -128,6 +128,9 @@ typedef struct s4g_mesh_opts {
                              1 full Cf-C (foam-extend) */
   int dic_subdomains;     /* 0: exact global DIC; 1: DIC restricted to each
                              part (processor-local DIC of a decomposed run) */
+  int no_autotune;        /* 1: skip the kernel-variant autotuner of the
+                             processor-local PCG (results are identical
+                             either way; only the speed differs) */
 } s4g_mesh_opts;
 
 typedef struct s4g_mesh s4g_mesh;
@@ -259,6 +262,14 @@ typedef struct s4g_perf {
   long long kernel_launches;  /* kernels launched by the library */
   int enforce_linear;         /* TL: linear geometry was enforced */
   int device_status;          /* raw device status word (0 = clean) */
+  int part_threads;           /* processor-local PCG: threads per part of the
+                                 preconditioner kernel in use (autotuned) */
+  int spmv_unroll;            /* processor-local PCG: SpMV form in use: entries
+                                 unrolled in the fused p-update + SpMV (1 or
+                                 6), or 0 for the split form */
+  double tune_us[6];          /* autotuner timings (us) of the variants:
+                                 preconditioner with 64/128/256 threads per
+                                 part, SpMV plain/unrolled/split; 0 if none */
   /* per kernel kind (S4G_K_*), only with s4g_ctx_opts.profile: summed
    * CUDA-event time and number of launches that did work */
   double kernel_ms[S4G_K_KINDS];

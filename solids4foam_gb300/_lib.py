@@ -43,7 +43,8 @@ class MeshDesc(ct.Structure):
 
 class MeshOpts(ct.Structure):
     _fields_ = [("renumber", ct.c_int), ("part_size", ct.c_int),
-                ("ls_boundary_delta", ct.c_int), ("dic_subdomains", ct.c_int)]
+                ("ls_boundary_delta", ct.c_int), ("dic_subdomains", ct.c_int),
+                ("no_autotune", ct.c_int)]
 
 
 class MeshInfo(ct.Structure):
@@ -78,12 +79,15 @@ class Perf(ct.Structure):
         ("initial_residual", ct.c_double), ("rel_residual", ct.c_double),
         ("solve_ms", ct.c_double), ("h2d_ms", ct.c_double), ("d2h_ms", ct.c_double),
         ("kernel_launches", ct.c_longlong), ("enforce_linear", ct.c_int),
-        ("device_status", ct.c_int),
-        ("kernel_ms", ct.c_double * 8), ("kernel_launches_by", ct.c_longlong * 8),
+        ("device_status", ct.c_int), ("part_threads", ct.c_int), ("spmv_unroll", ct.c_int),
+        ("tune_us", ct.c_double * 6),
+        ("kernel_ms", ct.c_double * len(KERNEL_KINDS)),
+        ("kernel_launches_by", ct.c_longlong * len(KERNEL_KINDS)),
     ]
 
     def as_dict(self):
         d = {f[0]: getattr(self, f[0]) for f in self._fields_[:-2]}
+        d["tune_us"] = list(self.tune_us)
         d["kernel_ms"] = dict(zip(KERNEL_KINDS, list(self.kernel_ms)))
         d["kernel_launches_by"] = dict(zip(KERNEL_KINDS, list(self.kernel_launches_by)))
         return d

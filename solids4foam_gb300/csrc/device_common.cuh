@@ -39,6 +39,7 @@ struct MeshView {
   // processor-local DIC tables (see HostPrep)
   const int* locEntStart; const int* locSrc; const uint16_t* locIdx;
   const int* locMetaStart; const uint32_t* locMeta;
+  const int4* locDesc;   // [nParts][2] part descriptors
   int maxLocEntries, maxLocMeta;
 };
 
@@ -278,6 +279,83 @@ __device__ __forceinline__ void reducePartials(const double* partials, int strid
 #pragma unroll
     for (int k = 0; k < N; ++k) out[k] += __ldcg(partials + (size_t)stride * q + k);
   blockSum<N>(out, smem);
+}
+
+// Sum of N values over the first 64 threads (two warps) by a fixed tree,
+// whatever the block size.  Result valid in thread 0; needs blockDim >= 64.
+template <int N>
+__device__ __forceinline__ void sum64(double (&v)[N], double* smem /* [2*N] */) {
+  if (threadIdx.x < 64) {
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    if (threadIdx.x == 32)
+#pragma unroll
+      for (int k = 0; k < N; ++k) smem[k] = v[k];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int k = 0; k < N; ++k) v[k] += smem[k];
+  __syncthreads();
+}
+
+// reducePartials with 64 fixed virtual lanes: the summation order depends on
+// `count` only, not on the block size of the kernel that reduces.
+template <int N>
+__device__ __forceinline__ void reducePartials64(const double* partials, int stride, int count,
+                                                 double (&out)[N], double* smem) {
+#pragma unroll
+  for (int k = 0; k < N; ++k) out[k] = 0;
+  if (threadIdx.x < 64)
+    for (int q = threadIdx.x; q < count; q += 64)
+#pragma unroll
+      for (int k = 0; k < N; ++k) out[k] += __ldcg(partials + (size_t)stride * q + k);
+  sum64<N>(out, smem);
+}
+
+// Fixed-order sum of `count` records of N values (`stride` doubles apart)
+// over 256 virtual lanes: lane v sums records v, v+256, ... in order (four
+// loads in flight), then lanes v, v+32, ..., v+224 are summed in order and
+// the 32 results by a fixed shuffle tree.  The order depends on `count`
+// only, and any block size works.  scratch: 256*N doubles of shared memory.
+// Result valid in thread 0.
+template <int N>
+__device__ __forceinline__ void reduceRecords(const double* rec, int stride, int count,
+                                              double (&out)[N], double* scratch) {
+  for (int v = threadIdx.x; v < 256; v += blockDim.x) {
+    double a[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) a[k] = 0;
+    int q = v;
+    for (; q + 3 * 256 < count; q += 4 * 256) {
+      double t[4][N];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int k = 0; k < N; ++k) t[u][k] = __ldcg(rec + (size_t)stride * (q + 256 * u) + k);
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int k = 0; k < N; ++k) a[k] += t[u][k];
+    }
+    for (; q < count; q += 256)
+#pragma unroll
+      for (int k = 0; k < N; ++k) a[k] += __ldcg(rec + (size_t)stride * q + k);
+#pragma unroll
+    for (int k = 0; k < N; ++k) scratch[v * N + k] = a[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+      double b = 0;
+      for (int j = 0; j < 8; ++j) b += scratch[(threadIdx.x + 32 * j) * N + k];
+      for (int o = 16; o > 0; o >>= 1) b += __shfl_down_sync(0xffffffffu, b, o);
+      out[k] = b;
+    }
+  }
+  __syncthreads();
 }
 
 template <int N>

@@ -133,7 +133,10 @@ struct Engine {
   // processor-local DIC path (subdomain runs with DIC)
   int nLoc = 0;
   int* dLocSrc = nullptr;
-  int localGrid = 1, localGrid32 = 1;
+  LocalTuning tune64, tune32;   // fused-iteration variants (FP64 / FP32 inner solve)
+  bool tuned64 = false, tuned32 = false;
+  bool autotune = true;
+  double tuneUs[2][kLocNumNT + kLocNumU] = {};  // last timings (us), for perf
   DevState* dState = nullptr;
   DevState* hState = nullptr;  // pinned
   double* dPartials = nullptr;
@@ -330,13 +333,20 @@ struct Engine {
       S4G_TRY(upload(&dMeta, hp.locMeta));
       mv.locSrc = dLocSrc; mv.locEntStart = dEs; mv.locMetaStart = dMs;
       mv.locIdx = dIdx; mv.locMeta = dMeta;
+      int* dDesc;
+      S4G_TRY(upload(&dDesc, hp.locDesc));
+      mv.locDesc = reinterpret_cast<const int4*>(dDesc);
       mv.maxLocEntries = hp.maxLocEntries; mv.maxLocMeta = hp.maxLocMeta;
       if (localSmemBytes<double>(mv) + 2048 > (size_t)maxSmem)
         return setErr(S4G_BAD_ARG, "a DIC part does not fit in shared memory; use a smaller part_size");
-      S4G_CUDA(localPrepare<double>(mv, &perSM));
-      localGrid = std::max(1, std::min(hp.nParts, std::max(1, perSM) * ctx->numSMs));
-      S4G_CUDA(localPrepare<float>(mv, &perSM));
-      localGrid32 = std::max(1, std::min(hp.nParts, std::max(1, perSM) * ctx->numSMs));
+      int per[kLocNumNT];
+      S4G_CUDA(localPrepare<double>(mv, per));
+      for (int k = 0; k < kLocNumNT; ++k)
+        tune64.grid[k] = std::max(1, std::min(hp.nParts, std::max(1, per[k]) * ctx->numSMs));
+      S4G_CUDA(localPrepare<float>(mv, per));
+      for (int k = 0; k < kLocNumNT; ++k)
+        tune32.grid[k] = std::max(1, std::min(hp.nParts, std::max(1, per[k]) * ctx->numSMs));
+      autotune = !(o && o->no_autotune);
       S4G_TRY(alloc(&pc.p2, 3 * (size_t)nC));
       double* lc;
       S4G_TRY(alloc(&lc, (size_t)nLoc));
@@ -558,6 +568,79 @@ struct Engine {
 
   // PCG loop of one corrector: launch batches, read the device decision.
   template <typename T>
+  LocalTuning& tuning() { return sizeof(T) == 4 ? tune32 : tune64; }
+
+  // Autotuner of the fused processor-local iteration: times every variant of
+  // its two kernels on this mesh and keeps the fastest.  Each timed launch
+  // starts from the same state (a scratch DevState reset before it, all
+  // components active, one pending update) on zeroed vectors, so every
+  // launch does the full work.  The vectors are reset by the corrector's
+  // right-hand side pass afterwards.  Variants give bit-identical results, so
+  // the choice changes only the speed.
+  template <typename T>
+  s4g_status tuneLocal(const Controls& c, const PcgPtrs<T>& p) {
+    bool& done = sizeof(T) == 4 ? tuned32 : tuned64;
+    if (done || !autotune) { done = true; return S4G_OK; }
+    cudaStream_t s = ctx->stream;
+    const size_t n3 = 3 * (size_t)hp.nC;
+    T* vecs[6] = {p.x, p.r, p.w, p.p, p.q, p.p2};
+    for (T* v : vecs) S4G_CUDA(cudaMemsetAsync(v, 0, n3 * sizeof(T), s));
+    DevState* dTune = nullptr;
+    S4G_TRY(alloc(&dTune, 1));
+    DevState init{};
+    init.pcgContinue = 1;
+    for (int k = 0; k < 3; ++k) {
+      init.active[k] = 1; init.pending[k] = 1; init.nIter[k] = 1;
+      init.normFactor[k] = 1; init.initRes[k] = 1; init.wArA[k] = 1; init.beta[k] = 0.5;
+    }
+    cudaEvent_t a, b;
+    S4G_CUDA(cudaEventCreate(&a));
+    S4G_CUDA(cudaEventCreate(&b));
+    LocalTuning& t = tuning<T>();
+    double* us = tuneUs[sizeof(T) == 4 ? 1 : 0];
+    auto timeIt = [&](auto launch) -> double {
+      float best = 1e30f;
+      for (int rep = 0; rep < 7; ++rep) {
+        cudaMemcpyAsync(dTune, &init, sizeof(DevState), cudaMemcpyHostToDevice, s);
+        cudaEventRecord(a, s);
+        launch();
+        cudaEventRecord(b, s);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep >= 2) best = std::min(best, ms);
+      }
+      return 1000.0 * best;
+    };
+    LocalTuning cand = t;
+    int bestNT = 0;
+    for (int k = 0; k < kLocNumNT; ++k) {
+      cand.ntIdx = k;
+      us[k] = timeIt([&] { launchLocalPrecond<T>(mv, c, p, dTune, dPartials, cand, s); });
+      launches += 7;
+      if (us[k] < us[bestNT]) bestNT = k;
+    }
+    int bestU = 0;
+    for (int k = 0; k < kLocNumU; ++k) {
+      cand.uIdx = k;
+      us[kLocNumNT + k] = timeIt([&] { launchLocalSpmv<T>(mv, p, dTune, dPartials, cand, s); });
+      launches += 7 * (kLocVariantsU[k] == 0 ? 2 : 1);
+      if (us[kLocNumNT + k] < us[kLocNumNT + bestU]) bestU = k;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    S4G_CUDA(cudaGetLastError());
+    S4G_CUDA(cudaStreamSynchronize(s));
+    allocs.erase(std::find(allocs.begin(), allocs.end(), (void*)dTune));
+    cudaFree(dTune);
+    bytes -= sizeof(DevState);
+    t.ntIdx = bestNT;
+    t.uIdx = bestU;
+    done = true;
+    return S4G_OK;
+  }
+
+  template <typename T>
   s4g_status pcgLoop(const Controls& c, const PcgPtrs<T>& p, int grid) {
     // Iterations are launched in growing batches; the launches after the
     // device's stop decision return at once.
@@ -567,7 +650,8 @@ struct Engine {
       for (int i = 0; i < chunk; ++i) {
         timer.tag = launched++;
         if (mv.subdomains && c.precond == 0)
-          launchLocalIteration<T>(mv, c, p, dState, dPartials, grid, ctx->stream, &launches, tm());
+          launchLocalIteration<T>(mv, c, p, dState, dPartials, tuning<T>(), ctx->stream,
+                                  &launches, tm());
         else
           launchPcgIteration<T>(mv, c, p, dState, dPartials, grid, ctx->stream, &launches, tm());
       }
@@ -622,6 +706,11 @@ struct Engine {
     cudaEvent_t e0, e1;
     S4G_CUDA(cudaEventCreate(&e0));
     S4G_CUDA(cudaEventCreate(&e1));
+    if (mv.subdomains && lin.preconditioner == S4G_PRECOND_DIC) {
+      const Controls ct = controls(tl);
+      if (mixed) S4G_TRY(tuneLocal<float>(ct, pc32));
+      else S4G_TRY(tuneLocal<double>(ct, pc));
+    }
     S4G_TRY(initFields(tl));
     S4G_TRY(resetSweepState());
     timer.reset();
@@ -629,9 +718,8 @@ struct Engine {
     Controls c = controls(tl);
     int nCorrTotal = 0;
     auto loop = [&](int isTl) -> s4g_status {
-      const bool local = mv.subdomains && c.precond == 0;
-      return mixed ? correctorLoop<float>(c, isTl, pc32, local ? localGrid32 : sweepGrid32)
-                   : correctorLoop<double>(c, isTl, pc, local ? localGrid : sweepGrid);
+      return mixed ? correctorLoop<float>(c, isTl, pc32, sweepGrid32)
+                   : correctorLoop<double>(c, isTl, pc, sweepGrid);
     };
     if (!tl) {
       launchTractionInit(mv, c, f, s);
@@ -689,6 +777,12 @@ struct Engine {
       perf->kernel_launches = launches - launches0;
       perf->enforce_linear = hState->enforceLinear;
       perf->device_status = (int)hState->status;
+      const bool local = mv.subdomains && lin.preconditioner == S4G_PRECOND_DIC;
+      const LocalTuning& lt = mixed ? tune32 : tune64;
+      perf->part_threads = local ? kLocVariantsNT[lt.ntIdx] : 0;
+      perf->spmv_unroll = local ? kLocVariantsU[lt.uIdx] : 0;
+      for (int k = 0; k < 6; ++k)
+        perf->tune_us[k] = (local && k < kLocNumNT + kLocNumU) ? tuneUs[mixed ? 1 : 0][k] : 0.0;
       timer.resolve();
       for (int k = 0; k < S4G_K_KINDS; ++k) {
         perf->kernel_ms[k] = timer.ms[k];

@@ -123,15 +123,36 @@ void launchPrecondOnly(const MeshView& mv, const Controls& c, const PcgPtrs<T>& 
 // lcoef[i] = rDa[src[i]], 0 where src[i] < 0 (padding).
 template <typename T>
 void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaStream_t s);
+// Variant choice of the fused iteration (set by the engine's autotuner):
+// ntIdx selects 64/128/256 threads per part for the preconditioner, with
+// grid[ntIdx] resident blocks; uIdx selects the fused SpMV with a plain (0)
+// or unrolled (1) entry loop, or the split p-update + SpMV (2).  All
+// variants compute bit-identical results.
+constexpr int kLocNumNT = 3, kLocNumU = 3;
+extern const int kLocVariantsNT[kLocNumNT];
+extern const int kLocVariantsU[kLocNumU];
+struct LocalTuning {
+  int ntIdx = 1, uIdx = 0;
+  int grid[kLocNumNT] = {1, 1, 1};
+};
 // One fused PCG iteration (two kernels): [x, r update of the previous
 // iteration + residual test + processor-local DIC + w.r] and
 // [p = w + beta p, q = A p, p.q].
 template <typename T>
 void launchLocalIteration(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p,
-                          DevState* st, double* partials, int grid, cudaStream_t s,
+                          DevState* st, double* partials, const LocalTuning& t, cudaStream_t s,
                           long long* launches, LaunchTimer* tm = nullptr);
+// The two kernels on their own (autotuner).
+template <typename T>
+void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
+                        double* partials, const LocalTuning& t, cudaStream_t s);
+template <typename T>
+void launchLocalSpmv(const MeshView& mv, const PcgPtrs<T>& p, DevState* st, double* partials,
+                     const LocalTuning& t, cudaStream_t s);
 template <typename T>
 size_t localSmemBytes(const MeshView& mv);
+// Sets the shared-memory attribute of every preconditioner variant and
+// returns resident blocks per SM of each (blocksPerSM[kLocNumNT]).
 template <typename T>
 cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM);
 

@@ -24,6 +24,13 @@
 // is the one of the separate kernels; only the order of the global sums
 // differs.
 //
+// Variants.  kLocPrecond runs with 64, 128 or 256 threads per part and
+// kLocSpmv with or without its loads unrolled; the autotuner (engine) times
+// them on the mesh and keeps the fastest.  Every sum is taken in an order
+// that does not depend on the variant (per part over 64 fixed lanes, then
+// over the parts in index order; the SpMV's grid is fixed), so all variants
+// give bit-identical results.
+//
 // Part tables (HostPrep step 9): in-part entries per row, lower entries in
 // CSR order then upper entries in reverse CSR order, coefficient rD_row*a_e
 // and the column's row index inside the part (16 bits); per-row metadata
@@ -31,13 +38,13 @@
 // they are staged with 16-byte cp.async copies while the CTA streams the
 // x/r update.
 
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "pcg_common.cuh"
 
 namespace s4g {
 namespace {
-
-constexpr int kLocBlock = 64;  // threads per part (levels of 8x8x8 parts hold <= 48 rows)
 
 template <typename T>
 struct LocSmem {
@@ -57,30 +64,91 @@ __device__ __forceinline__ LocSmem<T> locSmem(const MeshView& mv, unsigned char*
   return s;
 }
 
+// v -= sum_j c_j w_idx(j) over n staged entries from j0, in entry order.  The
+// first four entries have their operands loaded before the multiply-adds.
+template <typename T>
+__device__ __forceinline__ void locRow(const LocSmem<T>& sm, int j0, int n, T& v0, T& v1, T& v2) {
+  constexpr int U = 4;
+  T a[U], w0[U], w1[U], w2[U];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    if (u < n) {
+      const int q = sm.idx[j0 + u];
+      a[u] = sm.c[j0 + u];
+      w0[u] = sm.w[3 * q]; w1[u] = sm.w[3 * q + 1]; w2[u] = sm.w[3 * q + 2];
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u)
+    if (u < n) { v0 -= a[u] * w0[u]; v1 -= a[u] * w1[u]; v2 -= a[u] * w2[u]; }
+  for (int j = j0 + U; j < j0 + n; ++j) {
+    const int q = sm.idx[j];
+    const T c = sm.c[j];
+    v0 -= c * sm.w[3 * q]; v1 -= c * sm.w[3 * q + 1]; v2 -= c * sm.w[3 * q + 2];
+  }
+}
+
+// One substitution (DIR 0 forward, 1 backward) over the part's levels:
+// the rows of a level in parallel, a barrier between levels.
+template <int DIR, int NT, typename T>
+__device__ __forceinline__ void locSweep(const LocSmem<T>& sm, int nL) {
+  for (int s = 0; s < nL; ++s) {
+    const int l = DIR == 0 ? s : nL - 1 - s;
+    for (int i = sm.lv[l] + threadIdx.x; i < sm.lv[l + 1]; i += NT) {
+      const uint32_t m = sm.m[i];
+      const int nl = (m >> 16) & 0xff;
+      const int j0 = DIR == 0 ? (int)(m & 0xffff) : (int)(m & 0xffff) + nl;
+      const int n = DIR == 0 ? nl : (int)(m >> 24);
+      T v0 = sm.w[3 * i], v1 = sm.w[3 * i + 1], v2 = sm.w[3 * i + 2];
+      locRow(sm, j0, n, v0, v1, v2);
+      sm.w[3 * i] = v0; sm.w[3 * i + 1] = v1; sm.w[3 * i + 2] = v2;
+    }
+    __syncthreads();
+  }
+}
+
 template <typename T>
 __global__ void kLocGather(int n, const int* src, const double* rDa, T* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) out[i] = src[i] >= 0 ? (T)rDa[src[i]] : T(0);
 }
 
+// Resident blocks the register budget is set for: the shared memory of a
+// 512-row part (with the 1 KB each block reserves) allows six blocks per SM
+// in FP32 and four in FP64; wider blocks trade residency for registers.
 template <typename T, int NT>
-__global__ void __launch_bounds__(NT)
+constexpr int locMinBlocks() {
+  return sizeof(T) == 4 ? (NT <= 128 ? 6 : 3) : (NT <= 64 ? 4 : NT <= 128 ? 3 : 2);
+}
+
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT, (locMinBlocks<T, NT>()))
 kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partials) {
   if (!st->pcgContinue) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   const LocSmem<T> sm = locSmem<T>(mv, smraw);
   __shared__ double red[32 * 6];
-  const T* pp = st->pbuf ? p.p2 : p.p;  // p of the pending iteration
+  // the vectors never alias one another
+  const T* __restrict__ pg = st->pbuf ? p.p2 : p.p;  // p of the pending iteration
+  const T* __restrict__ qg = p.q;
+  const T* __restrict__ rDg = p.rD;
+  T* __restrict__ xg = p.x;
+  T* __restrict__ rg = p.r;
   bool pend[3];
   T al[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) { pend[k] = st->pending[k] != 0; al[k] = (T)st->alpha[k]; }
   const bool anyPend = pend[0] || pend[1] || pend[2];
-  Acc<T> wr[3], ar[3];
+  int4 dA, dB;
+  if (blockIdx.x < mv.nParts) { dA = mv.locDesc[2 * blockIdx.x]; dB = mv.locDesc[2 * blockIdx.x + 1]; }
   for (int part = blockIdx.x; part < mv.nParts; part += gridDim.x) {
-    const int pLo = mv.partStart[part], nR = mv.partStart[part + 1] - pLo;
-    const int eLo = mv.locEntStart[part], nE = mv.locEntStart[part + 1] - eLo;
-    const int mLo = mv.locMetaStart[part], nM = mv.locMetaStart[part + 1] - mLo;
+    const int pLo = dA.x, nR = dA.y, eLo = dA.z, nE = dA.w;
+    const int mLo = dB.x, nM = dB.y, l0 = dB.z, nL = dB.w;
+    // the next part's descriptor, needed after this part
+    if (part + gridDim.x < mv.nParts) {
+      dA = mv.locDesc[2 * (part + gridDim.x)];
+      dB = mv.locDesc[2 * (part + gridDim.x) + 1];
+    }
     // static part tables in flight while the vectors stream
     {
       const int nc = nE * (int)sizeof(T) / 16;
@@ -93,72 +161,74 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
       const char* gm = (const char*)(mv.locMeta + mLo);
       for (int k = threadIdx.x; k < nm; k += NT) cpAsync16((char*)sm.m + 16 * k, gm + 16 * k);
     }
-    const int l0 = mv.lvlOff[part], nL = mv.lvlOff[part + 1] - l0;
     for (int k = threadIdx.x; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
-    // pending update and residual sums; w starts as rD r
-    for (int i = threadIdx.x; i < nR; i += NT) {
-      const size_t g = 3 * (size_t)(pLo + i);
-      const T rd = p.rD[pLo + i];
+    // pending update (x += alpha p, r -= alpha q); w starts as rD r.  RB
+    // rows per thread at a time, every load issued before any store.
+    constexpr int RB = NT <= 64 ? 2 : 1;
+    for (int i0 = threadIdx.x; i0 < nR; i0 += RB * NT) {
+      T rv[RB][3], qv[RB][3], pv[RB][3], xv[RB][3], rd[RB];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        T rv = p.r[g + k];
-        if (pend[k]) {
-          p.x[g + k] += al[k] * pp[g + k];
-          rv -= al[k] * p.q[g + k];
-          p.r[g + k] = rv;
+      for (int h = 0; h < RB; ++h) {
+        const int i = i0 + h * NT;
+        if (i < nR) {
+          const size_t g = 3 * (size_t)(pLo + i);
+          rd[h] = rDg[pLo + i];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            rv[h][k] = rg[g + k];
+            if (pend[k]) { qv[h][k] = qg[g + k]; pv[h][k] = pg[g + k]; xv[h][k] = xg[g + k]; }
+          }
         }
-        ar[k].add(fabs(rv));
-        sm.r[3 * i + k] = rv;
-        sm.w[3 * i + k] = rd * rv;
+      }
+#pragma unroll
+      for (int h = 0; h < RB; ++h) {
+        const int i = i0 + h * NT;
+        if (i < nR) {
+          const size_t g = 3 * (size_t)(pLo + i);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            if (pend[k]) {
+              xg[g + k] = xv[h][k] + al[k] * pv[h][k];
+              rv[h][k] -= al[k] * qv[h][k];
+              rg[g + k] = rv[h][k];
+            }
+            sm.r[3 * i + k] = rv[h][k];
+            sm.w[3 * i + k] = rd[h] * rv[h][k];
+          }
+        }
       }
     }
     cpAsyncWaitAll();
     __syncthreads();
-    // forward substitution: w_u -= sum_{l<u in part} (rD_u a_ul) w_l
-    for (int l = 0; l < nL; ++l) {
-      for (int i = sm.lv[l] + threadIdx.x; i < sm.lv[l + 1]; i += NT) {
-        const uint32_t m = sm.m[i];
-        const int j0 = m & 0xffff, j1 = j0 + ((m >> 16) & 0xff);
-        T v0 = sm.w[3 * i], v1 = sm.w[3 * i + 1], v2 = sm.w[3 * i + 2];
-        for (int j = j0; j < j1; ++j) {
-          const int q = sm.idx[j];
-          const T a = sm.c[j];
-          v0 -= a * sm.w[3 * q]; v1 -= a * sm.w[3 * q + 1]; v2 -= a * sm.w[3 * q + 2];
-        }
-        sm.w[3 * i] = v0; sm.w[3 * i + 1] = v1; sm.w[3 * i + 2] = v2;
-      }
-      __syncthreads();
-    }
+    // forward substitution: w_u -= sum_{l<u in part} (rD_u a_ul) w_l, then
     // backward substitution: w_l -= sum_{u>l in part} (rD_l a_lu) w_u
-    for (int l = nL - 1; l >= 0; --l) {
-      for (int i = sm.lv[l] + threadIdx.x; i < sm.lv[l + 1]; i += NT) {
-        const uint32_t m = sm.m[i];
-        const int j0 = (m & 0xffff) + ((m >> 16) & 0xff), j1 = j0 + (m >> 24);
-        T v0 = sm.w[3 * i], v1 = sm.w[3 * i + 1], v2 = sm.w[3 * i + 2];
-        for (int j = j0; j < j1; ++j) {
-          const int q = sm.idx[j];
-          const T a = sm.c[j];
-          v0 -= a * sm.w[3 * q]; v1 -= a * sm.w[3 * q + 1]; v2 -= a * sm.w[3 * q + 2];
-        }
-        sm.w[3 * i] = v0; sm.w[3 * i + 1] = v1; sm.w[3 * i + 2] = v2;
-        wr[0].add(v0 * sm.r[3 * i]); wr[1].add(v1 * sm.r[3 * i + 1]); wr[2].add(v2 * sm.r[3 * i + 2]);
-      }
-      __syncthreads();
-    }
-    T* wg = p.w + 3 * (size_t)pLo;
+    locSweep<0, NT>(sm, nL);
+    locSweep<1, NT>(sm, nL);
+    // w out; the part's w.r and sum|r| over 64 fixed lanes
+    T* __restrict__ wg = p.w + 3 * (size_t)pLo;
     for (int k = threadIdx.x; k < 3 * nR; k += NT) wg[k] = sm.w[k];
-    __syncthreads();  // the next part reuses the shared memory
-  }
-  double acc[6] = {wr[0].value(), wr[1].value(), wr[2].value(),
-                   ar[0].value(), ar[1].value(), ar[2].value()};
-  blockSum<6>(acc, red);
-  if (threadIdx.x == 0) {
-    double* q = partials + 8 * (size_t)blockIdx.x;
-    for (int k = 0; k < 6; ++k) q[k] = acc[k];
+    double d6[6] = {0, 0, 0, 0, 0, 0};
+    if (threadIdx.x < 64) {
+      Acc<T> wr[3], ar[3];
+      for (int i = threadIdx.x; i < nR; i += 64)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const T rv = sm.r[3 * i + k];
+          wr[k].add(sm.w[3 * i + k] * rv);
+          ar[k].add(fabs(rv));
+        }
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
+    }
+    sum64<6>(d6, red);  // ends with a barrier: the next part may reuse the shared memory
+    if (threadIdx.x == 0) {
+      double* q = partials + 8 * (size_t)part;
+      for (int k = 0; k < 6; ++k) q[k] = d6[k];
+    }
   }
   if (!lastBlockDone(&st->counter[5], gridDim.x)) return;
   double S[6];
-  reducePartials<6>(partials, 8, gridDim.x, S, red);
+  reduceRecords<6>(partials, 8, mv.nParts, S, (double*)smraw);  // the part loop is over
   if (threadIdx.x != 0) return;
   st->counter[5] = 0;
   int any = 0;
@@ -187,14 +257,23 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
 template <typename T>
 __device__ __forceinline__ T pNew(bool first, T w, T b, T po) { return first ? w : w + b * po; }
 
-template <typename T>
-__global__ void __launch_bounds__(kRowBlock)
+// U > 1: the first U entries of a row have all their loads issued before the
+// multiply-adds; U == 1: a plain loop.
+template <typename T, int U>
+__global__ void __launch_bounds__(kRowBlock, (U > 1 ? (sizeof(T) == 4 ? 3 : 2) : 4))
 kLocSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   if (!st->pcgContinue) return;
   __shared__ double red[32 * 3];
   const int pb = st->pbuf;
-  const T* po = pb ? p.p2 : p.p;
-  T* pn = pb ? p.p : p.p2;
+  // the vectors never alias one another
+  const T* __restrict__ po = pb ? p.p2 : p.p;
+  T* __restrict__ pn = pb ? p.p : p.p2;
+  const T* __restrict__ wv = p.w;
+  const T* __restrict__ val = p.val;
+  const T* __restrict__ dia = p.diag;
+  const int* __restrict__ col = mv.col;
+  const int* __restrict__ rp = mv.rowptr;
+  T* __restrict__ qo = p.q;
   bool act[3], first[3];
   T b[3];
 #pragma unroll
@@ -203,22 +282,41 @@ kLocSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   }
   Acc<T> a0, a1, a2;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x) {
-    const T dg = p.diag[s];
-    const T v0 = pNew(first[0], p.w[3 * s], b[0], po[3 * s]);
-    const T v1 = pNew(first[1], p.w[3 * s + 1], b[1], po[3 * s + 1]);
-    const T v2 = pNew(first[2], p.w[3 * s + 2], b[2], po[3 * s + 2]);
+    const T dg = dia[s];
+    const T v0 = pNew(first[0], wv[3 * s], b[0], po[3 * s]);
+    const T v1 = pNew(first[1], wv[3 * s + 1], b[1], po[3 * s + 1]);
+    const T v2 = pNew(first[2], wv[3 * s + 2], b[2], po[3 * s + 2]);
     T y0 = dg * v0, y1 = dg * v1, y2 = dg * v2;
-    const int e1 = mv.rowptr[s + 1];
-    for (int e = mv.rowptr[s]; e < e1; ++e) {
-      const int cl = mv.col[e];
-      const T a = p.val[e];
-      y0 += a * pNew(first[0], p.w[3 * cl], b[0], po[3 * cl]);
-      y1 += a * pNew(first[1], p.w[3 * cl + 1], b[1], po[3 * cl + 1]);
-      y2 += a * pNew(first[2], p.w[3 * cl + 2], b[2], po[3 * cl + 2]);
+    const int e0 = rp[s], e1 = rp[s + 1];
+    int e = e0;
+    if (U > 1) {
+      int cl[U];
+      T a[U], n0[U], n1[U], n2[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (e0 + u < e1) { cl[u] = col[e0 + u]; a[u] = val[e0 + u]; }
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (e0 + u < e1) {
+          n0[u] = pNew(first[0], wv[3 * cl[u]], b[0], po[3 * cl[u]]);
+          n1[u] = pNew(first[1], wv[3 * cl[u] + 1], b[1], po[3 * cl[u] + 1]);
+          n2[u] = pNew(first[2], wv[3 * cl[u] + 2], b[2], po[3 * cl[u] + 2]);
+        }
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (e0 + u < e1) { y0 += a[u] * n0[u]; y1 += a[u] * n1[u]; y2 += a[u] * n2[u]; }
+      e = e0 + U;
     }
-    if (act[0]) { pn[3 * s] = v0; p.q[3 * s] = y0; }
-    if (act[1]) { pn[3 * s + 1] = v1; p.q[3 * s + 1] = y1; }
-    if (act[2]) { pn[3 * s + 2] = v2; p.q[3 * s + 2] = y2; }
+    for (; e < e1; ++e) {
+      const int c2 = col[e];
+      const T a2 = val[e];
+      y0 += a2 * pNew(first[0], wv[3 * c2], b[0], po[3 * c2]);
+      y1 += a2 * pNew(first[1], wv[3 * c2 + 1], b[1], po[3 * c2 + 1]);
+      y2 += a2 * pNew(first[2], wv[3 * c2 + 2], b[2], po[3 * c2 + 2]);
+    }
+    if (act[0]) { pn[3 * s] = v0; qo[3 * s] = y0; }
+    if (act[1]) { pn[3 * s + 1] = v1; qo[3 * s + 1] = y1; }
+    if (act[2]) { pn[3 * s + 2] = v2; qo[3 * s + 2] = y2; }
     a0.add(y0 * v0); a1.add(y1 * v1); a2.add(y2 * v2);
   }
   double acc[3] = {a0.value(), a1.value(), a2.value()};
@@ -249,22 +347,121 @@ kLocSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   st->pcgContinue = any;
 }
 
+// Split form of the second kernel (FP64 favours it: a neighbour's p_new is
+// formed once instead of once per face): p_new = w + beta p_old ...
+template <typename T>
+__global__ void __launch_bounds__(kRowBlock)
+kLocPUpdate(MeshView mv, PcgPtrs<T> p, const DevState* st) {
+  if (!st->pcgContinue) return;
+  const int pb = st->pbuf;
+  const T* __restrict__ po = pb ? p.p2 : p.p;
+  T* __restrict__ pn = pb ? p.p : p.p2;
+  const T* __restrict__ wv = p.w;
+  bool act[3], first[3];
+  T b[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    act[k] = st->active[k] != 0; first[k] = st->nIter[k] == 0; b[k] = (T)st->beta[k];
+  }
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (act[k]) pn[3 * s + k] = pNew(first[k], wv[3 * s + k], b[k], po[3 * s + k]);
+}
+
+// ... then q = A p_new with the p.q sums and the same decisions as kLocSpmv.
+template <typename T>
+__global__ void __launch_bounds__(kRowBlock, 4)
+kLocSpmvSplit(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
+  if (!st->pcgContinue) return;
+  __shared__ double red[32 * 3];
+  const int pb = st->pbuf;
+  const T* __restrict__ pn = pb ? p.p : p.p2;
+  const T* __restrict__ val = p.val;
+  const T* __restrict__ dia = p.diag;
+  const int* __restrict__ col = mv.col;
+  const int* __restrict__ rp = mv.rowptr;
+  T* __restrict__ qo = p.q;
+  bool act[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) act[k] = st->active[k] != 0;
+  Acc<T> a0, a1, a2;
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x) {
+    const T dg = dia[s];
+    const T v0 = pn[3 * s], v1 = pn[3 * s + 1], v2 = pn[3 * s + 2];
+    T y0 = dg * v0, y1 = dg * v1, y2 = dg * v2;
+    const int e1 = rp[s + 1];
+    for (int e = rp[s]; e < e1; ++e) {
+      const int c2 = col[e];
+      const T a2 = val[e];
+      y0 += a2 * pn[3 * c2]; y1 += a2 * pn[3 * c2 + 1]; y2 += a2 * pn[3 * c2 + 2];
+    }
+    if (act[0]) qo[3 * s] = y0;
+    if (act[1]) qo[3 * s + 1] = y1;
+    if (act[2]) qo[3 * s + 2] = y2;
+    a0.add(y0 * v0); a1.add(y1 * v1); a2.add(y2 * v2);
+  }
+  double acc[3] = {a0.value(), a1.value(), a2.value()};
+  blockSum<3>(acc, red);
+  if (threadIdx.x == 0) {
+    double* q = partials + 8 * (size_t)blockIdx.x;
+    q[0] = acc[0]; q[1] = acc[1]; q[2] = acc[2];
+  }
+  if (!lastBlockDone(&st->counter[6], gridDim.x)) return;
+  double sum[3];
+  reducePartials<3>(partials, 8, gridDim.x, sum, red);
+  if (threadIdx.x != 0) return;
+  st->counter[6] = 0;
+  int any = 0;
+  for (int k = 0; k < 3; ++k) {
+    if (!st->active[k]) continue;
+    st->wApA[k] = sum[k];
+    if (fabs(sum[k]) / st->normFactor[k] < 1e-300) {  // checkSingularity: stop this component
+      st->active[k] = 0;
+      continue;
+    }
+    if (sum[k] <= 0) atomicOr(&st->status, kErrIndefinite);
+    st->alpha[k] = st->wArA[k] / sum[k];
+    st->pending[k] = 1;
+    any = 1;
+  }
+  st->pbuf = pb ^ 1;
+  st->pcgContinue = any;
+}
+
+template <typename T, int NT>
+void launchPrecondNT(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
+                     double* partials, int grid, cudaStream_t s) {
+  kLocPrecond<T, NT><<<grid, NT, localSmemBytes<T>(mv), s>>>(mv, c, p, st, partials);
+}
+
+template <typename T, int NT>
+cudaError_t prepareNT(const MeshView& mv, int* blocksPerSM) {
+  const int sm = (int)localSmemBytes<T>(mv);
+  cudaError_t e = cudaFuncSetAttribute(kLocPrecond<T, NT>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, NT>, NT, sm);
+}
+
 }  // namespace
+
+const int kLocVariantsNT[kLocNumNT] = {64, 128, 256};
+const int kLocVariantsU[kLocNumU] = {1, 6, 0};
 
 template <typename T>
 size_t localSmemBytes(const MeshView& mv) {
   const size_t P = mv.maxRows, EL = mv.maxLocEntries, ML = mv.maxLocMeta;
-  return sizeof(T) * (EL + 6 * P) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
+  const size_t tables = sizeof(T) * (EL + 6 * P) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
+  return std::max(tables, (size_t)256 * 6 * sizeof(double));  // final reduction scratch
 }
 
 template <typename T>
 cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM) {
-  const int sm = (int)localSmemBytes<T>(mv);
-  cudaError_t e = cudaFuncSetAttribute(kLocPrecond<T, kLocBlock>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
-  if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, kLocBlock>,
-                                                       kLocBlock, sm);
+  cudaError_t e = prepareNT<T, 64>(mv, &blocksPerSM[0]);
+  if (e == cudaSuccess) e = prepareNT<T, 128>(mv, &blocksPerSM[1]);
+  if (e == cudaSuccess) e = prepareNT<T, 256>(mv, &blocksPerSM[2]);
+  return e;
 }
 
 template <typename T>
@@ -273,27 +470,54 @@ void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaS
 }
 
 template <typename T>
+void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
+                        double* partials, const LocalTuning& t, cudaStream_t s) {
+  switch (t.ntIdx) {
+    case 0: launchPrecondNT<T, 64>(mv, c, p, st, partials, t.grid[0], s); break;
+    case 2: launchPrecondNT<T, 256>(mv, c, p, st, partials, t.grid[2], s); break;
+    default: launchPrecondNT<T, 128>(mv, c, p, st, partials, t.grid[1], s); break;
+  }
+}
+
+template <typename T>
+void launchLocalSpmv(const MeshView& mv, const PcgPtrs<T>& p, DevState* st, double* partials,
+                     const LocalTuning& t, cudaStream_t s) {
+  if (t.uIdx == 2) {
+    kLocPUpdate<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, p, st);
+    kLocSpmvSplit<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, p, st, partials);
+  } else if (t.uIdx == 1) {
+    kLocSpmv<T, 6><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, p, st, partials);
+  } else {
+    kLocSpmv<T, 1><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, p, st, partials);
+  }
+}
+
+template <typename T>
 void launchLocalIteration(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p,
-                          DevState* st, double* partials, int grid, cudaStream_t s,
+                          DevState* st, double* partials, const LocalTuning& t, cudaStream_t s,
                           long long* launches, LaunchTimer* tm) {
   {
     TimeScope ts(tm, S4G_K_LOC_PRECOND, s);
-    kLocPrecond<T, kLocBlock><<<grid, kLocBlock, localSmemBytes<T>(mv), s>>>(mv, c, p, st, partials);
+    launchLocalPrecond<T>(mv, c, p, st, partials, t, s);
   }
   {
     TimeScope ts(tm, S4G_K_LOC_SPMV, s);
-    kLocSpmv<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, p, st, partials);
+    launchLocalSpmv<T>(mv, p, st, partials, t, s);
   }
-  *launches += 2;
+  *launches += t.uIdx == 2 ? 3 : 2;
 }
 
 #define S4G_INSTANTIATE(T)                                                                      \
   template size_t localSmemBytes<T>(const MeshView&);                                           \
   template cudaError_t localPrepare<T>(const MeshView&, int*);                                  \
   template void launchLocalGather<T>(int, const int*, const double*, T*, cudaStream_t);          \
+  template void launchLocalPrecond<T>(const MeshView&, const Controls&, const PcgPtrs<T>&,      \
+                                      DevState*, double*, const LocalTuning&, cudaStream_t);    \
+  template void launchLocalSpmv<T>(const MeshView&, const PcgPtrs<T>&, DevState*, double*,      \
+                                   const LocalTuning&, cudaStream_t);                           \
   template void launchLocalIteration<T>(const MeshView&, const Controls&, const PcgPtrs<T>&,    \
-                                        DevState*, double*, int, cudaStream_t, long long*,      \
-                                        LaunchTimer*);
+                                        DevState*, double*, const LocalTuning&, cudaStream_t,   \
+                                        long long*, LaunchTimer*);
 S4G_INSTANTIATE(double)
 S4G_INSTANTIATE(float)
 #undef S4G_INSTANTIATE

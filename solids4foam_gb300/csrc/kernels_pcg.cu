@@ -27,6 +27,8 @@
 // (L2), never from a possibly stale L1 line.  The coefficients rD_row*a_e are
 // precomputed once per matrix, as OpenFOAM's FDIC does (bit-identical to DIC).
 
+#include <algorithm>
+
 #include "kernels.cuh"
 #include "pcg_common.cuh"
 
@@ -324,7 +326,7 @@ kSweepSm(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
       __syncthreads();
       if (sLast) {
         double s[3];
-        reducePartials<3>(partials, 4, mv.nParts, s, red);
+        reduceRecords<3>(partials, 4, mv.nParts, s, (double*)smraw);  // the part is written back
         if (threadIdx.x == 0) {
           st->partsDone[1] = 0;
           for (int k = 0; k < 3; ++k)
@@ -522,8 +524,9 @@ void launchSweeps(const MeshView& mv, const PcgPtrs<T>& p, DevState* st, double*
 template <typename T>
 size_t sweepSmemBytes(const MeshView& mv) {
   const size_t P = mv.maxRows, H = mv.maxHalo, EM = mv.maxEntries;
-  return sizeof(T) * (3 * (P + H + 1) + 3 * P + P + EM) +
-         sizeof(int) * (EM + P + 1 + mv.maxLevels + 1 + P);
+  const size_t stage = sizeof(T) * (3 * (P + H + 1) + 3 * P + P + EM) +
+                       sizeof(int) * (EM + P + 1 + mv.maxLevels + 1 + P);
+  return std::max(stage, (size_t)256 * 3 * sizeof(double));  // final reduction scratch
 }
 
 template <typename T>

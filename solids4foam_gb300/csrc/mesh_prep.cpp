@@ -499,6 +499,14 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
       hp.maxLocEntries = std::max(hp.maxLocEntries, hp.locEntStart[p + 1] - hp.locEntStart[p]);
       hp.maxLocMeta = std::max(hp.maxLocMeta, hp.locMetaStart[p + 1] - hp.locMetaStart[p]);
     }
+    hp.locDesc.resize(8 * (size_t)hp.nParts);
+    for (int p = 0; p < hp.nParts; ++p) {
+      int* d8 = hp.locDesc.data() + 8 * (size_t)p;
+      d8[0] = hp.partStart[p]; d8[1] = hp.partStart[p + 1] - hp.partStart[p];
+      d8[2] = hp.locEntStart[p]; d8[3] = hp.locEntStart[p + 1] - hp.locEntStart[p];
+      d8[4] = hp.locMetaStart[p]; d8[5] = hp.locMetaStart[p + 1] - hp.locMetaStart[p];
+      d8[6] = hp.lvlOff[p]; d8[7] = hp.lvlOff[p + 1] - hp.lvlOff[p];
+    }
   }
   return S4G_OK;
 }

@@ -55,6 +55,9 @@ struct HostPrep {
   std::vector<int> locEntStart, locSrc, locMetaStart;
   std::vector<uint16_t> locIdx;
   std::vector<uint32_t> locMeta;
+  // per part, for one 32-byte load: {partStart, rows, locEntStart, entries}
+  // and {locMetaStart, metas, lvlOff, levels}
+  std::vector<int> locDesc;  // [nParts][8]
   int maxLocEntries = 0, maxLocMeta = 0;
 };
 

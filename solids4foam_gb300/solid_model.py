@@ -84,7 +84,8 @@ class SolidModel:
     def __init__(self, ctx: Context, mesh, law: dict, bcs: dict, model: str =
                  "linearGeometryTotalDisplacement", solver: dict | None = None,
                  outer: dict | None = None, precision: str = "FP64", renumber: str = "tiled",
-                 part_size: int = 512, ls_boundary_delta: int = 0, dic_subdomains: bool = False):
+                 part_size: int = 512, ls_boundary_delta: int = 0, dic_subdomains: bool = False,
+                 autotune: bool = True):
         if model not in MODELS:
             raise ValueError(f"unknown solidModel {model!r}; valid: {list(MODELS)}")
         self.ctx = ctx
@@ -95,7 +96,7 @@ class SolidModel:
         keep = []
         d = _desc(mesh, keep)
         opts = _lib.MeshOpts(RENUMBER[renumber], part_size, ls_boundary_delta,
-                             1 if dic_subdomains else 0)
+                             1 if dic_subdomains else 0, 0 if autotune else 1)
         h = ct.c_void_p()
         _lib.check(self.L.s4g_mesh_upload(ctx.h, ct.byref(d), ct.byref(opts), ct.byref(h)),
                    "s4g_mesh_upload")

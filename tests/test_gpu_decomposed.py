@@ -75,3 +75,23 @@ def test_decomposed_ragged_parts(ctx):
         assert perf["converged"] == 1 and po["converged"] == 1
         assert rel(D, Do) < 1e-6 and rel(sig, so) < 1e-5
         model.close()
+
+
+@pytest.mark.parametrize("precision", ["FP64", "FP32_REFINE"])
+def test_autotuned_variants_are_bit_identical(ctx, precision):
+    """The autotuner only picks among kernel variants whose sums run in the
+    same order: the tuned and the untuned run give identical bits."""
+    m = sg.box_mesh(14, 12, 10, 1.0, 0.9, 0.7, 0.2, 21)
+    bcs = {"zmin": ("fixedDisplacement", None, None),
+           "zmax": ("solidTraction", None, np.full(int(m["patch_size"][5]), 1e7))}
+    law = dict(type="linearElastic", E=70e9, nu=0.33)
+    out = []
+    for tune in (True, False):
+        model = sg.SolidModel(ctx, m, law, bcs, outer=dict(nCorrectors=2000), precision=precision,
+                              part_size=128, dic_subdomains=True, autotune=tune)
+        D, sig, perf = model.evolve()
+        assert perf["part_threads"] in (64, 128, 256) and perf["spmv_unroll"] in (0, 1, 6)
+        out.append((D, sig, perf["total_lin_iters"], perf["n_correctors"]))
+        model.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2:] == out[1][2:]

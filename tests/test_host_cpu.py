@@ -132,3 +132,37 @@ def test_no_device_is_reported_without_gpu(built):
     with pytest.raises(sg.S4GError) as e:
         sg.Context(0)
     assert e.value.status == _lib.NO_DEVICE
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """Every ctypes mirror has the size and field offsets of its C struct
+    (compiled against include/s4g.h with the host C compiler)."""
+    import ctypes as ct
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no host C compiler")
+    pairs = {"s4g_ctx_opts": _lib.CtxOpts, "s4g_mesh_desc": _lib.MeshDesc,
+             "s4g_mesh_opts": _lib.MeshOpts, "s4g_mesh_info": _lib.MeshInfo,
+             "s4g_law": _lib.Law, "s4g_lin_solver": _lib.LinSolver, "s4g_outer": _lib.Outer,
+             "s4g_perf": _lib.Perf}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "s4g.h"', "int main(void) {"]
+    for cname, py in pairs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    got = {}
+    for ln in out.splitlines():
+        c, f, v = ln.split()
+        got[(c, f)] = int(v)
+    for cname, py in pairs.items():
+        assert got[(cname, "size")] == ct.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
