@@ -303,6 +303,22 @@ s4g_status s4g_op_amul(s4g_mesh* mesh, int k, const double* x, double* y);
 s4g_status s4g_op_precondition(s4g_mesh* mesh, int k, const double* r,
                                double* w);
 
+/* y = A x and, per column j, xAx[j] = sum_i x_ij (A x)_ij; x, y [n_cells][k]
+ * in the caller's cell order, xAx [k]; k in 1..3.  No counterpart in the
+ * reference: an operator product for callers that must not allocate (a
+ * server that has given the free device memory to admitted solves, a
+ * latency-bound loop that must stay out of the CUDA allocator).  It
+ * allocates nothing: it works in the mesh's work vectors and in one fixed
+ * scratch block of static device memory.  Limits: meshes of at most 262,144
+ * cells (larger ones get S4G_BAD_ARG); the matrix must already be assembled
+ * (s4g_op_matrix or s4g_solve ran on this mesh); the scratch is shared by
+ * every mesh on the device, so calls that overlap in time on one device
+ * race and must be ordered by the caller; the first call on a device does a
+ * one-time set-up (a symbol-address lookup) and belongs before any stream
+ * capture. */
+s4g_status s4g_op_amul_dot_noalloc(s4g_mesh* mesh, int k, const double* x,
+                                   double* y, double* xAx);
+
 /* ---------------------------------------------------- case generation --
  * Seeded hexahedral box meshes (blockMesh + perturbMeshPoints stand-in,
  * applications/utilities/perturbMeshPoints/perturbMeshPoints.C:244-330):

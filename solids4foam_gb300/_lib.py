@@ -117,6 +117,8 @@ _SIGS = {
     "s4g_get_gradD": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "s4g_op_matrix": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "s4g_op_amul": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p]),
+    "s4g_op_amul_dot_noalloc": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p,
+                                           ct.c_void_p]),
     "s4g_op_precondition": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p]),
     "s4g_box_mesh_sizes": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int] + [ct.POINTER(ct.c_int)] * 4),
     "s4g_box_mesh_build": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_double, ct.c_double,

@@ -865,6 +865,18 @@ struct Engine {
     return S4G_OK;
   }
 
+  s4g_status opAmulDotNoAlloc(int k, const double* x, double* y, double* xAx) {
+    if (!matrixValid)
+      return setErr(S4G_BAD_ARG, "the matrix is not assembled yet: call s4g_op_matrix or s4g_solve "
+                                 "first (s4g_op_amul_dot_noalloc does no set-up work)");
+    std::string err;
+    const s4g_status st = s4g::opAmulDotNoAlloc(mv, dC2s, dVal, dDiag, pc.w, pc.q, ctx->device,
+                                                ctx->stream, k, x, y, xAx, err);
+    if (st != S4G_OK) return setErr(st, err);
+    launches += 3;
+    return S4G_OK;
+  }
+
   s4g_status getGradD(double* out) {
     if (lastModel < 0) return setErr(S4G_BAD_ARG, "no solve has run");
     const double* src = lastModel == S4G_NONLIN_GEOM_TOTAL_LAG ? f.GD : f.G;
@@ -1105,6 +1117,14 @@ s4g_status s4g_op_amul(s4g_mesh* mesh, int k, const double* x, double* y) {
 s4g_status s4g_op_precondition(s4g_mesh* mesh, int k, const double* r, double* w) {
   if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
   return mesh->e.opPrecondition(k, r, w);
+}
+
+s4g_status s4g_op_amul_dot_noalloc(s4g_mesh* mesh, int k, const double* x, double* y,
+                                   double* xAx) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  if (cudaSetDevice(mesh->e.ctx->device) != cudaSuccess)
+    return setErr(S4G_CUDA_ERROR, "cudaSetDevice failed");
+  return mesh->e.opAmulDotNoAlloc(k, x, y, xAx);
 }
 
 }  // extern "C"

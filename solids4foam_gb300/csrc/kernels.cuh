@@ -1,6 +1,8 @@
 // Kernel launchers (host-callable wrappers around the device kernels).
 #pragma once
 
+#include <string>
+
 #include "device_common.cuh"
 #include "s4g.h"
 
@@ -155,5 +157,14 @@ size_t localSmemBytes(const MeshView& mv);
 // returns resident blocks per SM of each (blocksPerSM[kLocNumNT]).
 template <typename T>
 cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM);
+
+// ---- operator product without allocation (noalloc.cu) ------------------------
+// y = A x and x.Ax for k columns of host vectors in caller order, through the
+// work vectors work0/work1 ([nC][3] doubles each) and a static scratch block;
+// the matrix (val, diag) must already be assembled.  See noalloc.cu.
+s4g_status opAmulDotNoAlloc(const MeshView& mv, const int* c2s, const double* val,
+                            const double* diag, double* work0, double* work1, int device,
+                            cudaStream_t s, int k, const double* x, double* y, double* xAx,
+                            std::string& err);
 
 }  // namespace s4g

@@ -213,6 +213,17 @@ class SolidModel:
         _lib.check(self.L.s4g_op_amul(self.h, k, x.ctypes.data, y.ctypes.data), "s4g_op_amul")
         return y
 
+    def op_amul_dot_noalloc(self, x):
+        """y = A x and the column products x.Ax through the entry point that
+        allocates nothing (meshes of at most 262,144 cells, matrix assembled)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        k = 1 if x.ndim == 1 else x.shape[1]
+        y = np.zeros_like(x)
+        xax = np.zeros(k)
+        _lib.check(self.L.s4g_op_amul_dot_noalloc(self.h, k, x.ctypes.data, y.ctypes.data,
+                                                   xax.ctypes.data), "s4g_op_amul_dot_noalloc")
+        return y, xax
+
     def op_precondition(self, r):
         r = np.ascontiguousarray(r, dtype=np.float64)
         k = 1 if r.ndim == 1 else r.shape[1]
