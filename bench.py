@@ -108,7 +108,7 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_bytes(kind, n_cells, n_faces, n_bfaces, v, n_loc=0):
+def algorithmic_bytes(kind, n_cells, n_faces, n_bfaces, v, n_loc=0, split=False):
     """Minimal DRAM bytes of one launch of a kernel kind (k = 3 columns,
     v = value bytes, 4-byte indices); the formulas follow the solve's
     scope table: SpMV nnz(v+i) + 4(N+1) + 2Nvk; one DIC sweep
@@ -116,13 +116,14 @@ def algorithmic_bytes(kind, n_cells, n_faces, n_bfaces, v, n_loc=0):
     Fused processor-local iteration: loc_precond reads r, q, p, x and
     writes r, x, w (7Nvk) plus rD (Nv), the in-part table (n_loc entries of
     v + 2 bytes) and 4 bytes of row metadata per row; loc_spmv reads w and
-    p_old, writes p_new and q (4Nvk), plus the matrix nnz(v+i) + Nv + 4(N+1)."""
+    p_old, writes p_new and q (4Nvk), plus the matrix nnz(v+i) + Nv + 4(N+1);
+    its split form (p-update pass, then SpMV on p_new) moves 5Nvk."""
     N, F, B, k = n_cells, n_faces, n_bfaces, 3
     nnz_l = F
     if kind == "loc_precond":
         return 7 * N * v * k + N * v + n_loc * (v + 2) + 4 * N
     if kind == "loc_spmv":
-        return 4 * N * v * k + 2 * F * (v + 4) + N * v + 4 * (N + 1)
+        return (5 if split else 4) * N * v * k + 2 * F * (v + 4) + N * v + 4 * (N + 1)
     if kind == "sweep_fwd":
         return nnz_l * (v + 4) + 4 * (N + 1) + N * v + 2 * N * v * k
     if kind == "sweep_bwd":
@@ -240,6 +241,99 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def run_batched(args, ctx):
+    """Batched load cases (one 64^3 mesh, 64 cases, FP32+refine, one
+    s4g_solve_cases call) against plain FP64 single solves of the same cases
+    one after another; both with the processor-local DIC."""
+    import solids4foam_gb300 as sg
+    from solids4foam_gb300.cases import load_cases
+    lc = load_cases(args.batch_n, args.batch_cases)
+    cases = lc["cases"]
+    kw = dict(solver=lc["solver"], outer=lc["outer"], dic_subdomains=True)
+    model = sg.SolidModel(ctx, lc["mesh"], lc["law"], cases[0], precision="FP32_REFINE", **kw)
+    model.evolve_cases(cases[:2])  # warm-up: tuning, FP32 copies
+    t0 = time.perf_counter()
+    Db, sb, perfs = model.evolve_cases(cases)
+    wall = time.perf_counter() - t0
+    model.close()
+    dev_s = perfs[0]["solve_ms"] / 1e3
+    n64 = min(args.batch_fp64_cases, len(cases))
+    m64 = sg.SolidModel(ctx, lc["mesh"], lc["law"], cases[0], precision="FP64", **kw)
+    m64.evolve()  # warm-up
+    t64, errD, errS = [], [], []
+    for c in range(n64):
+        for name, spec in cases[c].items():
+            m64.set_bc(["xmin", "xmax", "ymin", "ymax", "zmin", "zmax"].index(name), *spec)
+        t1 = time.perf_counter()
+        D64, s64, p64 = m64.evolve()
+        t64.append(time.perf_counter() - t1)
+        errD.append(rel_l2(Db[c], D64))
+        errS.append(rel_l2(sb[c], s64))
+    m64.close()
+    fp64_rate = 1.0 / statistics.mean(t64)
+    rate = len(cases) / wall
+    return {"workload": f"cube{args.batch_n}_x{len(cases)}_load_cases", "cases": len(cases),
+            "cells": int(lc["mesh"]["V"].shape[0]), "solves_per_s": rate,
+            "wall_s": wall, "device_s": dev_s,
+            "correctors_min_max": [min(p["n_correctors"] for p in perfs),
+                                   max(p["n_correctors"] for p in perfs)],
+            "all_converged": all(p["converged"] == 1 for p in perfs),
+            "plain_fp64_solves_per_s": fp64_rate, "plain_fp64_cases_timed": n64,
+            "speedup_vs_plain_fp64": rate / fp64_rate,
+            "max_rel_l2_D_vs_fp64": max(errD), "max_rel_l2_sigma_vs_fp64": max(errS)}
+
+
+def run_served(args):
+    """A Poisson stream of uneven solves (80% linear FP32+refine with the
+    processor-local DIC, 20% neoHookean total Lagrangian, 10 increments)
+    through the server, against the same requests solved one after another
+    in plain FP64."""
+    import solids4foam_gb300 as sg
+    from solids4foam_gb300.cases import served_stream
+    stream = served_stream(args.serve_n)
+    srv = sg.Server(max_slots=args.serve_slots)
+    t0 = time.perf_counter()
+    ids = []
+    for arrival, req in stream:
+        wait = arrival - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        kw = dict(req)
+        kw["precision"] = "FP32_REFINE"
+        if kw.get("model", "linearGeometryTotalDisplacement") == "linearGeometryTotalDisplacement":
+            kw["dic_subdomains"] = True
+        ids.append(srv.submit(**kw))
+    results = [srv.result(i) for i in ids]
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    # plain FP64, one request after another
+    ctx = sg.Context(0)
+    seq, errs = 0.0, []
+    for (arrival, req), res in zip(stream, results):
+        kw = dict(req)
+        n_inc = kw.pop("n_increments", 1)
+        m = sg.SolidModel(ctx, kw.pop("mesh"), kw.pop("law"), kw.pop("bcs"), precision="FP64", **kw)
+        t1 = time.perf_counter()
+        D, sig, perf = m.evolve(n_increments=n_inc)
+        seq += time.perf_counter() - t1
+        m.close()
+        errs.append(rel_l2(res[1], D))
+    ctx.close()
+    n = len(stream)
+    return {"workload": f"stream{n}_poisson_boxes_8^3-40^3_20pct_neoHookean",
+            "requests": n, "slots": args.serve_slots, "solves_per_s": n / wall,
+            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+            "all_ok": all(r[0] in (0, 3) for r in results),
+            "plain_fp64_sequential_solves_per_s": n / seq,
+            "speedup_vs_plain_fp64_sequential": (n / wall) / (n / seq),
+            "max_rel_l2_D_vs_fp64": max(errs)}
+
+
 def run_gb300(args):
     import solids4foam_gb300 as sg
     world, rank, local, dist = dist_init()
@@ -290,16 +384,18 @@ def run_gb300(args):
     peak, peak_kind = peaks()
     avg_ms = tot_ms[dom] / max(1, tot_n[dom])
     n_loc = model.info()["n_local_entries"]
-    ab = algorithmic_bytes(dom, nC, nI, nB, v, n_loc)
+    split = perfs[0]["spmv_unroll"] == 0 and perfs[0]["part_threads"] > 0
+    ab = algorithmic_bytes(dom, nC, nI, nB, v, n_loc, split)
     achieved = ab / (avg_ms * 1e-3) / 1e9 if ab else None
     workload = f"cube{args.n}_{args.precision.lower()}_{args.dic}"
     traffic = load_traffic(workload).get(dom)
     kernels = {k: {"launches": tot_n[k], "ms_total": round(tot_ms[k], 3),
                    "share": round(tot_ms[k] / max(1e-9, sum(tot_ms.values())), 4),
                    "avg_us": round(1000 * tot_ms[k] / max(1, tot_n[k]), 2),
-                   "gbs": (round(algorithmic_bytes(k, nC, nI, nB, v, n_loc) /
+                   "gbs": (round(algorithmic_bytes(k, nC, nI, nB, v, n_loc, split) /
                                  (tot_ms[k] / max(1, tot_n[k]) * 1e-3) / 1e9, 1)
-                           if tot_n[k] and algorithmic_bytes(k, nC, nI, nB, v, n_loc) else None)}
+                           if tot_n[k] and algorithmic_bytes(k, nC, nI, nB, v, n_loc, split)
+                           else None)}
                for k in tot_ms if tot_n[k]}
 
     # plain FP64 solve of the same case, for the FP32+refine comparison
@@ -315,6 +411,9 @@ def run_gb300(args):
                 "n_correctors": p64["n_correctors"], "pcg_iterations": p64["total_lin_iters"],
                 "speedup_of_fp32_refine": p64["solve_ms"] / ms_step,
                 "rel_l2_D_fp32_vs_fp64": relD, "rel_l2_sigma_fp32_vs_fp64": relS}
+
+    batched = run_batched(args, ctx) if (rank == 0 and not args.no_batched) else None
+    served = run_served(args) if (rank == 0 and not args.no_served) else None
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -338,6 +437,9 @@ def run_gb300(args):
                    "parallelism": f"replicas{world}",
                    "l2": "working set ~1.7 GB >> 129 MB L2 (no flush needed)",
                    "n_correctors": p0["n_correctors"], "converged": p0["converged"],
+                   "autotuned": {"part_threads": p0["part_threads"],
+                                 "spmv": ("split" if p0["spmv_unroll"] == 0 else
+                                          f"fused, unroll {p0['spmv_unroll']}")},
                    "pcg_iterations": p0["total_lin_iters"]},
         "e2e": {"value": (world * 1000.0 / e2e_step) if e2e_step else None, "unit": "solves/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -348,6 +450,8 @@ def run_gb300(args):
                      "algorithmic_bytes_per_launch": ab, "avg_launch_us": avg_ms * 1000},
         "kernels": kernels,
         "plain_fp64": fp64,
+        "batched": batched,
+        "served": served,
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
@@ -369,6 +473,14 @@ def main():
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)
     ap.add_argument("--full-correctors", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched load cases")
+    ap.add_argument("--batch-n", type=int, default=64)
+    ap.add_argument("--batch-cases", type=int, default=64)
+    ap.add_argument("--batch-fp64-cases", type=int, default=3,
+                    help="plain FP64 single solves timed for the batched comparison")
+    ap.add_argument("--no-served", action="store_true", help="skip the served stream")
+    ap.add_argument("--serve-n", type=int, default=24)
+    ap.add_argument("--serve-slots", type=int, default=8)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

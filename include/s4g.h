@@ -285,6 +285,25 @@ typedef struct s4g_perf {
 s4g_status s4g_solve(s4g_mesh* mesh, s4g_model model, int n_increments,
                      double* D_out, double* sigma_out, s4g_perf* perf);
 
+/* Batched load cases: n_cases independent solves of the
+ * linearGeometryTotalDisplacement model on this mesh, advanced together with
+ * every kernel launched once for all cases still running.  Replaces running
+ * solidModel::evolve (linGeomTotalDispSolid.C:111-232) once per load case.
+ * The cases share the mesh, the material, the solver controls and the
+ * boundary-condition types set by s4g_bc_set; each case has its own
+ * boundary values: bval [n_cases][n_boundary_faces][3] (fixedDisplacement:
+ * displacement; solidTraction: traction) and bpress
+ * [n_cases][n_boundary_faces] (solidTraction pressure, may be NULL), in the
+ * caller's boundary-face order (faces n_internal_faces .. n_faces-1).  Each
+ * case converges on its own, and its result is bit-identical to s4g_solve
+ * with its boundary values.  Requires dic_subdomains = 1 and the DIC
+ * preconditioner.  D_out [n_cases][n_cells][3], sigma_out
+ * [n_cases][n_cells][6], perf [n_cases]; any may be NULL.  Returns
+ * S4G_NOT_CONVERGED if any case did not converge. */
+s4g_status s4g_solve_cases(s4g_mesh* mesh, int n_cases, const double* bval,
+                           const double* bpress, double* D_out,
+                           double* sigma_out, s4g_perf* perf);
+
 /* Cell gradient of D from the last solve, [n_cells][9] row-major,
  * grad(D)_ij = dD_j/dx_i (the reference's gradD field). */
 s4g_status s4g_get_gradD(s4g_mesh* mesh, double* gradD_out);
@@ -318,6 +337,76 @@ s4g_status s4g_op_precondition(s4g_mesh* mesh, int k, const double* r,
  * capture. */
 s4g_status s4g_op_amul_dot_noalloc(s4g_mesh* mesh, int k, const double* x,
                                    double* y, double* xAx);
+
+/* ----------------------------------------------------------- serving --
+ * Continuous admission of solves of uneven sizes onto one GPU.  No single
+ * counterpart in the reference (one solids4Foam run is one solve); it
+ * replaces running many solids4Foam cases one after another.  The server's
+ * worker slots each own a context (a CUDA stream) and run one request at a
+ * time; a free slot takes the first queued request whose device footprint
+ * fits in the memory budget that running requests leave, so requests that
+ * arrive while others run are admitted as slots and memory free up, and
+ * their work overlaps on the device.  Each request computes exactly what a
+ * lone s4g_solve of its inputs computes.  All s4g_server_* calls may be made
+ * from any host thread. */
+typedef struct s4g_server s4g_server;
+
+typedef struct s4g_server_opts {
+  int device;
+  int max_slots;              /* requests running at once (0: 8; at most 64) */
+  long long memory_budget;    /* device bytes running requests may hold
+                                 (0: 80% of the free memory at creation) */
+  int dry_run;                /* 1: no GPU work; a request "runs" for
+                                 dry_run_us_per_kcell us per 1000 cells and
+                                 returns zero fields (scheduler tests) */
+  double dry_run_us_per_kcell;
+} s4g_server_opts;
+
+/* One solve: the mesh, its upload options, the law, boundary conditions
+ * (n_bc patches: index, type, vec3 [patch_size][3] or NULL, pressure
+ * [patch_size] or NULL), controls and the model.  Everything is copied at
+ * submit. */
+typedef struct s4g_request {
+  const s4g_mesh_desc* mesh;
+  s4g_mesh_opts mesh_opts;
+  s4g_law law;
+  int n_bc;
+  const int* bc_patch;
+  const s4g_bc_type* bc_type;
+  const double* const* bc_vec3;
+  const double* const* bc_pressure;
+  s4g_lin_solver lin;
+  s4g_outer outer;
+  s4g_precision precision;
+  s4g_model model;
+  int n_increments;
+} s4g_request;
+
+typedef struct s4g_server_stats {
+  long long submitted, completed, rejected, cancelled;
+  int running, queued;
+  long long bytes_in_use, memory_budget;  /* estimated footprints */
+  double p50_ms, p99_ms, mean_ms;         /* submit -> results ready */
+  double solves_per_s;                    /* completed / (last finish - first submit) */
+} s4g_server_stats;
+
+s4g_status s4g_server_create(const s4g_server_opts* opts, s4g_server** out);
+/* Queues a request; S4G_ADMISSION_REJECTED if its footprint exceeds the
+ * whole budget (it could never run). */
+s4g_status s4g_server_submit(s4g_server* server, const s4g_request* request,
+                             uint64_t* id);
+/* Result of request id: S4G_PENDING while queued or running (wait = 0), or
+ * the solve's status with D_out [n_cells][3], sigma_out [n_cells][6] and
+ * perf filled (each may be NULL); with wait = 1 it blocks until the request
+ * ends.  A finished or cancelled request is forgotten once polled. */
+s4g_status s4g_server_poll(s4g_server* server, uint64_t id, int wait,
+                           double* D_out, double* sigma_out, s4g_perf* perf);
+/* Removes a queued request (S4G_BAD_ARG once it runs); polling it then
+ * returns S4G_CANCELLED. */
+s4g_status s4g_server_cancel(s4g_server* server, uint64_t id);
+s4g_status s4g_server_get_stats(s4g_server* server, s4g_server_stats* out);
+/* Cancels queued requests, lets running ones finish, frees everything. */
+s4g_status s4g_server_destroy(s4g_server* server);
 
 /* ---------------------------------------------------- case generation --
  * Seeded hexahedral box meshes (blockMesh + perturbMeshPoints stand-in,

@@ -7,7 +7,7 @@ solidModel / mechanicalLaw interface.
 from . import _lib
 from ._lib import S4GError, lib
 from .cases import box_mesh, cantilever_case, cube_case
-from .solid_model import Context, SolidModel
+from .solid_model import Context, Server, SolidModel
 
 __all__ = ["S4GError", "lib", "box_mesh", "cantilever_case", "cube_case", "Context",
-           "SolidModel", "_lib"]
+           "Server", "SolidModel", "_lib"]

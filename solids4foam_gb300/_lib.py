@@ -72,6 +72,27 @@ class Outer(ct.Structure):
                 ("stab_scale", ct.c_double), ("info_frequency", ct.c_int)]
 
 
+class ServerOpts(ct.Structure):
+    _fields_ = [("device", ct.c_int), ("max_slots", ct.c_int), ("memory_budget", ct.c_longlong),
+                ("dry_run", ct.c_int), ("dry_run_us_per_kcell", ct.c_double)]
+
+
+class Request(ct.Structure):
+    _fields_ = [("mesh", ct.c_void_p), ("mesh_opts", MeshOpts), ("law", Law), ("n_bc", ct.c_int),
+                ("bc_patch", ct.c_void_p), ("bc_type", ct.c_void_p), ("bc_vec3", ct.c_void_p),
+                ("bc_pressure", ct.c_void_p), ("lin", LinSolver), ("outer", Outer),
+                ("precision", ct.c_int), ("model", ct.c_int), ("n_increments", ct.c_int)]
+
+
+class ServerStats(ct.Structure):
+    _fields_ = [("submitted", ct.c_longlong), ("completed", ct.c_longlong),
+                ("rejected", ct.c_longlong), ("cancelled", ct.c_longlong),
+                ("running", ct.c_int), ("queued", ct.c_int),
+                ("bytes_in_use", ct.c_longlong), ("memory_budget", ct.c_longlong),
+                ("p50_ms", ct.c_double), ("p99_ms", ct.c_double), ("mean_ms", ct.c_double),
+                ("solves_per_s", ct.c_double)]
+
+
 class Perf(ct.Structure):
     _fields_ = [
         ("n_correctors", ct.c_int), ("converged", ct.c_int),
@@ -116,6 +137,15 @@ _SIGS = {
                              ct.POINTER(Perf)]),
     "s4g_get_gradD": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "s4g_op_matrix": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "s4g_server_create": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "s4g_server_submit": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.POINTER(ct.c_uint64)]),
+    "s4g_server_poll": (ct.c_int, [ct.c_void_p, ct.c_uint64, ct.c_int, ct.c_void_p, ct.c_void_p,
+                                   ct.c_void_p]),
+    "s4g_server_cancel": (ct.c_int, [ct.c_void_p, ct.c_uint64]),
+    "s4g_server_get_stats": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "s4g_server_destroy": (ct.c_int, [ct.c_void_p]),
+    "s4g_solve_cases": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p,
+                                   ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "s4g_op_amul": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p]),
     "s4g_op_amul_dot_noalloc": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p,
                                            ct.c_void_p]),

@@ -86,3 +86,60 @@ def oracle_bcs(mesh, bcs):
         else:
             out.append((1, None, None))
     return out
+
+
+def load_cases(n=64, n_cases=64, mesh_seed=2, load_seed=3, jitter=0.2):
+    """Batched load cases on one mesh: the jittered unit cube n^3 (seeded),
+    E = 200 GPa, nu = 0.3, bottom fixed, and per case a uniform top traction
+    whose components are drawn i.i.d. N(0, 1 MPa) (seeded); sides
+    traction-free.  Returns the case dict of the first case plus the list of
+    per-case boundary conditions."""
+    mesh = box_mesh(n, n, n, 1.0, 1.0, 1.0, jitter, mesh_seed)
+    t = np.random.default_rng(load_seed).normal(0.0, 1e6, (n_cases, 3))
+    cases = [{"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", t[c], None)}
+             for c in range(n_cases)]
+    return dict(mesh=mesh, bcs=cases[0], law=dict(type="linearElastic", E=200e9, nu=0.3),
+                solver=dict(tolerance=1e-9, relTol=0.1, maxIter=1000),
+                outer=dict(nCorrectors=2000, solutionTolerance=1e-6), cases=cases)
+
+
+def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=40 ** 3, tl_fraction=0.2,
+                  rate_per_s=20.0):
+    """A stream of solve requests with Poisson arrivals (rate_per_s, seeded):
+    jittered boxes whose cell counts are log-uniform in [min_cells,
+    max_cells] with aspect ratios up to 2; a tl_fraction of them are
+    neoHookeanElastic nonLinearGeometryTotalLagrangian solves (mu uniform in
+    0.5-5 MPa, K/mu uniform in 10-50, traction ramped over 10 increments),
+    the rest linearElastic (E log-uniform 1-300 GPa, nu uniform 0.2-0.45).
+    Returns a list of (arrival_s, request kwargs)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n_requests):
+        t += rng.exponential(1.0 / rate_per_s)
+        cells = np.exp(rng.uniform(np.log(min_cells), np.log(max_cells)))
+        ar = rng.uniform(1.0, 2.0)
+        nz = max(4, int(round((cells / ar) ** (1.0 / 3.0))))
+        nx = max(4, int(round(nz * ar)))
+        ny = max(4, int(round(cells / (nx * nz))))
+        mesh = box_mesh(nx, ny, nz, nx / nz, ny / nz, 1.0, 0.2, 100 + i)
+        top = int(mesh["patch_size"][5])
+        if rng.uniform() < tl_fraction:
+            mu = rng.uniform(0.5e6, 5e6)
+            K = mu * rng.uniform(10.0, 50.0)
+            tr = np.tile([0.0, 0.05 * mu, -0.05 * mu], (top, 1))
+            req = dict(mesh=mesh, law=dict(type="neoHookeanElastic", mu=mu, K=K),
+                       bcs={"zmin": ("fixedDisplacement", None, None),
+                            "zmax": ("solidTraction", tr, None)},
+                       model="nonLinearGeometryTotalLagrangian", n_increments=10,
+                       outer=dict(nCorrectors=200))
+        else:
+            E = np.exp(rng.uniform(np.log(1e9), np.log(300e9)))
+            nu = rng.uniform(0.2, 0.45)
+            tr = rng.normal(0.0, 1e6, 3)
+            req = dict(mesh=mesh, law=dict(type="linearElastic", E=E, nu=nu),
+                       bcs={"zmin": ("fixedDisplacement", None, None),
+                            "zmax": ("solidTraction", tr, None)},
+                       outer=dict(nCorrectors=2000))
+        out.append((t, req))
+    return out

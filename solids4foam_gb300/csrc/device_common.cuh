@@ -41,7 +41,17 @@ struct MeshView {
   const int* locMetaStart; const uint32_t* locMeta;
   const int4* locDesc;   // [nParts][2] part descriptors
   int maxLocEntries, maxLocMeta;
+  // batched load cases: a launch's blockIdx.y is the case; per-case data
+  // lies caseRec doubles (reduction records) or one field size apart
+  long caseRec;
 };
+
+// Batched launches: the case's boundary values (bval [case][nB][3],
+// bpress [case][nB]).
+__device__ __forceinline__ void caseView(MeshView& mv, int cs) {
+  mv.bval += 3 * (size_t)cs * mv.nB;
+  mv.bpress += (size_t)cs * mv.nB;
+}
 
 // Material and solver constants of a solve.
 struct Controls {
@@ -72,6 +82,7 @@ struct DevState {
   double relRes, initResMag;
   double maxJ, minJ;     // TL
   int enforceLinear;
+  int caseLive;          // the corrector loop of this case is still running
   // PCG (three independent component solves)
   int pcgIter;
   int pcgContinue;

@@ -137,8 +137,11 @@ struct Engine {
   bool tuned64 = false, tuned32 = false;
   bool autotune = true;
   double tuneUs[2][kLocNumNT + kLocNumU] = {};  // last timings (us), for perf
-  DevState* dState = nullptr;
-  DevState* hState = nullptr;  // pinned
+  DevState* dState = nullptr;  // one per load case ([caseCap])
+  DevState* hState = nullptr;  // pinned mirror
+  int caseCap = 1;             // load cases the per-case arrays hold
+  int nRun = 1;                // load cases of the solve in progress
+  std::vector<int> pcgBase;    // per case: PCG iterations before the current loop
   double* dPartials = nullptr;
   double* dOut = nullptr;
   bool tlAllocated = false;
@@ -307,7 +310,8 @@ struct Engine {
     S4G_TRY(alloc(&dState, 1));
     S4G_CUDA(cudaMallocHost((void**)&hState, sizeof(DevState)));
     const size_t rowBlocks = (nC + kRowBlock - 1) / kRowBlock;
-    S4G_TRY(alloc(&dPartials, std::max(8 * rowBlocks, 8 * (size_t)hp.nParts)));
+    mv.caseRec = (long)std::max(8 * rowBlocks, 8 * (size_t)hp.nParts);
+    S4G_TRY(alloc(&dPartials, (size_t)mv.caseRec));
     S4G_TRY(alloc(&dOut, 9 * (size_t)nC));
     S4G_CUDA(cudaMemsetAsync(dState, 0, sizeof(DevState), s));
 
@@ -457,10 +461,19 @@ struct Engine {
     cudaStream_t s = ctx->stream;
     S4G_CUDA(cudaMemsetAsync(pc.flags[0], 0, sizeof(unsigned) * hp.nParts, s));
     S4G_CUDA(cudaMemsetAsync(pc.flags[1], 0, sizeof(unsigned) * hp.nParts, s));
-    S4G_CUDA(cudaMemsetAsync(dState, 0, sizeof(DevState), s));
+    S4G_CUDA(cudaMemsetAsync(dState, 0, sizeof(DevState) * nRun, s));
     DevState init{};
     init.epoch[0] = 1; init.epoch[1] = 1;
-    S4G_CUDA(cudaMemcpyAsync(&dState->epoch, &init.epoch, sizeof(init.epoch), cudaMemcpyHostToDevice, s));
+    for (int cs = 0; cs < nRun; ++cs)
+      S4G_CUDA(cudaMemcpyAsync(&dState[cs].epoch, &init.epoch, sizeof(init.epoch), cudaMemcpyHostToDevice, s));
+    return S4G_OK;
+  }
+
+  // Every case of the solve starts its corrector loop.
+  s4g_status setLive() {
+    static const int one = 1;
+    for (int cs = 0; cs < nRun; ++cs)
+      S4G_CUDA(cudaMemcpyAsync(&dState[cs].caseLive, &one, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
     return S4G_OK;
   }
 
@@ -504,12 +517,13 @@ struct Engine {
       float *val, *diag, *rD, *rDa;
       S4G_TRY(alloc(&val, nE)); S4G_TRY(alloc(&diag, nC)); S4G_TRY(alloc(&rD, nC)); S4G_TRY(alloc(&rDa, nE));
       pc32.val = val; pc32.diag = diag; pc32.rD = rD; pc32.rDa = rDa;
-      S4G_TRY(alloc(&pc32.x, 3 * nC)); S4G_TRY(alloc(&pc32.r, 3 * nC)); S4G_TRY(alloc(&pc32.w, 3 * nC));
-      S4G_TRY(alloc(&pc32.p, 3 * nC)); S4G_TRY(alloc(&pc32.q, 3 * nC));
+      const size_t nv = 3 * nC * (size_t)caseCap;  // one vector per load case
+      S4G_TRY(alloc(&pc32.x, nv)); S4G_TRY(alloc(&pc32.r, nv)); S4G_TRY(alloc(&pc32.w, nv));
+      S4G_TRY(alloc(&pc32.p, nv)); S4G_TRY(alloc(&pc32.q, nv));
       pc32.flags[0] = pc.flags[0]; pc32.flags[1] = pc.flags[1];
       if (mv.subdomains) {
         float* lc;
-        S4G_TRY(alloc(&pc32.p2, 3 * nC));
+        S4G_TRY(alloc(&pc32.p2, 3 * nC * (size_t)caseCap));
         S4G_TRY(alloc(&lc, (size_t)nLoc));
         pc32.lcoef = lc;
       }
@@ -532,16 +546,31 @@ struct Engine {
     return S4G_OK;
   }
 
-  s4g_status readState(int pcgBase = -1) {
-    S4G_CUDA(cudaMemcpyAsync(hState, dState, sizeof(DevState), cudaMemcpyDeviceToHost, ctx->stream));
+  // Reads the device state of the nRun cases.  In a PCG loop (inPcg), the
+  // profiler drops the launches past the last iteration any case ran.
+  s4g_status readState(bool inPcg = false) {
+    S4G_CUDA(cudaMemcpyAsync(hState, dState, sizeof(DevState) * nRun, cudaMemcpyDeviceToHost, ctx->stream));
     S4G_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (ctx->profile) timer.resolve(pcgBase >= 0 ? hState->pcgIter - pcgBase : 1 << 30);
+    if (ctx->profile) {
+      int keep = 1 << 30;
+      if (inPcg) {
+        keep = 0;
+        for (int cs = 0; cs < nRun; ++cs) keep = std::max(keep, hState[cs].pcgIter - pcgBase[cs]);
+      }
+      timer.resolve(keep);
+    }
     return S4G_OK;
+  }
+  bool anyCase(int DevState::*flag) const {
+    for (int cs = 0; cs < nRun; ++cs)
+      if (hState[cs].*flag) return true;
+    return false;
   }
 
   s4g_status initFields(int tl) {
     cudaStream_t s = ctx->stream;
-    const size_t nC = hp.nC, nB = hp.nB;
+    // per-case arrays of the nRun cases of this solve
+    const size_t nC = hp.nC * (size_t)nRun, nB = hp.nB * (size_t)nRun;
     auto z = [&](double* p, size_t n) { return cudaMemsetAsync(p, 0, n * sizeof(double), s); };
     S4G_CUDA(z(f.D[0], 3 * nC)); S4G_CUDA(z(f.D[1], 3 * nC)); S4G_CUDA(z(f.D0, 3 * nC));
     S4G_CUDA(z(f.D0b, 3 * nB)); S4G_CUDA(z(f.G, 9 * nC)); S4G_CUDA(z(f.sig, 6 * nC));
@@ -564,6 +593,166 @@ struct Engine {
       S4G_CUDA(cudaStreamSynchronize(s));
     }
     return S4G_OK;
+  }
+
+  template <class T>
+  s4g_status regrow(T*& ptr, size_t nOld, size_t nNew) {
+    if (ptr) {
+      cudaFree(ptr);
+      allocs.erase(std::find(allocs.begin(), allocs.end(), (void*)ptr));
+      bytes -= nOld * sizeof(T);
+    }
+    ptr = nullptr;
+    return alloc(&ptr, nNew);
+  }
+
+  // Per-case arrays for C load cases: fields, boundary values, PCG vectors,
+  // device states and reduction records.  Contents are not kept.
+  s4g_status ensureCases(int C) {
+    if (C <= caseCap) return S4G_OK;
+    S4G_CUDA(cudaStreamSynchronize(ctx->stream));
+    const size_t nC = hp.nC, nB = hp.nB, nI = hp.nI, o = caseCap, n = C;
+    for (int k = 0; k < 2; ++k) S4G_TRY(regrow(f.D[k], 3 * nC * o, 3 * nC * n));
+    S4G_TRY(regrow(f.D0, 3 * nC * o, 3 * nC * n));
+    S4G_TRY(regrow(f.D0b, 3 * nB * o, 3 * nB * n));
+    S4G_TRY(regrow(f.G, 9 * nC * o, 9 * nC * n));
+    S4G_TRY(regrow(f.sig, 6 * nC * o, 6 * nC * n));
+    S4G_TRY(regrow(f.Gb, 9 * nB * o, 9 * nB * n));
+    S4G_TRY(regrow(f.sigb, 6 * nB * o, 6 * nB * n));
+    S4G_TRY(regrow(f.g, 3 * nB * o, 3 * nB * n));
+    S4G_TRY(regrow(f.flux, 6 * nI * o, 6 * nI * n));
+    S4G_TRY(regrow(dBval, 3 * nB * o, 3 * nB * n));
+    S4G_TRY(regrow(dBpress, nB * o, nB * n));
+    mv.bval = dBval; mv.bpress = dBpress;
+    bcDirty = true;
+    for (double** v : {&pc.x, &pc.r, &pc.w, &pc.p, &pc.q}) S4G_TRY(regrow(*v, 3 * nC * o, 3 * nC * n));
+    if (pc.p2) S4G_TRY(regrow(pc.p2, 3 * nC * o, 3 * nC * n));
+    if (fp32Allocated) {
+      for (float** v : {&pc32.x, &pc32.r, &pc32.w, &pc32.p, &pc32.q}) S4G_TRY(regrow(*v, 3 * nC * o, 3 * nC * n));
+      if (pc32.p2) S4G_TRY(regrow(pc32.p2, 3 * nC * o, 3 * nC * n));
+    }
+    S4G_TRY(regrow(dState, o, n));
+    S4G_TRY(regrow(dPartials, (size_t)mv.caseRec * o, (size_t)mv.caseRec * n));
+    cudaFreeHost(hState);
+    hState = nullptr;
+    S4G_CUDA(cudaMallocHost((void**)&hState, sizeof(DevState) * n));
+    std::memset(hState, 0, sizeof(DevState) * n);
+    caseCap = C;
+    return S4G_OK;
+  }
+
+  // Batched load cases of the linear-geometry model on this mesh: C
+  // independent corrector loops (each case its own convergence, PCG state
+  // and boundary values) advanced together, every kernel launched once for
+  // all live cases (blockIdx.y = case).  Each case computes exactly what a
+  // single solve with its boundary values computes.
+  s4g_status solveCases(int C, const double* bval, const double* bpress, double* Dout,
+                        double* sigOut, s4g_perf* perfs) {
+    if (C < 1) return setErr(S4G_BAD_ARG, "n_cases must be >= 1");
+    if (!bval) return setErr(S4G_BAD_ARG, "bval is required");
+    if (!materialSet) return setErr(S4G_BAD_ARG, "material not set");
+    if (law.type != S4G_LINEAR_ELASTIC) return setErr(S4G_BAD_ARG, "batched load cases need a linearElastic law");
+    if (!(mv.subdomains && lin.preconditioner == S4G_PRECOND_DIC))
+      return setErr(S4G_BAD_ARG, "batched load cases run the processor-local DIC: upload the mesh with dic_subdomains=1 and use the DIC preconditioner");
+    const size_t nB = hp.nB, nC = hp.nC;
+    for (size_t i = 0; i < 3 * nB * C; ++i)
+      if (!std::isfinite(bval[i])) return setErr(S4G_BAD_ARG, "non-finite boundary value");
+    if (bpress)
+      for (size_t i = 0; i < nB * C; ++i)
+        if (!std::isfinite(bpress[i])) return setErr(S4G_BAD_ARG, "non-finite pressure");
+    cudaStream_t s = ctx->stream;
+    const long long launches0 = launches;
+    S4G_TRY(ensureCases(C));
+    S4G_TRY(ensureMatrix());
+    const bool mixed = precision == S4G_FP32_REFINE;
+    if (mixed) S4G_TRY(ensureFp32());
+    {
+      const Controls ct = controls(0);
+      if (mixed) S4G_TRY(tuneLocal<float>(ct, pc32));
+      else S4G_TRY(tuneLocal<double>(ct, pc));
+    }
+    // the cases' boundary values in storage order (types are the mesh's)
+    std::vector<double> hv(3 * nB * C), hpr(nB * C);
+    for (int cs = 0; cs < C; ++cs)
+      for (size_t k = 0; k < nB; ++k) {
+        const size_t b = (size_t)hp.bcaller[k];
+        for (int j = 0; j < 3; ++j) hv[3 * (cs * nB + k) + j] = bval[3 * (cs * nB + b) + j];
+        hpr[cs * nB + k] = (btypeH[k] == S4G_SOLID_TRACTION && bpress) ? bpress[cs * nB + b] : 0.0;
+      }
+    S4G_CUDA(cudaMemcpyAsync(dBval, hv.data(), sizeof(double) * hv.size(), cudaMemcpyHostToDevice, s));
+    S4G_CUDA(cudaMemcpyAsync(dBpress, hpr.data(), sizeof(double) * hpr.size(), cudaMemcpyHostToDevice, s));
+    bcDirty = true;  // a later single solve uploads the mesh's own values again
+    cudaEvent_t e0, e1;
+    S4G_CUDA(cudaEventCreate(&e0));
+    S4G_CUDA(cudaEventCreate(&e1));
+    nRun = C;
+    S4G_TRY(initFields(0));
+    S4G_TRY(resetSweepState());
+    S4G_TRY(setLive());
+    timer.reset();
+    S4G_CUDA(cudaEventRecord(e0, s));
+    Controls c = controls(0);
+    launchTractionInit(mv, c, f, s, C);
+    launchPost<double>(mv, c, f, pc.x, dState, dPartials, 0, s, nullptr, C);
+    launches += 2;
+    s4g_status st = mixed ? correctorLoop<float>(c, 0, pc32, sweepGrid32)
+                          : correctorLoop<double>(c, 0, pc, sweepGrid);
+    if (st != S4G_OK) { nRun = 1; return st; }
+    S4G_CUDA(cudaEventRecord(e1, s));
+    S4G_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    S4G_TRY(readState());
+    auto t0 = std::chrono::steady_clock::now();
+    for (int cs = 0; cs < C; ++cs) {
+      const FieldPtrs fc = caseFields(f, cs, hp.nC, hp.nB, hp.nI);
+      if (Dout) {
+        launchGather(hp.nC, 3, dC2s, fc.D[hState[cs].dcur], dOut, s);
+        S4G_CUDA(cudaMemcpyAsync(Dout + 3 * nC * cs, dOut, sizeof(double) * 3 * nC, cudaMemcpyDeviceToHost, s));
+      }
+      if (sigOut) {
+        launchGather(hp.nC, 6, dC2s, fc.sig, dOut + 3 * nC, s);
+        S4G_CUDA(cudaMemcpyAsync(sigOut + 6 * nC * cs, dOut + 3 * nC, sizeof(double) * 6 * nC, cudaMemcpyDeviceToHost, s));
+      }
+      S4G_CUDA(cudaStreamSynchronize(s));  // dOut is reused by the next case
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    lastModel = S4G_LIN_GEOM_TOTAL_DISP;
+    s4g_status ret = S4G_OK;
+    timer.resolve();
+    for (int cs = 0; cs < C; ++cs) {
+      const DevState& h = hState[cs];
+      if (perfs) {
+        s4g_perf* perf = perfs + cs;
+        std::memset(perf, 0, sizeof(*perf));
+        perf->n_correctors = h.nCorrDone;
+        perf->converged = h.converged;
+        perf->total_lin_iters = h.totalLinIters;
+        perf->last_max_lin_iters = h.lastMaxIters;
+        perf->initial_residual = h.initResMag;
+        perf->rel_residual = h.relRes;
+        perf->solve_ms = ms;
+        perf->d2h_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        perf->kernel_launches = launches - launches0;
+        perf->device_status = (int)h.status;
+        const LocalTuning& lt = mixed ? tune32 : tune64;
+        perf->part_threads = kLocVariantsNT[lt.ntIdx];
+        perf->spmv_unroll = kLocVariantsU[lt.uIdx];
+        for (int k = 0; k < 6; ++k)
+          perf->tune_us[k] = k < kLocNumNT + kLocNumU ? tuneUs[mixed ? 1 : 0][k] : 0.0;
+        for (int k = 0; k < S4G_K_KINDS; ++k) {
+          perf->kernel_ms[k] = timer.ms[k];
+          perf->kernel_launches_by[k] = timer.count[k];
+        }
+      }
+      if (h.status & kErrNaN) ret = setErr(S4G_NAN_DETECTED, "non-finite value in a load case");
+      else if (h.status & kErrIndefinite && ret == S4G_OK) ret = setErr(S4G_INDEFINITE, "PCG met p.Ap <= 0 in a load case");
+      else if (!h.converged && ret == S4G_OK) ret = S4G_NOT_CONVERGED;
+    }
+    nRun = 1;
+    return ret;
   }
 
   // PCG loop of one corrector: launch batches, read the device decision.
@@ -645,20 +834,22 @@ struct Engine {
     // Iterations are launched in growing batches; the launches after the
     // device's stop decision return at once.
     int chunk = 2, launched = 0;
-    const int base = hState->pcgIter;
+    pcgBase.resize(nRun);
+    for (int cs = 0; cs < nRun; ++cs) pcgBase[cs] = hState[cs].pcgIter;
     for (int guard = 0; guard < 1000000; ++guard) {
       for (int i = 0; i < chunk; ++i) {
         timer.tag = launched++;
         if (mv.subdomains && c.precond == 0)
           launchLocalIteration<T>(mv, c, p, dState, dPartials, tuning<T>(), ctx->stream,
-                                  &launches, tm());
+                                  &launches, tm(), nRun);
         else
           launchPcgIteration<T>(mv, c, p, dState, dPartials, grid, ctx->stream, &launches, tm());
       }
       timer.tag = -1;
       S4G_CUDA(cudaGetLastError());
-      S4G_TRY(readState(base));
-      if (!hState->pcgContinue || (hState->status & (kErrTimeout | kErrNaN))) return S4G_OK;
+      S4G_TRY(readState(true));
+      if (!anyCase(&DevState::pcgContinue)) return S4G_OK;
+      if (nRun == 1 && (hState->status & (kErrTimeout | kErrNaN))) return S4G_OK;
       chunk = std::min(chunk * 2, 16);
     }
     return setErr(S4G_TIMEOUT, "PCG loop did not end");
@@ -671,20 +862,20 @@ struct Engine {
   s4g_status correctorLoop(Controls& c, int tl, const PcgPtrs<T>& p, int grid) {
     cudaStream_t s = ctx->stream;
     for (;;) {
-      launchRhs<T>(mv, c, f, p.x, p.r, dState, dPartials, s, tm());
-      launches++;
+      launchRhs<T>(mv, c, f, p.x, p.r, dState, dPartials, s, tm(), nRun);
+      launches += 2;
       S4G_TRY(readState());
-      if (hState->pcgContinue) S4G_TRY(pcgLoop<T>(c, p, grid));
-      launchPost<T>(mv, c, f, p.x, dState, dPartials, 1, s, tm());
-      launches += tl ? 2 : 1;
+      if (anyCase(&DevState::pcgContinue)) S4G_TRY(pcgLoop<T>(c, p, grid));
+      launchPost<T>(mv, c, f, p.x, dState, dPartials, 1, s, tm(), nRun);
+      launches += tl ? 3 : 2;
       S4G_CUDA(cudaGetLastError());
       S4G_TRY(readState());
       if (ctx->verbose && outer.info_frequency > 0 &&
           ((hState->iCorr - 1) % outer.info_frequency == 0 || hState->converged))
         std::printf("    %d, %g, %g, 0, %d\n", hState->iCorr - 1, hState->initResMag, hState->relRes,
                     hState->lastMaxIters);
-      if (hState->status & (kErrTimeout | kErrNaN)) return S4G_OK;
-      if (!hState->outerContinue) return S4G_OK;
+      if (nRun == 1 && (hState->status & (kErrTimeout | kErrNaN))) return S4G_OK;
+      if (!anyCase(&DevState::caseLive)) return S4G_OK;
     }
   }
 
@@ -711,8 +902,10 @@ struct Engine {
       if (mixed) S4G_TRY(tuneLocal<float>(ct, pc32));
       else S4G_TRY(tuneLocal<double>(ct, pc));
     }
+    nRun = 1;
     S4G_TRY(initFields(tl));
     S4G_TRY(resetSweepState());
+    S4G_TRY(setLive());
     timer.reset();
     S4G_CUDA(cudaEventRecord(e0, s));
     Controls c = controls(tl);
@@ -734,6 +927,7 @@ struct Engine {
         int zero = 0;
         S4G_CUDA(cudaMemcpyAsync(&dState->enforceLinear, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
         S4G_CUDA(cudaMemcpyAsync(&dState->iCorr, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+        S4G_TRY(setLive());
         launchTractionInit(mv, c, f, s);
         launches++;
         S4G_TRY(loop(1));
@@ -1117,6 +1311,15 @@ s4g_status s4g_op_amul(s4g_mesh* mesh, int k, const double* x, double* y) {
 s4g_status s4g_op_precondition(s4g_mesh* mesh, int k, const double* r, double* w) {
   if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
   return mesh->e.opPrecondition(k, r, w);
+}
+
+s4g_status s4g_solve_cases(s4g_mesh* mesh, int n_cases, const double* bval,
+                           const double* bpress, double* D_out, double* sigma_out,
+                           s4g_perf* perf) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  if (cudaSetDevice(mesh->e.ctx->device) != cudaSuccess)
+    return setErr(S4G_CUDA_ERROR, "cudaSetDevice failed");
+  return mesh->e.solveCases(n_cases, bval, bpress, D_out, sigma_out, perf);
 }
 
 s4g_status s4g_op_amul_dot_noalloc(s4g_mesh* mesh, int k, const double* x, double* y,

@@ -59,21 +59,35 @@ struct FieldPtrs {
   double* flux;  // [nI][6] per internal face: owner-oriented flux of R and gamma|S|delta dU
 };
 
+// The fields of load case cs of a batch (linear-geometry model: the total
+// Lagrangian fields are never batched).
+__host__ __device__ inline FieldPtrs caseFields(FieldPtrs f, int cs, int nC, int nB, int nI) {
+  if (cs == 0) return f;
+  const size_t c = (size_t)cs;
+  f.D[0] += c * 3 * nC; f.D[1] += c * 3 * nC; f.D0 += c * 3 * nC;
+  if (f.D0b) f.D0b += c * 3 * nB;
+  f.G += c * 9 * nC; f.sig += c * 6 * nC;
+  f.Gb += c * 9 * nB; f.sigb += c * 6 * nB; f.g += c * 3 * nB;
+  f.flux += c * 6 * nI;
+  return f;
+}
+
 // g = tractionBoundarySnGrad with the current sigma_b / grad_b (constructor).
 void launchTractionInit(const MeshView& mv, const Controls& c, const FieldPtrs& f,
-                        cudaStream_t s);
+                        cudaStream_t s, int nCases = 1);
 // Post-solve pass: D += x, boundary values, leastSquares gradient, law,
 // boundary gradient/stress, next traction snGrad, convergence reductions.
 // mode 0: constructor pass (no correction, no stress); 1: corrector.
 template <typename T>
 void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const T* x,
                 DevState* st, double* partials, int mode, cudaStream_t s,
-                LaunchTimer* tm = nullptr);
+                LaunchTimer* tm = nullptr, int nCases = 1);
 // RHS pass (FP64): R = div(sigma) + RhieChow + boundary terms, M*D_old for the
 // residual normalisation; zeroes x, sets r = R rounded to the PCG type.
 template <typename T>
 void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, T* x, T* r,
-               DevState* st, double* partials, cudaStream_t s, LaunchTimer* tm = nullptr);
+               DevState* st, double* partials, cudaStream_t s, LaunchTimer* tm = nullptr,
+               int nCases = 1);
 // out[c] = in[c2s[c]] for rows of `width` doubles.
 void launchGather(int n, int width, const int* c2s, const double* in, double* out, cudaStream_t s);
 // TL: new time step -- old-time fields take the converged values.
@@ -92,6 +106,17 @@ struct PcgPtrs {
   T* p2;               // second p buffer of the fused iteration
   const T* lcoef;      // in-part FDIC coefficients (processor-local DIC tables)
 };
+
+// The PCG vectors of load case cs of a batch ([case][nC][3] each); the
+// matrix, the factor and the tables are shared.
+template <typename T>
+__host__ __device__ inline PcgPtrs<T> casePcg(PcgPtrs<T> p, int cs, int nC) {
+  if (cs == 0) return p;
+  const size_t o = (size_t)cs * 3 * nC;
+  p.x += o; p.r += o; p.w += o; p.p += o; p.q += o;
+  if (p.p2) p.p2 += o;
+  return p;
+}
 
 // DIC factor in FP64: rD64 = 1/pivots by a scheduled forward sweep
 // (flags[0] of the FP64 set), then rDa64 = rD64[row]*val64[e].
@@ -143,14 +168,14 @@ struct LocalTuning {
 template <typename T>
 void launchLocalIteration(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p,
                           DevState* st, double* partials, const LocalTuning& t, cudaStream_t s,
-                          long long* launches, LaunchTimer* tm = nullptr);
+                          long long* launches, LaunchTimer* tm = nullptr, int nCases = 1);
 // The two kernels on their own (autotuner).
 template <typename T>
 void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
-                        double* partials, const LocalTuning& t, cudaStream_t s);
+                        double* partials, const LocalTuning& t, cudaStream_t s, int nCases = 1);
 template <typename T>
 void launchLocalSpmv(const MeshView& mv, const PcgPtrs<T>& p, DevState* st, double* partials,
-                     const LocalTuning& t, cudaStream_t s);
+                     const LocalTuning& t, cudaStream_t s, int nCases = 1);
 template <typename T>
 size_t localSmemBytes(const MeshView& mv);
 // Sets the shared-memory attribute of every preconditioner variant and

@@ -174,6 +174,8 @@ __device__ __forceinline__ V3 tractionSnGrad(const MeshView& mv, const Controls&
 }
 
 __global__ void kTractionInit(MeshView mv, Controls c, FieldPtrs f) {
+  f = caseFields(f, blockIdx.y, mv.nC, mv.nB, mv.nI);
+  caseView(mv, blockIdx.y);
   int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= mv.nB || mv.btype[b] != 1) return;
   T9 Fi;
@@ -197,6 +199,11 @@ __device__ __forceinline__ V3 boundaryValue(const MeshView& mv, const Controls& 
 template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
 kApplyX(MeshView mv, FieldPtrs f, const T* __restrict__ x, const DevState* st) {
+  const int cs = blockIdx.y;
+  f = caseFields(f, cs, mv.nC, mv.nB, mv.nI);
+  x += (size_t)cs * 3 * mv.nC;
+  st += cs;
+  if (!st->caseLive) return;
   const int dc = st->dcur;
   const double* Uold = f.D[dc];
   double* Unew = f.D[dc ^ 1];
@@ -214,6 +221,15 @@ __global__ void __launch_bounds__(kRowBlock)
 kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* st,
       double* partials, int mode) {
   __shared__ double smem[32 * 6];
+  {
+    const int cs = blockIdx.y;
+    f = caseFields(f, cs, mv.nC, mv.nB, mv.nI);
+    caseView(mv, cs);
+    x += (size_t)cs * 3 * mv.nC;
+    st += cs;
+    partials += (size_t)cs * mv.caseRec;
+  }
+  if (mode == 1 && !st->caseLive) return;
   const int dc = st->dcur;
   const bool apply = (mode == 1);
   // the corrected field D + x, written by kApplyX (mode 1), or D (mode 0)
@@ -337,6 +353,7 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
   st->iCorr = iCorr + 1;
   st->outerContinue = (!conv && iCorr + 1 < c.nCorr) ? 1 : 0;
   if (st->status & kErrNaN) st->outerContinue = 0;
+  st->caseLive = st->outerContinue;
 }
 
 // TL second half: law (with the enforceLinear decision of this corrector),
@@ -379,6 +396,9 @@ kPostLawTL(MeshView mv, Controls c, FieldPtrs f, const DevState* st) {
 // cell pass adds it to the owner and subtracts it from the neighbour.
 __global__ void __launch_bounds__(kRowBlock)
 kRhsFace(MeshView mv, Controls c, FieldPtrs f, const DevState* st) {
+  f = caseFields(f, blockIdx.y, mv.nC, mv.nB, mv.nI);
+  st += blockIdx.y;
+  if (!st->caseLive) return;
   const double* U = f.D[st->dcur];
   const int el = c.tl ? st->enforceLinear : 1;
   for (int fi = blockIdx.x * blockDim.x + threadIdx.x; fi < mv.nI; fi += gridDim.x * blockDim.x) {
@@ -412,6 +432,16 @@ __global__ void __launch_bounds__(kRowBlock)
 kRhs(MeshView mv, Controls c, FieldPtrs f, T* __restrict__ x, T* __restrict__ r,
      DevState* st, double* partials) {
   __shared__ double smem[32 * 6];
+  {
+    const int cs = blockIdx.y;
+    f = caseFields(f, cs, mv.nC, mv.nB, mv.nI);
+    caseView(mv, cs);
+    x += (size_t)cs * 3 * mv.nC;
+    r += (size_t)cs * 3 * mv.nC;
+    st += cs;
+    partials += (size_t)cs * mv.caseRec;
+  }
+  if (!st->caseLive) return;
   const double* U = f.D[st->dcur];
   double part[6] = {0, 0, 0, 0, 0, 0};  // normFactor (3), sum|R| (3)
   const int el = c.tl ? st->enforceLinear : 1;
@@ -527,37 +557,40 @@ void launchMatrix(const MeshView& mv, double gamma, double* val, double* diag, c
 }
 
 void launchTractionInit(const MeshView& mv, const Controls& c, const FieldPtrs& f,
-                        cudaStream_t s) {
+                        cudaStream_t s, int nCases) {
   if (mv.nB == 0) return;
-  kTractionInit<<<(mv.nB + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, c, f);
+  kTractionInit<<<dim3((mv.nB + kRowBlock - 1) / kRowBlock, nCases), kRowBlock, 0, s>>>(mv, c, f);
 }
 
 template <typename T>
 void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const T* x,
-                DevState* st, double* partials, int mode, cudaStream_t s, LaunchTimer* tm) {
+                DevState* st, double* partials, int mode, cudaStream_t s, LaunchTimer* tm,
+                int nCases) {
   const int grid = (mv.nC + kRowBlock - 1) / kRowBlock;
   TimeScope ts(tm, S4G_K_POST, s);
-  if (mode == 1) kApplyX<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, f, x, st);
-  kPost<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, c, f, x, st, partials, mode);
+  const dim3 g(mv.rowGrid, nCases);
+  if (mode == 1) kApplyX<T><<<g, kRowBlock, 0, s>>>(mv, f, x, st);
+  kPost<T><<<g, kRowBlock, 0, s>>>(mv, c, f, x, st, partials, mode);
   if (c.tl && mode == 1) kPostLawTL<<<grid, kRowBlock, 0, s>>>(mv, c, f, st);
 }
 
 template <typename T>
 void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, T* x, T* r,
-               DevState* st, double* partials, cudaStream_t s, LaunchTimer* tm) {
+               DevState* st, double* partials, cudaStream_t s, LaunchTimer* tm, int nCases) {
   TimeScope ts(tm, S4G_K_RHS, s);
-  if (mv.nI > 0) kRhsFace<<<mv.rowGrid, kRowBlock, 0, s>>>(mv, c, f, st);
-  kRhs<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, c, f, x, r, st, partials);
+  const dim3 g(mv.rowGrid, nCases);
+  if (mv.nI > 0) kRhsFace<<<g, kRowBlock, 0, s>>>(mv, c, f, st);
+  kRhs<T><<<g, kRowBlock, 0, s>>>(mv, c, f, x, r, st, partials);
 }
 
 template void launchPost<double>(const MeshView&, const Controls&, const FieldPtrs&, const double*,
-                                 DevState*, double*, int, cudaStream_t, LaunchTimer*);
+                                 DevState*, double*, int, cudaStream_t, LaunchTimer*, int);
 template void launchPost<float>(const MeshView&, const Controls&, const FieldPtrs&, const float*,
-                                DevState*, double*, int, cudaStream_t, LaunchTimer*);
+                                DevState*, double*, int, cudaStream_t, LaunchTimer*, int);
 template void launchRhs<double>(const MeshView&, const Controls&, const FieldPtrs&, double*, double*,
-                                DevState*, double*, cudaStream_t, LaunchTimer*);
+                                DevState*, double*, cudaStream_t, LaunchTimer*, int);
 template void launchRhs<float>(const MeshView&, const Controls&, const FieldPtrs&, float*, float*,
-                               DevState*, double*, cudaStream_t, LaunchTimer*);
+                               DevState*, double*, cudaStream_t, LaunchTimer*, int);
 
 void launchGather(int n, int width, const int* c2s, const double* in, double* out, cudaStream_t s) {
   long tot = (long)n * width;

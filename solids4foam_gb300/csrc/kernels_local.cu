@@ -124,6 +124,9 @@ constexpr int locMinBlocks() {
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT, (locMinBlocks<T, NT>()))
 kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partials) {
+  p = casePcg(p, blockIdx.y, mv.nC);
+  st += blockIdx.y;
+  partials += (size_t)blockIdx.y * mv.caseRec;
   if (!st->pcgContinue) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   const LocSmem<T> sm = locSmem<T>(mv, smraw);
@@ -262,6 +265,9 @@ __device__ __forceinline__ T pNew(bool first, T w, T b, T po) { return first ? w
 template <typename T, int U>
 __global__ void __launch_bounds__(kRowBlock, (U > 1 ? (sizeof(T) == 4 ? 3 : 2) : 4))
 kLocSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
+  p = casePcg(p, blockIdx.y, mv.nC);
+  st += blockIdx.y;
+  partials += (size_t)blockIdx.y * mv.caseRec;
   if (!st->pcgContinue) return;
   __shared__ double red[32 * 3];
   const int pb = st->pbuf;
@@ -352,6 +358,8 @@ kLocSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
 template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
 kLocPUpdate(MeshView mv, PcgPtrs<T> p, const DevState* st) {
+  p = casePcg(p, blockIdx.y, mv.nC);
+  st += blockIdx.y;
   if (!st->pcgContinue) return;
   const int pb = st->pbuf;
   const T* __restrict__ po = pb ? p.p2 : p.p;
@@ -373,6 +381,9 @@ kLocPUpdate(MeshView mv, PcgPtrs<T> p, const DevState* st) {
 template <typename T>
 __global__ void __launch_bounds__(kRowBlock, 4)
 kLocSpmvSplit(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
+  p = casePcg(p, blockIdx.y, mv.nC);
+  st += blockIdx.y;
+  partials += (size_t)blockIdx.y * mv.caseRec;
   if (!st->pcgContinue) return;
   __shared__ double red[32 * 3];
   const int pb = st->pbuf;
@@ -431,8 +442,8 @@ kLocSpmvSplit(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
 
 template <typename T, int NT>
 void launchPrecondNT(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
-                     double* partials, int grid, cudaStream_t s) {
-  kLocPrecond<T, NT><<<grid, NT, localSmemBytes<T>(mv), s>>>(mv, c, p, st, partials);
+                     double* partials, int grid, cudaStream_t s, int nCases) {
+  kLocPrecond<T, NT><<<dim3(grid, nCases), NT, localSmemBytes<T>(mv), s>>>(mv, c, p, st, partials);
 }
 
 template <typename T, int NT>
@@ -471,38 +482,39 @@ void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaS
 
 template <typename T>
 void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
-                        double* partials, const LocalTuning& t, cudaStream_t s) {
+                        double* partials, const LocalTuning& t, cudaStream_t s, int nCases) {
   switch (t.ntIdx) {
-    case 0: launchPrecondNT<T, 64>(mv, c, p, st, partials, t.grid[0], s); break;
-    case 2: launchPrecondNT<T, 256>(mv, c, p, st, partials, t.grid[2], s); break;
-    default: launchPrecondNT<T, 128>(mv, c, p, st, partials, t.grid[1], s); break;
+    case 0: launchPrecondNT<T, 64>(mv, c, p, st, partials, t.grid[0], s, nCases); break;
+    case 2: launchPrecondNT<T, 256>(mv, c, p, st, partials, t.grid[2], s, nCases); break;
+    default: launchPrecondNT<T, 128>(mv, c, p, st, partials, t.grid[1], s, nCases); break;
   }
 }
 
 template <typename T>
 void launchLocalSpmv(const MeshView& mv, const PcgPtrs<T>& p, DevState* st, double* partials,
-                     const LocalTuning& t, cudaStream_t s) {
+                     const LocalTuning& t, cudaStream_t s, int nCases) {
+  const dim3 g(mv.rowGrid, nCases);
   if (t.uIdx == 2) {
-    kLocPUpdate<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, p, st);
-    kLocSpmvSplit<T><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, p, st, partials);
+    kLocPUpdate<T><<<g, kRowBlock, 0, s>>>(mv, p, st);
+    kLocSpmvSplit<T><<<g, kRowBlock, 0, s>>>(mv, p, st, partials);
   } else if (t.uIdx == 1) {
-    kLocSpmv<T, 6><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, p, st, partials);
+    kLocSpmv<T, 6><<<g, kRowBlock, 0, s>>>(mv, p, st, partials);
   } else {
-    kLocSpmv<T, 1><<<mv.rowGrid, kRowBlock, 0, s>>>(mv, p, st, partials);
+    kLocSpmv<T, 1><<<g, kRowBlock, 0, s>>>(mv, p, st, partials);
   }
 }
 
 template <typename T>
 void launchLocalIteration(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p,
                           DevState* st, double* partials, const LocalTuning& t, cudaStream_t s,
-                          long long* launches, LaunchTimer* tm) {
+                          long long* launches, LaunchTimer* tm, int nCases) {
   {
     TimeScope ts(tm, S4G_K_LOC_PRECOND, s);
-    launchLocalPrecond<T>(mv, c, p, st, partials, t, s);
+    launchLocalPrecond<T>(mv, c, p, st, partials, t, s, nCases);
   }
   {
     TimeScope ts(tm, S4G_K_LOC_SPMV, s);
-    launchLocalSpmv<T>(mv, p, st, partials, t, s);
+    launchLocalSpmv<T>(mv, p, st, partials, t, s, nCases);
   }
   *launches += t.uIdx == 2 ? 3 : 2;
 }
@@ -512,12 +524,13 @@ void launchLocalIteration(const MeshView& mv, const Controls& c, const PcgPtrs<T
   template cudaError_t localPrepare<T>(const MeshView&, int*);                                  \
   template void launchLocalGather<T>(int, const int*, const double*, T*, cudaStream_t);          \
   template void launchLocalPrecond<T>(const MeshView&, const Controls&, const PcgPtrs<T>&,      \
-                                      DevState*, double*, const LocalTuning&, cudaStream_t);    \
+                                      DevState*, double*, const LocalTuning&, cudaStream_t,     \
+                                      int);                                                     \
   template void launchLocalSpmv<T>(const MeshView&, const PcgPtrs<T>&, DevState*, double*,      \
-                                   const LocalTuning&, cudaStream_t);                           \
+                                   const LocalTuning&, cudaStream_t, int);                      \
   template void launchLocalIteration<T>(const MeshView&, const Controls&, const PcgPtrs<T>&,    \
                                         DevState*, double*, const LocalTuning&, cudaStream_t,   \
-                                        long long*, LaunchTimer*);
+                                        long long*, LaunchTimer*, int);
 S4G_INSTANTIATE(double)
 S4G_INSTANTIATE(float)
 #undef S4G_INSTANTIATE

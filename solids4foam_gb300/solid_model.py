@@ -78,6 +78,40 @@ def _desc(mesh, keep):
     return d
 
 
+def _law_struct(law: dict):
+    """constant/mechanicalProperties: one linearElastic or neoHookeanElastic law."""
+    t = law.get("type", "linearElastic")
+    if t not in ("linearElastic", "neoHookeanElastic"):
+        raise ValueError(f"unknown mechanical law {t!r}")
+    use_muK = "mu" in law and "K" in law
+    return _lib.Law(_lib.LINEAR_ELASTIC if t == "linearElastic" else _lib.NEO_HOOKEAN,
+                    1 if use_muK else 0, float(law.get("E", 0.0)), float(law.get("nu", 0.0)),
+                    float(law.get("mu", 0.0)), float(law.get("K", 0.0)),
+                    float(law.get("rho", 1000.0)))
+
+
+def _control_structs(L, solver: dict, outer: dict, precision: str = "FP64"):
+    """system/fvSolution solvers { D } and solidProperties <model>Coeffs."""
+    lin, out = _lib.LinSolver(), _lib.Outer()
+    L.s4g_default_controls(ct.byref(lin), ct.byref(out))
+    if "preconditioner" in solver:
+        lin.preconditioner = PRECONDITIONERS[solver["preconditioner"]]
+    lin.tolerance = solver.get("tolerance", lin.tolerance)
+    lin.rel_tol = solver.get("relTol", lin.rel_tol)
+    lin.max_iter = solver.get("maxIter", lin.max_iter)
+    out.n_correctors = outer.get("nCorrectors", out.n_correctors)
+    out.solution_tol = outer.get("solutionTolerance", out.solution_tol)
+    out.alternative_tol = outer.get("alternativeTolerance", out.alternative_tol)
+    out.material_tol = outer.get("materialTolerance", out.material_tol)
+    out.info_frequency = outer.get("infoFrequency", out.info_frequency)
+    stab = outer.get("stabilisation", {"type": "RhieChow", "scaleFactor": 0.1})
+    if stab.get("type", "RhieChow") != "RhieChow":
+        raise ValueError("only RhieChow stabilisation is built")
+    out.stab_scale = stab.get("scaleFactor", 0.1)
+    prec = {"FP64": _lib.FP64, "FP32_REFINE": _lib.FP32_REFINE}[precision]
+    return lin, out, prec
+
+
 class SolidModel:
     """GPU drop-in for one solid region's outer-corrector loop."""
 
@@ -121,14 +155,7 @@ class SolidModel:
 
     # -- constant/mechanicalProperties
     def set_law(self, law: dict):
-        t = law.get("type", "linearElastic")
-        if t not in ("linearElastic", "neoHookeanElastic"):
-            raise ValueError(f"unknown mechanical law {t!r}")
-        use_muK = "mu" in law and "K" in law
-        lw = _lib.Law(_lib.LINEAR_ELASTIC if t == "linearElastic" else _lib.NEO_HOOKEAN,
-                      1 if use_muK else 0, float(law.get("E", 0.0)), float(law.get("nu", 0.0)),
-                      float(law.get("mu", 0.0)), float(law.get("K", 0.0)),
-                      float(law.get("rho", 1000.0)))
+        lw = _law_struct(law)
         _lib.check(self.L.s4g_material_set(self.h, ct.byref(lw)), "s4g_material_set")
 
     # -- 0/D boundaryField
@@ -146,23 +173,7 @@ class SolidModel:
 
     # -- system/fvSolution and solidProperties <model>Coeffs
     def set_controls(self, solver: dict, outer: dict, precision: str = "FP64"):
-        lin, out = _lib.LinSolver(), _lib.Outer()
-        self.L.s4g_default_controls(ct.byref(lin), ct.byref(out))
-        if "preconditioner" in solver:
-            lin.preconditioner = PRECONDITIONERS[solver["preconditioner"]]
-        lin.tolerance = solver.get("tolerance", lin.tolerance)
-        lin.rel_tol = solver.get("relTol", lin.rel_tol)
-        lin.max_iter = solver.get("maxIter", lin.max_iter)
-        out.n_correctors = outer.get("nCorrectors", out.n_correctors)
-        out.solution_tol = outer.get("solutionTolerance", out.solution_tol)
-        out.alternative_tol = outer.get("alternativeTolerance", out.alternative_tol)
-        out.material_tol = outer.get("materialTolerance", out.material_tol)
-        out.info_frequency = outer.get("infoFrequency", out.info_frequency)
-        stab = outer.get("stabilisation", {"type": "RhieChow", "scaleFactor": 0.1})
-        if stab.get("type", "RhieChow") != "RhieChow":
-            raise ValueError("only RhieChow stabilisation is built")
-        out.stab_scale = stab.get("scaleFactor", 0.1)
-        prec = {"FP64": _lib.FP64, "FP32_REFINE": _lib.FP32_REFINE}[precision]
+        lin, out, prec = _control_structs(self.L, solver, outer, precision)
         _lib.check(self.L.s4g_solver_set(self.h, ct.byref(lin), ct.byref(out), prec),
                    "s4g_solver_set")
 
@@ -175,6 +186,37 @@ class SolidModel:
                               sig.ctypes.data, ct.byref(perf))
         _lib.check(st, "s4g_solve", allow=(_lib.OK, _lib.NOT_CONVERGED))
         return D, sig, perf.as_dict()
+
+    def evolve_cases(self, case_bcs: list):
+        """Batched load cases (s4g_solve_cases): case_bcs is a list of
+        dicts {patch name: (type, value, pressure)} like the constructor's
+        bcs, one per case, with the model's boundary-condition types.
+        Returns (D [C,n,3], sigma [C,n,6], [perf per case])."""
+        C = len(case_bcs)
+        nI = int(np.asarray(self.mesh["neighbour"]).shape[0])
+        nB = int(np.asarray(self.mesh["owner"]).shape[0]) - nI
+        names = list(self.mesh.get("patch_names", PATCHES))
+        starts = np.asarray(self.mesh["patch_start"]) - nI
+        sizes = np.asarray(self.mesh["patch_size"])
+        bval = np.zeros((C, nB, 3))
+        bpress = np.zeros((C, nB))
+        for c, bcs in enumerate(case_bcs):
+            for name, spec in bcs.items():
+                i = names.index(name)
+                lo, hi = int(starts[i]), int(starts[i] + sizes[i])
+                value = spec[1] if len(spec) > 1 else None
+                pressure = spec[2] if len(spec) > 2 else None
+                if value is not None:
+                    bval[c, lo:hi] = np.broadcast_to(np.asarray(value, np.float64), (hi - lo, 3))
+                if pressure is not None:
+                    bpress[c, lo:hi] = np.broadcast_to(np.asarray(pressure, np.float64), (hi - lo,))
+        D = np.zeros((C, self.n_cells, 3))
+        sig = np.zeros((C, self.n_cells, 6))
+        perfs = (_lib.Perf * C)()
+        st = self.L.s4g_solve_cases(self.h, C, bval.ctypes.data, bpress.ctypes.data, D.ctypes.data,
+                                    sig.ctypes.data, ct.cast(perfs, ct.c_void_p))
+        _lib.check(st, "s4g_solve_cases", allow=(_lib.OK, _lib.NOT_CONVERGED))
+        return D, sig, [p.as_dict() for p in perfs]
 
     def gradD(self):
         G = np.zeros((self.n_cells, 9))
@@ -245,3 +287,102 @@ def plan(mesh, renumber: str = "tiled", part_size: int = 512, dic_subdomains: bo
     _lib.check(L.s4g_mesh_plan(ct.byref(d), ct.byref(opts), perm.ctypes.data, ct.byref(inf)),
                "s4g_mesh_plan")
     return perm, {f[0]: getattr(inf, f[0]) for f in inf._fields_}
+
+
+BC_TYPES = {"fixedDisplacement": _lib.FIXED_DISPLACEMENT, "solidTraction": _lib.SOLID_TRACTION,
+            "solidTractionFree": _lib.SOLID_TRACTION}
+
+
+class Server:
+    """Continuous admission of solves onto one GPU (s4g_server_*): submit
+    requests from any thread, poll their results; p50/p99 latency and
+    throughput from stats()."""
+
+    def __init__(self, device: int = 0, max_slots: int = 8, memory_budget: int = 0,
+                 dry_run: bool = False, dry_run_us_per_kcell: float = 50.0):
+        self.L = _lib.lib()
+        o = _lib.ServerOpts(device, max_slots, int(memory_budget), 1 if dry_run else 0,
+                            float(dry_run_us_per_kcell))
+        h = ct.c_void_p()
+        _lib.check(self.L.s4g_server_create(ct.byref(o), ct.byref(h)), "s4g_server_create")
+        self.h = h
+        self.n_cells = {}
+
+    def submit(self, mesh, law: dict, bcs: dict, model: str = "linearGeometryTotalDisplacement",
+               solver: dict | None = None, outer: dict | None = None, precision: str = "FP64",
+               n_increments: int = 1, renumber: str = "tiled", part_size: int = 512,
+               dic_subdomains: bool = False):
+        keep = []
+        d = _desc(mesh, keep)
+        names = list(mesh.get("patch_names", PATCHES))
+        patches, types, vecs, press = [], [], [], []
+        for name, spec in bcs.items():
+            i = names.index(name)
+            size = int(np.asarray(mesh["patch_size"])[i])
+            patches.append(i)
+            types.append(BC_TYPES[spec[0]])
+            v = spec[1] if len(spec) > 1 else None
+            p = spec[2] if len(spec) > 2 else None
+            va = None if v is None else np.ascontiguousarray(
+                np.broadcast_to(np.asarray(v, np.float64), (size, 3)))
+            pa = None if p is None else np.ascontiguousarray(
+                np.broadcast_to(np.asarray(p, np.float64), (size,)))
+            keep += [va, pa]
+            vecs.append(None if va is None else va.ctypes.data)
+            press.append(None if pa is None else pa.ctypes.data)
+        nb = len(patches)
+        pa_ = (ct.c_int * max(nb, 1))(*patches)
+        ta_ = (ct.c_int * max(nb, 1))(*types)
+        va_ = (ct.c_void_p * max(nb, 1))(*vecs)
+        pr_ = (ct.c_void_p * max(nb, 1))(*press)
+        lin, out, prec = _control_structs(self.L, solver or {}, outer or {}, precision)
+        rq = _lib.Request()
+        rq.mesh = ct.cast(ct.pointer(d), ct.c_void_p)
+        rq.mesh_opts = _lib.MeshOpts(RENUMBER[renumber], part_size, 0,
+                                     1 if dic_subdomains else 0, 0)
+        rq.law = _law_struct(law)
+        rq.n_bc = nb
+        rq.bc_patch = ct.cast(pa_, ct.c_void_p)
+        rq.bc_type = ct.cast(ta_, ct.c_void_p)
+        rq.bc_vec3 = ct.cast(va_, ct.c_void_p)
+        rq.bc_pressure = ct.cast(pr_, ct.c_void_p)
+        rq.lin, rq.outer, rq.precision = lin, out, prec
+        rq.model = MODELS[model]
+        rq.n_increments = int(n_increments)
+        rid = ct.c_uint64()
+        _lib.check(self.L.s4g_server_submit(self.h, ct.byref(rq), ct.byref(rid)),
+                   "s4g_server_submit")
+        self.n_cells[rid.value] = d.n_cells
+        return rid.value
+
+    def result(self, rid: int, wait: bool = True):
+        """(status, D, sigma, perf); None while pending (wait=False)."""
+        n = self.n_cells[rid]
+        D = np.zeros((n, 3))
+        sig = np.zeros((n, 6))
+        perf = _lib.Perf()
+        st = self.L.s4g_server_poll(self.h, rid, 1 if wait else 0, D.ctypes.data, sig.ctypes.data,
+                                    ct.byref(perf))
+        if st == _lib.PENDING:
+            return None
+        del self.n_cells[rid]
+        return st, D, sig, perf.as_dict()
+
+    def cancel(self, rid: int):
+        _lib.check(self.L.s4g_server_cancel(self.h, rid), "s4g_server_cancel")
+
+    def stats(self):
+        st = _lib.ServerStats()
+        _lib.check(self.L.s4g_server_get_stats(self.h, ct.byref(st)), "s4g_server_get_stats")
+        return {f[0]: getattr(st, f[0]) for f in st._fields_}
+
+    def close(self):
+        if self.h:
+            self.L.s4g_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -146,7 +146,8 @@ def test_ctypes_structs_match_the_c_header(tmp_path):
     pairs = {"s4g_ctx_opts": _lib.CtxOpts, "s4g_mesh_desc": _lib.MeshDesc,
              "s4g_mesh_opts": _lib.MeshOpts, "s4g_mesh_info": _lib.MeshInfo,
              "s4g_law": _lib.Law, "s4g_lin_solver": _lib.LinSolver, "s4g_outer": _lib.Outer,
-             "s4g_perf": _lib.Perf}
+             "s4g_perf": _lib.Perf, "s4g_server_opts": _lib.ServerOpts,
+             "s4g_server_stats": _lib.ServerStats, "s4g_request": _lib.Request}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "s4g.h"', "int main(void) {"]
     for cname, py in pairs.items():
         lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
@@ -166,3 +167,51 @@ def test_ctypes_structs_match_the_c_header(tmp_path):
         assert got[(cname, "size")] == ct.sizeof(py), cname
         for fname, _ in py._fields_:
             assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
+
+
+def test_server_scheduler_dry_run(built):
+    """The serving scheduler without a GPU (dry run): rejection of what can
+    never fit, cancellation of a queued request, first-fit admission by
+    footprint (small requests pass a large one that waits for memory), the
+    memory budget never exceeded, and the latency statistics."""
+    import time
+    m_small = sg.box_mesh(6, 6, 6, 1.0, 1.0, 1.0, 0.1, 1)
+    m_big = sg.box_mesh(40, 40, 40, 1.0, 1.0, 1.0, 0.1, 1)
+    law = dict(type="linearElastic", E=70e9, nu=0.33)
+    bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", [0, 0, -1e5], None)}
+    # one slot: a queued request can be cancelled; an oversized one is rejected
+    srv = sg.Server(max_slots=1, memory_budget=1 << 30, dry_run=True, dry_run_us_per_kcell=2000)
+    with pytest.raises(_lib.S4GError, match="ADMISSION_REJECTED"):
+        srv.submit(sg.box_mesh(160, 160, 160, 1.0, 1.0, 1.0, 0.1, 1), law, bcs)
+    big = srv.submit(m_big, law, bcs)  # 64,000 cells: about 128 ms
+    time.sleep(0.02)
+    big_bytes = srv.stats()["bytes_in_use"]
+    queued = srv.submit(m_small, law, bcs)
+    srv.cancel(queued)
+    assert srv.result(queued)[0] == _lib.CANCELLED
+    assert srv.result(big)[0] == _lib.OK
+    st = srv.stats()
+    assert st["rejected"] == 1 and st["cancelled"] == 1 and st["completed"] == 1
+    srv.close()
+    # two slots, memory for one large request: small ones pass the second large one
+    srv = sg.Server(max_slots=2, memory_budget=int(1.5 * big_bytes), dry_run=True,
+                    dry_run_us_per_kcell=2000)
+    b1 = srv.submit(m_big, law, bcs)
+    b2 = srv.submit(m_big, law, bcs)
+    smalls = [srv.submit(m_small, law, bcs) for _ in range(4)]
+    time.sleep(0.03)
+    st = srv.stats()
+    # the four small ones ran beside the first large one; the second waits
+    assert st["completed"] == 4 and st["running"] == 1 and st["queued"] == 1
+    assert st["bytes_in_use"] <= st["memory_budget"]
+    done = {}
+    for rid in smalls + [b1, b2]:
+        status, D, sig, perf = srv.result(rid)
+        assert status == _lib.OK and D.shape == (sig.shape[0], 3)
+        done[rid] = time.perf_counter()
+    st = srv.stats()
+    assert st["completed"] == 6
+    assert 0 < st["p50_ms"] <= st["p99_ms"] and st["solves_per_s"] > 0
+    # the second large request finished last: the small ones did not wait for it
+    assert st["p99_ms"] > 200
+    srv.close()
