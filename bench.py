@@ -288,13 +288,13 @@ def run_batched(args, ctx):
 
 
 def run_served(args):
-    """A Poisson stream of uneven solves (80% linear FP32+refine with the
-    processor-local DIC, 20% neoHookean total Lagrangian, 10 increments)
-    through the server, against the same requests solved one after another
-    in plain FP64."""
+    """A Poisson stream of uneven solves (linear FP32+refine with the
+    processor-local DIC; a --serve-tl-fraction share of neoHookean total
+    Lagrangian requests, 0 by default) through the server, against the same
+    requests solved one after another in plain FP64."""
     import solids4foam_gb300 as sg
     from solids4foam_gb300.cases import served_stream
-    stream = served_stream(args.serve_n)
+    stream = served_stream(args.serve_n, tl_fraction=args.serve_tl_fraction)
     srv = sg.Server(max_slots=args.serve_slots)
     t0 = time.perf_counter()
     ids = []
@@ -325,7 +325,8 @@ def run_served(args):
         errs.append(rel_l2(res[1], D))
     ctx.close()
     n = len(stream)
-    return {"workload": f"stream{n}_poisson_boxes_8^3-40^3_20pct_neoHookean",
+    return {"workload": f"stream{n}_poisson_boxes_8^3-40^3",
+            "neoHookean_fraction": args.serve_tl_fraction,
             "requests": n, "slots": args.serve_slots, "solves_per_s": n / wall,
             "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
             "all_ok": all(r[0] in (0, 3) for r in results),
@@ -481,6 +482,8 @@ def main():
     ap.add_argument("--no-served", action="store_true", help="skip the served stream")
     ap.add_argument("--serve-n", type=int, default=24)
     ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--serve-tl-fraction", type=float, default=0.0,
+                    help="share of neoHookean total Lagrangian requests in the stream")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

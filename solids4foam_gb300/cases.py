@@ -104,13 +104,15 @@ def load_cases(n=64, n_cases=64, mesh_seed=2, load_seed=3, jitter=0.2):
 
 
 def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=40 ** 3, tl_fraction=0.2,
-                  rate_per_s=20.0):
+                  rate_per_s=20.0, nu_max=0.4):
     """A stream of solve requests with Poisson arrivals (rate_per_s, seeded):
     jittered boxes whose cell counts are log-uniform in [min_cells,
     max_cells] with aspect ratios up to 2; a tl_fraction of them are
     neoHookeanElastic nonLinearGeometryTotalLagrangian solves (mu uniform in
     0.5-5 MPa, K/mu uniform in 10-50, traction ramped over 10 increments),
-    the rest linearElastic (E log-uniform 1-300 GPa, nu uniform 0.2-0.45).
+    the rest linearElastic (E log-uniform 1-300 GPa, nu uniform in
+    0.2-nu_max; the segregated corrector loop stops converging near nu = 0.42
+    on these meshes, in the CPU oracle as well, so nu_max defaults to 0.4).
     Returns a list of (arrival_s, request kwargs)."""
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -135,7 +137,7 @@ def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=40 ** 3, tl
                        outer=dict(nCorrectors=200))
         else:
             E = np.exp(rng.uniform(np.log(1e9), np.log(300e9)))
-            nu = rng.uniform(0.2, 0.45)
+            nu = rng.uniform(0.2, nu_max)
             tr = rng.normal(0.0, 1e6, 3)
             req = dict(mesh=mesh, law=dict(type="linearElastic", E=E, nu=nu),
                        bcs={"zmin": ("fixedDisplacement", None, None),

@@ -102,6 +102,24 @@ struct DevState {
   unsigned ticket[2], ctasDone[2], partsDone[2], epoch[2];
 };
 
+// The dynamic shared-memory limit of a kernel is a process-wide attribute:
+// it is set to the device's opt-in maximum (not to one mesh's need), so
+// that meshes of different sizes, uploaded in any order or from several
+// threads, can all launch.  Occupancy follows the size each launch asks for.
+template <typename K>
+inline cudaError_t setMaxDynamicSmem(K kernel) {
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)fa.sharedSizeBytes);
+}
+
 // ---- memory-order helpers --------------------------------------------------
 __device__ __forceinline__ unsigned ldAcquire(const unsigned* p) {
   unsigned v;

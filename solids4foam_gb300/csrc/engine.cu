@@ -26,6 +26,8 @@ namespace s4g {
 
 thread_local std::string gLastError;
 
+void setLastError(const std::string& msg) { gLastError = msg; }
+
 static s4g_status setErr(s4g_status st, const std::string& msg) {
   gLastError = msg;
   return st;

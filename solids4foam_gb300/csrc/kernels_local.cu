@@ -449,8 +449,7 @@ void launchPrecondNT(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p,
 template <typename T, int NT>
 cudaError_t prepareNT(const MeshView& mv, int* blocksPerSM) {
   const int sm = (int)localSmemBytes<T>(mv);
-  cudaError_t e = cudaFuncSetAttribute(kLocPrecond<T, NT>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaError_t e = setMaxDynamicSmem(kLocPrecond<T, NT>);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, NT>, NT, sm);
 }

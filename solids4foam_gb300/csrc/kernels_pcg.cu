@@ -532,10 +532,9 @@ size_t sweepSmemBytes(const MeshView& mv) {
 template <typename T>
 cudaError_t sweepPrepare(const MeshView& mv, int* blocksPerSM) {
   const int sm = (int)sweepSmemBytes<T>(mv);
-  cudaError_t e = cudaFuncSetAttribute(kSweepSm<0, kSweepSmBlock, T>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  cudaError_t e = setMaxDynamicSmem(kSweepSm<0, kSweepSmBlock, T>);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(kSweepSm<1, kSweepSmBlock, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm);
+  e = setMaxDynamicSmem(kSweepSm<1, kSweepSmBlock, T>);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kSweepSm<0, kSweepSmBlock, T>,
                                                        kSweepSmBlock, sm);

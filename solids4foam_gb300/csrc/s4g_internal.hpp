@@ -61,6 +61,10 @@ struct HostPrep {
   int maxLocEntries = 0, maxLocMeta = 0;
 };
 
+// Sets the calling thread's s4g_last_error message (the server reports a
+// worker's error to the thread that polls).
+void setLastError(const std::string& msg);
+
 // Builds the preparation.  Returns S4G_OK or S4G_BAD_ARG with `err` set.
 s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o,
                        HostPrep& hp, std::string& err);

@@ -33,6 +33,7 @@
 #include <cuda_runtime.h>
 
 #include "s4g.h"
+#include "s4g_internal.hpp"
 
 namespace {
 
@@ -307,6 +308,7 @@ s4g_status s4g_server_poll(s4g_server* sv, uint64_t id, int wait, double* D_out,
     std::memcpy(sigma_out, r->sigma.data(), sizeof(double) * r->sigma.size());
   if (perf) *perf = r->perf;
   const s4g_status st = r->status;
+  if (!r->error.empty()) s4g::setLastError(r->error);
   sv->all.erase(it);
   delete r;
   return st;
