@@ -317,6 +317,8 @@ def run_served(args):
     for (arrival, req), res in zip(stream, results):
         kw = dict(req)
         n_inc = kw.pop("n_increments", 1)
+        if kw.get("model", "linearGeometryTotalDisplacement") == "linearGeometryTotalDisplacement":
+            kw["dic_subdomains"] = True  # the same preconditioner as the served run
         m = sg.SolidModel(ctx, kw.pop("mesh"), kw.pop("law"), kw.pop("bcs"), precision="FP64", **kw)
         t1 = time.perf_counter()
         D, sig, perf = m.evolve(n_increments=n_inc)

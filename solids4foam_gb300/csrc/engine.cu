@@ -17,6 +17,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <map>
 #include <vector>
 
 #include "kernels.cuh"
@@ -162,7 +163,28 @@ struct Engine {
   EventTimer timer;
   LaunchTimer* tm() { return ctx->profile ? &timer : nullptr; }
 
+  // CUDA graphs of the PCG launch batches: one per (value type, batch
+  // length, case count), captured on first use and replayed with one launch.
+  // A graph holds the kernels' arguments, so it is dropped when buffers are
+  // reallocated (generation) and recaptured when the controls or the tuned
+  // variants differ from the captured ones.
+  struct PcgGraph {
+    cudaGraphExec_t exec = nullptr;
+    int generation = -1, ntIdx = -1, uIdx = -1, grid = -1;
+    Controls c{};
+  };
+  std::map<long, PcgGraph> pcgGraphs;
+  int generation = 0;
+  bool graphsOk = true;
+
+  void dropGraphs() {
+    for (auto& kv : pcgGraphs)
+      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    pcgGraphs.clear();
+  }
+
   ~Engine() {
+    dropGraphs();
     for (void* p : allocs) cudaFree(p);
     if (hState) cudaFreeHost(hState);
   }
@@ -523,6 +545,7 @@ struct Engine {
       S4G_TRY(alloc(&pc32.x, nv)); S4G_TRY(alloc(&pc32.r, nv)); S4G_TRY(alloc(&pc32.w, nv));
       S4G_TRY(alloc(&pc32.p, nv)); S4G_TRY(alloc(&pc32.q, nv));
       pc32.flags[0] = pc.flags[0]; pc32.flags[1] = pc.flags[1];
+      ++generation;
       if (mv.subdomains) {
         float* lc;
         S4G_TRY(alloc(&pc32.p2, 3 * nC * (size_t)caseCap));
@@ -640,6 +663,8 @@ struct Engine {
     S4G_CUDA(cudaMallocHost((void**)&hState, sizeof(DevState) * n));
     std::memset(hState, 0, sizeof(DevState) * n);
     caseCap = C;
+    ++generation;  // captured graphs refer to the old buffers
+    dropGraphs();
     return S4G_OK;
   }
 
@@ -831,6 +856,40 @@ struct Engine {
     return S4G_OK;
   }
 
+  // The graph of a batch of n PCG iterations for the current state of the
+  // engine (captured on first use); nullptr if capture is not possible, in
+  // which case the caller launches directly.
+  template <typename T, typename F>
+  cudaGraphExec_t pcgGraph(const Controls& c, const PcgPtrs<T>& p, int grid, int n, F& launchBatch) {
+    const long key = ((long)(sizeof(T)) << 40) | ((long)nRun << 8) | (long)n;
+    PcgGraph& g = pcgGraphs[key];
+    const LocalTuning& t = tuning<T>();
+    if (g.exec && g.generation == generation && g.ntIdx == t.ntIdx && g.uIdx == t.uIdx &&
+        g.grid == grid && std::memcmp(&g.c, &c, sizeof(Controls)) == 0)
+      return g.exec;
+    if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      graphsOk = false;
+      cudaGetLastError();
+      return nullptr;
+    }
+    long long dummy = 0;
+    launchBatch(n, &dummy);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&g.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      graphsOk = false;
+      g.exec = nullptr;
+      cudaGetLastError();
+      return nullptr;
+    }
+    g.generation = generation; g.ntIdx = t.ntIdx; g.uIdx = t.uIdx; g.grid = grid; g.c = c;
+    (void)p;
+    return g.exec;
+  }
+
   template <typename T>
   s4g_status pcgLoop(const Controls& c, const PcgPtrs<T>& p, int grid) {
     // Iterations are launched in growing batches; the launches after the
@@ -838,14 +897,28 @@ struct Engine {
     int chunk = 2, launched = 0;
     pcgBase.resize(nRun);
     for (int cs = 0; cs < nRun; ++cs) pcgBase[cs] = hState[cs].pcgIter;
-    for (int guard = 0; guard < 1000000; ++guard) {
-      for (int i = 0; i < chunk; ++i) {
-        timer.tag = launched++;
+    auto launchBatch = [&](int n, long long* count) {
+      for (int i = 0; i < n; ++i) {
+        if (tm()) timer.tag = launched++;
         if (mv.subdomains && c.precond == 0)
           launchLocalIteration<T>(mv, c, p, dState, dPartials, tuning<T>(), ctx->stream,
-                                  &launches, tm(), nRun);
+                                  count, tm(), nRun);
         else
-          launchPcgIteration<T>(mv, c, p, dState, dPartials, grid, ctx->stream, &launches, tm());
+          launchPcgIteration<T>(mv, c, p, dState, dPartials, grid, ctx->stream, count, tm());
+      }
+    };
+    for (int guard = 0; guard < 1000000; ++guard) {
+      cudaGraphExec_t exec = (!ctx->profile && graphsOk) ? pcgGraph<T>(c, p, grid, chunk, launchBatch)
+                                                         : nullptr;
+      if (exec) {
+        S4G_CUDA(cudaGraphLaunch(exec, ctx->stream));
+        long long perBatch = 0;  // count what the batch launches
+        const int ut = tuning<T>().uIdx;
+        perBatch = (mv.subdomains && c.precond == 0) ? (long long)chunk * (ut == 2 ? 3 : 2)
+                                                     : (long long)chunk * (c.precond == 0 ? 5 : 4);
+        launches += perBatch;
+      } else {
+        launchBatch(chunk, &launches);
       }
       timer.tag = -1;
       S4G_CUDA(cudaGetLastError());
