@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define S4G_ABI_VERSION 2
+#define S4G_ABI_VERSION 3
 
 /* Status codes.  Reference convention for errors is FatalError (abort), see
  * src/solids4FoamModels/solidModels/solidModel/solidModel.C:1735-1742; a
@@ -67,7 +67,10 @@ typedef struct s4g_ctx_opts {
   int verbose;  /* 1: print the reference's residual table every
                    infoFrequency correctors */
   int profile;  /* 1: time every kernel kind with CUDA events on the
-                   library's stream (s4g_perf.kernel_ms / kernel_launches_by) */
+                   library's stream (s4g_perf.kernel_ms / kernel_launches_by);
+                   PCG batches are then launched kernel by kernel */
+  int no_graphs; /* 1: launch PCG batches kernel by kernel instead of
+                   replaying captured CUDA graphs (same results) */
 } s4g_ctx_opts;
 
 /* Kernel kinds of the per-kernel timers. */

@@ -24,7 +24,8 @@ LIN_GEOM_TOTAL_DISP, NONLIN_GEOM_TOTAL_LAG = 0, 1
 
 
 class CtxOpts(ct.Structure):
-    _fields_ = [("device", ct.c_int), ("verbose", ct.c_int), ("profile", ct.c_int)]
+    _fields_ = [("device", ct.c_int), ("verbose", ct.c_int), ("profile", ct.c_int),
+                ("no_graphs", ct.c_int)]
 
 
 # kernel kinds of the per-kernel timers (S4G_K_*)

@@ -47,6 +47,7 @@ struct Ctx {
   int device = 0;
   int verbose = 0;
   int profile = 0;
+  int noGraphs = 0;
   int numSMs = 0;
   cudaStream_t stream = nullptr;
 };
@@ -908,8 +909,9 @@ struct Engine {
       }
     };
     for (int guard = 0; guard < 1000000; ++guard) {
-      cudaGraphExec_t exec = (!ctx->profile && graphsOk) ? pcgGraph<T>(c, p, grid, chunk, launchBatch)
-                                                         : nullptr;
+      cudaGraphExec_t exec = (!ctx->profile && !ctx->noGraphs && graphsOk)
+                                 ? pcgGraph<T>(c, p, grid, chunk, launchBatch)
+                                 : nullptr;
       if (exec) {
         S4G_CUDA(cudaGraphLaunch(exec, ctx->stream));
         long long perBatch = 0;  // count what the batch launches
@@ -1209,6 +1211,7 @@ s4g_status s4g_ctx_create(s4g_ctx** out, const s4g_ctx_opts* opts) {
   c->c.device = dev;
   c->c.verbose = opts ? opts->verbose : 0;
   c->c.profile = opts ? opts->profile : 0;
+  c->c.noGraphs = opts ? opts->no_graphs : 0;
   if (cudaSetDevice(dev) != cudaSuccess) return setErr(S4G_CUDA_ERROR, "cudaSetDevice failed");
   cudaDeviceGetAttribute(&c->c.numSMs, cudaDevAttrMultiProcessorCount, dev);
   if (cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking) != cudaSuccess)

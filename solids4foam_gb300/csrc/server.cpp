@@ -133,7 +133,7 @@ void workerLoop(s4g_server* sv, int slot) {
   s4g_ctx* ctx = nullptr;
   s4g_status ctxStatus = S4G_OK;
   if (!sv->opts.dry_run) {
-    s4g_ctx_opts co{sv->opts.device, 0, 0};
+    s4g_ctx_opts co{sv->opts.device, 0, 0, 0};
     ctxStatus = s4g_ctx_create(&ctx, &co);
   }
   (void)slot;

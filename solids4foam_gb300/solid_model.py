@@ -37,10 +37,11 @@ RENUMBER = {"none": _lib.RENUMBER_NONE, "RCM": _lib.RENUMBER_RCM, "tiled": _lib.
 class Context:
     """One GPU (s4g_ctx)."""
 
-    def __init__(self, device: int = 0, verbose: bool = False, profile: bool = False):
+    def __init__(self, device: int = 0, verbose: bool = False, profile: bool = False,
+                 graphs: bool = True):
         self.L = _lib.lib()
         h = ct.c_void_p()
-        opts = _lib.CtxOpts(device, 1 if verbose else 0, 1 if profile else 0)
+        opts = _lib.CtxOpts(device, 1 if verbose else 0, 1 if profile else 0, 0 if graphs else 1)
         _lib.check(self.L.s4g_ctx_create(ct.byref(h), ct.byref(opts)), "s4g_ctx_create")
         self.h = h
         self.models = weakref.WeakSet()

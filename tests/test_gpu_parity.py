@@ -236,3 +236,22 @@ def test_fp32_refine_default_tolerance_error(ctx):
     assert perf["converged"] == 1 and po["converged"] == 1
     assert rel(D, Do) < TOL_D and rel(sig, so) < TOL_S
     model.close()
+
+
+@pytest.mark.parametrize("precision,sub", [("FP64", False), ("FP32_REFINE", True)])
+def test_cuda_graph_batches_are_bit_identical(precision, sub):
+    """PCG batches replayed from captured CUDA graphs give the same bits as
+    kernel-by-kernel launches."""
+    m, bcs = cube(10, seed=8)
+    law = dict(type="linearElastic", E=70e9, nu=0.33)
+    out = []
+    for graphs in (True, False):
+        c = sg.Context(0, graphs=graphs)
+        model = sg.SolidModel(c, m, law, bcs, outer=dict(nCorrectors=2000), precision=precision,
+                              part_size=64, dic_subdomains=sub)
+        D, sig, perf = model.evolve()
+        out.append((D, sig, perf["total_lin_iters"]))
+        model.close()
+        c.close()
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == out[1][2]
