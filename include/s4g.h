@@ -270,9 +270,9 @@ typedef struct s4g_perf {
   int spmv_unroll;            /* processor-local PCG: SpMV form in use: entries
                                  unrolled in the fused p-update + SpMV (1 or
                                  6), or 0 for the split form */
-  double tune_us[6];          /* autotuner timings (us) of the variants:
-                                 preconditioner with 64/128/256 threads per
-                                 part, SpMV plain/unrolled/split; 0 if none */
+  double tune_us[6];          /* autotuner timings (us): the preconditioner,
+                                 then the SpMV step plain/unrolled/split;
+                                 the rest 0 */
   /* per kernel kind (S4G_K_*), only with s4g_ctx_opts.profile: summed
    * CUDA-event time and number of launches that did work */
   double kernel_ms[S4G_K_KINDS];

@@ -94,6 +94,7 @@ struct DevState {
   // r -= alpha q is pending per component; which p buffer is the newest
   int pending[3];
   int pbuf;
+  unsigned locTicket;    // next part of the processor-local preconditioner
   // error bits
   unsigned status;
   // last-block counters (one per kernel kind)

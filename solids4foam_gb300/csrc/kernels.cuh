@@ -151,16 +151,16 @@ void launchPrecondOnly(const MeshView& mv, const Controls& c, const PcgPtrs<T>& 
 template <typename T>
 void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaStream_t s);
 // Variant choice of the fused iteration (set by the engine's autotuner):
-// ntIdx selects 64/128/256 threads per part for the preconditioner, with
-// grid[ntIdx] resident blocks; uIdx selects the fused SpMV with a plain (0)
-// or unrolled (1) entry loop, or the split p-update + SpMV (2).  All
+// the preconditioner runs with kLocVariantsNT[0] threads per part on
+// grid[0] resident blocks; uIdx selects the fused SpMV with a plain (0) or
+// unrolled (1) entry loop, or the split p-update + SpMV (2).  All SpMV
 // variants compute bit-identical results.
-constexpr int kLocNumNT = 3, kLocNumU = 3;
+constexpr int kLocNumNT = 1, kLocNumU = 3;
 extern const int kLocVariantsNT[kLocNumNT];
 extern const int kLocVariantsU[kLocNumU];
 struct LocalTuning {
-  int ntIdx = 1, uIdx = 0;
-  int grid[kLocNumNT] = {1, 1, 1};
+  int ntIdx = 0, uIdx = 0;
+  int grid[kLocNumNT] = {1};
 };
 // One fused PCG iteration (two kernels): [x, r update of the previous
 // iteration + residual test + processor-local DIC + w.r] and

@@ -24,12 +24,12 @@
 // is the one of the separate kernels; only the order of the global sums
 // differs.
 //
-// Variants.  kLocPrecond runs with 64, 128 or 256 threads per part and
-// kLocSpmv with or without its loads unrolled; the autotuner (engine) times
-// them on the mesh and keeps the fastest.  Every sum is taken in an order
-// that does not depend on the variant (per part over 64 fixed lanes, then
-// over the parts in index order; the SpMV's grid is fixed), so all variants
-// give bit-identical results.
+// Variants.  The SpMV step runs fused with a plain or an unrolled entry
+// loop, or split into a p-update pass and an SpMV; the autotuner (engine)
+// times them on the mesh and keeps the fastest.  They sum in the same order
+// (same grid and block), so all variants give bit-identical results.
+// kLocPrecond runs with kLocBlock threads per part; its sums are per part
+// (fixed block tree) and then over the parts in index order.
 //
 // Part tables (HostPrep step 9): in-part entries per row, lower entries in
 // CSR order then upper entries in reverse CSR order, coefficient rD_row*a_e
@@ -46,9 +46,13 @@
 namespace s4g {
 namespace {
 
+// Threads per part: the streaming phase wants many loads in flight, the
+// level walk uses at most a level's rows (<= 48 for 8x8x8 parts).
+constexpr int kLocBlock = 64;
+
 template <typename T>
 struct LocSmem {
-  T* c; uint32_t* m; uint16_t* idx; T* w; T* r; int* lv;
+  T* c; uint32_t* m; uint16_t* idx; T* w; int* lv;
 };
 
 template <typename T>
@@ -59,8 +63,7 @@ __device__ __forceinline__ LocSmem<T> locSmem(const MeshView& mv, unsigned char*
   s.m = (uint32_t*)(s.c + EL);                // ML row metadata (ML % 4 == 0)
   s.idx = (uint16_t*)(s.m + ML);              // EL local columns
   s.w = (T*)(s.idx + EL);                     // 3P
-  s.r = s.w + 3 * P;                          // 3P
-  s.lv = (int*)(s.r + 3 * P);                 // maxLevels + 1
+  s.lv = (int*)(s.w + 3 * P);                 // maxLevels + 1
   return s;
 }
 
@@ -114,11 +117,11 @@ __global__ void kLocGather(int n, const int* src, const double* rDa, T* out) {
 }
 
 // Resident blocks the register budget is set for: the shared memory of a
-// 512-row part (with the 1 KB each block reserves) allows six blocks per SM
-// in FP32 and four in FP64; wider blocks trade residency for registers.
+// 512-row part (with the 1 KB each block reserves) allows eight blocks per
+// SM in FP32 and five in FP64.
 template <typename T, int NT>
 constexpr int locMinBlocks() {
-  return sizeof(T) == 4 ? (NT <= 128 ? 6 : 3) : (NT <= 64 ? 4 : NT <= 128 ? 3 : 2);
+  return sizeof(T) == 4 ? 8 : 5;
 }
 
 template <typename T, int NT>
@@ -142,16 +145,28 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
 #pragma unroll
   for (int k = 0; k < 3; ++k) { pend[k] = st->pending[k] != 0; al[k] = (T)st->alpha[k]; }
   const bool anyPend = pend[0] || pend[1] || pend[2];
-  int4 dA, dB;
-  if (blockIdx.x < mv.nParts) { dA = mv.locDesc[2 * blockIdx.x]; dB = mv.locDesc[2 * blockIdx.x + 1]; }
-  for (int part = blockIdx.x; part < mv.nParts; part += gridDim.x) {
+  // Part assignment.  FP64 (long parts): parts come from a ticket counter,
+  // so CTAs that finish early take more (no tail of CTAs with one part more
+  // than the others); the next ticket is taken while the current part runs,
+  // and the sums are recorded per part, so the result does not depend on
+  // which CTA ran which part.  FP32 (short parts, where the ticket traffic
+  // costs more than the tail): CTA b takes parts b, b+G, ..., and sums its
+  // parts in that order (G, the grid, is fixed for a mesh).
+  constexpr bool kTicket = sizeof(T) == 8;
+  __shared__ int sTicket;
+  if (threadIdx.x == 0) sTicket = kTicket ? (int)atomicAdd(&st->locTicket, 1u) : (int)blockIdx.x;
+  __syncthreads();
+  Acc<T> wr[3], ar[3];  // w.r and sum|r|: of a part (tickets) or of the CTA's parts
+  for (int part = sTicket; part < mv.nParts;) {
+    const int4 dA = mv.locDesc[2 * part], dB = mv.locDesc[2 * part + 1];
     const int pLo = dA.x, nR = dA.y, eLo = dA.z, nE = dA.w;
     const int mLo = dB.x, nM = dB.y, l0 = dB.z, nL = dB.w;
-    // the next part's descriptor, needed after this part
-    if (part + gridDim.x < mv.nParts) {
-      dA = mv.locDesc[2 * (part + gridDim.x)];
-      dB = mv.locDesc[2 * (part + gridDim.x) + 1];
-    }
+    int nextTicket = 0;
+    if (threadIdx.x == 0)
+      nextTicket = kTicket ? (int)atomicAdd(&st->locTicket, 1u) : part + (int)gridDim.x;
+    if (kTicket)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { wr[k] = Acc<T>(); ar[k] = Acc<T>(); }
     // static part tables in flight while the vectors stream
     {
       const int nc = nE * (int)sizeof(T) / 16;
@@ -166,9 +181,15 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
     }
     for (int k = threadIdx.x; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
     // pending update (x += alpha p, r -= alpha q); w starts as rD r.  RB
-    // rows per thread at a time, every load issued before any store.
-    constexpr int RB = NT <= 64 ? 2 : 1;
-    for (int i0 = threadIdx.x; i0 < nR; i0 += RB * NT) {
+    // rows per thread at a time, every load issued before any store.  In
+    // FP32 a thread keeps its rows' residual in registers for the dot
+    // products after the substitutions (rows t, t+NT, ..., at most kRegRows).
+    constexpr int RB = 2;
+    constexpr bool kRegR = sizeof(T) == 4;
+    constexpr int kRegRows = kRegR ? 8 : 1;
+    const bool regR = kRegR && nR <= kRegRows * NT;
+    T rKeep[kRegRows][3];
+    for (int i0 = threadIdx.x, jr = 0; i0 < nR; i0 += RB * NT, jr += RB) {
       T rv[RB][3], qv[RB][3], pv[RB][3], xv[RB][3], rd[RB];
 #pragma unroll
       for (int h = 0; h < RB; ++h) {
@@ -195,10 +216,18 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
               rv[h][k] -= al[k] * qv[h][k];
               rg[g + k] = rv[h][k];
             }
-            sm.r[3 * i + k] = rv[h][k];
             sm.w[3 * i + k] = rd[h] * rv[h][k];
           }
         }
+      }
+      if (kRegR) {
+#pragma unroll
+        for (int jj = 0; jj < kRegRows; ++jj)
+#pragma unroll
+          for (int h = 0; h < RB; ++h)
+            if (jj == jr + h)
+#pragma unroll
+              for (int k = 0; k < 3; ++k) rKeep[jj][k] = rv[h][k];
       }
     }
     cpAsyncWaitAll();
@@ -207,33 +236,79 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
     // backward substitution: w_l -= sum_{u>l in part} (rD_l a_lu) w_u
     locSweep<0, NT>(sm, nL);
     locSweep<1, NT>(sm, nL);
-    // w out; the part's w.r and sum|r| over 64 fixed lanes
+    // w out; w.r and sum|r| accumulated by the threads of the streaming
+    // phase over the same rows, from the residual kept in registers (FP32)
+    // or re-read (each thread reads back what it wrote)
     T* __restrict__ wg = p.w + 3 * (size_t)pLo;
     for (int k = threadIdx.x; k < 3 * nR; k += NT) wg[k] = sm.w[k];
-    double d6[6] = {0, 0, 0, 0, 0, 0};
-    if (threadIdx.x < 64) {
-      Acc<T> wr[3], ar[3];
-      for (int i = threadIdx.x; i < nR; i += 64)
+    if (regR) {
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const T rv = sm.r[3 * i + k];
-          wr[k].add(sm.w[3 * i + k] * rv);
-          ar[k].add(fabs(rv));
+      for (int jj = 0; jj < kRegRows; ++jj) {
+        const int i = threadIdx.x + jj * NT;
+        if (i < nR)
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            wr[k].add(sm.w[3 * i + k] * rKeep[jj][k]);
+            ar[k].add(fabs(rKeep[jj][k]));
+          }
+      }
+    } else {
+      constexpr int U = 4;
+      for (int i0 = threadIdx.x; i0 < nR; i0 += U * NT) {
+        T rv[U][3];
+#pragma unroll
+        for (int h = 0; h < U; ++h) {
+          const int i = i0 + h * NT;
+          if (i < nR)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) rv[h][k] = rg[3 * (size_t)(pLo + i) + k];
         }
 #pragma unroll
-      for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
+        for (int h = 0; h < U; ++h) {
+          const int i = i0 + h * NT;
+          if (i < nR)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              wr[k].add(sm.w[3 * i + k] * rv[h][k]);
+              ar[k].add(fabs(rv[h][k]));
+            }
+        }
+      }
     }
-    sum64<6>(d6, red);  // ends with a barrier: the next part may reuse the shared memory
+    if (kTicket) {
+      // the part's record: a fixed block tree over the threads' sums
+      double d6[6];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
+      blockSum<6>(d6, red);  // ends with a barrier
+      if (threadIdx.x == 0) {
+        double* q = partials + 8 * (size_t)part;
+        for (int k = 0; k < 6; ++k) q[k] = d6[k];
+      }
+    }
+    __syncthreads();  // the next part may reuse the shared memory
+    if (threadIdx.x == 0) sTicket = nextTicket;
+    __syncthreads();
+    part = sTicket;
+  }
+  if (!kTicket) {
+    // the CTA's record: a fixed block tree over the threads' sums
+    double d6[6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
+    blockSum<6>(d6, red);
     if (threadIdx.x == 0) {
-      double* q = partials + 8 * (size_t)part;
+      double* q = partials + 8 * (size_t)blockIdx.x;
       for (int k = 0; k < 6; ++k) q[k] = d6[k];
     }
   }
+  // the last CTA sums the records (parts or CTAs) in index order
   if (!lastBlockDone(&st->counter[5], gridDim.x)) return;
   double S[6];
-  reduceRecords<6>(partials, 8, mv.nParts, S, (double*)smraw);  // the part loop is over
+  reduceRecords<6>(partials, 8, kTicket ? mv.nParts : (int)gridDim.x, S, (double*)smraw);
   if (threadIdx.x != 0) return;
   st->counter[5] = 0;
+  st->locTicket = 0;
   int any = 0;
   for (int k = 0; k < 3; ++k) {
     if (st->pending[k]) {
@@ -456,22 +531,19 @@ cudaError_t prepareNT(const MeshView& mv, int* blocksPerSM) {
 
 }  // namespace
 
-const int kLocVariantsNT[kLocNumNT] = {64, 128, 256};
+const int kLocVariantsNT[kLocNumNT] = {64};
 const int kLocVariantsU[kLocNumU] = {1, 6, 0};
 
 template <typename T>
 size_t localSmemBytes(const MeshView& mv) {
   const size_t P = mv.maxRows, EL = mv.maxLocEntries, ML = mv.maxLocMeta;
-  const size_t tables = sizeof(T) * (EL + 6 * P) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
+  const size_t tables = sizeof(T) * (EL + 3 * P) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
   return std::max(tables, (size_t)256 * 6 * sizeof(double));  // final reduction scratch
 }
 
 template <typename T>
 cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM) {
-  cudaError_t e = prepareNT<T, 64>(mv, &blocksPerSM[0]);
-  if (e == cudaSuccess) e = prepareNT<T, 128>(mv, &blocksPerSM[1]);
-  if (e == cudaSuccess) e = prepareNT<T, 256>(mv, &blocksPerSM[2]);
-  return e;
+  return prepareNT<T, kLocBlock>(mv, &blocksPerSM[0]);
 }
 
 template <typename T>
@@ -482,11 +554,7 @@ void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaS
 template <typename T>
 void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                         double* partials, const LocalTuning& t, cudaStream_t s, int nCases) {
-  switch (t.ntIdx) {
-    case 0: launchPrecondNT<T, 64>(mv, c, p, st, partials, t.grid[0], s, nCases); break;
-    case 2: launchPrecondNT<T, 256>(mv, c, p, st, partials, t.grid[2], s, nCases); break;
-    default: launchPrecondNT<T, 128>(mv, c, p, st, partials, t.grid[1], s, nCases); break;
-  }
+  launchPrecondNT<T, kLocBlock>(mv, c, p, st, partials, t.grid[0], s, nCases);
 }
 
 template <typename T>

@@ -90,7 +90,7 @@ def test_autotuned_variants_are_bit_identical(ctx, precision):
         model = sg.SolidModel(ctx, m, law, bcs, outer=dict(nCorrectors=2000), precision=precision,
                               part_size=128, dic_subdomains=True, autotune=tune)
         D, sig, perf = model.evolve()
-        assert perf["part_threads"] in (64, 128, 256) and perf["spmv_unroll"] in (0, 1, 6)
+        assert perf["part_threads"] == 64 and perf["spmv_unroll"] in (0, 1, 6)
         out.append((D, sig, perf["total_lin_iters"], perf["n_correctors"]))
         model.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
