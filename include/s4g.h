@@ -206,6 +206,13 @@ typedef enum s4g_bc_type {
 s4g_status s4g_bc_set(s4g_mesh* mesh, int patch, s4g_bc_type type,
                       const double* vec3, const double* pressure);
 
+/* relaxationFactor of a solidTraction patch (solidTractionFvPatchVectorField.C:82,
+ * 387-392): each update of the traction gradient becomes
+ * g = factor * g_new + (1 - factor) * g.  factor in (0, 1]; 1 (the default)
+ * is no relaxation.  Kept across s4g_bc_set calls; ignored on
+ * fixedDisplacement patches. */
+s4g_status s4g_bc_set_relaxation(s4g_mesh* mesh, int patch, double factor);
+
 /* ------------------------------------------------------------- solver -- */
 
 typedef enum s4g_precond {

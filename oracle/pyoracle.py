@@ -40,7 +40,8 @@ class MeshDesc(ct.Structure):
 
 
 class Bc(ct.Structure):
-    _fields_ = [("type", ct.c_int), ("value", ct.c_void_p), ("pressure", ct.c_void_p)]
+    _fields_ = [("type", ct.c_int), ("value", ct.c_void_p), ("pressure", ct.c_void_p),
+                ("relaxation_factor", ct.c_double)]
 
 
 class Settings(ct.Structure):
@@ -120,13 +121,14 @@ def _desc(mesh, keep):
 
 def _bcs(bcs, mesh, keep):
     arr = (Bc * len(bcs))()
-    for i, (t, v, p) in enumerate(bcs):
+    for i, (t, v, p, *rest) in enumerate(bcs):
         v2 = None if v is None else np.ascontiguousarray(v, dtype=np.float64)
         p2 = None if p is None else np.ascontiguousarray(p, dtype=np.float64)
         keep.append((v2, p2))
         arr[i].type = int(t)
         arr[i].value = _ptr(v2)
         arr[i].pressure = _ptr(p2)
+        arr[i].relaxation_factor = float(rest[0]) if rest else 1.0
     return arr
 
 

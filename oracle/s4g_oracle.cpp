@@ -462,6 +462,7 @@ struct Bc {
   int type;
   std::vector<V3> value;   // per patch face
   std::vector<double> p;   // per patch face
+  double relax = 1.0;      // relaxationFactor (traction patches)
 };
 
 struct Solver {
@@ -513,6 +514,7 @@ struct Solver {
     bcs.resize(m.pStart.size());
     for (size_t p = 0; p < bcs.size(); ++p) {
       bcs[p].type = in[p].type;
+      bcs[p].relax = in[p].relaxation_factor > 0 ? in[p].relaxation_factor : 1.0;
       int n = m.pSize[p];
       bcs[p].value.assign(n, V3{0, 0, 0});
       bcs[p].p.assign(n, 0.0);
@@ -575,7 +577,8 @@ struct Solver {
   }
 
   // solidTraction::updateCoeffs (solidTraction...C:321-395) with the model's
-  // tractionBoundarySnGrad.
+  // tractionBoundarySnGrad, relaxed against the previous gradient
+  // (solidTraction...C:387-392): g = f g_new + (1 - f) g.
   void updateTraction() {
     for (int b = 0; b < m.nB; ++b) {
       if (patchType(b) != ORC_SOLID_TRACTION) continue;
@@ -584,19 +587,21 @@ struct Solver {
       V3 t = loadFactor * bc.value[i];
       double p = loadFactor * bc.p[i];
       V3 n = m.nf[m.nI + b];
+      V3 gn;
       if (!tl) {
         // linGeomTotalDispSolid.C:261-270
         T9 a = fromS(sigb[b]) - impK * Gb[b];
-        g[b] = rImpK * ((t - p * n) - dotVT(n, a));
+        gn = rImpK * ((t - p * n) - dotVT(n, a));
       } else if (enforceLinear) {
         // nonLinGeomTotalLagSolid.C:296-305
-        g[b] = rImpK * ((t - p * n) - dotVS(n, sigb[b]) + impK * dotVT(n, Gb[b]));
+        gn = rImpK * ((t - p * n) - dotVS(n, sigb[b]) + impK * dotVT(n, Gb[b]));
       } else {
         // nonLinGeomTotalLagSolid.C:307-323: deformed normal
         V3 nc = dotVT(n, Finvb[b]);  // Finv^T & n
         nc = (1.0 / mag(nc)) * nc;
-        g[b] = rImpK * ((t - p * nc) - dotVS(nc, sigb[b]) + impK * dotVT(n, Gb[b]));
+        gn = rImpK * ((t - p * nc) - dotVS(nc, sigb[b]) + impK * dotVT(n, Gb[b]));
       }
+      g[b] = bc.relax == 1.0 ? gn : bc.relax * gn + (1.0 - bc.relax) * g[b];
     }
     for (int b = 0; b < m.nB; ++b)
       if (patchType(b) == ORC_FIXED_DISPLACEMENT) Ub[b] = fixedValue(b);

@@ -47,6 +47,9 @@ typedef struct {
   int type;               /* ORC_FIXED_DISPLACEMENT or ORC_SOLID_TRACTION */
   const double* value;    /* [size][3]: total displacement or traction; NULL = 0 */
   const double* pressure; /* [size]: traction patches only; NULL = 0 */
+  double relaxation_factor; /* traction patches: relaxationFactor of the
+                               traction gradient; 0 means 1, the reference's
+                               default (solidTractionFvPatchVectorField.C:82) */
 } orc_bc;
 
 typedef struct {

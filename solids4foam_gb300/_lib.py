@@ -132,6 +132,7 @@ _SIGS = {
     "s4g_mesh_destroy": (ct.c_int, [ct.c_void_p]),
     "s4g_material_set": (ct.c_int, [ct.c_void_p, ct.POINTER(Law)]),
     "s4g_bc_set": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p]),
+    "s4g_bc_set_relaxation": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_double]),
     "s4g_solver_set": (ct.c_int, [ct.c_void_p, ct.POINTER(LinSolver), ct.POINTER(Outer), ct.c_int]),
     "s4g_default_controls": (None, [ct.POINTER(LinSolver), ct.POINTER(Outer)]),
     "s4g_solve": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,

@@ -75,14 +75,14 @@ def cube_case(n=128, seed=1, jitter=0.2):
 
 
 def oracle_bcs(mesh, bcs):
-    """The same boundary conditions as (type, value, pressure) per patch for
-    the CPU oracle: 0 fixedDisplacement, 1 solidTraction; unnamed patches are
-    traction-free."""
+    """The same boundary conditions as (type, value, pressure, relaxation)
+    per patch for the CPU oracle: 0 fixedDisplacement, 1 solidTraction;
+    unnamed patches are traction-free."""
     out = []
     for name in PATCHES:
         if name in bcs:
-            t, v, p = bcs[name]
-            out.append((0 if t == "fixedDisplacement" else 1, v, p))
+            t, v, p, *rest = bcs[name]
+            out.append((0 if t == "fixedDisplacement" else 1, v, p, rest[0] if rest else 1.0))
         else:
             out.append((1, None, None))
     return out

@@ -28,6 +28,7 @@ struct MeshView {
   const double* bdelta; const double* bls;
   const double* lsv;                                       // [2 nI][3] per CSR entry
   const double* bval; const double* bpress;                // BC data [nB][3], [nB]
+  const double* brelax;                                    // [nB] traction relaxationFactor
   const int* partStart; const int* lvlOff; const int* lvlStart;
   const int* upPtr; const int* upIdx; const int* dnPtr; const int* dnIdx;
   // shared-memory staging of the sweeps (see HostPrep)

@@ -116,13 +116,15 @@ struct Engine {
   int nPatches = 0;
   std::vector<int> patchStart, patchSize;
   std::vector<int> patchType;
-  std::vector<double> bvalH, bpressH;
+  std::vector<double> patchRelax;  // relaxationFactor per patch
+  std::vector<double> bvalH, bpressH, brelaxH;
   std::vector<int> btypeH;
   bool bcDirty = true;
   // device arrays not in MeshView
   int* dBtype = nullptr;
   double* dBval = nullptr;
   double* dBpress = nullptr;
+  double* dBrelax = nullptr;
   int* dC2s = nullptr;
   double* dVal = nullptr;
   double* dDiag = nullptr;
@@ -265,6 +267,7 @@ struct Engine {
     S4G_TRY(alloc(&dBtype, nB));
     S4G_TRY(alloc(&dBval, 3 * (size_t)nB));
     S4G_TRY(alloc(&dBpress, nB));
+    S4G_TRY(alloc(&dBrelax, nB));
 
     mv.nC = nC; mv.nI = nI; mv.nB = nB; mv.nParts = hp.nParts;
     mv.subdomains = (o && o->dic_subdomains) ? 1 : 0;
@@ -276,6 +279,7 @@ struct Engine {
     mv.browptr = dBrow; mv.btype = dBtype;
     mv.bS = geo.bS; mv.bmagS = geo.bmagS; mv.bn = geo.bn; mv.bk = geo.bk;
     mv.bdelta = geo.bdelta; mv.bls = geo.bls; mv.bval = dBval; mv.bpress = dBpress;
+    mv.brelax = dBrelax;
     mv.lsv = geo.lsv;
     mv.partStart = dPartStart; mv.lvlOff = dLvlOff; mv.lvlStart = dLvlStart;
     mv.upPtr = dUpPtr; mv.upIdx = dUpIdx; mv.dnPtr = dDnPtr; mv.dnIdx = dDnIdx;
@@ -305,8 +309,10 @@ struct Engine {
     patchStart.assign(d->patch_start, d->patch_start + nPatches);
     patchSize.assign(d->patch_size, d->patch_size + nPatches);
     patchType.assign(nPatches, S4G_SOLID_TRACTION);
+    patchRelax.assign(nPatches, 1.0);
     bvalH.assign(3 * (size_t)nB, 0.0);
     bpressH.assign(nB, 0.0);
+    brelaxH.assign(nB, 1.0);
     btypeH.assign(nB, 1);
     bcDirty = true;
 
@@ -401,6 +407,7 @@ struct Engine {
     S4G_TRY(alloc(&f.FL, 9 * nC)); S4G_TRY(alloc(&f.FL0, 9 * nC));
     S4G_TRY(alloc(&f.FLb, 9 * nB)); S4G_TRY(alloc(&f.FL0b, 9 * nB));
     S4G_TRY(alloc(&f.sig0, 6 * nC)); S4G_TRY(alloc(&f.sig0b, 6 * nB));
+    S4G_TRY(alloc(&f.gPrev, 3 * nB));
     tlAllocated = true;
     return S4G_OK;
   }
@@ -452,6 +459,22 @@ struct Engine {
       btypeH[k] = (int)type;
       for (int j = 0; j < 3; ++j) bvalH[3 * (size_t)k + j] = vec3 ? vec3[3 * i + j] : 0.0;
       bpressH[k] = (type == S4G_SOLID_TRACTION && pressure) ? pressure[i] : 0.0;
+      brelaxH[k] = type == S4G_SOLID_TRACTION ? patchRelax[patch] : 1.0;
+    }
+    bcDirty = true;
+    return S4G_OK;
+  }
+
+  s4g_status setRelaxation(int patch, double factor) {
+    if (patch < 0 || patch >= nPatches) return setErr(S4G_BAD_ARG, "patch index out of range");
+    if (!(factor > 0.0 && factor <= 1.0)) return setErr(S4G_BAD_ARG, "relaxation factor must be in (0, 1]");
+    patchRelax[patch] = factor;
+    const int nI = hp.nI;
+    const int ps = patchStart[patch], sz = patchSize[patch];
+    for (int k = 0; k < hp.nB; ++k) {
+      const int i = hp.bcaller[k] + nI - ps;
+      if (i < 0 || i >= sz) continue;
+      brelaxH[k] = btypeH[k] == S4G_SOLID_TRACTION ? factor : 1.0;
     }
     bcDirty = true;
     return S4G_OK;
@@ -463,6 +486,7 @@ struct Engine {
     S4G_CUDA(cudaMemcpyAsync(dBtype, btypeH.data(), sizeof(int) * hp.nB, cudaMemcpyHostToDevice, s));
     S4G_CUDA(cudaMemcpyAsync(dBval, bvalH.data(), sizeof(double) * 3 * hp.nB, cudaMemcpyHostToDevice, s));
     S4G_CUDA(cudaMemcpyAsync(dBpress, bpressH.data(), sizeof(double) * hp.nB, cudaMemcpyHostToDevice, s));
+    S4G_CUDA(cudaMemcpyAsync(dBrelax, brelaxH.data(), sizeof(double) * hp.nB, cudaMemcpyHostToDevice, s));
     bcDirty = false;
     return S4G_OK;
   }
@@ -609,6 +633,7 @@ struct Engine {
     if (tl) {
       S4G_CUDA(z(f.GD, 9 * nC)); S4G_CUDA(z(f.GD0, 9 * nC)); S4G_CUDA(z(f.GDb, 9 * nB));
       S4G_CUDA(z(f.GD0b, 9 * nB)); S4G_CUDA(z(f.sig0, 6 * nC)); S4G_CUDA(z(f.sig0b, 6 * nB));
+      S4G_CUDA(z(f.gPrev, 3 * nB));
       // F = I, F^-1 = I, J = 1 (nonLinGeomTotalLagSolid.C:57-93)
       std::vector<double> I9(9 * std::max(nC, nB), 0.0), one(std::max(nC, nB), 1.0);
       for (size_t i = 0; i < std::max(nC, nB); ++i) { I9[9 * i] = 1; I9[9 * i + 4] = 1; I9[9 * i + 8] = 1; }
@@ -1326,6 +1351,11 @@ s4g_status s4g_bc_set(s4g_mesh* mesh, int patch, s4g_bc_type type, const double*
                       const double* pressure) {
   if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
   return mesh->e.setBC(patch, type, vec3, pressure);
+}
+
+s4g_status s4g_bc_set_relaxation(s4g_mesh* mesh, int patch, double factor) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  return mesh->e.setRelaxation(patch, factor);
 }
 
 void s4g_default_controls(s4g_lin_solver* lin, s4g_outer* outer) {

@@ -51,6 +51,7 @@ struct FieldPtrs {
   double* Gb;    // [nB][9]
   double* sigb;  // [nB][6]
   double* g;     // [nB][3] traction snGrad
+  double* gPrev; // [nB][3] TL: the g of the corrector before the last update
   // total Lagrangian extras
   double* GD;  double* GD0;  double* GDb; double* GD0b;  // total gradient and old time
   double* Finv; double* Finvb; double* J; double* Jb;

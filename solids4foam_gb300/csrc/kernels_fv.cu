@@ -173,6 +173,18 @@ __device__ __forceinline__ V3 tractionSnGrad(const MeshView& mv, const Controls&
   return c.rImpK * ((t - p * nc) - dotVS(nc, sb) + c.impK * dotVT(n, Gb));
 }
 
+// Relaxed update of the traction gradient (solidTraction...C:387-392):
+// g = f g_new + (1 - f) g_old; f = 1 leaves g_new as it is.
+__device__ __forceinline__ V3 relaxG(const MeshView& mv, int b, V3 gNew, V3 gOld) {
+  const double rf = mv.brelax[b];
+  return rf == 1.0 ? gNew : rf * gNew + (1.0 - rf) * gOld;
+}
+
+// The first update of an increment.  The g it relaxes against is the one
+// the previous corrector used: g itself for the linear-geometry model
+// (zero at the start), gPrev for the TL model, whose last corrector of the
+// previous increment has already written the update it would have used
+// next.
 __global__ void kTractionInit(MeshView mv, Controls c, FieldPtrs f) {
   f = caseFields(f, blockIdx.y, mv.nC, mv.nB, mv.nI);
   caseView(mv, blockIdx.y);
@@ -181,7 +193,8 @@ __global__ void kTractionInit(MeshView mv, Controls c, FieldPtrs f) {
   T9 Fi;
   const T9* pF = nullptr;
   if (c.tl) { Fi = ldT(f.Finvb, b); pF = &Fi; }
-  stV(f.g, b, tractionSnGrad(mv, c, b, ldS(f.sigb, b), ldT(f.Gb, b), pF, 0));
+  const V3 gOld = c.tl ? ldV(f.gPrev, b) : ldV(f.g, b);
+  stV(f.g, b, relaxG(mv, b, tractionSnGrad(mv, c, b, ldS(f.sigb, b), ldT(f.Gb, b), pF, 0), gOld));
 }
 
 // Boundary value of the solved field on face b of cell s (correctBoundaryConditions).
@@ -266,7 +279,7 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
       if (!c.tl) {
         S6 sb = mode == 1 ? hooke(c, Gb) : ldS(f.sigb, b);
         if (mode == 1) stS(f.sigb, b, sb);
-        if (mv.btype[b] == 1) stV(f.g, b, tractionSnGrad(mv, c, b, sb, Gb, nullptr, 0));
+        if (mv.btype[b] == 1) stV(f.g, b, relaxG(mv, b, tractionSnGrad(mv, c, b, sb, Gb, nullptr, 0), sg));
       }
     }
     if (!c.tl) {
@@ -384,7 +397,9 @@ kPostLawTL(MeshView mv, Controls c, FieldPtrs f, const DevState* st) {
     stS(f.sigb, b, sb);
     if (mv.btype[b] == 1) {
       T9 Fi = ldT(f.Finvb, b);
-      stV(f.g, b, tractionSnGrad(mv, c, b, sb, Gb, &Fi, el));
+      const V3 gOld = ldV(f.g, b);
+      stV(f.gPrev, b, gOld);
+      stV(f.g, b, relaxG(mv, b, tractionSnGrad(mv, c, b, sb, Gb, &Fi, el), gOld));
     }
   }
 }

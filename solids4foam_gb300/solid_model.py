@@ -160,7 +160,9 @@ class SolidModel:
         _lib.check(self.L.s4g_material_set(self.h, ct.byref(lw)), "s4g_material_set")
 
     # -- 0/D boundaryField
-    def set_bc(self, patch: int, bc_type: str, value=None, pressure=None):
+    def set_bc(self, patch: int, bc_type: str, value=None, pressure=None,
+               relaxation: float | None = None):
+        """relaxation: the solidTraction relaxationFactor (default 1)."""
         t = {"fixedDisplacement": _lib.FIXED_DISPLACEMENT,
              "solidTraction": _lib.SOLID_TRACTION,
              "solidTractionFree": _lib.SOLID_TRACTION}[bc_type]
@@ -171,6 +173,9 @@ class SolidModel:
             np.broadcast_to(np.asarray(pressure, dtype=np.float64), (size,)))
         _lib.check(self.L.s4g_bc_set(self.h, patch, t, None if v is None else v.ctypes.data,
                                      None if p is None else p.ctypes.data), "s4g_bc_set")
+        if relaxation is not None:
+            _lib.check(self.L.s4g_bc_set_relaxation(self.h, patch, float(relaxation)),
+                       "s4g_bc_set_relaxation")
 
     # -- system/fvSolution and solidProperties <model>Coeffs
     def set_controls(self, solver: dict, outer: dict, precision: str = "FP64"):
@@ -324,6 +329,8 @@ class Server:
             types.append(BC_TYPES[spec[0]])
             v = spec[1] if len(spec) > 1 else None
             p = spec[2] if len(spec) > 2 else None
+            if len(spec) > 3 and spec[3] not in (None, 1.0):
+                raise ValueError("the solve server takes no traction relaxationFactor")
             va = None if v is None else np.ascontiguousarray(
                 np.broadcast_to(np.asarray(v, np.float64), (size, 3)))
             pa = None if p is None else np.ascontiguousarray(

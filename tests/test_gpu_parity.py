@@ -191,6 +191,44 @@ def test_tl_neo_hookean_matches_oracle(ctx):
     model.close()
 
 
+def test_traction_relaxation_matches_oracle(ctx):
+    """solidTraction relaxationFactor 0.5 on the linear-geometry model."""
+    m, _ = cube(8, seed=3)
+    t = np.tile([1e5, 0.0, -1e6], (int(m["patch_size"][5]), 1))
+    bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", t, None, 0.5)}
+    law = dict(type="linearElastic", E=200e9, nu=0.3)
+    model = sg.SolidModel(ctx, m, law, bcs, outer=dict(nCorrectors=4000))
+    D, sig, perf = model.evolve()
+    Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=model.permutation(), E=200e9,
+                                   nu=0.3, n_correctors=4000)
+    assert po["converged"] == 1
+    assert perf["n_correctors"] == po["n_correctors"]
+    assert perf["total_lin_iters"] == po["total_lin_iters"]
+    assert rel(D, Do) < 1e-10 and rel(sig, so) < 1e-9
+    model.close()
+
+
+def test_tl_traction_increments_relaxed_match_oracle(ctx):
+    """Total Lagrangian traction load over two increments with
+    relaxationFactor 0.5: the first update of the second increment relaxes
+    against the gradient the last corrector of the first one used."""
+    m = sg.box_mesh(6, 5, 5, 1.0, 0.8, 0.8, 0.15, 12)
+    t = np.tile([0.0, 2e4, 0.0], (int(m["patch_size"][5]), 1))
+    bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", t, None, 0.5)}
+    law = dict(type="neoHookeanElastic", mu=1e6, K=2e7)
+    model = sg.SolidModel(ctx, m, law, bcs, model="nonLinearGeometryTotalLagrangian",
+                          outer=dict(nCorrectors=6000))
+    D, sig, perf = model.evolve(n_increments=2)
+    Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=model.permutation(), model=1,
+                                   law=1, use_mu_K=1, mu=1e6, K=2e7, n_correctors=6000,
+                                   n_increments=2)
+    assert po["converged"] == 1 and perf["converged"] == 1
+    assert perf["n_correctors"] == po["n_correctors"]
+    assert perf["total_lin_iters"] == po["total_lin_iters"]
+    assert rel(D, Do) < 1e-10 and rel(sig, so) < 1e-9
+    model.close()
+
+
 def test_golden_fixture_tl(ctx):
     g = np.load(os.path.join(HERE, "golden", "oracle_small.npz"))
     m = sg.box_mesh(5, 4, 4, 1.0, 0.8, 0.8, 0.15, 12)

@@ -167,3 +167,44 @@ def test_tl_small_strain_matches_linear():
     Dn, _, _, _ = pyoracle.solve(m, bcs, model=1, law=1, use_mu_K=1, mu=mu, K=K,
                                  n_correctors=3000, solution_tol=1e-10, alternative_tol=1e-11)
     assert np.linalg.norm(Dn - Dl) / np.linalg.norm(Dl) < 1e-3
+
+
+def test_traction_relaxation_keeps_the_fixed_point():
+    """solidTraction relaxationFactor (solidTractionFvPatchVectorField.C:387-392)
+    changes the path of the corrector loop, not where it ends."""
+    m = sg.box_mesh(8, 8, 8, 1.0, 1.0, 1.0, 0.2, 3)
+    t = np.tile([1e5, 0.0, -1e6], (int(m["patch_size"][5]), 1))
+    out = {}
+    for rf in (1.0, 0.5):
+        bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", t, None, rf)}
+        D, _, _, p = pyoracle.solve(m, oracle_bcs(m, bcs), E=200e9, nu=0.3, n_correctors=4000,
+                                    solution_tol=1e-10, alternative_tol=1e-11)
+        assert p["converged"] == 1
+        out[rf] = (D, p["n_correctors"])
+    assert out[0.5][1] > out[1.0][1]
+    assert np.linalg.norm(out[0.5][0] - out[1.0][0]) / np.linalg.norm(out[1.0][0]) < 1e-6
+
+
+def test_tl_traction_increments_need_relaxation():
+    """Total Lagrangian neo-Hookean, traction load over two increments: with
+    the reference's default relaxationFactor 1 the traction-gradient update
+    does not settle after the first increment; with 0.5 it converges, and
+    (RhieChow off, so the discrete equations do not depend on the split)
+    ends at the one-increment answer."""
+    m = sg.box_mesh(6, 5, 5, 1.0, 0.8, 0.8, 0.0, 12)
+    t = np.tile([0.0, 2e3, 0.0], (int(m["patch_size"][5]), 1))
+    kw = dict(model=1, law=1, use_mu_K=1, mu=1e6, K=2e7, n_correctors=8000, stab_scale=0.0,
+              solution_tol=1e-9, alternative_tol=1e-10)
+
+    def run(rf, n_increments):
+        bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", t, None, rf)}
+        D, _, _, p = pyoracle.solve(m, oracle_bcs(m, bcs), n_increments=n_increments, **kw)
+        return D, p
+
+    D1, p1 = run(1.0, 1)
+    assert p1["converged"] == 1
+    _, pd = run(1.0, 2)
+    assert pd["converged"] == 0
+    D2, p2 = run(0.5, 2)
+    assert p2["converged"] == 1
+    assert np.linalg.norm(D2 - D1) / np.linalg.norm(D1) < 1e-5
