@@ -257,7 +257,8 @@ void s4g_default_controls(s4g_lin_solver* lin, s4g_outer* outer);
 
 typedef enum s4g_model {
   S4G_LIN_GEOM_TOTAL_DISP = 0,   /* linGeomTotalDispSolid.C:111-232 */
-  S4G_NONLIN_GEOM_TOTAL_LAG = 1  /* nonLinGeomTotalLagSolid.C:125-260 */
+  S4G_NONLIN_GEOM_TOTAL_LAG = 1, /* nonLinGeomTotalLagSolid.C:125-260 */
+  S4G_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP = 2 /* nonLinGeomTotalLagTotalDispSolid.C:173-328 */
 } s4g_model;
 
 typedef struct s4g_perf {

@@ -470,7 +470,8 @@ struct Solver {
   const orc_settings& s;
   std::vector<Bc> bcs;
   int nt;
-  bool tl;                 // total Lagrangian (incremental, solves DD)
+  bool tl;                 // total Lagrangian (either form)
+  bool incr;               // incremental form (solves DD); else total D
   double mu, K, lambda, impK, rImpK;
   double loadFactor = 1.0;
 
@@ -495,7 +496,8 @@ struct Solver {
   Solver(const Mesh& mesh, const orc_settings& st, const orc_bc* in)
       : m(mesh), s(st) {
     nt = std::max(1, s.n_threads);
-    tl = s.model == ORC_NONLIN_GEOM_TOTAL_LAG;
+    tl = s.model == ORC_NONLIN_GEOM_TOTAL_LAG || s.model == ORC_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP;
+    incr = s.model == ORC_NONLIN_GEOM_TOTAL_LAG;
     if (s.use_mu_K) {
       mu = s.mu; K = s.K; lambda = K - 2.0 * mu / 3.0;
     } else {
@@ -572,7 +574,7 @@ struct Solver {
   // Fixed displacement value of the solved field on face b.
   V3 fixedValue(int b) const {
     V3 v = loadFactor * bcs[m.patchOfB[b]].value[patchLocal(b)];
-    if (tl) v -= D0b[b];  // fixedDisplacement...C:273-285: DD = D - D.oldTime
+    if (incr) v -= D0b[b];  // fixedDisplacement...C:273-285: DD = D - D.oldTime
     return v;
   }
 
@@ -678,10 +680,11 @@ struct Solver {
       for (int b = 0; b < m.nB; ++b) sigb[b] = hooke(Gb[b]);
       return;
     }
-    // updateF, TL incremental: F = F.oldTime + gradDD^T
+    // updateF (mechanicalLaw.C:1041-1160): TL incremental F = F.oldTime +
+    // gradDD^T; TL total F = I + gradD^T
 #pragma omp parallel for num_threads(nt) if (nt > 1)
-    for (int c = 0; c < m.nC; ++c) FL[c] = FL0[c] + transposeT(G[c]);
-    for (int b = 0; b < m.nB; ++b) FLb[b] = FL0b[b] + transposeT(Gb[b]);
+    for (int c = 0; c < m.nC; ++c) FL[c] = (incr ? FL0[c] : identT()) + transposeT(G[c]);
+    for (int b = 0; b < m.nB; ++b) FLb[b] = (incr ? FL0b[b] : identT()) + transposeT(Gb[b]);
     if (enforceLinear) {
       auto lin = [&](const S6& s0, const T9& gdd) {
         return addI(s0 + (2.0 * mu) * devS(symmT(gdd)), K * trT(gdd));
@@ -793,20 +796,24 @@ struct Solver {
         gradient();
         correctStress();
       } else {
-        for (int c = 0; c < m.nC; ++c) D[c] = D0[c] + U[c];
-        for (int b = 0; b < m.nB; ++b) Db[b] = D0b[b] + Ub[b];
-        gradient();                      // gradDD
+        // incremental: D = D.oldTime + DD, gradD = gradD.oldTime + gradDD;
+        // total (nonLinGeomTotalLagTotalDispSolid.C:214-230): D and gradD
+        // are the solved field and its gradient
+        for (int c = 0; c < m.nC; ++c) D[c] = incr ? D0[c] + U[c] : U[c];
+        for (int b = 0; b < m.nB; ++b) Db[b] = incr ? D0b[b] + Ub[b] : Ub[b];
+        gradient();
         for (int c = 0; c < m.nC; ++c) {
-          GD[c] = GD0[c] + G[c];
+          GD[c] = incr ? GD0[c] + G[c] : G[c];
           T9 F = identT() + transposeT(GD[c]);
           Finv[c] = invT(F); J[c] = detT(F);
         }
         for (int b = 0; b < m.nB; ++b) {
-          GDb[b] = GD0b[b] + Gb[b];
+          GDb[b] = incr ? GD0b[b] + Gb[b] : Gb[b];
           T9 F = identT() + transposeT(GDb[b]);
           Finvb[b] = invT(F); Jb[b] = detT(F);
         }
-        if (!enforceLinear) {
+        // only the incremental form checks J (nonLinGeomTotalLagSolid.C:203-207)
+        if (incr && !enforceLinear) {
           double minJ = 1e300, maxJ = -1e300;
           for (int c = 0; c < m.nC; ++c) { minJ = std::min(minJ, J[c]); maxJ = std::max(maxJ, J[c]); }
           for (int b = 0; b < m.nB; ++b) { minJ = std::min(minJ, Jb[b]); maxJ = std::max(maxJ, Jb[b]); }
@@ -817,7 +824,7 @@ struct Solver {
       // converged(): solidModelTemplates.C:26-188
       double denom = 0, resMax = 0;
       for (int c = 0; c < m.nC; ++c) {
-        double dn = tl ? mag(U[c]) : mag(U[c] - D0[c]);
+        double dn = incr ? mag(U[c]) : mag(U[c] - D0[c]);
         denom = std::max(denom, dn);
         resMax = std::max(resMax, mag(U[c] - prev[c]));
       }
@@ -864,19 +871,23 @@ struct Solver {
       D = U; Db = Ub;
       return;
     }
-    // TL constructor: DD.correctBoundaryConditions() at time 0
+    // TL constructor: DD (or D).correctBoundaryConditions() at time 0
     loadFactor = 0.0;
     updateTraction();
     evaluateBoundary();
     const int nInc = std::max(1, s.n_increments);
     for (int n = 1; n <= nInc; ++n) {
-      // new time step: old-time fields take the converged values
-      D0 = D; D0b = Db; GD0 = GD; GD0b = GDb; FL0 = FL; FL0b = FLb;
-      sig0 = sig; sig0b = sigb;
+      // new time step: old-time fields take the converged values; the total
+      // form reads only D.oldTime (converged()), the solved D carries over
+      D0 = D; D0b = Db;
+      if (incr) {
+        GD0 = GD; GD0b = GDb; FL0 = FL; FL0b = FLb;
+        sig0 = sig; sig0b = sigb;
+      }
       loadFactor = (double)n / nInc;
       evolve(left);
-      for (int c = 0; c < m.nC; ++c) D[c] = D0[c] + U[c];
-      for (int b = 0; b < m.nB; ++b) Db[b] = D0b[b] + Ub[b];
+      for (int c = 0; c < m.nC; ++c) D[c] = incr ? D0[c] + U[c] : U[c];
+      for (int b = 0; b < m.nB; ++b) Db[b] = incr ? D0b[b] + Ub[b] : Ub[b];
       if (left == 0) break;
     }
   }
@@ -884,8 +895,9 @@ struct Solver {
 
 bool validSettings(const orc_settings* s) {
   if (!s) return false;
-  if (s->model != ORC_LIN_GEOM_TOTAL_DISP && s->model != ORC_NONLIN_GEOM_TOTAL_LAG) return false;
-  if (s->model == ORC_NONLIN_GEOM_TOTAL_LAG && s->law != ORC_NEO_HOOKEAN) return false;
+  if (s->model != ORC_LIN_GEOM_TOTAL_DISP && s->model != ORC_NONLIN_GEOM_TOTAL_LAG &&
+      s->model != ORC_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP) return false;
+  if (s->model != ORC_LIN_GEOM_TOTAL_DISP && s->law != ORC_NEO_HOOKEAN) return false;
   if (s->model == ORC_LIN_GEOM_TOTAL_DISP && s->law != ORC_LINEAR_ELASTIC) return false;
   if (s->max_iter < 1 || s->n_correctors < 1) return false;
   return true;
@@ -927,7 +939,7 @@ int orc_solve(const orc_mesh_desc* md, const orc_bc* bcs, const orc_settings* s,
   // caller cell perm[i] is solver cell i
   std::vector<int> newOf(md->n_cells);
   for (int i = 0; i < md->n_cells; ++i) newOf[perm ? perm[i] : i] = i;
-  const std::vector<T9>& gradOut = s->model == ORC_NONLIN_GEOM_TOTAL_LAG ? sol.GD : sol.G;
+  const std::vector<T9>& gradOut = s->model != ORC_LIN_GEOM_TOTAL_DISP ? sol.GD : sol.G;
   for (int c = 0; c < md->n_cells; ++c) {
     int i = newOf[c];
     if (D_out) { D_out[3 * c] = sol.D[i].x; D_out[3 * c + 1] = sol.D[i].y; D_out[3 * c + 2] = sol.D[i].z; }

@@ -40,7 +40,8 @@ typedef struct {
 
 enum { ORC_FIXED_DISPLACEMENT = 0, ORC_SOLID_TRACTION = 1 };
 enum { ORC_LINEAR_ELASTIC = 0, ORC_NEO_HOOKEAN = 1 };
-enum { ORC_LIN_GEOM_TOTAL_DISP = 0, ORC_NONLIN_GEOM_TOTAL_LAG = 1 };
+enum { ORC_LIN_GEOM_TOTAL_DISP = 0, ORC_NONLIN_GEOM_TOTAL_LAG = 1,
+       ORC_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP = 2 };
 enum { ORC_DIC = 0, ORC_DIAGONAL = 1 };
 
 typedef struct {
@@ -53,7 +54,8 @@ typedef struct {
 } orc_bc;
 
 typedef struct {
-  int model;              /* ORC_LIN_GEOM_TOTAL_DISP / ORC_NONLIN_GEOM_TOTAL_LAG */
+  int model;              /* ORC_LIN_GEOM_TOTAL_DISP / ORC_NONLIN_GEOM_TOTAL_LAG /
+                             ORC_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP */
   int law;                /* ORC_LINEAR_ELASTIC / ORC_NEO_HOOKEAN */
   double E, nu;           /* used when use_mu_K == 0 */
   double mu, K;           /* used when use_mu_K == 1 */

@@ -20,7 +20,7 @@ LINEAR_ELASTIC, NEO_HOOKEAN = 0, 1
 FIXED_DISPLACEMENT, SOLID_TRACTION = 0, 1
 PRECOND_DIC, PRECOND_DIAGONAL = 0, 1
 FP64, FP32_REFINE = 0, 1
-LIN_GEOM_TOTAL_DISP, NONLIN_GEOM_TOTAL_LAG = 0, 1
+LIN_GEOM_TOTAL_DISP, NONLIN_GEOM_TOTAL_LAG, NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP = 0, 1, 2
 
 
 class CtxOpts(ct.Structure):

@@ -57,7 +57,8 @@ __device__ __forceinline__ void caseView(MeshView& mv, int cs) {
 // Material and solver constants of a solve.
 struct Controls {
   int law;               // 0 linear elastic, 1 neo-Hookean
-  int tl;                // total Lagrangian (incremental) model
+  int tl;                // 0 linear geometry; total Lagrangian: 1 incremental
+                         // (solves DD), 2 total (solves D)
   double mu, K, lambda, impK, rImpK;
   double gamma, gammaS;  // impKf and RhieChow gamma on internal faces
   double loadFactor;

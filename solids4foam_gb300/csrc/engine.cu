@@ -982,10 +982,13 @@ struct Engine {
   }
 
   s4g_status solve(s4g_model model, int nInc, double* Dout, double* sigOut, s4g_perf* perf) {
-    if (model != S4G_LIN_GEOM_TOTAL_DISP && model != S4G_NONLIN_GEOM_TOTAL_LAG)
+    if (model != S4G_LIN_GEOM_TOTAL_DISP && model != S4G_NONLIN_GEOM_TOTAL_LAG &&
+        model != S4G_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP)
       return setErr(S4G_BAD_ARG, "unknown model");
     if (!materialSet) return setErr(S4G_BAD_ARG, "material not set");
-    const int tl = model == S4G_NONLIN_GEOM_TOTAL_LAG;
+    // Controls::tl: 0 linear geometry, 1 TL incremental, 2 TL total
+    const int tl = model == S4G_NONLIN_GEOM_TOTAL_LAG ? 1
+                 : model == S4G_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP ? 2 : 0;
     if (tl && law.type != S4G_NEO_HOOKEAN) return setErr(S4G_BAD_ARG, "the TL model needs a neoHookeanElastic law");
     if (!tl && law.type != S4G_LINEAR_ELASTIC) return setErr(S4G_BAD_ARG, "the linear-geometry model needs a linearElastic law");
     if (tl) S4G_TRY(allocTL());
@@ -1034,7 +1037,7 @@ struct Engine {
         launches++;
         S4G_TRY(loop(1));
         launchTlShift(mv, c, f, dState, s);
-        launches += 2;
+        launches += c.tl == 1 ? 2 : 1;
         if (hState->status & (kErrTimeout | kErrNaN)) break;
       }
       S4G_TRY(readState());
@@ -1175,7 +1178,7 @@ struct Engine {
 
   s4g_status getGradD(double* out) {
     if (lastModel < 0) return setErr(S4G_BAD_ARG, "no solve has run");
-    const double* src = lastModel == S4G_NONLIN_GEOM_TOTAL_LAG ? f.GD : f.G;
+    const double* src = lastModel != S4G_LIN_GEOM_TOTAL_DISP ? f.GD : f.G;
     launchGather(hp.nC, 9, dC2s, src, dOut, ctx->stream);
     S4G_CUDA(cudaMemcpyAsync(out, dOut, sizeof(double) * 9 * hp.nC, cudaMemcpyDeviceToHost, ctx->stream));
     S4G_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -203,7 +203,7 @@ __device__ __forceinline__ V3 boundaryValue(const MeshView& mv, const Controls& 
   if (mv.btype[b] == 1)
     return Up + dotVT(ldV(mv.bk, b), Gold) + (1.0 / mv.bdelta[b]) * ldV(f.g, b);
   V3 v = c.loadFactor * ldV(mv.bval, b);
-  if (c.tl) v = v - ldV(f.D0b, b);
+  if (c.tl == 1) v = v - ldV(f.D0b, b);  // DD = D - D.oldTime
   return v;
 }
 
@@ -309,7 +309,7 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
       // maxima of squared magnitudes; the square root is taken once at the end
       V3 xs = ldVT(x, s);
       mx[0] = fmax(mx[0], magSqr(xs));
-      mx[1] = fmax(mx[1], c.tl ? magSqr(Up) : magSqr(Up - ldV(f.D0, s)));
+      mx[1] = fmax(mx[1], c.tl == 1 ? magSqr(Up) : magSqr(Up - ldV(f.D0, s)));
       mx[2] = fmax(mx[2], magSqr(Up));
       red[0] += Up.x; red[1] += Up.y; red[2] += Up.z;
       if (!(isfinite(Up.x) && isfinite(Up.y) && isfinite(Up.z))) atomicOr(&st->status, kErrNaN);
@@ -351,7 +351,9 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
   for (int k = 0; k < 3; ++k) st->xbar[k] = S[k] / mv.nC;
   if (c.tl) {
     st->minJ = -M[3]; st->maxJ = M[4];
-    if (!st->enforceLinear && (st->minJ < 0.01 || st->maxJ > 100)) st->enforceLinear = 1;
+    // only the incremental form checks J (nonLinGeomTotalLagSolid.C:203-207)
+    if (c.tl == 1 && !st->enforceLinear && (st->minJ < 0.01 || st->maxJ > 100))
+      st->enforceLinear = 1;
   }
   const int iCorr = st->iCorr;
   const double materialResidual = 0.0;
@@ -531,10 +533,17 @@ __global__ void kGather(int n, int width, const int* c2s, const double* in, doub
 
 // New load increment: D.oldTime = D, gradD.oldTime = gradD, F.oldTime = F,
 // sigma.oldTime = sigma (OpenFOAM stores old-time values when time advances).
-__global__ void kTlShift(MeshView mv, FieldPtrs f, const DevState* st) {
+// The total form (tl == 2) keeps gradD.oldTime = 0 and F.oldTime = I, so
+// that the TL kinematics give gradD = grad D and F = I + gradD^T; only
+// D.oldTime, which converged() reads, moves on.
+__global__ void kTlShift(MeshView mv, Controls c, FieldPtrs f, const DevState* st) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s < mv.nC) {
     const double* U = f.D[st->dcur];
+    if (c.tl == 2) {
+      stV(f.D0, s, ldV(U, s));
+      return;
+    }
     stV(f.D0, s, ldV(f.D0, s) + ldV(U, s));
     stT(f.GD0, s, ldT(f.GD, s));
     stT(f.FL0, s, ldT(f.FL, s));
@@ -614,8 +623,8 @@ void launchGather(int n, int width, const int* c2s, const double* in, double* ou
 
 void launchTlShift(const MeshView& mv, const Controls& c, const FieldPtrs& f, DevState* st,
                    cudaStream_t s) {
-  kTlShift<<<(mv.nC + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, f, st);
-  if (mv.nB > 0) kTlShiftB<<<(mv.nB + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, c, f);
+  kTlShift<<<(mv.nC + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, c, f, st);
+  if (mv.nB > 0 && c.tl == 1) kTlShiftB<<<(mv.nB + kRowBlock - 1) / kRowBlock, kRowBlock, 0, s>>>(mv, c, f);
 }
 
 }  // namespace s4g

@@ -101,7 +101,7 @@ long long estimateFootprint(const Request& r) {
   b += N * 24 * 6;
   if (r.precision == S4G_FP32_REFINE) b += N * (8 + 12 * 6) + F * 16;
   if (r.meshOpts.dic_subdomains) b += F * 2 * 18 + N * 8;
-  if (r.model == S4G_NONLIN_GEOM_TOTAL_LAG) b += N * (72 * 6 + 48 + 8) + B * (72 * 6 + 48 + 8);
+  if (r.model != S4G_LIN_GEOM_TOTAL_DISP) b += N * (72 * 6 + 48 + 8) + B * (72 * 6 + 48 + 8);
   return (long long)(b * 1.15) + (16ll << 20);
 }
 

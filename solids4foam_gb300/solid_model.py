@@ -28,6 +28,7 @@ from .cases import PATCHES
 MODELS = {
     "linearGeometryTotalDisplacement": _lib.LIN_GEOM_TOTAL_DISP,
     "nonLinearGeometryTotalLagrangian": _lib.NONLIN_GEOM_TOTAL_LAG,
+    "nonLinearGeometryTotalLagrangianTotalDisplacement": _lib.NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP,
 }
 PRECONDITIONERS = {"DIC": _lib.PRECOND_DIC, "FDIC": _lib.PRECOND_DIC,
                    "diagonal": _lib.PRECOND_DIAGONAL}

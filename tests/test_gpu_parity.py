@@ -229,6 +229,38 @@ def test_tl_traction_increments_relaxed_match_oracle(ctx):
     model.close()
 
 
+@pytest.mark.parametrize("load,n_increments", [("traction", 2), ("displacement", 3)])
+def test_tl_total_displacement_matches_oracle(ctx, load, n_increments):
+    """nonLinearGeometryTotalLagrangianTotalDisplacement + neoHookeanElastic
+    over several increments, against the oracle in the same DIC order."""
+    m = sg.box_mesh(6, 5, 5, 1.0, 0.8, 0.8, 0.15, 12)
+    top = int(m["patch_size"][5])
+    if load == "traction":
+        zmax = ("solidTraction", np.tile([0.0, 2e4, 0.0], (top, 1)), None)
+    else:
+        zmax = ("fixedDisplacement", np.tile([0.0, 0.05, 0.1], (top, 1)), None)
+    bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": zmax}
+    law = dict(type="neoHookeanElastic", mu=1e6, K=2e7)
+    model = sg.SolidModel(ctx, m, law, bcs,
+                          model="nonLinearGeometryTotalLagrangianTotalDisplacement",
+                          outer=dict(nCorrectors=6000))
+    D, sig, perf = model.evolve(n_increments=n_increments)
+    Do, so, Go, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=model.permutation(), model=2,
+                                    law=1, use_mu_K=1, mu=1e6, K=2e7, n_correctors=6000,
+                                    n_increments=n_increments)
+    assert po["converged"] == 1 and perf["converged"] == 1
+    # The right-hand side is summed in another order on the GPU (residual
+    # form, face pass), so over ~10^3 converged correctors an inner solve
+    # may stop one iteration apart.
+    assert abs(perf["n_correctors"] - po["n_correctors"]) <= 1
+    assert abs(perf["total_lin_iters"] - po["total_lin_iters"]) <= 0.005 * po["total_lin_iters"]
+    assert rel(D, Do) < TOL_D and rel(sig, so) < TOL_S
+    assert rel(model.gradD(), Go) < TOL_S
+    if perf["total_lin_iters"] == po["total_lin_iters"]:
+        assert rel(D, Do) < 1e-10 and rel(sig, so) < 1e-9
+    model.close()
+
+
 def test_golden_fixture_tl(ctx):
     g = np.load(os.path.join(HERE, "golden", "oracle_small.npz"))
     m = sg.box_mesh(5, 4, 4, 1.0, 0.8, 0.8, 0.15, 12)

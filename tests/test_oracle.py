@@ -208,3 +208,37 @@ def test_tl_traction_increments_need_relaxation():
     D2, p2 = run(0.5, 2)
     assert p2["converged"] == 1
     assert np.linalg.norm(D2 - D1) / np.linalg.norm(D1) < 1e-5
+
+
+def _tl_box():
+    m = sg.box_mesh(6, 5, 5, 1.0, 0.8, 0.8, 0.15, 12)
+    t = np.tile([0.0, 2e4, 0.0], (int(m["patch_size"][5]), 1))
+    bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", t, None)}
+    return m, oracle_bcs(m, bcs)
+
+
+def test_tl_total_one_increment_equals_incremental():
+    """With one increment (D.oldTime = 0) the total form
+    (nonLinGeomTotalLagTotalDispSolid) and the incremental form
+    (nonLinGeomTotalLagSolid) solve the same equations: bit for bit the
+    same correctors and fields."""
+    m, bcs = _tl_box()
+    kw = dict(law=1, use_mu_K=1, mu=1e6, K=2e7, n_correctors=3000, n_increments=1)
+    Di, si, Gi, pi_ = pyoracle.solve(m, bcs, model=1, **kw)
+    Dt, st, Gt, pt = pyoracle.solve(m, bcs, model=2, **kw)
+    assert pi_["converged"] == pt["converged"] == 1
+    assert pi_["n_correctors"] == pt["n_correctors"]
+    assert np.array_equal(Di, Dt) and np.array_equal(si, st) and np.array_equal(Gi, Gt)
+
+
+def test_tl_total_path_independent_without_stabilisation():
+    """The total form solves for D itself: with RhieChow off its discrete
+    equations do not depend on the increments, so three increments end at
+    the one-increment answer."""
+    m, bcs = _tl_box()
+    kw = dict(model=2, law=1, use_mu_K=1, mu=1e6, K=2e7, n_correctors=8000, stab_scale=0.0,
+              solution_tol=1e-9, alternative_tol=1e-10)
+    D1, _, _, p1 = pyoracle.solve(m, bcs, n_increments=1, **kw)
+    D3, _, _, p3 = pyoracle.solve(m, bcs, n_increments=3, **kw)
+    assert p1["converged"] == p3["converged"] == 1
+    assert np.linalg.norm(D3 - D1) / np.linalg.norm(D1) < 1e-6
