@@ -432,6 +432,55 @@ s4g_status s4g_box_mesh_build(int nx, int ny, int nz, double lx, double ly,
                               int* owner, int* neighbour, double* C, double* V,
                               double* Cf, double* Sf, int* patch_start,
                               int* patch_size, double* points);
+/* Point ids of each face [n_faces][4] in the storage order of
+ * s4g_box_mesh_build (right-hand rule: the area vector points out of the
+ * owner), e.g. to write the box as an OpenFOAM polyMesh. */
+s4g_status s4g_box_mesh_faces(int nx, int ny, int nz, int* face_points);
+
+/* -------------------------------------------------- OpenFOAM case files --
+ * Host-only reading of an OpenFOAM case's mesh and D boundary conditions
+ * (ASCII format), for a caller without OpenFOAM: the reference builds the
+ * same data with OpenFOAM's polyMesh/fvMesh constructors and the D
+ * volVectorField's boundaryField (solidModel.C:954-1330); these entry
+ * points hand the same arrays to s4g_mesh_upload and s4g_bc_set. */
+typedef struct s4g_foam_case s4g_foam_case;
+
+/* Reads <polymesh_dir>/{points,faces,owner,neighbour,boundary}: faces as a
+ * faceList or a faceCompactList; any patch types.  C, V, Cf and Sf are
+ * computed as OpenFOAM's primitiveMesh does: triangles directly, other
+ * faces by a triangle fan about the average point; cells by pyramids about
+ * the average face centre. */
+s4g_status s4g_foam_read_mesh(const char* polymesh_dir, s4g_foam_case** out);
+/* The mesh as an s4g_mesh_desc (pointers valid until s4g_foam_free) and
+ * its number of points. */
+s4g_status s4g_foam_mesh_desc(const s4g_foam_case* fc, s4g_mesh_desc* desc, int* n_points);
+/* Patch name and OpenFOAM patch type ("patch", "wall", "empty", ...), or
+ * NULL for an index out of range. */
+const char* s4g_foam_patch_name(const s4g_foam_case* fc, int patch);
+const char* s4g_foam_patch_type(const s4g_foam_case* fc, int patch);
+/* Reads the boundaryField of a D file: per patch fixedDisplacement (value)
+ * or solidTraction (traction, pressure, relaxationFactor), uniform or
+ * nonuniform.  Another type, a time series, a missing patch or a
+ * malformed entry is S4G_BAD_ARG, named in s4g_last_error. */
+s4g_status s4g_foam_read_d(s4g_foam_case* fc, const char* d_file);
+/* The condition read for a patch: type; vec3 [patch_size][3] (value or
+ * traction); pressure [patch_size] (NULL for fixedDisplacement);
+ * relaxation factor.  Pointers valid until s4g_foam_free. */
+s4g_status s4g_foam_bc(const s4g_foam_case* fc, int patch, s4g_bc_type* type,
+                       const double** vec3, const double** pressure,
+                       double* relaxation_factor);
+/* s4g_bc_set and s4g_bc_set_relaxation on every patch of an uploaded mesh
+ * (uploaded from this case's s4g_mesh_desc). */
+s4g_status s4g_foam_apply_bcs(const s4g_foam_case* fc, s4g_mesh* mesh);
+void s4g_foam_free(s4g_foam_case* fc);
+/* Writes an ASCII polyMesh (points, faces, owner, neighbour, boundary with
+ * patch type "patch") into an existing directory; face f has the points
+ * face_points[face_start[f] .. face_start[f+1]). */
+s4g_status s4g_foam_write_mesh(const char* polymesh_dir, int n_points, const double* points,
+                               int n_faces, const int* face_start, const int* face_points,
+                               int n_internal_faces, const int* owner, const int* neighbour,
+                               int n_patches, const char* const* patch_names,
+                               const int* patch_start, const int* patch_size);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,689 @@
+// OpenFOAM case files on the host: the polyMesh (points, faces, owner,
+// neighbour, boundary) and the boundaryField of the D field, read from the
+// ASCII format OpenFOAM writes, and a polyMesh writer.
+//
+// The reader stands in for OpenFOAM's polyMesh constructor (the five files
+// of constant/polyMesh) and for primitiveMesh's geometry, so that a caller
+// without OpenFOAM can hand a meshed case to s4g_mesh_upload.  Of the D
+// file it reads the two patch types the solve path builds:
+//   fixedDisplacement  value                       (fixedDisplacementFvPatchVectorField.C:63-110)
+//   solidTraction      traction, pressure,         (solidTractionFvPatchVectorField.C:60-125)
+//                      relaxationFactor
+// and rejects everything else by name.
+//
+// Format handled: a FoamFile header dictionary (format ascii), C and C++
+// comments, dictionaries `key value;` and `key { ... }`, lists `N ( ... )`,
+// `( ... )` and `N{v}`, `uniform v`, `nonuniform List<T> N ( ... )`, faces
+// as `faceList` (`n(a b c)`) or `faceCompactList` (offsets, then labels).
+
+#include "s4g.h"
+#include "host_geometry.hpp"
+#include "s4g_internal.hpp"
+
+#include <algorithm>
+#include <cerrno>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <functional>
+#include <regex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+struct s4g_foam_case {
+  // mesh
+  int nPoints = 0, nCells = 0, nFaces = 0, nInt = 0;
+  std::vector<double> points;              // [nPoints][3]
+  std::vector<int> faceStart, facePoints;  // CSR of the faces' points
+  std::vector<int> owner, neighbour;
+  std::vector<double> C, V, Cf, Sf;
+  std::vector<std::string> patchName, patchType;
+  std::vector<int> patchStart, patchSize;
+  // D boundary conditions, per patch
+  struct Bc {
+    bool set = false;
+    s4g_bc_type type = S4G_SOLID_TRACTION;
+    std::vector<double> vec3, pressure;
+    double relax = 1.0;
+  };
+  std::vector<Bc> bcs;
+};
+
+namespace {
+
+using namespace s4g_host;
+
+struct FoamError {
+  std::string msg;
+};
+
+[[noreturn]] void fail(const std::string& msg) { throw FoamError{msg}; }
+
+// ------------------------------------------------------------- tokens ---
+
+struct Tok {
+  enum Kind { Word, Str, Punct } kind;
+  std::string s;
+  bool is(char c) const { return kind == Punct && s[0] == c; }
+};
+
+bool isPunct(char c) {
+  return c == '{' || c == '}' || c == '(' || c == ')' || c == '[' || c == ']' || c == ';';
+}
+
+std::vector<Tok> tokenize(const std::string& t, const std::string& where) {
+  std::vector<Tok> out;
+  size_t i = 0, n = t.size();
+  while (i < n) {
+    char c = t[i];
+    if (c == ' ' || c == '\t' || c == '\n' || c == '\r' || c == '\f' || c == '\v') { ++i; continue; }
+    if (c == '/' && i + 1 < n && t[i + 1] == '/') {
+      while (i < n && t[i] != '\n') ++i;
+      continue;
+    }
+    if (c == '/' && i + 1 < n && t[i + 1] == '*') {
+      size_t e = t.find("*/", i + 2);
+      if (e == std::string::npos) fail(where + ": unterminated comment");
+      i = e + 2;
+      continue;
+    }
+    if (isPunct(c)) { out.push_back({Tok::Punct, std::string(1, c)}); ++i; continue; }
+    if (c == '"') {
+      std::string s;
+      ++i;
+      while (i < n && t[i] != '"') {
+        if (t[i] == '\\' && i + 1 < n) ++i;
+        s += t[i++];
+      }
+      if (i >= n) fail(where + ": unterminated string");
+      ++i;
+      out.push_back({Tok::Str, s});
+      continue;
+    }
+    size_t b = i;
+    while (i < n && !isPunct(t[i]) && t[i] != '"' && !(t[i] == ' ' || t[i] == '\t' || t[i] == '\n' ||
+                                                          t[i] == '\r' || t[i] == '\f' || t[i] == '\v'))
+      ++i;
+    out.push_back({Tok::Word, t.substr(b, i - b)});
+  }
+  return out;
+}
+
+std::string readFile(const std::string& path) {
+  std::ifstream in(path, std::ios::binary);
+  if (!in) fail("cannot open " + path);
+  std::stringstream ss;
+  ss << in.rdbuf();
+  return ss.str();
+}
+
+// ------------------------------------------------------- dictionaries ---
+
+struct Entry {
+  std::string key;
+  bool quoted = false;       // a quoted key is a regular expression
+  bool isDict = false;
+  std::vector<Tok> val;      // tokens up to the terminating ';'
+  std::vector<Entry> sub;    // sub-dictionary
+};
+
+struct Cursor {
+  const std::vector<Tok>& t;
+  size_t p;
+  std::string where;
+  bool end() const { return p >= t.size(); }
+  const Tok& peek() const {
+    if (end()) fail(where + ": unexpected end of file");
+    return t[p];
+  }
+  const Tok& next() {
+    const Tok& k = peek();
+    ++p;
+    return k;
+  }
+  void expect(char c) {
+    const Tok& k = next();
+    if (!k.is(c)) fail(where + ": expected '" + std::string(1, c) + "', found '" + k.s + "'");
+  }
+};
+
+std::vector<Entry> parseDict(Cursor& c, bool braced) {
+  std::vector<Entry> out;
+  for (;;) {
+    if (c.end()) {
+      if (braced) fail(c.where + ": missing '}'");
+      return out;
+    }
+    if (c.peek().is('}')) {
+      if (!braced) fail(c.where + ": unexpected '}'");
+      c.next();
+      return out;
+    }
+    const Tok& k = c.next();
+    if (k.kind == Tok::Punct) fail(c.where + ": unexpected '" + k.s + "'");
+    if (k.kind == Tok::Word && k.s[0] == '#') {
+      // a directive (#include "file", #inputMode merge, ...): its argument
+      // is skipped; what it would have added is then missing and reported
+      if (!c.end() && !c.peek().is(';') && c.peek().kind != Tok::Punct) c.next();
+      continue;
+    }
+    Entry e;
+    e.key = k.s;
+    e.quoted = k.kind == Tok::Str;
+    if (!c.end() && c.peek().is('{')) {
+      c.next();
+      e.isDict = true;
+      e.sub = parseDict(c, true);
+    } else {
+      int depth = 0;
+      for (;;) {
+        const Tok& v = c.next();
+        if (v.kind == Tok::Punct) {
+          char ch = v.s[0];
+          if (ch == '(' || ch == '[' || ch == '{') ++depth;
+          if (ch == ')' || ch == ']' || ch == '}') {
+            if (--depth < 0) fail(c.where + ": unbalanced '" + v.s + "' in entry " + e.key);
+          }
+          if (ch == ';' && depth == 0) break;
+        }
+        e.val.push_back(v);
+      }
+    }
+    out.push_back(std::move(e));
+  }
+}
+
+const Entry* find(const std::vector<Entry>& d, const std::string& key) {
+  for (const Entry& e : d)
+    if (e.key == key) return &e;
+  return nullptr;
+}
+
+// The file's tokens after its FoamFile header (format ascii required).
+std::vector<Tok> payload(const std::string& path, std::string* cls = nullptr) {
+  std::vector<Tok> t = tokenize(readFile(path), path);
+  if (t.size() >= 2 && t[0].kind == Tok::Word && t[0].s == "FoamFile" && t[1].is('{')) {
+    Cursor c{t, 2, path};
+    std::vector<Entry> h = parseDict(c, true);
+    if (const Entry* f = find(h, "format"))
+      if (!f->val.empty() && f->val[0].s != "ascii")
+        fail(path + ": format " + f->val[0].s + " is not read (ASCII only)");
+    if (cls)
+      if (const Entry* k = find(h, "class"))
+        if (!k->val.empty()) *cls = k->val[0].s;
+    t.erase(t.begin(), t.begin() + (std::ptrdiff_t)c.p);
+  }
+  return t;
+}
+
+// ------------------------------------------------------------ numbers ---
+
+double toDouble(const Tok& k, const std::string& where) {
+  if (k.kind != Tok::Word) fail(where + ": expected a number, found '" + k.s + "'");
+  errno = 0;
+  char* e = nullptr;
+  double v = std::strtod(k.s.c_str(), &e);
+  if (e == k.s.c_str() || *e != '\0' || errno == ERANGE) fail(where + ": bad number '" + k.s + "'");
+  return v;
+}
+
+long toLong(const Tok& k, const std::string& where) {
+  if (k.kind != Tok::Word) fail(where + ": expected an integer, found '" + k.s + "'");
+  errno = 0;
+  char* e = nullptr;
+  long v = std::strtol(k.s.c_str(), &e, 10);
+  if (e == k.s.c_str() || *e != '\0' || errno == ERANGE) fail(where + ": bad integer '" + k.s + "'");
+  return v;
+}
+
+int toLabel(const Tok& k, const std::string& where) {
+  long v = toLong(k, where);
+  if (v < 0 || v > 0x7fffffff) fail(where + ": label out of range: " + k.s);
+  return (int)v;
+}
+
+bool isInteger(const Tok& k) {
+  if (k.kind != Tok::Word || k.s.empty()) return false;
+  for (char ch : k.s)
+    if (ch < '0' || ch > '9') return false;
+  return true;
+}
+
+// A list of items: `N ( item ... )`, `( item ... )` or `N{item}`; an
+// optional leading `List<...>` word is skipped.  item(c) reads one item.
+template <class Item>
+void parseList(Cursor& c, Item item) {
+  if (!c.end() && c.peek().kind == Tok::Word && c.peek().s.rfind("List<", 0) == 0) c.next();
+  long n = -1;
+  if (isInteger(c.peek())) n = toLong(c.next(), c.where);
+  if (c.peek().is('{')) {
+    if (n < 0) fail(c.where + ": a uniform list needs a size");
+    c.next();
+    size_t at = c.p;
+    for (long i = 0; i < n; ++i) {
+      c.p = at;
+      item(c);
+    }
+    if (n == 0) {  // skip the item without reading it
+      int depth = 0;
+      while (!(c.peek().is('}') && depth == 0)) {
+        const Tok& k = c.next();
+        if (k.is('(')) ++depth;
+        if (k.is(')')) --depth;
+      }
+    }
+    c.expect('}');
+    return;
+  }
+  c.expect('(');
+  long got = 0;
+  while (!c.peek().is(')')) {
+    item(c);
+    ++got;
+  }
+  c.next();
+  if (n >= 0 && got != n) fail(c.where + ": list of " + std::to_string(n) + " has " + std::to_string(got) + " items");
+}
+
+P3 parseVector(Cursor& c) {
+  c.expect('(');
+  P3 v;
+  v.x = toDouble(c.next(), c.where);
+  v.y = toDouble(c.next(), c.where);
+  v.z = toDouble(c.next(), c.where);
+  c.expect(')');
+  return v;
+}
+
+std::vector<int> parseLabels(Cursor& c) {
+  std::vector<int> out;
+  parseList(c, [&](Cursor& cc) { out.push_back(toLabel(cc.next(), cc.where)); });
+  return out;
+}
+
+// ----------------------------------------------------------- polyMesh ---
+
+void readMesh(s4g_foam_case& m, const std::string& dir) {
+  {  // points
+    std::string path = dir + "/points";
+    std::vector<Tok> t = payload(path);
+    Cursor c{t, 0, path};
+    parseList(c, [&](Cursor& cc) {
+      P3 v = parseVector(cc);
+      m.points.push_back(v.x); m.points.push_back(v.y); m.points.push_back(v.z);
+    });
+    m.nPoints = (int)(m.points.size() / 3);
+  }
+  {  // faces
+    std::string path = dir + "/faces", cls;
+    std::vector<Tok> t = payload(path, &cls);
+    Cursor c{t, 0, path};
+    m.faceStart.assign(1, 0);
+    if (cls == "faceCompactList") {
+      std::vector<int> offsets = parseLabels(c);
+      m.facePoints = parseLabels(c);
+      if (offsets.empty() || offsets[0] != 0 || offsets.back() != (int)m.facePoints.size())
+        fail(path + ": faceCompactList offsets do not match its labels");
+      for (size_t f = 1; f < offsets.size(); ++f) {
+        if (offsets[f] < offsets[f - 1]) fail(path + ": decreasing faceCompactList offsets");
+        m.faceStart.push_back(offsets[f]);
+      }
+    } else {
+      parseList(c, [&](Cursor& cc) {
+        std::vector<int> f = parseLabels(cc);
+        m.facePoints.insert(m.facePoints.end(), f.begin(), f.end());
+        m.faceStart.push_back((int)m.facePoints.size());
+      });
+    }
+    m.nFaces = (int)m.faceStart.size() - 1;
+  }
+  {
+    std::string path = dir + "/owner";
+    std::vector<Tok> t = payload(path);
+    Cursor c{t, 0, path};
+    m.owner = parseLabels(c);
+  }
+  {
+    std::string path = dir + "/neighbour";
+    std::vector<Tok> t = payload(path);
+    Cursor c{t, 0, path};
+    m.neighbour = parseLabels(c);
+  }
+  {  // boundary: N ( name { type ..; nFaces ..; startFace ..; } ... )
+    std::string path = dir + "/boundary";
+    std::vector<Tok> t = payload(path);
+    Cursor c{t, 0, path};
+    if (isInteger(c.peek())) c.next();
+    c.expect('(');
+    while (!c.peek().is(')')) {
+      const Tok& name = c.next();
+      if (name.kind == Tok::Punct) fail(path + ": expected a patch name");
+      c.expect('{');
+      std::vector<Entry> d = parseDict(c, true);
+      const Entry* ty = find(d, "type");
+      const Entry* nf = find(d, "nFaces");
+      const Entry* sf = find(d, "startFace");
+      if (!ty || !nf || !sf || ty->val.empty() || nf->val.size() != 1 || sf->val.size() != 1)
+        fail(path + ": patch " + name.s + " needs type, nFaces and startFace");
+      m.patchName.push_back(name.s);
+      m.patchType.push_back(ty->val[0].s);
+      m.patchSize.push_back(toLabel(nf->val[0], path));
+      m.patchStart.push_back(toLabel(sf->val[0], path));
+    }
+    c.next();
+  }
+
+  // consistency
+  const std::string where = dir;
+  m.nInt = (int)m.neighbour.size();
+  if ((int)m.owner.size() != m.nFaces)
+    fail(where + ": owner has " + std::to_string(m.owner.size()) + " labels for " + std::to_string(m.nFaces) + " faces");
+  if (m.nInt > m.nFaces) fail(where + ": more neighbours than faces");
+  int maxCell = -1;
+  for (int v : m.owner) maxCell = std::max(maxCell, v);
+  for (int v : m.neighbour) maxCell = std::max(maxCell, v);
+  m.nCells = maxCell + 1;
+  if (m.nCells < 1) fail(where + ": no cells");
+  for (int p : m.facePoints)
+    if (p >= m.nPoints) fail(where + ": face point label " + std::to_string(p) + " out of range");
+  for (int f = 0; f < m.nFaces; ++f)
+    if (m.faceStart[f + 1] - m.faceStart[f] < 3) fail(where + ": face " + std::to_string(f) + " has fewer than 3 points");
+  int expect = m.nInt;
+  for (size_t p = 0; p < m.patchName.size(); ++p) {
+    if (m.patchStart[p] != expect)
+      fail(where + ": patch " + m.patchName[p] + " does not start where the previous one ends");
+    expect += m.patchSize[p];
+  }
+  if (expect != m.nFaces) fail(where + ": the patches do not cover the boundary faces");
+
+  // geometry
+  m.Cf.assign(3 * (size_t)m.nFaces, 0.0);
+  m.Sf.assign(3 * (size_t)m.nFaces, 0.0);
+  std::vector<P3> poly;
+  for (int f = 0; f < m.nFaces; ++f) {
+    const int b = m.faceStart[f], n = m.faceStart[f + 1] - b;
+    poly.resize((size_t)n);
+    for (int i = 0; i < n; ++i) {
+      const double* q = &m.points[3 * (size_t)m.facePoints[b + i]];
+      poly[(size_t)i] = P3{q[0], q[1], q[2]};
+    }
+    P3 ctr, area;
+    if (n == 3) {  // primitiveMesh takes triangles directly
+      ctr = scl(1.0 / 3.0, add(add(poly[0], poly[1]), poly[2]));
+      area = scl(0.5, cross(sub(poly[1], poly[0]), sub(poly[2], poly[0])));
+    } else {
+      polygonGeometry(poly.data(), n, ctr, area);
+    }
+    m.Cf[3 * (size_t)f] = ctr.x; m.Cf[3 * (size_t)f + 1] = ctr.y; m.Cf[3 * (size_t)f + 2] = ctr.z;
+    m.Sf[3 * (size_t)f] = area.x; m.Sf[3 * (size_t)f + 1] = area.y; m.Sf[3 * (size_t)f + 2] = area.z;
+  }
+  m.C.assign(3 * (size_t)m.nCells, 0.0);
+  m.V.assign((size_t)m.nCells, 0.0);
+  if (!cellGeometry(m.nCells, m.nFaces, m.nInt, m.owner.data(), m.neighbour.data(), m.Cf.data(),
+                    m.Sf.data(), m.C.data(), m.V.data()))
+    fail(where + ": a cell has no faces or a volume that is not positive");
+  m.bcs.assign(m.patchName.size(), s4g_foam_case::Bc{});
+}
+
+// ----------------------------------------------------------------- D ---
+
+// `uniform v` or `nonuniform List<T> N (...)` of width 1 or 3, for n faces.
+std::vector<double> fieldValues(const Entry& e, int width, int n, const std::string& where) {
+  std::vector<double> out;
+  Cursor c{e.val, 0, where + " " + e.key};
+  if (c.end()) fail(c.where + ": empty entry");
+  const Tok& form = c.next();
+  auto item = [&](Cursor& cc) {
+    if (width == 3) {
+      P3 v = parseVector(cc);
+      out.push_back(v.x); out.push_back(v.y); out.push_back(v.z);
+    } else {
+      out.push_back(toDouble(cc.next(), cc.where));
+    }
+  };
+  if (form.s == "uniform") {
+    item(c);
+    std::vector<double> one = out;
+    out.clear();
+    for (int i = 0; i < n; ++i) out.insert(out.end(), one.begin(), one.end());
+  } else if (form.s == "nonuniform") {
+    parseList(c, item);
+    if ((int)out.size() != width * n)
+      fail(c.where + ": " + std::to_string(out.size() / width) + " values for " + std::to_string(n) + " faces");
+  } else {
+    fail(c.where + ": expected uniform or nonuniform, found '" + form.s + "'");
+  }
+  if (!c.end()) fail(c.where + ": unexpected '" + c.peek().s + "'");
+  return out;
+}
+
+// The patch's entry: an exact name, else a quoted key read as a regular
+// expression (OpenFOAM's "(left|right)" or ".*" keys).
+const Entry* patchEntry(const std::vector<Entry>& bf, const std::string& name) {
+  if (const Entry* e = find(bf, name)) return e;
+  for (auto it = bf.rbegin(); it != bf.rend(); ++it) {
+    if (!it->quoted) continue;
+    try {
+      if (std::regex_match(name, std::regex(it->key))) return &*it;
+    } catch (const std::regex_error&) {
+    }
+  }
+  return nullptr;
+}
+
+void readD(s4g_foam_case& m, const std::string& path) {
+  std::vector<Tok> t = payload(path);
+  Cursor c{t, 0, path};
+  std::vector<Entry> d = parseDict(c, false);
+  const Entry* bf = find(d, "boundaryField");
+  if (!bf || !bf->isDict) fail(path + ": no boundaryField dictionary");
+  std::vector<s4g_foam_case::Bc> bcs(m.patchName.size());
+  for (size_t p = 0; p < m.patchName.size(); ++p) {
+    const std::string& name = m.patchName[p];
+    const std::string where = path + ": patch " + name;
+    const Entry* e = patchEntry(bf->sub, name);
+    if (!e || !e->isDict) fail(where + " has no entry in boundaryField");
+    const Entry* ty = find(e->sub, "type");
+    if (!ty || ty->val.size() != 1) fail(where + " has no type");
+    const std::string type = ty->val[0].s;
+    const int n = m.patchSize[p];
+    s4g_foam_case::Bc& bc = bcs[p];
+    bc.set = true;
+    if (type == "fixedDisplacement") {
+      for (const char* series : {"displacementSeries", "constantDisplacement"})
+        if (find(e->sub, series)) fail(where + ": " + series + " is not built");
+      bc.type = S4G_FIXED_DISPLACEMENT;
+      const Entry* v = find(e->sub, "value");
+      bc.vec3 = v ? fieldValues(*v, 3, n, where) : std::vector<double>(3 * (size_t)n, 0.0);
+    } else if (type == "solidTraction") {
+      for (const char* series : {"tractionSeries", "pressureSeries", "tractionField", "pressureField"})
+        if (find(e->sub, series)) fail(where + ": " + series + " is not built");
+      if (const Entry* s = find(e->sub, "setEffectiveTraction"))
+        if (!s->val.empty() && (s->val[0].s == "true" || s->val[0].s == "yes" || s->val[0].s == "on"))
+          fail(where + ": setEffectiveTraction is not built");
+      if (const Entry* s = find(e->sub, "nonOrthogonalCorrections"))
+        if (!s->val.empty() && (s->val[0].s == "false" || s->val[0].s == "no" || s->val[0].s == "off"))
+          fail(where + ": nonOrthogonalCorrections false is not built");
+      bc.type = S4G_SOLID_TRACTION;
+      const Entry* tr = find(e->sub, "traction");
+      const Entry* pr = find(e->sub, "pressure");
+      if (!tr || !pr) fail(where + ": solidTraction needs traction and pressure");
+      bc.vec3 = fieldValues(*tr, 3, n, where);
+      bc.pressure = fieldValues(*pr, 1, n, where);
+      if (const Entry* rf = find(e->sub, "relaxationFactor")) {
+        if (rf->val.size() != 1) fail(where + ": bad relaxationFactor");
+        bc.relax = toDouble(rf->val[0], where);
+        if (!(bc.relax > 0.0 && bc.relax <= 1.0)) fail(where + ": relaxationFactor must be in (0, 1]");
+      }
+    } else {
+      fail(where + ": type " + type + " is not built (fixedDisplacement and solidTraction are)");
+    }
+  }
+  m.bcs = std::move(bcs);
+}
+
+// ------------------------------------------------------------- writer ---
+
+bool writeFile(const std::string& path, const std::string& cls, const std::string& object,
+               const std::string& body) {
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) return false;
+  std::fprintf(f,
+               "FoamFile\n{\n    version     2.0;\n    format      ascii;\n"
+               "    class       %s;\n    location    \"constant/polyMesh\";\n"
+               "    object      %s;\n}\n\n",
+               cls.c_str(), object.c_str());
+  std::fwrite(body.data(), 1, body.size(), f);
+  bool ok = std::fclose(f) == 0;
+  return ok;
+}
+
+std::string labels(const int* v, int n) {
+  std::string s = std::to_string(n) + "\n(\n";
+  for (int i = 0; i < n; ++i) s += std::to_string(v[i]) + "\n";
+  return s + ")\n";
+}
+
+s4g_status guarded(const std::function<void()>& body) {
+  try {
+    body();
+    return S4G_OK;
+  } catch (const FoamError& e) {
+    s4g::setLastError(e.msg);
+    return S4G_BAD_ARG;
+  } catch (const std::bad_alloc&) {
+    s4g::setLastError("out of host memory reading an OpenFOAM case");
+    return S4G_OOM;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+s4g_status s4g_foam_read_mesh(const char* polymesh_dir, s4g_foam_case** out) {
+  if (!polymesh_dir || !out) return S4G_BAD_ARG;
+  *out = nullptr;
+  auto* m = new s4g_foam_case();
+  s4g_status st = guarded([&] { readMesh(*m, polymesh_dir); });
+  if (st != S4G_OK) {
+    delete m;
+    return st;
+  }
+  *out = m;
+  return S4G_OK;
+}
+
+s4g_status s4g_foam_mesh_desc(const s4g_foam_case* m, s4g_mesh_desc* d, int* n_points) {
+  if (!m || !d) return S4G_BAD_ARG;
+  d->n_cells = m->nCells;
+  d->n_faces = m->nFaces;
+  d->n_internal_faces = m->nInt;
+  d->owner = m->owner.data();
+  d->neighbour = m->neighbour.data();
+  d->C = m->C.data();
+  d->V = m->V.data();
+  d->Cf = m->Cf.data();
+  d->Sf = m->Sf.data();
+  d->n_patches = (int)m->patchName.size();
+  d->patch_start = m->patchStart.data();
+  d->patch_size = m->patchSize.data();
+  if (n_points) *n_points = m->nPoints;
+  return S4G_OK;
+}
+
+const char* s4g_foam_patch_name(const s4g_foam_case* m, int p) {
+  if (!m || p < 0 || p >= (int)m->patchName.size()) return nullptr;
+  return m->patchName[(size_t)p].c_str();
+}
+
+const char* s4g_foam_patch_type(const s4g_foam_case* m, int p) {
+  if (!m || p < 0 || p >= (int)m->patchType.size()) return nullptr;
+  return m->patchType[(size_t)p].c_str();
+}
+
+s4g_status s4g_foam_read_d(s4g_foam_case* m, const char* d_file) {
+  if (!m || !d_file) return S4G_BAD_ARG;
+  return guarded([&] { readD(*m, d_file); });
+}
+
+s4g_status s4g_foam_bc(const s4g_foam_case* m, int p, s4g_bc_type* type, const double** vec3,
+                       const double** pressure, double* relaxation_factor) {
+  if (!m || p < 0 || p >= (int)m->bcs.size()) return S4G_BAD_ARG;
+  const s4g_foam_case::Bc& bc = m->bcs[(size_t)p];
+  if (!bc.set) {
+    s4g::setLastError("no D file has been read for this case");
+    return S4G_BAD_ARG;
+  }
+  if (type) *type = bc.type;
+  if (vec3) *vec3 = bc.vec3.data();
+  if (pressure) *pressure = bc.type == S4G_SOLID_TRACTION ? bc.pressure.data() : nullptr;
+  if (relaxation_factor) *relaxation_factor = bc.relax;
+  return S4G_OK;
+}
+
+s4g_status s4g_foam_apply_bcs(const s4g_foam_case* m, s4g_mesh* mesh) {
+  if (!m || !mesh) return S4G_BAD_ARG;
+  for (size_t p = 0; p < m->bcs.size(); ++p) {
+    const s4g_foam_case::Bc& bc = m->bcs[p];
+    if (!bc.set) {
+      s4g::setLastError("no D file has been read for this case");
+      return S4G_BAD_ARG;
+    }
+    s4g_status st = s4g_bc_set(mesh, (int)p, bc.type, bc.vec3.data(),
+                               bc.type == S4G_SOLID_TRACTION ? bc.pressure.data() : nullptr);
+    if (st != S4G_OK) return st;
+    if (bc.type == S4G_SOLID_TRACTION) {
+      st = s4g_bc_set_relaxation(mesh, (int)p, bc.relax);
+      if (st != S4G_OK) return st;
+    }
+  }
+  return S4G_OK;
+}
+
+void s4g_foam_free(s4g_foam_case* m) { delete m; }
+
+s4g_status s4g_foam_write_mesh(const char* dir, int n_points, const double* points, int n_faces,
+                               const int* face_start, const int* face_points, int n_int,
+                               const int* owner, const int* neighbour, int n_patches,
+                               const char* const* names, const int* patch_start,
+                               const int* patch_size) {
+  if (!dir || n_points < 0 || n_faces < 0 || n_int < 0 || n_int > n_faces || n_patches < 0 ||
+      !points || !face_start || !face_points || !owner || (n_int > 0 && !neighbour) ||
+      (n_patches > 0 && (!names || !patch_start || !patch_size)))
+    return S4G_BAD_ARG;
+  const std::string d(dir);
+  char buf[128];
+  std::string s = std::to_string(n_points) + "\n(\n";
+  for (int i = 0; i < n_points; ++i) {
+    std::snprintf(buf, sizeof buf, "(%.17g %.17g %.17g)\n", points[3 * (size_t)i],
+                  points[3 * (size_t)i + 1], points[3 * (size_t)i + 2]);
+    s += buf;
+  }
+  s += ")\n";
+  if (!writeFile(d + "/points", "vectorField", "points", s)) return S4G_BAD_ARG;
+  s = std::to_string(n_faces) + "\n(\n";
+  for (int f = 0; f < n_faces; ++f) {
+    s += std::to_string(face_start[f + 1] - face_start[f]) + "(";
+    for (int k = face_start[f]; k < face_start[f + 1]; ++k)
+      s += std::to_string(face_points[k]) + (k + 1 < face_start[f + 1] ? " " : "");
+    s += ")\n";
+  }
+  s += ")\n";
+  if (!writeFile(d + "/faces", "faceList", "faces", s)) return S4G_BAD_ARG;
+  if (!writeFile(d + "/owner", "labelList", "owner", labels(owner, n_faces))) return S4G_BAD_ARG;
+  if (!writeFile(d + "/neighbour", "labelList", "neighbour", labels(neighbour, n_int)))
+    return S4G_BAD_ARG;
+  s = std::to_string(n_patches) + "\n(\n";
+  for (int p = 0; p < n_patches; ++p)
+    s += std::string("    ") + names[p] + "\n    {\n        type            patch;\n        nFaces          " +
+         std::to_string(patch_size[p]) + ";\n        startFace       " + std::to_string(patch_start[p]) +
+         ";\n    }\n";
+  s += ")\n";
+  if (!writeFile(d + "/boundary", "polyBoundaryMesh", "boundary", s)) return S4G_BAD_ARG;
+  return S4G_OK;
+}
+
+}  // extern "C"

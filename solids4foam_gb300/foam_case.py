@@ -1,0 +1,163 @@
+"""OpenFOAM case files on the host (s4g_foam_* in libs4g): read a meshed
+case's constant/polyMesh and 0/D into the mesh and boundary-condition
+dictionaries SolidModel takes, and write meshes as ASCII polyMesh.
+
+The mesh dictionary has the keys of box_mesh (owner, neighbour, C, V, Cf,
+Sf, patch_start, patch_size, patch_names) plus patch_types, points,
+face_start and face_points.  The boundary conditions are
+{patch name: (type, value or traction [n,3], pressure [n] or None,
+relaxationFactor)}."""
+import ctypes as ct
+import os
+
+import numpy as np
+
+from . import _lib
+from .cases import box_mesh
+
+BC_NAMES = {_lib.FIXED_DISPLACEMENT: "fixedDisplacement", _lib.SOLID_TRACTION: "solidTraction"}
+
+
+def _arr(ptr, n, dtype):
+    if n == 0:
+        return np.zeros(0, dtype)
+    ctype = {np.float64: ct.c_double, np.int32: ct.c_int}[dtype]
+    return np.ctypeslib.as_array(ct.cast(ptr, ct.POINTER(ctype)), shape=(n,)).copy()
+
+
+def read_case(case_dir: str, d_file: str | None = "0/D", polymesh: str = "constant/polyMesh"):
+    """Reads <case_dir>/<polymesh> and, unless d_file is None, the
+    boundaryField of <case_dir>/<d_file>.  Returns (mesh, bcs); bcs is None
+    when no D file is read."""
+    L = _lib.lib()
+    h = ct.c_void_p()
+    _lib.check(L.s4g_foam_read_mesh(os.path.join(case_dir, polymesh).encode(), ct.byref(h)),
+               "s4g_foam_read_mesh")
+    try:
+        d = _lib.MeshDesc()
+        npts = ct.c_int()
+        _lib.check(L.s4g_foam_mesh_desc(h, ct.byref(d), ct.byref(npts)), "s4g_foam_mesh_desc")
+        nc, nf, ni, npch = d.n_cells, d.n_faces, d.n_internal_faces, d.n_patches
+        mesh = dict(owner=_arr(d.owner, nf, np.int32), neighbour=_arr(d.neighbour, ni, np.int32),
+                    C=_arr(d.C, 3 * nc, np.float64).reshape(nc, 3), V=_arr(d.V, nc, np.float64),
+                    Cf=_arr(d.Cf, 3 * nf, np.float64).reshape(nf, 3),
+                    Sf=_arr(d.Sf, 3 * nf, np.float64).reshape(nf, 3),
+                    patch_start=_arr(d.patch_start, npch, np.int32),
+                    patch_size=_arr(d.patch_size, npch, np.int32))
+        mesh["patch_names"] = [L.s4g_foam_patch_name(h, p).decode() for p in range(npch)]
+        mesh["patch_types"] = [L.s4g_foam_patch_type(h, p).decode() for p in range(npch)]
+        bcs = None
+        if d_file is not None:
+            _lib.check(L.s4g_foam_read_d(h, os.path.join(case_dir, d_file).encode()),
+                       "s4g_foam_read_d")
+            bcs = {}
+            for p, name in enumerate(mesh["patch_names"]):
+                t, v, pr, rf = ct.c_int(), ct.c_void_p(), ct.c_void_p(), ct.c_double()
+                _lib.check(L.s4g_foam_bc(h, p, ct.byref(t), ct.byref(v), ct.byref(pr), ct.byref(rf)),
+                           "s4g_foam_bc")
+                n = int(mesh["patch_size"][p])
+                vec = _arr(v.value, 3 * n, np.float64).reshape(n, 3)
+                press = None if not pr.value else _arr(pr.value, n, np.float64)
+                bcs[name] = (BC_NAMES[t.value], vec, press, rf.value)
+        return mesh, bcs
+    finally:
+        L.s4g_foam_free(h)
+
+
+def write_polymesh(polymesh_dir: str, points, face_start, face_points, owner, neighbour,
+                   patch_names, patch_start, patch_size):
+    """Writes an ASCII polyMesh (all patches of type patch) into
+    polymesh_dir, which is created if needed."""
+    os.makedirs(polymesh_dir, exist_ok=True)
+    keep = [np.ascontiguousarray(points, np.float64), np.ascontiguousarray(face_start, np.int32),
+            np.ascontiguousarray(face_points, np.int32), np.ascontiguousarray(owner, np.int32),
+            np.ascontiguousarray(neighbour, np.int32), np.ascontiguousarray(patch_start, np.int32),
+            np.ascontiguousarray(patch_size, np.int32)]
+    names = (ct.c_char_p * len(patch_names))(*[n.encode() for n in patch_names])
+    pts, fs, fp, own, nei, ps, pz = keep
+    _lib.check(_lib.lib().s4g_foam_write_mesh(
+        polymesh_dir.encode(), pts.shape[0], pts.ctypes.data, fs.shape[0] - 1, fs.ctypes.data,
+        fp.ctypes.data, nei.shape[0], own.ctypes.data, nei.ctypes.data, len(patch_names), names,
+        ps.ctypes.data, pz.ctypes.data), "s4g_foam_write_mesh")
+
+
+def box_polymesh(nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=1):
+    """box_mesh with its points and faces (four point ids per face)."""
+    m = box_mesh(nx, ny, nz, lx, ly, lz, jitter, seed, points=True)
+    nf = m["owner"].shape[0]
+    fp = np.zeros((nf, 4), np.int32)
+    _lib.check(_lib.lib().s4g_box_mesh_faces(nx, ny, nz, fp.ctypes.data), "s4g_box_mesh_faces")
+    m["face_points"] = fp.reshape(-1)
+    m["face_start"] = np.arange(0, 4 * nf + 1, 4, dtype=np.int32)
+    return m
+
+
+def write_box_case(polymesh_dir: str, mesh):
+    """Writes a box_polymesh mesh as an ASCII polyMesh."""
+    write_polymesh(polymesh_dir, mesh["points"], mesh["face_start"], mesh["face_points"],
+                   mesh["owner"], mesh["neighbour"], list(mesh["patch_names"]),
+                   mesh["patch_start"], mesh["patch_size"])
+
+
+def prism_box_polymesh(nx, ny, nz, lx=1.0, ly=1.0, lz=1.0):
+    """An nx x ny x nz box whose hexahedra are each split along their x = y
+    diagonal into two triangular prisms (cells 2h and 2h+1 of hex h), in
+    OpenFOAM polyMesh order: internal faces sorted by (owner, neighbour),
+    then the patches xmin, xmax, ymin, ymax, zmin, zmax.  Returns points,
+    face_start, face_points, owner, neighbour, patch_names, patch_start,
+    patch_size -- the arguments of write_polymesh."""
+    px, py = nx + 1, ny + 1
+    pid = lambda i, j, k: i + px * (j + py * k)
+    g = np.meshgrid(np.arange(px) * (lx / nx), np.arange(py) * (ly / ny),
+                    np.arange(nz + 1) * (lz / nz), indexing="ij")
+    points = np.stack([a.transpose(2, 1, 0).reshape(-1) for a in g], axis=1)
+    faces = {}  # sorted point ids -> [(cell, ids oriented out of that cell)]
+    for k in range(nz):
+        for j in range(ny):
+            for i in range(nx):
+                h = i + nx * (j + ny * k)
+                for s, tri in enumerate((((i, j), (i + 1, j), (i + 1, j + 1)),
+                                         ((i, j), (i + 1, j + 1), (i, j + 1)))):
+                    cell = 2 * h + s
+                    lo = [pid(a, b, k) for a, b in tri]
+                    hi = [pid(a, b, k + 1) for a, b in tri]
+                    cell_faces = [lo, hi] + [[lo[e], lo[(e + 1) % 3], hi[(e + 1) % 3], hi[e]]
+                                             for e in range(3)]
+                    cc = points[lo + hi].mean(axis=0)
+                    for f in cell_faces:
+                        q = points[f]
+                        area = 0.5 * sum(np.cross(q[e] - q[0], q[e + 1] - q[0])
+                                         for e in range(1, len(f) - 1))
+                        if np.dot(area, q.mean(axis=0) - cc) < 0:
+                            f = f[::-1]
+                        faces.setdefault(tuple(sorted(f)), []).append((cell, f))
+    internal, boundary = [], [[] for _ in range(6)]
+    tol = 1e-12
+    for users in faces.values():
+        if len(users) == 2:
+            (a, fa), (b, _) = sorted(users)
+            internal.append((a, b, fa))
+        else:
+            (a, fa), = users
+            c = points[fa].mean(axis=0)
+            for p, (axis, val) in enumerate(((0, 0.0), (0, lx), (1, 0.0), (1, ly),
+                                             (2, 0.0), (2, lz))):
+                if abs(c[axis] - val) < tol * max(lx, ly, lz):
+                    boundary[p].append((a, fa))
+                    break
+            else:
+                raise RuntimeError("boundary face off the box")
+    internal.sort(key=lambda t: (t[0], t[1]))
+    for b in boundary:
+        b.sort(key=lambda t: t[0])
+    owner = [a for a, _, _ in internal] + [a for b in boundary for a, _ in b]
+    neighbour = [b for _, b, _ in internal]
+    flist = [f for _, _, f in internal] + [f for b in boundary for _, f in b]
+    face_start = np.cumsum([0] + [len(f) for f in flist]).astype(np.int32)
+    sizes = [len(b) for b in boundary]
+    starts = list(np.cumsum([len(internal)] + sizes[:-1]))
+    return dict(points=points, face_start=face_start,
+                face_points=np.concatenate([np.asarray(f) for f in flist]).astype(np.int32),
+                owner=np.asarray(owner, np.int32), neighbour=np.asarray(neighbour, np.int32),
+                patch_names=["xmin", "xmax", "ymin", "ymax", "zmin", "zmax"],
+                patch_start=np.asarray(starts, np.int32), patch_size=np.asarray(sizes, np.int32))

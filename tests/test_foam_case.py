@@ -1,0 +1,158 @@
+"""OpenFOAM case files (s4g_foam_*): the polyMesh reader against the box
+generator (written out and read back: bit-identical geometry), against a
+hand-written two-prism mesh with known volumes and centroids, the D
+boundaryField subset, and the errors it must raise.  No GPU needed."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle
+from solids4foam_gb300 import _lib
+from solids4foam_gb300.cases import oracle_bcs
+from solids4foam_gb300.foam_case import box_polymesh, read_case, write_box_case
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PRISMS = os.path.join(HERE, "golden", "foam_prisms")
+HEADER = "FoamFile\n{\n    version 2.0;\n    format ascii;\n    class volVectorField;\n    object D;\n}\n"
+
+
+def test_box_written_and_read_back_is_bit_identical(tmp_path):
+    m = box_polymesh(5, 4, 3, 1.2, 1.0, 0.8, 0.2, 11)
+    write_box_case(str(tmp_path / "constant" / "polyMesh"), m)
+    r, bcs = read_case(str(tmp_path), d_file=None)
+    assert bcs is None
+    for k in ("owner", "neighbour", "C", "V", "Cf", "Sf", "patch_start", "patch_size"):
+        assert np.array_equal(r[k], m[k]), k
+    assert r["patch_names"] == list(m["patch_names"])
+    assert r["patch_types"] == ["patch"] * 6
+
+
+def test_two_prisms_geometry():
+    r, _ = read_case(PRISMS, d_file=None)
+    assert r["patch_names"] == ["bottom", "top", "sides"]
+    assert r["patch_types"] == ["wall", "patch", "patch"]
+    assert list(r["patch_start"]) == [1, 3, 5] and list(r["patch_size"]) == [2, 2, 4]
+    np.testing.assert_allclose(r["V"], [0.5, 0.5], rtol=1e-14)
+    np.testing.assert_allclose(r["C"], [[2 / 3, 1 / 3, 0.5], [1 / 3, 2 / 3, 0.5]], rtol=1e-14)
+    np.testing.assert_allclose(r["Sf"][0], [-1.0, 1.0, 0.0], atol=1e-15)   # diagonal, owner -> neighbour
+    np.testing.assert_allclose(r["Sf"][1], [0.0, 0.0, -0.5], atol=1e-15)   # bottom triangle, outward
+    np.testing.assert_allclose(r["Cf"][1], [2 / 3, 1 / 3, 0.0], atol=1e-15)
+    # closed cells: the area vectors of each cell sum to zero
+    for c in range(2):
+        s = sum(r["Sf"][f] * (1 if r["owner"][f] == c else -1)
+                for f in range(9) if r["owner"][f] == c or (f < 1 and r["neighbour"][f] == c))
+        np.testing.assert_allclose(s, 0.0, atol=1e-15)
+
+
+def test_two_prisms_d_file():
+    r, bcs = read_case(PRISMS)
+    t, v, p, rf = bcs["bottom"]
+    assert t == "fixedDisplacement" and p is None and rf == 1.0 and np.all(v == 0)
+    t, v, p, rf = bcs["top"]
+    assert t == "solidTraction" and rf == 0.5
+    assert np.array_equal(v, [[1e5, 0, -1e6], [2e5, 0, -1e6]]) and np.array_equal(p, [3e5, 3e5])
+    t, v, p, rf = bcs["sides"]   # matched by the ".*" key
+    assert t == "solidTraction" and np.all(v == 0) and np.all(p == 0) and v.shape == (4, 3)
+
+
+def test_read_case_solves_like_the_box(tmp_path):
+    """A box written as a case with a D file and read back gives the
+    oracle exactly the same solve as the box and the same conditions."""
+    m = box_polymesh(6, 5, 4, 1.2, 1.0, 0.8, 0.2, 11)
+    case = tmp_path
+    write_box_case(str(case / "constant" / "polyMesh"), m)
+    top = int(m["patch_size"][5])
+    tr = np.tile([1e5, 0.0, -2e5], (top, 1))
+    lines = " ".join(f"({a:.17g} {b:.17g} {c:.17g})" for a, b, c in tr)
+    (case / "0").mkdir()
+    (case / "0" / "D").write_text(HEADER + f"""
+dimensions [0 1 0 0 0 0 0];
+internalField uniform (0 0 0);
+boundaryField
+{{
+    zmin {{ type fixedDisplacement; value uniform (0 0 0); }}
+    zmax
+    {{
+        type solidTraction;
+        traction nonuniform List<vector> {top} ({lines});
+        pressure uniform 3e5;
+        value uniform (0 0 0);
+    }}
+    "(x|y)(min|max)" {{ type solidTraction; traction uniform (0 0 0); pressure uniform 0; }}
+}}
+""")
+    r, bcs = read_case(str(case))
+    direct = {"zmin": ("fixedDisplacement", None, None),
+              "zmax": ("solidTraction", tr, np.full(top, 3e5))}
+    kw = dict(E=70e9, nu=0.33, n_correctors=300)
+    Dr, sr, _, pr = pyoracle.solve(r, oracle_bcs(r, bcs), **kw)
+    Db, sb, _, pb = pyoracle.solve(m, oracle_bcs(m, direct), **kw)
+    assert pr["n_correctors"] == pb["n_correctors"]
+    assert np.array_equal(Dr, Db) and np.array_equal(sr, sb)
+
+
+def _d_error(tmp_path, body, match):
+    case = tmp_path
+    write_box_case(str(case / "constant" / "polyMesh"), box_polymesh(2, 2, 2))
+    (case / "0").mkdir(exist_ok=True)
+    (case / "0" / "D").write_text(HEADER + body)
+    with pytest.raises(_lib.S4GError, match=match):
+        read_case(str(case))
+
+
+def test_d_errors_name_the_problem(tmp_path):
+    free = "{ type solidTraction; traction uniform (0 0 0); pressure uniform 0; }"
+    rest = " ".join(f"{n} {free}" for n in ("xmin", "xmax", "ymin", "ymax", "zmax"))
+    _d_error(tmp_path, "boundaryField { zmin { type solidSymmetry; } " + rest + " }",
+             "zmin: type solidSymmetry is not built")
+    _d_error(tmp_path, "boundaryField { " + rest + " }", "zmin has no entry")
+    _d_error(tmp_path, "boundaryField { zmin { type solidTraction; traction uniform (0 0 0); "
+             "pressure uniform 0; tractionSeries { file \"t\"; } } " + rest + " }",
+             "tractionSeries is not built")
+    _d_error(tmp_path, "boundaryField { zmin { type fixedDisplacement; value nonuniform "
+             "List<vector> 3((0 0 0) (0 0 0) (0 0 0)); } " + rest + " }", "3 values for 4 faces")
+
+
+def test_mesh_errors(tmp_path):
+    pm = tmp_path / "constant" / "polyMesh"
+    write_box_case(str(pm), box_polymesh(2, 2, 2))
+    text = (pm / "points").read_text()
+    (pm / "points").write_text(text.replace("format      ascii", "format      binary"))
+    with pytest.raises(_lib.S4GError, match="ASCII only"):
+        read_case(str(tmp_path), d_file=None)
+    (pm / "points").write_text(text)
+    (pm / "owner").write_text("3\n(\n0\n1\n2\n)\n")
+    with pytest.raises(_lib.S4GError, match="owner has 3 labels"):
+        read_case(str(tmp_path), d_file=None)
+    with pytest.raises(_lib.S4GError, match="cannot open"):
+        read_case(str(tmp_path / "nowhere"), d_file=None)
+
+
+def _prism_case(tmp_path, nx=4, ny=3, nz=3):
+    from solids4foam_gb300.foam_case import prism_box_polymesh, write_polymesh
+    write_polymesh(str(tmp_path / "constant" / "polyMesh"), **prism_box_polymesh(nx, ny, nz, 1.0, 0.9, 0.8))
+    return read_case(str(tmp_path), d_file=None)[0]
+
+
+def _linear_bcs(mesh, a, b):
+    out = []
+    for p in range(6):
+        s, n = int(mesh["patch_start"][p]), int(mesh["patch_size"][p])
+        out.append((0, a + mesh["Cf"][s:s + n] @ b.T, None))
+    return out
+
+
+def test_prism_mesh_patch_test(tmp_path):
+    """The constant-strain patch test on a mesh of triangular prisms written
+    and read back as a polyMesh: the linear field is reproduced to
+    round-off (leastSquares with full boundary vectors)."""
+    m = _prism_case(tmp_path)
+    a = np.array([1e-6, 4e-6, 0.0])
+    b = np.array([[2e-6, 3e-6, 0.0], [5e-6, 6e-6, 0.0], [0.0, 0.0, 0.0]])
+    D, sig, G, perf = pyoracle.solve(m, _linear_bcs(m, a, b), E=200e9, nu=0.3, n_correctors=400,
+                                     solution_tol=1e-13, alternative_tol=1e-14, tolerance=1e-15,
+                                     rel_tol=0.0, ls_boundary_delta=1)
+    np.testing.assert_allclose(D, a + m["C"] @ b.T, atol=1e-15, rtol=1e-8)
+    np.testing.assert_allclose(G.reshape(-1, 3, 3), np.broadcast_to(b.T, (len(D), 3, 3)),
+                               atol=1e-13)

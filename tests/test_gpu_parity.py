@@ -261,6 +261,33 @@ def test_tl_total_displacement_matches_oracle(ctx, load, n_increments):
     model.close()
 
 
+@pytest.mark.parametrize("dic_subdomains", [False, True])
+def test_prism_mesh_from_polymesh_matches_oracle(ctx, tmp_path, dic_subdomains):
+    """A mesh of triangular prisms written and read back as an OpenFOAM
+    polyMesh: the GPU solve against the oracle in the same DIC order (exact
+    DIC, or processor-local DIC over 64-cell parts)."""
+    from solids4foam_gb300.foam_case import prism_box_polymesh, read_case, write_polymesh
+    write_polymesh(str(tmp_path / "constant" / "polyMesh"),
+                   **prism_box_polymesh(6, 5, 4, 1.0, 0.9, 0.8))
+    m, _ = read_case(str(tmp_path), d_file=None)
+    top = int(m["patch_size"][5])
+    bcs = {"zmin": ("fixedDisplacement", None, None),
+           "zmax": ("solidTraction", np.tile([1e5, 0.0, -1e6], (top, 1)), None)}
+    law = dict(type="linearElastic", E=200e9, nu=0.3)
+    model = sg.SolidModel(ctx, m, law, bcs, outer=dict(nCorrectors=3000), ls_boundary_delta=1,
+                          part_size=64, dic_subdomains=dic_subdomains)
+    D, sig, perf = model.evolve()
+    kw = dict(perm=model.permutation(), E=200e9, nu=0.3, n_correctors=3000, ls_boundary_delta=1)
+    if dic_subdomains:
+        kw["dic_domain"] = model.parts()
+    Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), **kw)
+    assert po["converged"] == 1 and perf["converged"] == 1
+    assert abs(perf["n_correctors"] - po["n_correctors"]) <= 1
+    assert abs(perf["total_lin_iters"] - po["total_lin_iters"]) <= 0.005 * po["total_lin_iters"]
+    assert rel(D, Do) < TOL_D and rel(sig, so) < TOL_S
+    model.close()
+
+
 def test_golden_fixture_tl(ctx):
     g = np.load(os.path.join(HERE, "golden", "oracle_small.npz"))
     m = sg.box_mesh(5, 4, 4, 1.0, 0.8, 0.8, 0.15, 12)
