@@ -419,6 +419,31 @@ s4g_status s4g_server_get_stats(s4g_server* server, s4g_server_stats* out);
 /* Cancels queued requests, lets running ones finish, frees everything. */
 s4g_status s4g_server_destroy(s4g_server* server);
 
+/* ------------------------------------------------ after the solve loop --
+ * Host-only steps the reference runs after evolve()'s corrector loop. */
+
+/* The cells of every point (OpenFOAM pointCells), from the faces:
+ * point_cell_start [n_points + 1]; point_cells [point_cell_start[n_points]]
+ * in increasing cell order, or NULL to get the sizes only. */
+s4g_status s4g_point_cells(int n_points, int n_faces, const int* face_start,
+                           const int* face_points, int n_internal_faces, const int* owner,
+                           const int* neighbour, int* point_cell_start, int* point_cells);
+/* pointD [n_points][3] as enhancedVolPointInterpolation::interpolate(D,
+ * gradD, pointD) computes it (enhancedVolPointInterpolate.C:351-423, from
+ * mechanicalModel.C:829-841 after each evolve(), linGeomTotalDispSolid.C:212):
+ * the inverse-distance-weighted average over the point's cells of
+ * D_c + (x_p - C_c) . gradD_c.  D [n_cells][3], gradD [n_cells][9]
+ * (s4g_get_gradD), C [n_cells][3] the cell centres. */
+s4g_status s4g_point_interpolate(int n_points, const double* points, const int* point_cell_start,
+                                 const int* point_cells, int n_cells, const double* C,
+                                 const double* D, const double* gradD, double* pointD);
+/* solidModel::writeFields (solidModel.C:1936-1962): sigmaEq [n] =
+ * sqrt(3/2 |dev sigma|^2); epsilon [n][6] = symm(gradD) and epsilonEq [n]
+ * = sqrt(2/3 |dev epsilon|^2) (written by the reference for the
+ * linear-geometry model).  Any output may be NULL. */
+s4g_status s4g_derived_fields(int n, const double* sigma, const double* gradD, double* sigmaEq,
+                              double* epsilon, double* epsilonEq);
+
 /* ---------------------------------------------------- case generation --
  * Seeded hexahedral box meshes (blockMesh + perturbMeshPoints stand-in,
  * applications/utilities/perturbMeshPoints/perturbMeshPoints.C:244-330):
@@ -454,6 +479,11 @@ s4g_status s4g_foam_read_mesh(const char* polymesh_dir, s4g_foam_case** out);
 /* The mesh as an s4g_mesh_desc (pointers valid until s4g_foam_free) and
  * its number of points. */
 s4g_status s4g_foam_mesh_desc(const s4g_foam_case* fc, s4g_mesh_desc* desc, int* n_points);
+/* The points [n_points][3] and faces (face f has the points
+ * face_points[face_start[f] .. face_start[f+1])) as read; pointers valid
+ * until s4g_foam_free. */
+s4g_status s4g_foam_mesh_points(const s4g_foam_case* fc, const double** points,
+                                const int** face_start, const int** face_points);
 /* Patch name and OpenFOAM patch type ("patch", "wall", "empty", ...), or
  * NULL for an index out of range. */
 const char* s4g_foam_patch_name(const s4g_foam_case* fc, int patch);

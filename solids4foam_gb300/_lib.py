@@ -156,8 +156,17 @@ _SIGS = {
     "s4g_box_mesh_build": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_double, ct.c_double,
                                       ct.c_double, ct.c_double, ct.c_uint64] + [ct.c_void_p] * 9),
     "s4g_box_mesh_faces": (ct.c_int, [ct.c_int, ct.c_int, ct.c_int, ct.c_void_p]),
+    "s4g_point_cells": (ct.c_int, [ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
+                                   ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "s4g_point_interpolate": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                         ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                         ct.c_void_p]),
+    "s4g_derived_fields": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                      ct.c_void_p, ct.c_void_p]),
     "s4g_foam_read_mesh": (ct.c_int, [ct.c_char_p, ct.POINTER(ct.c_void_p)]),
     "s4g_foam_mesh_desc": (ct.c_int, [ct.c_void_p, ct.POINTER(MeshDesc), ct.POINTER(ct.c_int)]),
+    "s4g_foam_mesh_points": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_void_p),
+                                        ct.POINTER(ct.c_void_p), ct.POINTER(ct.c_void_p)]),
     "s4g_foam_patch_name": (ct.c_char_p, [ct.c_void_p, ct.c_int]),
     "s4g_foam_patch_type": (ct.c_char_p, [ct.c_void_p, ct.c_int]),
     "s4g_foam_read_d": (ct.c_int, [ct.c_void_p, ct.c_char_p]),

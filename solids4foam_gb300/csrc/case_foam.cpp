@@ -594,6 +594,15 @@ s4g_status s4g_foam_mesh_desc(const s4g_foam_case* m, s4g_mesh_desc* d, int* n_p
   return S4G_OK;
 }
 
+s4g_status s4g_foam_mesh_points(const s4g_foam_case* m, const double** points,
+                                const int** face_start, const int** face_points) {
+  if (!m) return S4G_BAD_ARG;
+  if (points) *points = m->points.data();
+  if (face_start) *face_start = m->faceStart.data();
+  if (face_points) *face_points = m->facePoints.data();
+  return S4G_OK;
+}
+
 const char* s4g_foam_patch_name(const s4g_foam_case* m, int p) {
   if (!m || p < 0 || p >= (int)m->patchName.size()) return nullptr;
   return m->patchName[(size_t)p].c_str();

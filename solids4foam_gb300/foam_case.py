@@ -44,6 +44,12 @@ def read_case(case_dir: str, d_file: str | None = "0/D", polymesh: str = "consta
                     Sf=_arr(d.Sf, 3 * nf, np.float64).reshape(nf, 3),
                     patch_start=_arr(d.patch_start, npch, np.int32),
                     patch_size=_arr(d.patch_size, npch, np.int32))
+        pp, fs, fp = ct.c_void_p(), ct.c_void_p(), ct.c_void_p()
+        _lib.check(L.s4g_foam_mesh_points(h, ct.byref(pp), ct.byref(fs), ct.byref(fp)),
+                   "s4g_foam_mesh_points")
+        mesh["points"] = _arr(pp.value, 3 * npts.value, np.float64).reshape(-1, 3)
+        mesh["face_start"] = _arr(fs.value, nf + 1, np.int32)
+        mesh["face_points"] = _arr(fp.value, int(mesh["face_start"][-1]), np.int32)
         mesh["patch_names"] = [L.s4g_foam_patch_name(h, p).decode() for p in range(npch)]
         mesh["patch_types"] = [L.s4g_foam_patch_type(h, p).decode() for p in range(npch)]
         bcs = None
