@@ -303,53 +303,183 @@ std::vector<int> parseLabels(Cursor& c) {
   return out;
 }
 
+// ------------------------------------------------- large list files ---
+// points, faces, owner and neighbour hold one list each (faceCompactList:
+// two), of up to millions of items: they are read straight from the text
+// with a pointer scanner, without a token per number.
+
+struct Scan {
+  std::string text;
+  const char* p;
+  const char* e;
+  std::string where;
+  std::string cls;  // the header's class
+
+  explicit Scan(const std::string& path) : text(readFile(path)), where(path) {
+    p = text.data();
+    e = p + text.size();
+    header();
+  }
+  void skip() {
+    for (;;) {
+      while (p < e && (*p == ' ' || *p == '\t' || *p == '\n' || *p == '\r' || *p == '\f' || *p == '\v')) ++p;
+      if (p + 1 < e && p[0] == '/' && p[1] == '/') {
+        while (p < e && *p != '\n') ++p;
+      } else if (p + 1 < e && p[0] == '/' && p[1] == '*') {
+        const char* q = p + 2;
+        while (q + 1 < e && !(q[0] == '*' && q[1] == '/')) ++q;
+        if (q + 1 >= e) fail(where + ": unterminated comment");
+        p = q + 2;
+      } else {
+        return;
+      }
+    }
+  }
+  char peek() {
+    skip();
+    if (p >= e) fail(where + ": unexpected end of file");
+    return *p;
+  }
+  void expect(char c) {
+    if (peek() != c) fail(where + ": expected '" + std::string(1, c) + "', found '" + std::string(1, *p) + "'");
+    ++p;
+  }
+  bool delimiter(const char* q) const {
+    return q >= e || *q == ' ' || *q == '\t' || *q == '\n' || *q == '\r' || *q == '\f' ||
+           *q == '\v' || isPunct(*q) || *q == '/';
+  }
+  long integer() {
+    skip();
+    char* end = nullptr;
+    errno = 0;
+    long v = std::strtol(p, &end, 10);
+    if (end == p || errno == ERANGE || !delimiter(end)) fail(where + ": bad integer near '" + std::string(p, std::min<size_t>(16, (size_t)(e - p))) + "'");
+    p = end;
+    return v;
+  }
+  int label() {
+    long v = integer();
+    if (v < 0 || v > 0x7fffffff) fail(where + ": label out of range: " + std::to_string(v));
+    return (int)v;
+  }
+  double number() {
+    skip();
+    char* end = nullptr;
+    errno = 0;
+    double v = std::strtod(p, &end);
+    if (end == p || errno == ERANGE || !delimiter(end)) fail(where + ": bad number near '" + std::string(p, std::min<size_t>(16, (size_t)(e - p))) + "'");
+    p = end;
+    return v;
+  }
+  // The FoamFile header dictionary, if any: format ascii required; class kept.
+  void header() {
+    skip();
+    static const char kw[] = "FoamFile";
+    if ((size_t)(e - p) < sizeof(kw) - 1 || std::strncmp(p, kw, sizeof(kw) - 1) != 0) return;
+    const char* b = p;
+    p += sizeof(kw) - 1;
+    expect('{');
+    int depth = 1;
+    while (depth > 0) {
+      skip();
+      if (p >= e) fail(where + ": unterminated FoamFile header");
+      if (*p == '"') {
+        ++p;
+        while (p < e && *p != '"') ++p;
+      }
+      if (p < e && *p == '{') ++depth;
+      if (p < e && *p == '}') --depth;
+      ++p;
+    }
+    std::vector<Tok> t = tokenize(std::string(b, p), where);
+    Cursor c{t, 2, where};
+    std::vector<Entry> h = parseDict(c, true);
+    if (const Entry* f = find(h, "format"))
+      if (!f->val.empty() && f->val[0].s != "ascii")
+        fail(where + ": format " + f->val[0].s + " is not read (ASCII only)");
+    if (const Entry* k = find(h, "class"))
+      if (!k->val.empty()) cls = k->val[0].s;
+  }
+};
+
+// `N ( item ... )`, `( item ... )` or `N{item}`, with an optional leading
+// List<...> word; item(s) reads one item.
+template <class Item>
+void scanList(Scan& s, Item item) {
+  if (s.peek() == 'L') {
+    while (!s.delimiter(s.p)) ++s.p;
+  }
+  long n = -1;
+  if (s.peek() >= '0' && s.peek() <= '9') n = s.integer();
+  if (s.peek() == '{') {
+    if (n < 0) fail(s.where + ": a uniform list needs a size");
+    ++s.p;
+    const char* at = s.p;
+    for (long i = 0; i < n; ++i) {
+      s.p = at;
+      item(s);
+    }
+    if (n == 0)  // an empty list: its one item is not read
+      while (s.peek() != '}') ++s.p;
+    s.expect('}');
+    return;
+  }
+  s.expect('(');
+  long got = 0;
+  while (s.peek() != ')') {
+    item(s);
+    ++got;
+  }
+  ++s.p;
+  if (n >= 0 && got != n)
+    fail(s.where + ": list of " + std::to_string(n) + " has " + std::to_string(got) + " items");
+}
+
+std::vector<int> scanLabels(Scan& s) {
+  std::vector<int> out;
+  scanList(s, [&](Scan& ss) { out.push_back(ss.label()); });
+  return out;
+}
+
 // ----------------------------------------------------------- polyMesh ---
 
 void readMesh(s4g_foam_case& m, const std::string& dir) {
   {  // points
-    std::string path = dir + "/points";
-    std::vector<Tok> t = payload(path);
-    Cursor c{t, 0, path};
-    parseList(c, [&](Cursor& cc) {
-      P3 v = parseVector(cc);
-      m.points.push_back(v.x); m.points.push_back(v.y); m.points.push_back(v.z);
+    Scan s(dir + "/points");
+    scanList(s, [&](Scan& ss) {
+      ss.expect('(');
+      for (int k = 0; k < 3; ++k) m.points.push_back(ss.number());
+      ss.expect(')');
     });
     m.nPoints = (int)(m.points.size() / 3);
   }
   {  // faces
-    std::string path = dir + "/faces", cls;
-    std::vector<Tok> t = payload(path, &cls);
-    Cursor c{t, 0, path};
+    Scan s(dir + "/faces");
     m.faceStart.assign(1, 0);
-    if (cls == "faceCompactList") {
-      std::vector<int> offsets = parseLabels(c);
-      m.facePoints = parseLabels(c);
+    if (s.cls == "faceCompactList") {
+      std::vector<int> offsets = scanLabels(s);
+      m.facePoints = scanLabels(s);
       if (offsets.empty() || offsets[0] != 0 || offsets.back() != (int)m.facePoints.size())
-        fail(path + ": faceCompactList offsets do not match its labels");
+        fail(s.where + ": faceCompactList offsets do not match its labels");
       for (size_t f = 1; f < offsets.size(); ++f) {
-        if (offsets[f] < offsets[f - 1]) fail(path + ": decreasing faceCompactList offsets");
+        if (offsets[f] < offsets[f - 1]) fail(s.where + ": decreasing faceCompactList offsets");
         m.faceStart.push_back(offsets[f]);
       }
     } else {
-      parseList(c, [&](Cursor& cc) {
-        std::vector<int> f = parseLabels(cc);
-        m.facePoints.insert(m.facePoints.end(), f.begin(), f.end());
+      scanList(s, [&](Scan& ss) {
+        scanList(ss, [&](Scan& s3) { m.facePoints.push_back(s3.label()); });
         m.faceStart.push_back((int)m.facePoints.size());
       });
     }
     m.nFaces = (int)m.faceStart.size() - 1;
   }
   {
-    std::string path = dir + "/owner";
-    std::vector<Tok> t = payload(path);
-    Cursor c{t, 0, path};
-    m.owner = parseLabels(c);
+    Scan s(dir + "/owner");
+    m.owner = scanLabels(s);
   }
   {
-    std::string path = dir + "/neighbour";
-    std::vector<Tok> t = payload(path);
-    Cursor c{t, 0, path};
-    m.neighbour = parseLabels(c);
+    Scan s(dir + "/neighbour");
+    m.neighbour = scanLabels(s);
   }
   {  // boundary: N ( name { type ..; nFaces ..; startFace ..; } ... )
     std::string path = dir + "/boundary";
