@@ -291,7 +291,7 @@ typedef struct s4g_perf {
  * the linear model) on the device: every corrector, PCG iteration and
  * convergence test stays on the GPU; only the final fields come back.
  * D_out [n_cells][3]; sigma_out [n_cells][6] (XX XY XZ YY YZ ZZ); either may
- * be NULL.  Replaces solidModel::evolve (solidModel.H:759) of the two
+ * be NULL.  Replaces solidModel::evolve (solidModel.H:759) of the
  * models named above, with tractionBoundarySnGrad evaluated on the device. */
 s4g_status s4g_solve(s4g_mesh* mesh, s4g_model model, int n_increments,
                      double* D_out, double* sigma_out, s4g_perf* perf);

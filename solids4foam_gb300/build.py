@@ -1,4 +1,5 @@
-"""Builds libs4g.so in-tree (solids4foam_gb300/_build/) with nvcc for sm_103a.
+"""Builds libs4g.so in-tree (solids4foam_gb300/_build/) with nvcc for sm_103a,
+and the standalone C++ driver s4g_solve_case linked against it.
 
 Translation units compile in parallel; the CUDA runtime is linked
 statically, so the library only needs the NVIDIA driver at run time.
@@ -16,6 +17,8 @@ ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libs4g.so")
+DRIVER_SRC = os.path.join(HERE, "driver", "s4g_solve_case.cpp")
+DRIVER = os.path.join(OUT, "s4g_solve_case")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(ROOT, "include"),
@@ -55,8 +58,27 @@ def _stale() -> bool:
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+def build_driver(force: bool = False) -> str:
+    """The standalone driver, linked to libs4g.so with an $ORIGIN rpath."""
+    if (not force and os.path.exists(DRIVER)
+            and all(os.path.getmtime(DRIVER) >= os.path.getmtime(d)
+                    for d in (DRIVER_SRC, LIB, os.path.join(ROOT, "include", "s4g.h")))):
+        return DRIVER
+    cxx = shutil.which("g++") or shutil.which("c++")
+    if not cxx:
+        raise RuntimeError("no C++ compiler for the driver")
+    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), DRIVER_SRC,
+           "-L", OUT, "-ls4g", "-Wl,-rpath,$ORIGIN", "-o", DRIVER + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"driver build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    os.replace(DRIVER + ".tmp", DRIVER)
+    return DRIVER
+
+
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if not force and not _stale():
+        build_driver()
         return LIB
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
@@ -69,6 +91,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver(force=True)
     return LIB
 
 

@@ -1,0 +1,233 @@
+// s4g_solve_case: the standalone C++ driver of libs4g.  It does for a meshed
+// OpenFOAM case directory what the OpenFOAM-side solid-model class does
+// inside solids4Foam, through the same C ABI and without OpenFOAM:
+//   read constant/polyMesh and 0/D            s4g_foam_read_mesh, s4g_foam_read_d
+//   upload the mesh, set law, BCs, controls   s4g_mesh_upload, s4g_material_set,
+//                                             s4g_foam_apply_bcs, s4g_solver_set
+//   evolve()                                  s4g_solve, s4g_get_gradD
+//   after the loop                            s4g_point_interpolate, s4g_derived_fields
+// and prints one JSON line with the run's figures.  The material, model and
+// controls come from the command line (the reference reads them from
+// constant/mechanicalProperties, constant/solidProperties and
+// system/fvSolution).  --plan-only stops after the host-side mesh planning
+// and needs no GPU.  --write writes pointD as an ASCII pointVectorField into
+// <case>/<time>/pointD.
+
+#include "s4g.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+namespace {
+
+void usage() {
+  std::fprintf(stderr,
+               "usage: s4g_solve_case CASE_DIR [options]\n"
+               "  --model linearGeometryTotalDisplacement | nonLinearGeometryTotalLagrangian |\n"
+               "          nonLinearGeometryTotalLagrangianTotalDisplacement\n"
+               "  --E E --nu NU            linearElastic (default 200e9, 0.3)\n"
+               "  --mu MU --K K            neoHookeanElastic (the total Lagrangian models)\n"
+               "  --increments N           load increments of the total Lagrangian models (1)\n"
+               "  --precision FP64|FP32_REFINE\n"
+               "  --preconditioner DIC|diagonal  --tolerance T  --relTol R  --maxIter N\n"
+               "  --nCorrectors N  --solutionTolerance T  --alternativeTolerance T\n"
+               "  --scaleFactor S          RhieChow scale factor (0.1)\n"
+               "  --renumber none|RCM|tiled  --part-size N  --dic-subdomains  --ls-full-delta\n"
+               "  --device N  --plan-only  --write TIME\n");
+}
+
+[[noreturn]] void die(const char* what, s4g_status st) {
+  std::fprintf(stderr, "s4g_solve_case: %s: %s (%s)\n", what, s4g_status_str(st), s4g_last_error());
+  std::exit(2);
+}
+
+void check(s4g_status st, const char* what) {
+  if (st != S4G_OK) die(what, st);
+}
+
+bool writePointField(const std::string& dir, const std::string& time, const double* v, int n,
+                     const s4g_foam_case* fc, int nPatches) {
+  const std::string tdir = dir + "/" + time;
+  mkdir(tdir.c_str(), 0755);
+  FILE* f = std::fopen((tdir + "/pointD").c_str(), "w");
+  if (!f) return false;
+  std::fprintf(f,
+               "FoamFile\n{\n    version     2.0;\n    format      ascii;\n"
+               "    class       pointVectorField;\n    location    \"%s\";\n"
+               "    object      pointD;\n}\n\ndimensions      [0 1 0 0 0 0 0];\n\n"
+               "internalField   nonuniform List<vector>\n%d\n(\n",
+               time.c_str(), n);
+  for (int i = 0; i < n; ++i)
+    std::fprintf(f, "(%.17g %.17g %.17g)\n", v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+  std::fprintf(f, ")\n;\n\nboundaryField\n{\n");
+  for (int p = 0; p < nPatches; ++p)
+    std::fprintf(f, "    %s\n    {\n        type            calculated;\n    }\n",
+                 s4g_foam_patch_name(fc, p));
+  std::fprintf(f, "}\n");
+  return std::fclose(f) == 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  if (argc < 2 || !std::strcmp(argv[1], "--help") || !std::strcmp(argv[1], "-h")) {
+    usage();
+    return argc < 2 ? 1 : 0;
+  }
+  const std::string caseDir = argv[1];
+  std::string modelName = "linearGeometryTotalDisplacement", writeTime;
+  s4g_law law{};
+  law.type = S4G_LINEAR_ELASTIC;
+  law.E = 200e9;
+  law.nu = 0.3;
+  law.mu = 1e6;
+  law.K = 2e7;
+  s4g_lin_solver lin;
+  s4g_outer outer;
+  s4g_default_controls(&lin, &outer);
+  s4g_mesh_opts mo{S4G_RENUMBER_TILED, 512, 0, 0, 0};
+  s4g_precision precision = S4G_FP64;
+  int increments = 1, device = 0;
+  bool planOnly = false, muK = false;
+  for (int i = 2; i < argc; ++i) {
+    const std::string a = argv[i];
+    auto val = [&]() -> const char* {
+      if (i + 1 >= argc) {
+        std::fprintf(stderr, "s4g_solve_case: %s needs a value\n", a.c_str());
+        std::exit(1);
+      }
+      return argv[++i];
+    };
+    if (a == "--model") modelName = val();
+    else if (a == "--E") law.E = std::atof(val());
+    else if (a == "--nu") law.nu = std::atof(val());
+    else if (a == "--mu") { law.mu = std::atof(val()); muK = true; }
+    else if (a == "--K") { law.K = std::atof(val()); muK = true; }
+    else if (a == "--increments") increments = std::atoi(val());
+    else if (a == "--precision") {
+      const std::string p = val();
+      if (p == "FP64") precision = S4G_FP64;
+      else if (p == "FP32_REFINE") precision = S4G_FP32_REFINE;
+      else { usage(); return 1; }
+    }
+    else if (a == "--preconditioner") {
+      const std::string p = val();
+      if (p == "DIC" || p == "FDIC") lin.preconditioner = S4G_PRECOND_DIC;
+      else if (p == "diagonal") lin.preconditioner = S4G_PRECOND_DIAGONAL;
+      else { usage(); return 1; }
+    }
+    else if (a == "--tolerance") lin.tolerance = std::atof(val());
+    else if (a == "--relTol") lin.rel_tol = std::atof(val());
+    else if (a == "--maxIter") lin.max_iter = std::atoi(val());
+    else if (a == "--nCorrectors") outer.n_correctors = std::atoi(val());
+    else if (a == "--solutionTolerance") outer.solution_tol = std::atof(val());
+    else if (a == "--alternativeTolerance") outer.alternative_tol = std::atof(val());
+    else if (a == "--scaleFactor") outer.stab_scale = std::atof(val());
+    else if (a == "--renumber") {
+      const std::string r = val();
+      if (r == "none") mo.renumber = S4G_RENUMBER_NONE;
+      else if (r == "RCM") mo.renumber = S4G_RENUMBER_RCM;
+      else if (r == "tiled") mo.renumber = S4G_RENUMBER_TILED;
+      else { usage(); return 1; }
+    }
+    else if (a == "--part-size") mo.part_size = std::atoi(val());
+    else if (a == "--dic-subdomains") mo.dic_subdomains = 1;
+    else if (a == "--ls-full-delta") mo.ls_boundary_delta = 1;
+    else if (a == "--device") device = std::atoi(val());
+    else if (a == "--plan-only") planOnly = true;
+    else if (a == "--write") writeTime = val();
+    else { usage(); return 1; }
+  }
+  s4g_model model;
+  if (modelName == "linearGeometryTotalDisplacement") model = S4G_LIN_GEOM_TOTAL_DISP;
+  else if (modelName == "nonLinearGeometryTotalLagrangian") model = S4G_NONLIN_GEOM_TOTAL_LAG;
+  else if (modelName == "nonLinearGeometryTotalLagrangianTotalDisplacement")
+    model = S4G_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP;
+  else { usage(); return 1; }
+  if (model != S4G_LIN_GEOM_TOTAL_DISP) {
+    law.type = S4G_NEO_HOOKEAN;
+    law.use_mu_K = 1;
+  } else if (muK) {
+    law.use_mu_K = 1;
+  }
+
+  // the case
+  s4g_foam_case* fc = nullptr;
+  check(s4g_foam_read_mesh((caseDir + "/constant/polyMesh").c_str(), &fc), "reading constant/polyMesh");
+  s4g_mesh_desc desc;
+  int nPoints = 0;
+  check(s4g_foam_mesh_desc(fc, &desc, &nPoints), "s4g_foam_mesh_desc");
+  s4g_mesh_info info;
+  check(s4g_mesh_plan(&desc, &mo, nullptr, &info), "s4g_mesh_plan");
+  if (planOnly) {
+    std::printf("{\"case\": \"%s\", \"cells\": %d, \"faces\": %d, \"internal_faces\": %d, "
+                "\"points\": %d, \"patches\": %d, \"parts\": %d, \"part_depth\": %d, "
+                "\"levels\": %d}\n",
+                caseDir.c_str(), desc.n_cells, desc.n_faces, desc.n_internal_faces, nPoints,
+                desc.n_patches, info.n_parts, info.part_depth, info.n_levels_global);
+    s4g_foam_free(fc);
+    return 0;
+  }
+  check(s4g_foam_read_d(fc, (caseDir + "/0/D").c_str()), "reading 0/D");
+
+  // the solve
+  s4g_ctx_opts co{device, 0, 0, 0};
+  s4g_ctx* ctx = nullptr;
+  check(s4g_ctx_create(&ctx, &co), "s4g_ctx_create");
+  s4g_mesh* mesh = nullptr;
+  check(s4g_mesh_upload(ctx, &desc, &mo, &mesh), "s4g_mesh_upload");
+  check(s4g_material_set(mesh, &law), "s4g_material_set");
+  check(s4g_foam_apply_bcs(fc, mesh), "applying 0/D");
+  check(s4g_solver_set(mesh, &lin, &outer, precision), "s4g_solver_set");
+  const int n = desc.n_cells;
+  std::vector<double> D(3 * (size_t)n), sigma(6 * (size_t)n), gradD(9 * (size_t)n);
+  s4g_perf perf;
+  s4g_status st = s4g_solve(mesh, model, increments, D.data(), sigma.data(), &perf);
+  if (st != S4G_OK && st != S4G_NOT_CONVERGED) die("s4g_solve", st);
+  if (st == S4G_NOT_CONVERGED) std::fprintf(stderr, "Max iterations reached within momentum loop\n");
+  check(s4g_get_gradD(mesh, gradD.data()), "s4g_get_gradD");
+
+  // after the loop
+  const double *points = nullptr;
+  const int *faceStart = nullptr, *facePoints = nullptr;
+  check(s4g_foam_mesh_points(fc, &points, &faceStart, &facePoints), "s4g_foam_mesh_points");
+  std::vector<int> pcStart((size_t)nPoints + 1);
+  check(s4g_point_cells(nPoints, desc.n_faces, faceStart, facePoints, desc.n_internal_faces,
+                        desc.owner, desc.neighbour, pcStart.data(), nullptr), "s4g_point_cells");
+  std::vector<int> pcCells((size_t)pcStart[(size_t)nPoints]);
+  check(s4g_point_cells(nPoints, desc.n_faces, faceStart, facePoints, desc.n_internal_faces,
+                        desc.owner, desc.neighbour, pcStart.data(), pcCells.data()), "s4g_point_cells");
+  std::vector<double> pointD(3 * (size_t)nPoints), sigmaEq((size_t)n);
+  check(s4g_point_interpolate(nPoints, points, pcStart.data(), pcCells.data(), n, desc.C, D.data(),
+                              gradD.data(), pointD.data()), "s4g_point_interpolate");
+  check(s4g_derived_fields(n, sigma.data(), gradD.data(), sigmaEq.data(), nullptr, nullptr),
+        "s4g_derived_fields");
+  double maxD = 0, maxSeq = 0, maxPD = 0;
+  for (int c = 0; c < n; ++c) {
+    maxD = std::fmax(maxD, std::sqrt(D[3 * c] * D[3 * c] + D[3 * c + 1] * D[3 * c + 1] + D[3 * c + 2] * D[3 * c + 2]));
+    maxSeq = std::fmax(maxSeq, sigmaEq[(size_t)c]);
+  }
+  for (int p = 0; p < nPoints; ++p)
+    maxPD = std::fmax(maxPD, std::sqrt(pointD[3 * p] * pointD[3 * p] + pointD[3 * p + 1] * pointD[3 * p + 1] +
+                                       pointD[3 * p + 2] * pointD[3 * p + 2]));
+  std::printf("{\"case\": \"%s\", \"model\": \"%s\", \"cells\": %d, \"status\": \"%s\", "
+              "\"converged\": %d, \"correctors\": %d, \"pcg_iterations\": %lld, "
+              "\"solve_ms\": %.3f, \"max_mag_D\": %.9g, \"max_mag_pointD\": %.9g, "
+              "\"max_sigmaEq\": %.9g}\n",
+              caseDir.c_str(), modelName.c_str(), n, s4g_status_str(st), perf.converged,
+              perf.n_correctors, perf.total_lin_iters, perf.solve_ms, maxD, maxPD, maxSeq);
+  if (!writeTime.empty() &&
+      !writePointField(caseDir, writeTime, pointD.data(), nPoints, fc, desc.n_patches)) {
+    std::fprintf(stderr, "s4g_solve_case: cannot write %s/%s/pointD\n", caseDir.c_str(), writeTime.c_str());
+    return 2;
+  }
+  s4g_mesh_destroy(mesh);
+  s4g_ctx_destroy(ctx);
+  s4g_foam_free(fc);
+  return st == S4G_OK ? 0 : 3;
+}
