@@ -215,3 +215,31 @@ def test_server_scheduler_dry_run(built):
     # the second large request finished last: the small ones did not wait for it
     assert st["p99_ms"] > 200
     srv.close()
+
+
+def test_server_footprint_of_the_models(built):
+    """Dry run: both total Lagrangian forms are admitted and sized above the
+    linear-geometry model (their extra fields); a traction relaxation
+    factor, which requests cannot carry, is refused."""
+    import time
+    m = sg.box_mesh(12, 12, 12, 1.0, 1.0, 1.0, 0.1, 1)
+    bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", [0, 0, -1e5], None)}
+    lin = dict(type="linearElastic", E=70e9, nu=0.33)
+    neo = dict(type="neoHookeanElastic", mu=1e6, K=2e7)
+    used = {}
+    for model, law in (("linearGeometryTotalDisplacement", lin),
+                       ("nonLinearGeometryTotalLagrangian", neo),
+                       ("nonLinearGeometryTotalLagrangianTotalDisplacement", neo)):
+        srv = sg.Server(max_slots=1, memory_budget=1 << 32, dry_run=True, dry_run_us_per_kcell=50000)
+        rid = srv.submit(m, law, bcs, model=model)
+        time.sleep(0.02)
+        used[model] = srv.stats()["bytes_in_use"]
+        assert srv.result(rid)[0] == _lib.OK
+        srv.close()
+    assert used["nonLinearGeometryTotalLagrangian"] > used["linearGeometryTotalDisplacement"] > 0
+    assert (used["nonLinearGeometryTotalLagrangianTotalDisplacement"]
+            == used["nonLinearGeometryTotalLagrangian"])
+    srv = sg.Server(max_slots=1, dry_run=True)
+    with pytest.raises(ValueError, match="relaxationFactor"):
+        srv.submit(m, lin, {"zmax": ("solidTraction", [0, 0, -1e5], None, 0.5)})
+    srv.close()
