@@ -156,3 +156,48 @@ def test_prism_mesh_patch_test(tmp_path):
     np.testing.assert_allclose(D, a + m["C"] @ b.T, atol=1e-15, rtol=1e-8)
     np.testing.assert_allclose(G.reshape(-1, 3, 3), np.broadcast_to(b.T, (len(D), 3, 3)),
                                atol=1e-13)
+
+
+def test_bad_arguments_are_errors_not_crashes(tmp_path):
+    import ctypes as ct
+    L = _lib.lib()
+    h = ct.c_void_p()
+    assert L.s4g_foam_read_mesh(None, ct.byref(h)) == _lib.BAD_ARG
+    assert L.s4g_foam_read_mesh(PRISMS.encode(), None) == _lib.BAD_ARG
+    d = _lib.MeshDesc()
+    assert L.s4g_foam_mesh_desc(None, ct.byref(d), None) == _lib.BAD_ARG
+    assert L.s4g_foam_read_mesh(os.path.join(PRISMS, "constant", "polyMesh").encode(),
+                                ct.byref(h)) == _lib.OK
+    try:
+        assert L.s4g_foam_patch_name(h, -1) is None and L.s4g_foam_patch_type(h, 3) is None
+        t, v = ct.c_int(), ct.c_void_p()
+        assert L.s4g_foam_bc(h, 0, ct.byref(t), ct.byref(v), None, None) == _lib.BAD_ARG
+        assert b"no D file" in L.s4g_last_error()
+        assert L.s4g_foam_bc(h, 7, None, None, None, None) == _lib.BAD_ARG
+        assert L.s4g_foam_apply_bcs(h, None) == _lib.BAD_ARG
+        assert L.s4g_foam_read_d(h, None) == _lib.BAD_ARG
+    finally:
+        L.s4g_foam_free(h)
+    L.s4g_foam_free(None)
+    fs = np.array([0, 3], np.int32)
+    fp = np.array([0, 1, 5], np.int32)
+    own = np.zeros(1, np.int32)
+    start = np.zeros(4, np.int32)
+    assert L.s4g_point_cells(3, 1, fs.ctypes.data, fp.ctypes.data, 0, own.ctypes.data, None,
+                             start.ctypes.data, None) == _lib.BAD_ARG
+    pts = np.zeros((1, 3))
+    pcs, pcc = np.array([0, 1], np.int32), np.array([4], np.int32)
+    C, D, G, out = np.zeros((2, 3)), np.zeros((2, 3)), np.zeros((2, 9)), np.zeros((1, 3))
+    assert L.s4g_point_interpolate(1, pts.ctypes.data, pcs.ctypes.data, pcc.ctypes.data, 2,
+                                   C.ctypes.data, D.ctypes.data, G.ctypes.data,
+                                   out.ctypes.data) == _lib.BAD_ARG
+    assert b"cell out of range" in L.s4g_last_error()
+    assert L.s4g_derived_fields(2, None, None, out.ctypes.data, None, None) == _lib.BAD_ARG
+    assert L.s4g_box_mesh_faces(0, 1, 1, out.ctypes.data) == _lib.BAD_ARG
+    m = box_polymesh(1, 1, 1)
+    names = (ct.c_char_p * 6)(*[n.encode() for n in m["patch_names"]])
+    assert L.s4g_foam_write_mesh(str(tmp_path / "missing" / "dir").encode(), 8,
+                                 m["points"].ctypes.data, 6, m["face_start"].ctypes.data,
+                                 m["face_points"].ctypes.data, 0, m["owner"].ctypes.data, None,
+                                 6, names, m["patch_start"].ctypes.data,
+                                 m["patch_size"].ctypes.data) == _lib.BAD_ARG
