@@ -76,9 +76,18 @@ def build_driver(force: bool = False) -> str:
     return DRIVER
 
 
+def _try_driver(force: bool) -> None:
+    """The driver is an extra beside the library: a failure to build it is
+    reported, not raised (its own tests then fail)."""
+    try:
+        build_driver(force=force)
+    except (RuntimeError, OSError) as e:
+        print(f"warning: s4g_solve_case not built: {e}", file=sys.stderr)
+
+
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if not force and not _stale():
-        build_driver()
+        _try_driver(False)
         return LIB
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
@@ -91,7 +100,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
-    build_driver(force=True)
+    _try_driver(True)
     return LIB
 
 
