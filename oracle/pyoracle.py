@@ -64,7 +64,7 @@ class Perf(ct.Structure):
         ("n_correctors", ct.c_int), ("converged", ct.c_int),
         ("total_lin_iters", ct.c_longlong), ("initial_residual", ct.c_double),
         ("rel_residual", ct.c_double), ("seconds", ct.c_double),
-        ("enforce_linear", ct.c_int),
+        ("enforce_linear", ct.c_int), ("nan_detected", ct.c_int),
     ]
 
 

@@ -834,6 +834,18 @@ struct Solver {
         denom = std::max(mx, SMALL);
       }
       relRes = resMax / denom;
+      // The max-reductions above drop NaN (std::max(0, NaN) is 0), so a
+      // non-finite field is caught here and ends the solve, unconverged.
+      bool finite = true;
+      for (int c = 0; c < m.nC && finite; ++c)
+        finite = std::isfinite(U[c].x) && std::isfinite(U[c].y) && std::isfinite(U[c].z);
+      if (!finite) {
+        perf.nan_detected = 1;
+        perf.n_correctors++;
+        conv = false;
+        correctorsLeft = 0;
+        break;
+      }
       const double materialResidual = 0.0;
       conv = false;
       if (iCorr > 1 && materialResidual < s.material_tol) {

@@ -84,6 +84,9 @@ typedef struct {
   double rel_residual;    /* last corrector: relative displacement residual */
   double seconds;         /* wall time of the solve loop */
   int enforce_linear;     /* TL: linear geometry was enforced */
+  int nan_detected;       /* a corrector produced a non-finite D: the solve
+                             stopped there, unconverged (the library's
+                             S4G_NAN_DETECTED) */
 } orc_perf;
 
 void orc_default_settings(orc_settings* s);

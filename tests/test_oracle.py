@@ -242,3 +242,17 @@ def test_tl_total_path_independent_without_stabilisation():
     D3, _, _, p3 = pyoracle.solve(m, bcs, n_increments=3, **kw)
     assert p1["converged"] == p3["converged"] == 1
     assert np.linalg.norm(D3 - D1) / np.linalg.norm(D1) < 1e-6
+
+
+def test_non_finite_field_stops_the_solve():
+    """A neoHookean total Lagrangian solve that blows up (K/mu = 10, ten
+    traction increments, no relaxation) stops at the first non-finite
+    corrector, unconverged, as the library does (S4G_NAN_DETECTED); the
+    NaN must not pass the convergence test."""
+    m = sg.box_mesh(8, 8, 8, 1.0, 1.0, 1.0, 0.2, 5)
+    t = np.tile(np.random.default_rng(5).normal(0, 1e5, 3), (int(m["patch_size"][5]), 1))
+    bcs = [(1, None, None)] * 4 + [(0, None, None), (1, t, None)]
+    D, _, _, p = pyoracle.solve(m, bcs, model=2, law=1, use_mu_K=1, mu=1e6, K=1e7,
+                                n_correctors=3000, n_increments=10)
+    assert p["nan_detected"] == 1 and p["converged"] == 0
+    assert p["n_correctors"] < 200
