@@ -363,7 +363,9 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
     else if (relRes < c.altTol) conv = true;
     else if (initResMag < c.altTol) conv = true;
   }
-  st->converged = conv ? 1 : 0;
+  // fmax drops NaN, so a non-finite field can pass the test above: the
+  // NaN flag (set by any block's isfinite check) overrides it
+  st->converged = (conv && !(st->status & kErrNaN)) ? 1 : 0;
   st->nCorrDone += 1;
   st->iCorr = iCorr + 1;
   st->outerContinue = (!conv && iCorr + 1 < c.nCorr) ? 1 : 0;
