@@ -256,3 +256,27 @@ def test_non_finite_field_stops_the_solve():
                                 n_correctors=3000, n_increments=10)
     assert p["nan_detected"] == 1 and p["converged"] == 0
     assert p["n_correctors"] < 200
+
+
+@pytest.mark.parametrize("model", [1, 2])
+def test_rigid_rotation_is_stress_free(model):
+    """Frame indifference, as the reference's rigidRotation tutorials test
+    it: a rigid rotation of 90 degrees about z prescribed on every boundary
+    (fixedDisplacement (R - I) x, ramped over 45 increments) is recovered
+    exactly -- D = (R - I) C, the leastSquares gradient being exact for a
+    linear field -- and the neoHookean stress vanishes, in both total
+    Lagrangian forms (1 incremental, 2 total displacement)."""
+    m = sg.box_mesh(6, 5, 4, 1.0, 0.9, 0.8, 0.2, 3)
+    th = np.radians(90.0)
+    R = np.array([[np.cos(th), -np.sin(th), 0.0], [np.sin(th), np.cos(th), 0.0], [0.0, 0.0, 1.0]])
+    bcs = []
+    for p in range(6):
+        s, n = int(m["patch_start"][p]), int(m["patch_size"][p])
+        bcs.append((0, m["Cf"][s:s + n] @ (R - np.eye(3)).T, None))
+    D, sig, G, p = pyoracle.solve(m, bcs, model=model, law=1, use_mu_K=1, mu=1e6, K=5e6,
+                                  n_correctors=4000, n_increments=45, solution_tol=1e-10,
+                                  alternative_tol=1e-11, ls_boundary_delta=1)
+    assert p["converged"] == 1 and p["nan_detected"] == 0 and p["enforce_linear"] == 0
+    exact = m["C"] @ (R - np.eye(3)).T
+    assert np.abs(D - exact).max() < 1e-7 * np.abs(exact).max()
+    assert np.abs(sig).max() < 1e-6 * 1e6          # below 1e-6 mu
