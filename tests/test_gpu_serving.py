@@ -1,4 +1,4 @@
-"""Serving (s4g_server_*): requests of uneven sizes and both models run at
+"""Serving (s4g_server_*): requests of uneven sizes and two models run at
 the same time on one GPU, and each result is the same alone and in the mix
 (tolerance 1e-12 relative L2; the runs are in fact bit-identical), and the
 same as a direct solve of the same inputs."""
