@@ -40,6 +40,7 @@ struct s4g_foam_case {
   std::vector<int> owner, neighbour;
   std::vector<double> C, V, Cf, Sf;
   std::vector<std::string> patchName, patchType;
+  std::vector<std::vector<std::string>> patchGroups;  // inGroups
   std::vector<int> patchStart, patchSize;
   // D boundary conditions, per patch
   struct Bc {
@@ -499,6 +500,11 @@ void readMesh(s4g_foam_case& m, const std::string& dir) {
         fail(path + ": patch " + name.s + " needs type, nFaces and startFace");
       m.patchName.push_back(name.s);
       m.patchType.push_back(ty->val[0].s);
+      std::vector<std::string> groups;
+      if (const Entry* g = find(d, "inGroups"))
+        for (const Tok& k : g->val)
+          if (k.kind == Tok::Word && !isInteger(k) && k.s.rfind("List<", 0) != 0) groups.push_back(k.s);
+      m.patchGroups.push_back(groups);
       m.patchSize.push_back(toLabel(nf->val[0], path));
       m.patchStart.push_back(toLabel(sf->val[0], path));
     }
@@ -589,10 +595,14 @@ std::vector<double> fieldValues(const Entry& e, int width, int n, const std::str
   return out;
 }
 
-// The patch's entry: an exact name, else a quoted key read as a regular
-// expression (OpenFOAM's "(left|right)" or ".*" keys).
-const Entry* patchEntry(const std::vector<Entry>& bf, const std::string& name) {
+// The patch's entry, in OpenFOAM's order: its name, then one of its groups
+// (inGroups), then a quoted key read as a regular expression ("(left|right)",
+// ".*"), the last such key first.
+const Entry* patchEntry(const std::vector<Entry>& bf, const std::string& name,
+                        const std::vector<std::string>& groups) {
   if (const Entry* e = find(bf, name)) return e;
+  for (const std::string& g : groups)
+    if (const Entry* e = find(bf, g)) return e;
   for (auto it = bf.rbegin(); it != bf.rend(); ++it) {
     if (!it->quoted) continue;
     try {
@@ -613,7 +623,7 @@ void readD(s4g_foam_case& m, const std::string& path) {
   for (size_t p = 0; p < m.patchName.size(); ++p) {
     const std::string& name = m.patchName[p];
     const std::string where = path + ": patch " + name;
-    const Entry* e = patchEntry(bf->sub, name);
+    const Entry* e = patchEntry(bf->sub, name, m.patchGroups[p]);
     if (!e || !e->isDict) fail(where + " has no entry in boundaryField");
     const Entry* ty = find(e->sub, "type");
     if (!ty || ty->val.size() != 1) fail(where + " has no type");

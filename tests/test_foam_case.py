@@ -201,3 +201,23 @@ def test_bad_arguments_are_errors_not_crashes(tmp_path):
                                  m["face_points"].ctypes.data, 0, m["owner"].ctypes.data, None,
                                  6, names, m["patch_start"].ctypes.data,
                                  m["patch_size"].ctypes.data) == _lib.BAD_ARG
+
+
+def test_d_entries_by_group_and_regex(tmp_path):
+    """OpenFOAM's lookup order: a patch's own name, then its groups
+    (inGroups in the boundary file), then quoted regular-expression keys."""
+    import shutil
+    shutil.copytree(os.path.join(PRISMS, "constant"), tmp_path / "constant")
+    (tmp_path / "0").mkdir()
+    (tmp_path / "0" / "D").write_text(HEADER + """
+boundaryField
+{
+    ".*"  { type solidTraction; traction uniform (0 0 0); pressure uniform 0; }
+    wall  { type fixedDisplacement; value uniform (0 0 1e-3); }
+    top   { type solidTraction; traction uniform (1 2 3); pressure uniform 4; }
+}
+""")
+    _, bcs = read_case(str(tmp_path))
+    assert bcs["bottom"][0] == "fixedDisplacement" and np.all(bcs["bottom"][1] == [0, 0, 1e-3])
+    assert bcs["top"][0] == "solidTraction" and np.all(bcs["top"][1] == [1, 2, 3])
+    assert bcs["sides"][0] == "solidTraction" and np.all(bcs["sides"][2] == 0)
