@@ -13,6 +13,11 @@ oracle_small.npz -- outputs of the CPU oracle on two small seeded cases
   of the oracle and a fixture the GPU tests compare against without running
   the oracle.
 
+foam_prisms/ -- not written by this script: a hand-written OpenFOAM case
+  (ASCII polyMesh of a unit cube split along x = y into two triangular
+  prisms, faces as a faceCompactList, and a 0/D boundaryField) whose
+  volumes, centroids and area vectors are known exactly.
+
 Run from the repository root:  python tests/golden/make_golden.py
 """
 from __future__ import annotations
