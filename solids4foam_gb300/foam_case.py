@@ -105,65 +105,104 @@ def write_box_case(polymesh_dir: str, mesh):
                    mesh["patch_start"], mesh["patch_size"])
 
 
+def polymesh_from_cells(points, cells, patch_of, patch_names):
+    """An OpenFOAM polyMesh from cells given as lists of faces (point-id
+    lists, any orientation): shared faces become internal faces (owner the
+    lower cell, sorted by owner then neighbour), each face oriented out of
+    its owner (by its area vector against the cell's point average; convex
+    cells); every other face goes to patch patch_of(face centre).  Returns
+    the arguments of write_polymesh."""
+    points = np.asarray(points, np.float64)
+    faces = {}  # sorted point ids -> [(cell, ids oriented out of that cell)]
+    for cell, cell_faces in enumerate(cells):
+        cc = points[sorted({i for f in cell_faces for i in f})].mean(axis=0)
+        for f in cell_faces:
+            q = points[f]
+            area = 0.5 * sum(np.cross(q[e] - q[0], q[e + 1] - q[0]) for e in range(1, len(f) - 1))
+            if np.dot(area, q.mean(axis=0) - cc) < 0:
+                f = f[::-1]
+            faces.setdefault(tuple(sorted(f)), []).append((cell, list(f)))
+    internal, boundary = [], [[] for _ in patch_names]
+    for users in faces.values():
+        if len(users) == 2:
+            (a, fa), (b, _) = sorted(users, key=lambda u: u[0])
+            internal.append((a, b, fa))
+        elif len(users) == 1:
+            (a, fa), = users
+            boundary[patch_of(points[fa].mean(axis=0))].append((a, fa))
+        else:
+            raise RuntimeError("a face shared by more than two cells")
+    internal.sort(key=lambda t: (t[0], t[1]))
+    for b in boundary:
+        b.sort(key=lambda t: t[0])
+    owner = [a for a, _, _ in internal] + [a for b in boundary for a, _ in b]
+    flist = [f for _, _, f in internal] + [f for b in boundary for _, f in b]
+    sizes = [len(b) for b in boundary]
+    return dict(points=points,
+                face_start=np.cumsum([0] + [len(f) for f in flist]).astype(np.int32),
+                face_points=np.concatenate([np.asarray(f) for f in flist]).astype(np.int32),
+                owner=np.asarray(owner, np.int32),
+                neighbour=np.asarray([b for _, b, _ in internal], np.int32),
+                patch_names=list(patch_names),
+                patch_start=np.asarray(np.cumsum([len(internal)] + sizes[:-1]), np.int32),
+                patch_size=np.asarray(sizes, np.int32))
+
+
+def _box_patch(lx, ly, lz):
+    def patch_of(c):
+        for p, (axis, val) in enumerate(((0, 0.0), (0, lx), (1, 0.0), (1, ly), (2, 0.0), (2, lz))):
+            if abs(c[axis] - val) < 1e-12 * max(lx, ly, lz):
+                return p
+        raise RuntimeError("boundary face off the box")
+    return patch_of
+
+
 def prism_box_polymesh(nx, ny, nz, lx=1.0, ly=1.0, lz=1.0):
     """An nx x ny x nz box whose hexahedra are each split along their x = y
-    diagonal into two triangular prisms (cells 2h and 2h+1 of hex h), in
-    OpenFOAM polyMesh order: internal faces sorted by (owner, neighbour),
-    then the patches xmin, xmax, ymin, ymax, zmin, zmax.  Returns points,
-    face_start, face_points, owner, neighbour, patch_names, patch_start,
-    patch_size -- the arguments of write_polymesh."""
+    diagonal into two triangular prisms (cells 2h and 2h+1 of hex h), with
+    the patches xmin, xmax, ymin, ymax, zmin, zmax.  Returns the arguments
+    of write_polymesh."""
     px, py = nx + 1, ny + 1
     pid = lambda i, j, k: i + px * (j + py * k)
     g = np.meshgrid(np.arange(px) * (lx / nx), np.arange(py) * (ly / ny),
                     np.arange(nz + 1) * (lz / nz), indexing="ij")
     points = np.stack([a.transpose(2, 1, 0).reshape(-1) for a in g], axis=1)
-    faces = {}  # sorted point ids -> [(cell, ids oriented out of that cell)]
+    cells = []
     for k in range(nz):
         for j in range(ny):
             for i in range(nx):
-                h = i + nx * (j + ny * k)
-                for s, tri in enumerate((((i, j), (i + 1, j), (i + 1, j + 1)),
-                                         ((i, j), (i + 1, j + 1), (i, j + 1)))):
-                    cell = 2 * h + s
+                for tri in (((i, j), (i + 1, j), (i + 1, j + 1)), ((i, j), (i + 1, j + 1), (i, j + 1))):
                     lo = [pid(a, b, k) for a, b in tri]
                     hi = [pid(a, b, k + 1) for a, b in tri]
-                    cell_faces = [lo, hi] + [[lo[e], lo[(e + 1) % 3], hi[(e + 1) % 3], hi[e]]
-                                             for e in range(3)]
-                    cc = points[lo + hi].mean(axis=0)
-                    for f in cell_faces:
-                        q = points[f]
-                        area = 0.5 * sum(np.cross(q[e] - q[0], q[e + 1] - q[0])
-                                         for e in range(1, len(f) - 1))
-                        if np.dot(area, q.mean(axis=0) - cc) < 0:
-                            f = f[::-1]
-                        faces.setdefault(tuple(sorted(f)), []).append((cell, f))
-    internal, boundary = [], [[] for _ in range(6)]
-    tol = 1e-12
-    for users in faces.values():
-        if len(users) == 2:
-            (a, fa), (b, _) = sorted(users)
-            internal.append((a, b, fa))
-        else:
-            (a, fa), = users
-            c = points[fa].mean(axis=0)
-            for p, (axis, val) in enumerate(((0, 0.0), (0, lx), (1, 0.0), (1, ly),
-                                             (2, 0.0), (2, lz))):
-                if abs(c[axis] - val) < tol * max(lx, ly, lz):
-                    boundary[p].append((a, fa))
-                    break
-            else:
-                raise RuntimeError("boundary face off the box")
-    internal.sort(key=lambda t: (t[0], t[1]))
-    for b in boundary:
-        b.sort(key=lambda t: t[0])
-    owner = [a for a, _, _ in internal] + [a for b in boundary for a, _ in b]
-    neighbour = [b for _, b, _ in internal]
-    flist = [f for _, _, f in internal] + [f for b in boundary for _, f in b]
-    face_start = np.cumsum([0] + [len(f) for f in flist]).astype(np.int32)
-    sizes = [len(b) for b in boundary]
-    starts = list(np.cumsum([len(internal)] + sizes[:-1]))
-    return dict(points=points, face_start=face_start,
-                face_points=np.concatenate([np.asarray(f) for f in flist]).astype(np.int32),
-                owner=np.asarray(owner, np.int32), neighbour=np.asarray(neighbour, np.int32),
-                patch_names=["xmin", "xmax", "ymin", "ymax", "zmin", "zmax"],
-                patch_start=np.asarray(starts, np.int32), patch_size=np.asarray(sizes, np.int32))
+                    cells.append([lo, hi] + [[lo[e], lo[(e + 1) % 3], hi[(e + 1) % 3], hi[e]]
+                                             for e in range(3)])
+    return polymesh_from_cells(points, cells, _box_patch(lx, ly, lz),
+                               ["xmin", "xmax", "ymin", "ymax", "zmin", "zmax"])
+
+
+def annulus_polymesh(nr, nt, nz, a, b, h):
+    """A thick-walled cylinder a <= r <= b, 0 <= z <= h, of nr x nt x nz
+    hexahedra (radial, circumferential, axial), closed around the axis, with
+    the patches inner, outer, front (z = 0), back (z = h).  Returns the
+    arguments of write_polymesh."""
+    r = np.linspace(a, b, nr + 1)
+    t = np.linspace(0.0, 2.0 * np.pi, nt + 1)[:-1]
+    z = np.linspace(0.0, h, nz + 1)
+    pid = lambda i, j, k: i + (nr + 1) * ((j % nt) + nt * k)
+    points = np.array([[ri * np.cos(tj), ri * np.sin(tj), zk] for zk in z for tj in t for ri in r])
+    cells = []
+    for k in range(nz):
+        for j in range(nt):
+            for i in range(nr):
+                v = [pid(i, j, k), pid(i + 1, j, k), pid(i + 1, j + 1, k), pid(i, j + 1, k)]
+                w = [pid(i, j, k + 1), pid(i + 1, j, k + 1), pid(i + 1, j + 1, k + 1), pid(i, j + 1, k + 1)]
+                cells.append([v, w] + [[v[e], v[(e + 1) % 4], w[(e + 1) % 4], w[e]] for e in range(4)])
+
+    def patch_of(c):
+        rc = np.hypot(c[0], c[1])
+        if abs(c[2]) < 1e-12 * h:
+            return 2
+        if abs(c[2] - h) < 1e-12 * h:
+            return 3
+        return 0 if rc < 0.5 * (a + b) else 1
+    return polymesh_from_cells(points, cells, patch_of, ["inner", "outer", "front", "back"])

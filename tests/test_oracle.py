@@ -280,3 +280,36 @@ def test_rigid_rotation_is_stress_free(model):
     exact = m["C"] @ (R - np.eye(3)).T
     assert np.abs(D - exact).max() < 1e-7 * np.abs(exact).max()
     assert np.abs(sig).max() < 1e-6 * 1e6          # below 1e-6 mu
+
+
+def test_lame_cylinder_converges_at_second_order(tmp_path):
+    """Thick-walled cylinder under internal pressure (the reference's
+    pressurisedCylinder problem; Lame solution in plane strain) on curved
+    annulus meshes written and read back as polyMesh: inner wall loaded by
+    the pressure, outer wall and end faces given the exact displacement, so
+    that the plane-strain field solves the 3-D problem.  The cell
+    displacement converges to it at second order."""
+    from solids4foam_gb300.foam_case import annulus_polymesh, read_case, write_polymesh
+    a, b, h, E, nu, p = 0.5, 1.0, 0.1, 200e9, 0.3, 1e6
+
+    def u_exact(X):
+        r = np.hypot(X[:, 0], X[:, 1])
+        ur = p * a ** 2 * (1 + nu) * ((1 - 2 * nu) * r + b ** 2 / r) / (E * (b ** 2 - a ** 2))
+        return np.stack([ur * X[:, 0] / r, ur * X[:, 1] / r, 0 * r], axis=1)
+
+    err = []
+    for nr, nt in ((8, 64), (16, 128), (32, 256)):
+        case = tmp_path / f"c{nr}"
+        write_polymesh(str(case / "constant" / "polyMesh"), **annulus_polymesh(nr, nt, 1, a, b, h))
+        m, _ = read_case(str(case), d_file=None)
+        bcs = []
+        for k in range(4):
+            s, n = int(m["patch_start"][k]), int(m["patch_size"][k])
+            bcs.append((1, None, np.full(n, p)) if k == 0 else (0, u_exact(m["Cf"][s:s + n]), None))
+        D, sig, _, pf = pyoracle.solve(m, bcs, E=E, nu=nu, n_correctors=20000,
+                                       solution_tol=1e-10, alternative_tol=1e-11)
+        assert pf["converged"] == 1
+        ue = u_exact(m["C"])
+        err.append(np.linalg.norm(D - ue) / np.linalg.norm(ue))
+    assert err[2] < 5e-5
+    assert np.log2(err[1] / err[2]) > 1.8
