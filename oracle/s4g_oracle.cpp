@@ -477,7 +477,6 @@ struct Solver {
 
   // fields (cells + boundary faces)
   std::vector<V3> U, Ub;         // the solved field: D (linear) or DD (TL)
-  std::vector<V3> U0b;           // unused placeholder for symmetry
   std::vector<T9> G, Gb;         // grad of the solved field
   std::vector<S6> sig, sigb;
   std::vector<V3> g;             // traction snGrad per boundary face
