@@ -221,3 +221,29 @@ boundaryField
     assert bcs["bottom"][0] == "fixedDisplacement" and np.all(bcs["bottom"][1] == [0, 0, 1e-3])
     assert bcs["top"][0] == "solidTraction" and np.all(bcs["top"][1] == [1, 2, 3])
     assert bcs["sides"][0] == "solidTraction" and np.all(bcs["sides"][2] == 0)
+
+
+@pytest.mark.parametrize("kind", ["prisms", "annulus"])
+def test_planning_general_meshes(tmp_path, kind):
+    """Host-side mesh planning (renumbering, parts, DIC levels) of meshes
+    that are not boxes: every renumbering gives a permutation, and the
+    processor-local parts cover the cells."""
+    import ctypes as ct
+    from solids4foam_gb300.foam_case import annulus_polymesh, prism_box_polymesh, write_polymesh
+    from solids4foam_gb300.solid_model import RENUMBER, _desc
+    pm = (prism_box_polymesh(6, 5, 4, 1.0, 0.9, 0.8) if kind == "prisms"
+          else annulus_polymesh(6, 48, 3, 0.5, 1.0, 0.3))
+    write_polymesh(str(tmp_path / "constant" / "polyMesh"), **pm)
+    m, _ = read_case(str(tmp_path), d_file=None)
+    n = len(m["V"])
+    for code in RENUMBER.values():
+        for sub in (0, 1):
+            keep = []
+            d = _desc(m, keep)
+            info = _lib.MeshInfo()
+            perm = np.full(n, -1, np.int32)
+            st = _lib.lib().s4g_mesh_plan(ct.byref(d), ct.byref(_lib.MeshOpts(code, 64, 0, sub, 0)),
+                                          perm.ctypes.data, ct.byref(info))
+            assert st == _lib.OK, _lib.lib().s4g_last_error()
+            assert np.array_equal(np.sort(perm), np.arange(n))
+            assert info.n_cells == n and info.n_parts >= n // 64 and info.n_levels_global >= 1
