@@ -796,7 +796,7 @@ struct Solver {
         correctStress();
       } else {
         // incremental: D = D.oldTime + DD, gradD = gradD.oldTime + gradDD;
-        // total (nonLinGeomTotalLagTotalDispSolid.C:214-230): D and gradD
+        // total (nonLinGeomTotalLagTotalDispSolid.C:224-239): D and gradD
         // are the solved field and its gradient
         for (int c = 0; c < m.nC; ++c) D[c] = incr ? D0[c] + U[c] : U[c];
         for (int b = 0; b < m.nB; ++b) Db[b] = incr ? D0b[b] + Ub[b] : Ub[b];
