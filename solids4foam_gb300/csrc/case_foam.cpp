@@ -6,8 +6,8 @@
 // of constant/polyMesh) and for primitiveMesh's geometry, so that a caller
 // without OpenFOAM can hand a meshed case to s4g_mesh_upload.  Of the D
 // file it reads the two patch types the solve path builds:
-//   fixedDisplacement  value                       (fixedDisplacementFvPatchVectorField.C:63-110)
-//   solidTraction      traction, pressure,         (solidTractionFvPatchVectorField.C:60-125)
+//   fixedDisplacement  value                       (fixedDisplacementFvPatchVectorField.C:156-186)
+//   solidTraction      traction, pressure,         (solidTractionFvPatchVectorField.C:58-209)
 //                      relaxationFactor
 // and rejects everything else by name.
 //
@@ -632,8 +632,10 @@ void readD(s4g_foam_case& m, const std::string& path) {
     s4g_foam_case::Bc& bc = bcs[p];
     bc.set = true;
     if (type == "fixedDisplacement") {
-      for (const char* series : {"displacementSeries", "constantDisplacement"})
-        if (find(e->sub, series)) fail(where + ": " + series + " is not built");
+      if (find(e->sub, "displacementSeries")) fail(where + ": displacementSeries is not built");
+      if (const Entry* s = find(e->sub, "nonOrthogonalCorrections"))
+        if (!s->val.empty() && (s->val[0].s == "false" || s->val[0].s == "no" || s->val[0].s == "off"))
+          fail(where + ": nonOrthogonalCorrections false is not built");
       bc.type = S4G_FIXED_DISPLACEMENT;
       const Entry* v = find(e->sub, "value");
       bc.vec3 = v ? fieldValues(*v, 3, n, where) : std::vector<double>(3 * (size_t)n, 0.0);
