@@ -488,10 +488,12 @@ s4g_status s4g_foam_mesh_points(const s4g_foam_case* fc, const double** points,
  * NULL for an index out of range. */
 const char* s4g_foam_patch_name(const s4g_foam_case* fc, int patch);
 const char* s4g_foam_patch_type(const s4g_foam_case* fc, int patch);
-/* Reads the boundaryField of a D file: per patch fixedDisplacement (value)
- * or solidTraction (traction, pressure, relaxationFactor), uniform or
- * nonuniform.  Another type, a time series, a missing patch or a
- * malformed entry is S4G_BAD_ARG, named in s4g_last_error. */
+/* Reads the boundaryField of a D file: per patch fixedDisplacement (value,
+ * or displacementSeries) or solidTraction (traction or tractionSeries,
+ * pressure or pressureSeries, relaxationFactor), uniform or nonuniform;
+ * series as s4g_foam_load_ramp describes.  Another type, a *Field input, a
+ * missing patch or a malformed entry is S4G_BAD_ARG, named in
+ * s4g_last_error. */
 s4g_status s4g_foam_read_d(s4g_foam_case* fc, const char* d_file);
 /* The condition read for a patch: type; vec3 [patch_size][3] (value or
  * traction); pressure [patch_size] (NULL for fixedDisplacement);
@@ -499,6 +501,19 @@ s4g_status s4g_foam_read_d(s4g_foam_case* fc, const char* d_file);
 s4g_status s4g_foam_bc(const s4g_foam_case* fc, int patch, s4g_bc_type* type,
                        const double** vec3, const double** pressure,
                        double* relaxation_factor);
+/* Load series read by s4g_foam_read_d: tractionSeries, pressureSeries and
+ * displacementSeries are accepted when they are linear ramps from zero at
+ * time 0 (any other table is S4G_BAD_ARG).  Such a series is what the load
+ * increments of s4g_solve apply (load factor n/N over n_increments), and
+ * s4g_foam_bc returns its end value.  end_time: the ramps' common end time,
+ * 0 if the case has none; constant_loads: 1 if a constant nonzero load sits
+ * beside them (the increments would ramp it as well). */
+s4g_status s4g_foam_load_ramp(const s4g_foam_case* fc, double* end_time, int* constant_loads);
+/* startTime (default 0), endTime and deltaT of a system/controlDict: the
+ * time steps the reference's loop takes, which a caller maps to load
+ * increments, (endTime - startTime) / deltaT. */
+s4g_status s4g_foam_read_time(const char* control_dict, double* start_time, double* end_time,
+                              double* delta_t);
 /* s4g_bc_set and s4g_bc_set_relaxation on every patch of an uploaded mesh
  * (uploaded from this case's s4g_mesh_desc). */
 s4g_status s4g_foam_apply_bcs(const s4g_foam_case* fc, s4g_mesh* mesh);

@@ -22,6 +22,7 @@
 
 #include <algorithm>
 #include <cerrno>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -50,6 +51,9 @@ struct s4g_foam_case {
     double relax = 1.0;
   };
   std::vector<Bc> bcs;
+  // load series read from the D file (linear ramps from zero)
+  double rampEnd = 0;              // their common end time; 0: none
+  bool constantBesideRamp = false; // a constant nonzero load beside them
 };
 
 namespace {
@@ -613,13 +617,111 @@ const Entry* patchEntry(const std::vector<Entry>& bf, const std::string& name,
   return nullptr;
 }
 
+// A dictionary entry by name, else by a quoted key whose regular expression
+// matches the name (OpenFOAM's "fileName|file").
+const Entry* lookup(const std::vector<Entry>& d, const std::string& name) {
+  if (const Entry* e = find(d, name)) return e;
+  for (auto it = d.rbegin(); it != d.rend(); ++it) {
+    if (!it->quoted) continue;
+    try {
+      if (std::regex_match(name, std::regex(it->key))) return &*it;
+    } catch (const std::regex_error&) {
+    }
+  }
+  return nullptr;
+}
+
+std::string expandCase(std::string s, const std::string& caseDir) {
+  for (const char* var : {"${FOAM_CASE}", "$FOAM_CASE"}) {
+    size_t at;
+    while ((at = s.find(var)) != std::string::npos) s.replace(at, std::strlen(var), caseDir);
+  }
+  return s;
+}
+
+struct Ramp {
+  double end = 0;
+  std::vector<double> value;  // the value at the end, width 1 or 3
+};
+
+// A time series (interpolationTable, read from its file as a list of
+// (time value) pairs) that is a linear ramp from zero: value(0) = 0 and
+// every point on the line to the last one.  Such a series is what the
+// load increments apply (load factor n/N); any other is rejected.
+Ramp readRamp(const Entry& series, int width, const std::string& caseDir, const std::string& where) {
+  if (!series.isDict) fail(where + ": " + series.key + " must be a dictionary");
+  const Entry* f = lookup(series.sub, "file");
+  if (!f) f = lookup(series.sub, "fileName");
+  if (!f || f->val.size() != 1) fail(where + ": " + series.key + " has no file");
+  if (const Entry* is = lookup(series.sub, "interpolationScheme"))
+    if (!is->val.empty() && is->val[0].s != "linear")
+      fail(where + ": " + series.key + ": interpolationScheme " + is->val[0].s + " is not built");
+  const std::string file = expandCase(f->val[0].s, caseDir);
+  std::vector<Tok> t = payload(file);
+  Cursor c{t, 0, file};
+  std::vector<double> times, vals;
+  parseList(c, [&](Cursor& cc) {
+    cc.expect('(');
+    times.push_back(toDouble(cc.next(), cc.where));
+    if (width == 3) {
+      P3 v = parseVector(cc);
+      vals.push_back(v.x); vals.push_back(v.y); vals.push_back(v.z);
+    } else {
+      vals.push_back(toDouble(cc.next(), cc.where));
+    }
+    cc.expect(')');
+  });
+  const size_t n = times.size();
+  if (n < 2) fail(file + ": a series needs at least two points");
+  Ramp r;
+  r.end = times[n - 1];
+  r.value.assign(vals.end() - width, vals.end());
+  double scale = 0;
+  for (double v : r.value) scale = std::max(scale, std::fabs(v));
+  for (size_t i = 0; i < n; ++i) {
+    if (i > 0 && !(times[i] > times[i - 1])) fail(file + ": times must increase");
+    for (int k = 0; k < width; ++k) {
+      const double expect = r.value[(size_t)k] * (times[i] / r.end);
+      if (std::fabs(vals[i * width + k] - expect) > 1e-12 * scale + (i == 0 ? 0.0 : 1e-300))
+        fail(where + ": " + series.key + " (" + file +
+             ") is not a linear ramp from zero at time 0; only such series are built");
+    }
+  }
+  if (times[0] != 0.0) fail(where + ": " + series.key + " must start at time 0");
+  return r;
+}
+
 void readD(s4g_foam_case& m, const std::string& path) {
   std::vector<Tok> t = payload(path);
   Cursor c{t, 0, path};
   std::vector<Entry> d = parseDict(c, false);
   const Entry* bf = find(d, "boundaryField");
   if (!bf || !bf->isDict) fail(path + ": no boundaryField dictionary");
+  // the case directory holds 0/D
+  std::string caseDir = path;
+  for (int up = 0; up < 2; ++up) {
+    size_t at = caseDir.find_last_of('/');
+    caseDir = at == std::string::npos ? std::string(".") : caseDir.substr(0, at);
+  }
   std::vector<s4g_foam_case::Bc> bcs(m.patchName.size());
+  double rampEnd = 0;
+  bool anyRamp = false, anyConstantLoad = false;
+  auto ramped = [&](const Ramp& r, const std::string& where) {
+    if (anyRamp && r.end != rampEnd) fail(where + ": load series end at different times");
+    anyRamp = true;
+    rampEnd = r.end;
+  };
+  auto nonzero = [](const std::vector<double>& v) {
+    for (double x : v)
+      if (x != 0.0) return true;
+    return false;
+  };
+  auto isOff = [](const Entry* s) {
+    return s && !s->val.empty() && (s->val[0].s == "false" || s->val[0].s == "no" || s->val[0].s == "off");
+  };
+  auto isOn = [](const Entry* s) {
+    return s && !s->val.empty() && (s->val[0].s == "true" || s->val[0].s == "yes" || s->val[0].s == "on");
+  };
   for (size_t p = 0; p < m.patchName.size(); ++p) {
     const std::string& name = m.patchName[p];
     const std::string where = path + ": patch " + name;
@@ -631,29 +733,48 @@ void readD(s4g_foam_case& m, const std::string& path) {
     const int n = m.patchSize[p];
     s4g_foam_case::Bc& bc = bcs[p];
     bc.set = true;
+    auto tile = [n](const std::vector<double>& v) {
+      std::vector<double> out;
+      for (int i = 0; i < n; ++i) out.insert(out.end(), v.begin(), v.end());
+      return out;
+    };
+    if (isOff(find(e->sub, "nonOrthogonalCorrections")))
+      fail(where + ": nonOrthogonalCorrections false is not built");
     if (type == "fixedDisplacement") {
-      if (find(e->sub, "displacementSeries")) fail(where + ": displacementSeries is not built");
-      if (const Entry* s = find(e->sub, "nonOrthogonalCorrections"))
-        if (!s->val.empty() && (s->val[0].s == "false" || s->val[0].s == "no" || s->val[0].s == "off"))
-          fail(where + ": nonOrthogonalCorrections false is not built");
       bc.type = S4G_FIXED_DISPLACEMENT;
-      const Entry* v = find(e->sub, "value");
-      bc.vec3 = v ? fieldValues(*v, 3, n, where) : std::vector<double>(3 * (size_t)n, 0.0);
+      if (const Entry* ds = find(e->sub, "displacementSeries")) {
+        Ramp r = readRamp(*ds, 3, caseDir, where);
+        ramped(r, where);
+        bc.vec3 = tile(r.value);
+      } else {
+        const Entry* v = find(e->sub, "value");
+        bc.vec3 = v ? fieldValues(*v, 3, n, where) : std::vector<double>(3 * (size_t)n, 0.0);
+        anyConstantLoad = anyConstantLoad || nonzero(bc.vec3);
+      }
     } else if (type == "solidTraction") {
-      for (const char* series : {"tractionSeries", "pressureSeries", "tractionField", "pressureField"})
-        if (find(e->sub, series)) fail(where + ": " + series + " is not built");
-      if (const Entry* s = find(e->sub, "setEffectiveTraction"))
-        if (!s->val.empty() && (s->val[0].s == "true" || s->val[0].s == "yes" || s->val[0].s == "on"))
-          fail(where + ": setEffectiveTraction is not built");
-      if (const Entry* s = find(e->sub, "nonOrthogonalCorrections"))
-        if (!s->val.empty() && (s->val[0].s == "false" || s->val[0].s == "no" || s->val[0].s == "off"))
-          fail(where + ": nonOrthogonalCorrections false is not built");
       bc.type = S4G_SOLID_TRACTION;
-      const Entry* tr = find(e->sub, "traction");
-      const Entry* pr = find(e->sub, "pressure");
-      if (!tr || !pr) fail(where + ": solidTraction needs traction and pressure");
-      bc.vec3 = fieldValues(*tr, 3, n, where);
-      bc.pressure = fieldValues(*pr, 1, n, where);
+      if (isOn(find(e->sub, "setEffectiveTraction"))) fail(where + ": setEffectiveTraction is not built");
+      // exactly one of each (solidTractionFvPatchVectorField.C:105-193)
+      for (const char* q : {"traction", "pressure"}) {
+        const std::string k(q);
+        const Entry* plain = find(e->sub, k);
+        const Entry* series = find(e->sub, k + "Series");
+        const Entry* field = find(e->sub, k + "Field");
+        if ((plain != nullptr) + (series != nullptr) + (field != nullptr) > 1)
+          fail(where + ": only one of " + k + ", " + k + "Series or " + k + "Field can be specified");
+        if (field) fail(where + ": " + k + "Field is not built");
+        std::vector<double>& out = k == "traction" ? bc.vec3 : bc.pressure;
+        const int width = k == "traction" ? 3 : 1;
+        if (series) {
+          Ramp r = readRamp(*series, width, caseDir, where);
+          ramped(r, where);
+          out = tile(r.value);
+        } else {
+          if (!plain) fail(where + ": solidTraction needs " + k);
+          out = fieldValues(*plain, width, n, where);
+          anyConstantLoad = anyConstantLoad || nonzero(out);
+        }
+      }
       if (const Entry* rf = find(e->sub, "relaxationFactor")) {
         if (rf->val.size() != 1) fail(where + ": bad relaxationFactor");
         bc.relax = toDouble(rf->val[0], where);
@@ -664,6 +785,8 @@ void readD(s4g_foam_case& m, const std::string& path) {
     }
   }
   m.bcs = std::move(bcs);
+  m.rampEnd = anyRamp ? rampEnd : 0.0;
+  m.constantBesideRamp = anyRamp && anyConstantLoad;
 }
 
 // ------------------------------------------------------------- writer ---
@@ -791,6 +914,38 @@ s4g_status s4g_foam_apply_bcs(const s4g_foam_case* m, s4g_mesh* mesh) {
       if (st != S4G_OK) return st;
     }
   }
+  return S4G_OK;
+}
+
+s4g_status s4g_foam_read_time(const char* control_dict, double* start_time, double* end_time,
+                              double* delta_t) {
+  if (!control_dict) return S4G_BAD_ARG;
+  return guarded([&] {
+    std::vector<Tok> t = payload(control_dict);
+    Cursor c{t, 0, control_dict};
+    std::vector<Entry> d = parseDict(c, false);
+    auto num = [&](const char* key, double dflt, bool required) {
+      const Entry* e = find(d, key);
+      if (!e) {
+        if (required) fail(std::string(control_dict) + ": no " + key);
+        return dflt;
+      }
+      if (e->val.size() != 1) fail(std::string(control_dict) + ": bad " + key);
+      return toDouble(e->val[0], control_dict);
+    };
+    const double t0 = num("startTime", 0.0, false), t1 = num("endTime", 0.0, true),
+                 dt = num("deltaT", 0.0, true);
+    if (!(dt > 0) || !(t1 > t0)) fail(std::string(control_dict) + ": need endTime > startTime and deltaT > 0");
+    if (start_time) *start_time = t0;
+    if (end_time) *end_time = t1;
+    if (delta_t) *delta_t = dt;
+  });
+}
+
+s4g_status s4g_foam_load_ramp(const s4g_foam_case* m, double* end_time, int* constant_loads) {
+  if (!m) return S4G_BAD_ARG;
+  if (end_time) *end_time = m->rampEnd;
+  if (constant_loads) *constant_loads = m->constantBesideRamp ? 1 : 0;
   return S4G_OK;
 }
 

@@ -2,6 +2,7 @@
 // OpenFOAM case directory what the OpenFOAM-side solid-model class does
 // inside solids4Foam, through the same C ABI and without OpenFOAM:
 //   read constant/polyMesh and 0/D            s4g_foam_read_mesh, s4g_foam_read_d
+//   load series -> increments                 s4g_foam_load_ramp, s4g_foam_read_time
 //   upload the mesh, set law, BCs, controls   s4g_mesh_upload, s4g_material_set,
 //                                             s4g_foam_apply_bcs, s4g_solver_set
 //   evolve()                                  s4g_solve, s4g_get_gradD
@@ -9,9 +10,11 @@
 // and prints one JSON line with the run's figures.  The material, model and
 // controls come from the command line (the reference reads them from
 // constant/mechanicalProperties, constant/solidProperties and
-// system/fvSolution).  --plan-only stops after the host-side mesh planning
-// and needs no GPU.  --write writes pointD as an ASCII pointVectorField into
-// <case>/<time>/pointD.
+// system/fvSolution).  A total Lagrangian case whose loads are series
+// (linear ramps from zero) runs one increment per time step of
+// system/controlDict unless --increments is given.  --plan-only stops after
+// the host-side mesh planning and needs no GPU.  --write writes pointD as an
+// ASCII pointVectorField into <case>/<time>/pointD.
 
 #include "s4g.h"
 
@@ -21,6 +24,7 @@
 #include <cstring>
 #include <string>
 #include <sys/stat.h>
+#include <unistd.h>
 #include <vector>
 
 namespace {
@@ -93,7 +97,7 @@ int main(int argc, char** argv) {
   s4g_mesh_opts mo{S4G_RENUMBER_TILED, 512, 0, 0, 0};
   s4g_precision precision = S4G_FP64;
   int increments = 1, device = 0;
-  bool planOnly = false, muK = false;
+  bool planOnly = false, muK = false, incrementsGiven = false;
   for (int i = 2; i < argc; ++i) {
     const std::string a = argv[i];
     auto val = [&]() -> const char* {
@@ -108,7 +112,7 @@ int main(int argc, char** argv) {
     else if (a == "--nu") law.nu = std::atof(val());
     else if (a == "--mu") { law.mu = std::atof(val()); muK = true; }
     else if (a == "--K") { law.K = std::atof(val()); muK = true; }
-    else if (a == "--increments") increments = std::atoi(val());
+    else if (a == "--increments") { increments = std::atoi(val()); incrementsGiven = true; }
     else if (a == "--precision") {
       const std::string p = val();
       if (p == "FP64") precision = S4G_FP64;
@@ -164,16 +168,42 @@ int main(int argc, char** argv) {
   check(s4g_foam_mesh_desc(fc, &desc, &nPoints), "s4g_foam_mesh_desc");
   s4g_mesh_info info;
   check(s4g_mesh_plan(&desc, &mo, nullptr, &info), "s4g_mesh_plan");
+  // the boundary conditions (optional for --plan-only) and their load ramp
+  const std::string dFile = caseDir + "/0/D";
+  const bool haveD = access(dFile.c_str(), R_OK) == 0;
+  if (!planOnly || haveD) check(s4g_foam_read_d(fc, dFile.c_str()), "reading 0/D");
+  double rampEnd = 0;
+  int constantLoads = 0;
+  if (haveD) check(s4g_foam_load_ramp(fc, &rampEnd, &constantLoads), "s4g_foam_load_ramp");
+  if (model != S4G_LIN_GEOM_TOTAL_DISP && rampEnd > 0) {
+    if (constantLoads) {
+      std::fprintf(stderr, "s4g_solve_case: constant loads beside load series are not built for the "
+                           "total Lagrangian models (the increments would ramp them too)\n");
+      return 2;
+    }
+    double t0 = 0, t1 = 0, dt = 0;
+    if (!incrementsGiven &&
+        s4g_foam_read_time((caseDir + "/system/controlDict").c_str(), &t0, &t1, &dt) == S4G_OK) {
+      increments = (int)std::lround((t1 - t0) / dt);
+      if (std::fabs(t1 - rampEnd) > 1e-9 * rampEnd)
+        std::fprintf(stderr, "s4g_solve_case: warning: endTime %g is not the load series' end %g\n", t1,
+                     rampEnd);
+    }
+  }
+  if (increments < 1) {
+    std::fprintf(stderr, "s4g_solve_case: increments must be >= 1\n");
+    return 1;
+  }
   if (planOnly) {
     std::printf("{\"case\": \"%s\", \"cells\": %d, \"faces\": %d, \"internal_faces\": %d, "
                 "\"points\": %d, \"patches\": %d, \"parts\": %d, \"part_depth\": %d, "
-                "\"levels\": %d}\n",
+                "\"levels\": %d, \"load_ramp_end\": %g, \"increments\": %d}\n",
                 caseDir.c_str(), desc.n_cells, desc.n_faces, desc.n_internal_faces, nPoints,
-                desc.n_patches, info.n_parts, info.part_depth, info.n_levels_global);
+                desc.n_patches, info.n_parts, info.part_depth, info.n_levels_global, rampEnd,
+                model == S4G_LIN_GEOM_TOTAL_DISP ? 1 : increments);
     s4g_foam_free(fc);
     return 0;
   }
-  check(s4g_foam_read_d(fc, (caseDir + "/0/D").c_str()), "reading 0/D");
 
   // the solve
   s4g_ctx_opts co{device, 0, 0, 0};
@@ -215,11 +245,12 @@ int main(int argc, char** argv) {
   for (int p = 0; p < nPoints; ++p)
     maxPD = std::fmax(maxPD, std::sqrt(pointD[3 * p] * pointD[3 * p] + pointD[3 * p + 1] * pointD[3 * p + 1] +
                                        pointD[3 * p + 2] * pointD[3 * p + 2]));
-  std::printf("{\"case\": \"%s\", \"model\": \"%s\", \"cells\": %d, \"status\": \"%s\", "
+  std::printf("{\"case\": \"%s\", \"model\": \"%s\", \"cells\": %d, \"increments\": %d, \"status\": \"%s\", "
               "\"converged\": %d, \"correctors\": %d, \"pcg_iterations\": %lld, "
               "\"solve_ms\": %.3f, \"max_mag_D\": %.9g, \"max_mag_pointD\": %.9g, "
               "\"max_sigmaEq\": %.9g}\n",
-              caseDir.c_str(), modelName.c_str(), n, s4g_status_str(st), perf.converged,
+              caseDir.c_str(), modelName.c_str(), n, model == S4G_LIN_GEOM_TOTAL_DISP ? 1 : increments,
+              s4g_status_str(st), perf.converged,
               perf.n_correctors, perf.total_lin_iters, perf.solve_ms, maxD, maxPD, maxSeq);
   if (!writeTime.empty() &&
       !writePointField(caseDir, writeTime, pointD.data(), nPoints, fc, desc.n_patches)) {

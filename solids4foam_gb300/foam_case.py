@@ -4,7 +4,9 @@ dictionaries SolidModel takes, and write meshes as ASCII polyMesh.
 
 The mesh dictionary has the keys of box_mesh (owner, neighbour, C, V, Cf,
 Sf, patch_start, patch_size, patch_names) plus patch_types, points,
-face_start and face_points.  The boundary conditions are
+face_start and face_points; with a D file also load_ramp_end (the end time
+of its load series, which are linear ramps from zero, or None) and
+constant_loads_beside_ramp.  The boundary conditions are
 {patch name: (type, value or traction [n,3], pressure [n] or None,
 relaxationFactor)}."""
 import ctypes as ct
@@ -65,6 +67,11 @@ def read_case(case_dir: str, d_file: str | None = "0/D", polymesh: str = "consta
                 vec = _arr(v.value, 3 * n, np.float64).reshape(n, 3)
                 press = None if not pr.value else _arr(pr.value, n, np.float64)
                 bcs[name] = (BC_NAMES[t.value], vec, press, rf.value)
+            end, mixed = ct.c_double(), ct.c_int()
+            _lib.check(L.s4g_foam_load_ramp(h, ct.byref(end), ct.byref(mixed)),
+                       "s4g_foam_load_ramp")
+            mesh["load_ramp_end"] = end.value or None
+            mesh["constant_loads_beside_ramp"] = bool(mixed.value)
         return mesh, bcs
     finally:
         L.s4g_foam_free(h)

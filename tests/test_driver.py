@@ -47,3 +47,45 @@ def test_no_device_is_an_error():
         pytest.skip("a GPU is present")
     r = run(PRISMS)
     assert r.returncode == 2 and "NO_DEVICE" in r.stderr
+
+
+def _ramp_case(tmp_path, xmin_traction="0 0 0"):
+    write_box_case(str(tmp_path / "constant" / "polyMesh"), box_polymesh(3, 3, 3))
+    (tmp_path / "constant" / "timeVsTraction").write_text("((0 (0 0 0)) (10 (0 0 -1e5)))")
+    (tmp_path / "system").mkdir()
+    (tmp_path / "system" / "controlDict").write_text(
+        "FoamFile { version 2.0; format ascii; class dictionary; object controlDict; }\n"
+        "application solids4Foam;\nstartTime 0;\nendTime 10;\ndeltaT 0.5;\n")
+    (tmp_path / "0").mkdir()
+    free = "{ type solidTraction; traction uniform (0 0 0); pressure uniform 0; }"
+    (tmp_path / "0" / "D").write_text(
+        "FoamFile { version 2.0; format ascii; class volVectorField; object D; }\n"
+        "boundaryField {\n"
+        f"  xmin {{ type solidTraction; traction uniform ({xmin_traction}); pressure uniform 0; }}\n"
+        f"  xmax {free} ymin {free} ymax {free}\n"
+        "  zmin { type fixedDisplacement; value uniform (0 0 0); }\n"
+        "  zmax { type solidTraction; pressure uniform 0;\n"
+        "         tractionSeries { file \"$FOAM_CASE/constant/timeVsTraction\"; outOfBounds clamp; } }\n"
+        "}\n")
+    return str(tmp_path)
+
+
+def test_load_ramp_sets_the_increments(tmp_path):
+    """A total Lagrangian case whose load is a series ramping from zero runs
+    one increment per time step of its controlDict (10 / 0.5 = 20)."""
+    case = _ramp_case(tmp_path)
+    r = run(case, "--plan-only", "--model", "nonLinearGeometryTotalLagrangian")
+    assert r.returncode == 0, r.stderr
+    out = json.loads(r.stdout)
+    assert out["load_ramp_end"] == 10 and out["increments"] == 20
+    out = json.loads(run(case, "--plan-only", "--model", "nonLinearGeometryTotalLagrangian",
+                         "--increments", "4").stdout)
+    assert out["increments"] == 4
+    out = json.loads(run(case, "--plan-only").stdout)   # linear geometry: one solve
+    assert out["increments"] == 1
+
+
+def test_constant_load_beside_a_ramp_is_refused_for_tl(tmp_path):
+    case = _ramp_case(tmp_path, xmin_traction="1e5 0 0")
+    r = run(case, "--plan-only", "--model", "nonLinearGeometryTotalLagrangianTotalDisplacement")
+    assert r.returncode == 2 and "constant loads beside load series" in r.stderr

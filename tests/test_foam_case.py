@@ -109,7 +109,9 @@ def test_d_errors_name_the_problem(tmp_path):
     _d_error(tmp_path, "boundaryField { " + rest + " }", "zmin has no entry")
     _d_error(tmp_path, "boundaryField { zmin { type solidTraction; traction uniform (0 0 0); "
              "pressure uniform 0; tractionSeries { file \"t\"; } } " + rest + " }",
-             "tractionSeries is not built")
+             "only one of traction, tractionSeries or tractionField")
+    _d_error(tmp_path, "boundaryField { zmin { type solidTraction; tractionField T; "
+             "pressure uniform 0; } " + rest + " }", "tractionField is not built")
     _d_error(tmp_path, "boundaryField { zmin { type fixedDisplacement; value nonuniform "
              "List<vector> 3((0 0 0) (0 0 0) (0 0 0)); } " + rest + " }", "3 values for 4 faces")
 
@@ -247,3 +249,57 @@ def test_planning_general_meshes(tmp_path, kind):
             assert st == _lib.OK, _lib.lib().s4g_last_error()
             assert np.array_equal(np.sort(perm), np.arange(n))
             assert info.n_cells == n and info.n_parts >= n // 64 and info.n_levels_global >= 1
+
+
+def _series_case(tmp_path, zmax, xmin="{ type solidTraction; traction uniform (0 0 0); pressure uniform 0; }"):
+    write_box_case(str(tmp_path / "constant" / "polyMesh"), box_polymesh(2, 2, 2))
+    (tmp_path / "constant" / "timeVsTraction").write_text(
+        "// time (traction)\n(\n    (0 (0 0 0))\n    (4 (-20e6 0 5e6))\n    (10 (-50e6 0 12.5e6))\n)\n")
+    (tmp_path / "constant" / "timeVsPressure").write_text("(\n(0 0)\n(10 3e5)\n)\n")
+    (tmp_path / "constant" / "bent").write_text("((0 (0 0 0)) (5 (1 0 0)) (10 (1 0 0)))")
+    (tmp_path / "0").mkdir(exist_ok=True)
+    free = "{ type solidTraction; traction uniform (0 0 0); pressure uniform 0; }"
+    (tmp_path / "0" / "D").write_text(HEADER + f"""
+boundaryField
+{{
+    xmin {xmin}
+    xmax {free}  ymin {free}  ymax {free}
+    zmin {{ type fixedDisplacement; value uniform (0 0 0); }}
+    zmax {zmax}
+}}
+""")
+    return read_case(str(tmp_path))
+
+
+def test_load_series_that_ramp_from_zero(tmp_path):
+    """tractionSeries / pressureSeries / displacementSeries that are linear
+    ramps from zero (the load-increment ramp) are read as their end value
+    and end time; the file may be named by a regex key and $FOAM_CASE."""
+    m, bcs = _series_case(tmp_path, """{ type solidTraction;
+        tractionSeries { "fileName|file" "$FOAM_CASE/constant/timeVsTraction"; outOfBounds clamp; }
+        pressureSeries { file "${FOAM_CASE}/constant/timeVsPressure"; }
+        value uniform (0 0 0); }""")
+    t, v, p, rf = bcs["zmax"]
+    assert t == "solidTraction" and np.all(v == [-50e6, 0, 12.5e6]) and np.all(p == 3e5)
+    assert m["load_ramp_end"] == 10.0 and not m["constant_loads_beside_ramp"]
+    # a constant load beside a ramp is reported
+    m, bcs = _series_case(tmp_path, """{ type fixedDisplacement;
+        displacementSeries { file "$FOAM_CASE/constant/timeVsTraction"; } value uniform (0 0 0); }""",
+                          xmin="{ type solidTraction; traction uniform (1e5 0 0); pressure uniform 0; }")
+    assert bcs["zmax"][0] == "fixedDisplacement" and np.all(bcs["zmax"][1] == [-50e6, 0, 12.5e6])
+    assert m["load_ramp_end"] == 10.0 and m["constant_loads_beside_ramp"]
+    # no series at all
+    m, _ = read_case(PRISMS)
+    assert m["load_ramp_end"] is None
+
+
+def test_other_load_series_are_rejected(tmp_path):
+    with pytest.raises(_lib.S4GError, match="not a linear ramp from zero"):
+        _series_case(tmp_path, """{ type solidTraction; pressure uniform 0;
+            tractionSeries { file "$FOAM_CASE/constant/bent"; } }""")
+    with pytest.raises(_lib.S4GError, match="interpolationScheme step is not built"):
+        _series_case(tmp_path, """{ type solidTraction; pressure uniform 0;
+            tractionSeries { file "$FOAM_CASE/constant/timeVsTraction"; interpolationScheme step; } }""")
+    with pytest.raises(_lib.S4GError, match="cannot open"):
+        _series_case(tmp_path, """{ type solidTraction; pressure uniform 0;
+            tractionSeries { file "$FOAM_CASE/constant/missing"; } }""")
