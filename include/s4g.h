@@ -514,6 +514,15 @@ s4g_status s4g_foam_load_ramp(const s4g_foam_case* fc, double* end_time, int* co
  * increments, (endTime - startTime) / deltaT. */
 s4g_status s4g_foam_read_time(const char* control_dict, double* start_time, double* end_time,
                               double* delta_t);
+/* relaxationFactors of a system/fvSolution for one field ("D" or "DD"):
+ * field_factor from fields { } (or the older flat form), equation_factor
+ * from equations { }; 1 where none is set.  Field relaxation (the
+ * reference's "fixed" relaxField, D == D.prevIter + f (D - D.prevIter),
+ * solidModel.C:837-841) and equation relaxation (fvMatrix::relax) are not
+ * built on the device path, so a caller refuses a case that sets either
+ * below 1. */
+s4g_status s4g_foam_read_relaxation(const char* fv_solution, const char* field,
+                                    double* field_factor, double* equation_factor);
 /* s4g_bc_set and s4g_bc_set_relaxation on every patch of an uploaded mesh
  * (uploaded from this case's s4g_mesh_desc). */
 s4g_status s4g_foam_apply_bcs(const s4g_foam_case* fc, s4g_mesh* mesh);

@@ -771,6 +771,7 @@ struct Solver {
     if (tl) enforceLinear = false;
     do {
       prev = U;                          // storePrevIter
+      const std::vector<V3> prevB = Ub;  // (the boundary values too)
       updateTraction();                  // fvMatrix construction: updateCoeffs
       buildSource(src);
       double r2 = 0;
@@ -791,6 +792,14 @@ struct Solver {
       }
       initResMag = std::sqrt(r2);
       evaluateBoundary();                // psi.correctBoundaryConditions()
+      // relaxField, "fixed" (solidModel.C:837-841): D.relax() with the field's
+      // relaxation factor, D == D.prevIter + f (D - D.prevIter) on the cells
+      // and, by the forced assignment, on every boundary face
+      const double fr = s.field_relaxation;
+      if (fr > 0 && fr != 1.0) {
+        for (int c = 0; c < m.nC; ++c) U[c] = prev[c] + fr * (U[c] - prev[c]);
+        for (int b = 0; b < m.nB; ++b) Ub[b] = prevB[b] + fr * (Ub[b] - prevB[b]);
+      }
       if (!tl) {
         gradient();
         correctStress();

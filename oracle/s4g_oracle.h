@@ -74,6 +74,10 @@ typedef struct {
                              order): DIC restricted to each subdomain */
   double max_seconds;     /* >0: stop after the corrector that passes this wall
                              time (bounded timing samples) */
+  double field_relaxation; /* fvSolution relaxationFactors { fields { "D|DD" f; } }:
+                             after each solve D == D.prevIter + f (D - D.prevIter),
+                             cells and boundary faces (solidModel.C:837-841,
+                             GeometricField::relax); 0 or 1: none */
 } orc_settings;
 
 typedef struct {

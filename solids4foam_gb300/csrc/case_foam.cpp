@@ -942,6 +942,36 @@ s4g_status s4g_foam_read_time(const char* control_dict, double* start_time, doub
   });
 }
 
+s4g_status s4g_foam_read_relaxation(const char* fv_solution, const char* field,
+                                    double* field_factor, double* equation_factor) {
+  if (!fv_solution || !field) return S4G_BAD_ARG;
+  return guarded([&] {
+    std::vector<Tok> t = payload(fv_solution);
+    Cursor c{t, 0, fv_solution};
+    std::vector<Entry> d = parseDict(c, false);
+    double ff = 1.0, ef = 1.0;
+    auto factor = [&](const Entry* e) {
+      if (!e || e->isDict || e->val.size() != 1) fail(std::string(fv_solution) + ": bad relaxation factor");
+      return toDouble(e->val[0], fv_solution);
+    };
+    if (const Entry* rf = find(d, "relaxationFactors")) {
+      if (!rf->isDict) fail(std::string(fv_solution) + ": relaxationFactors must be a dictionary");
+      const Entry* fields = find(rf->sub, "fields");
+      const Entry* eqns = find(rf->sub, "equations");
+      if (fields || eqns) {
+        if (fields && fields->isDict)
+          if (const Entry* e = lookup(fields->sub, field)) ff = factor(e);
+        if (eqns && eqns->isDict)
+          if (const Entry* e = lookup(eqns->sub, field)) ef = factor(e);
+      } else if (const Entry* e = lookup(rf->sub, field)) {
+        ff = factor(e);  // the older form: field factors directly in relaxationFactors
+      }
+    }
+    if (field_factor) *field_factor = ff;
+    if (equation_factor) *equation_factor = ef;
+  });
+}
+
 s4g_status s4g_foam_load_ramp(const s4g_foam_case* m, double* end_time, int* constant_loads) {
   if (!m) return S4G_BAD_ARG;
   if (end_time) *end_time = m->rampEnd;

@@ -3,6 +3,7 @@
 // inside solids4Foam, through the same C ABI and without OpenFOAM:
 //   read constant/polyMesh and 0/D            s4g_foam_read_mesh, s4g_foam_read_d
 //   load series -> increments                 s4g_foam_load_ramp, s4g_foam_read_time
+//   refuse relaxationFactors below 1          s4g_foam_read_relaxation
 //   upload the mesh, set law, BCs, controls   s4g_mesh_upload, s4g_material_set,
 //                                             s4g_foam_apply_bcs, s4g_solver_set
 //   evolve()                                  s4g_solve, s4g_get_gradD
@@ -193,6 +194,21 @@ int main(int argc, char** argv) {
   if (increments < 1) {
     std::fprintf(stderr, "s4g_solve_case: increments must be >= 1\n");
     return 1;
+  }
+  // field and equation relaxation of the solved field are not built
+  const std::string fvSolution = caseDir + "/system/fvSolution";
+  if (access(fvSolution.c_str(), R_OK) == 0) {
+    const char* solved = model == S4G_NONLIN_GEOM_TOTAL_LAG ? "DD" : "D";
+    double fieldFactor = 1, eqnFactor = 1;
+    check(s4g_foam_read_relaxation(fvSolution.c_str(), solved, &fieldFactor, &eqnFactor),
+          "reading system/fvSolution");
+    if (fieldFactor != 1.0 || eqnFactor != 1.0) {
+      std::fprintf(stderr,
+                   "s4g_solve_case: relaxationFactors for %s (field %g, equation %g) are not built "
+                   "on the GPU path\n",
+                   solved, fieldFactor, eqnFactor);
+      return 2;
+    }
   }
   if (planOnly) {
     std::printf("{\"case\": \"%s\", \"cells\": %d, \"faces\": %d, \"internal_faces\": %d, "

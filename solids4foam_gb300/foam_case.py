@@ -213,3 +213,15 @@ def annulus_polymesh(nr, nt, nz, a, b, h):
             return 3
         return 0 if rc < 0.5 * (a + b) else 1
     return polymesh_from_cells(points, cells, patch_of, ["inner", "outer", "front", "back"])
+
+
+def read_relaxation(case_dir: str, field: str = "D"):
+    """(field factor, equation factor) of system/fvSolution's
+    relaxationFactors for the solved field ("D", or "DD" for the incremental
+    total Lagrangian model); 1.0 where none is set.  Neither is built on the
+    device path: a case that sets one below 1 must be refused."""
+    ff, ef = ct.c_double(), ct.c_double()
+    _lib.check(_lib.lib().s4g_foam_read_relaxation(
+        os.path.join(case_dir, "system", "fvSolution").encode(), field.encode(), ct.byref(ff),
+        ct.byref(ef)), "s4g_foam_read_relaxation")
+    return ff.value, ef.value

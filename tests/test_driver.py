@@ -89,3 +89,22 @@ def test_constant_load_beside_a_ramp_is_refused_for_tl(tmp_path):
     case = _ramp_case(tmp_path, xmin_traction="1e5 0 0")
     r = run(case, "--plan-only", "--model", "nonLinearGeometryTotalLagrangianTotalDisplacement")
     assert r.returncode == 2 and "constant loads beside load series" in r.stderr
+
+
+def test_relaxation_factors_are_refused(tmp_path):
+    """relaxationFactors of the solved field are not built on the device
+    path: a case that sets them is refused by name, in either fvSolution
+    form, and a factor for another field is ignored."""
+    case = _ramp_case(tmp_path)
+    fvs = tmp_path / "system" / "fvSolution"
+    head = "FoamFile { version 2.0; format ascii; class dictionary; object fvSolution; }\n"
+    fvs.write_text(head + 'relaxationFactors { fields { "D|DD" 0.9; } equations { U 0.5; } }\n')
+    r = run(case, "--plan-only")
+    assert r.returncode == 2 and "relaxationFactors for D (field 0.9, equation 1)" in r.stderr
+    fvs.write_text(head + "relaxationFactors { equations { DD 0.99; } }\n")
+    r = run(case, "--plan-only", "--model", "nonLinearGeometryTotalLagrangian")
+    assert r.returncode == 2 and "relaxationFactors for DD (field 1, equation 0.99)" in r.stderr
+    fvs.write_text(head + "relaxationFactors { D 0.7; }\n")          # the older flat form
+    assert run(case, "--plan-only").returncode == 2
+    fvs.write_text(head + "relaxationFactors { fields { p 0.3; } }\n")
+    assert run(case, "--plan-only").returncode == 0

@@ -313,3 +313,20 @@ def test_lame_cylinder_converges_at_second_order(tmp_path):
         err.append(np.linalg.norm(D - ue) / np.linalg.norm(ue))
     assert err[2] < 5e-5
     assert np.log2(err[1] / err[2]) > 1.8
+
+
+def test_field_relaxation_rescues_the_corrector_loop():
+    """relaxationFactors { fields { "D|DD" f; } } (the reference's "fixed"
+    relaxField, used by its pressurisedCylinder tutorial with f = 0.9): on a
+    jittered box at nu = 0.4 with a shear traction the unrelaxed loop runs
+    away, while f = 0.9 and f = 0.7 converge to the same fixed point."""
+    m = sg.box_mesh(10, 10, 10, 1.0, 1.0, 1.0, 0.2, 3)
+    t = np.tile([1e5, 0.0, -1e6], (int(m["patch_size"][5]), 1))
+    bcs = [(1, None, None)] * 4 + [(0, None, None), (1, t, None)]
+    kw = dict(E=200e9, nu=0.4, n_correctors=3000, solution_tol=1e-10, alternative_tol=1e-11)
+    D0, _, _, p0 = pyoracle.solve(m, bcs, **kw)
+    assert p0["converged"] == 0 and np.abs(D0).max() > 1.0          # ran away
+    D9, _, _, p9 = pyoracle.solve(m, bcs, field_relaxation=0.9, **kw)
+    D7, _, _, p7 = pyoracle.solve(m, bcs, field_relaxation=0.7, **kw)
+    assert p9["converged"] == 1 and p7["converged"] == 1
+    assert np.linalg.norm(D9 - D7) / np.linalg.norm(D7) < 1e-6
