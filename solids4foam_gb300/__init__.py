@@ -7,7 +7,10 @@ solidModel / mechanicalLaw interface.
 from . import _lib
 from ._lib import S4GError, lib
 from .cases import box_mesh, cantilever_case, cube_case
+from .foam_case import read_case, read_relaxation
+from .post import derived_fields, point_displacement
 from .solid_model import Context, Server, SolidModel
 
 __all__ = ["S4GError", "lib", "box_mesh", "cantilever_case", "cube_case", "Context",
-           "Server", "SolidModel", "_lib"]
+           "Server", "SolidModel", "read_case", "read_relaxation", "point_displacement",
+           "derived_fields", "_lib"]

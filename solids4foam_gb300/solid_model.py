@@ -2,12 +2,15 @@
 
 A ``SolidModel`` is built from the same vocabulary as a solids4foam case:
 the ``solidModel`` type name of constant/solidProperties
-(``linearGeometryTotalDisplacement`` or ``nonLinearGeometryTotalLagrangian``),
-a ``mechanical`` law entry of constant/mechanicalProperties
-(``linearElastic`` with E/nu, ``neoHookeanElastic`` with E/nu or mu/K), the
-``0/D`` patch types ``fixedDisplacement`` / ``solidTraction`` (with traction
-and pressure), the ``solvers { "D|DD" {...} }`` entry of system/fvSolution and
-the ``<model>Coeffs`` keys of solidProperties.  ``evolve()`` runs the model's
+(``linearGeometryTotalDisplacement``, ``nonLinearGeometryTotalLagrangian`` or
+``nonLinearGeometryTotalLagrangianTotalDisplacement``), a ``mechanical`` law
+entry of constant/mechanicalProperties (``linearElastic`` with E/nu,
+``neoHookeanElastic`` with E/nu or mu/K), the ``0/D`` patch types
+``fixedDisplacement`` / ``solidTraction`` as ``(type, value or traction,
+pressure[, relaxationFactor])`` tuples, the ``solvers { "D|DD" {...} }``
+entry of system/fvSolution and the ``<model>Coeffs`` keys of
+solidProperties.  A meshed OpenFOAM case reads into these arguments with
+``foam_case.read_case``.  ``evolve()`` runs the model's
 outer-corrector loop on the GPU through the C ABI (include/s4g.h), as
 solidModel::evolve does in the reference (solidModel.H:759).
 
