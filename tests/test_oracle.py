@@ -330,3 +330,30 @@ def test_field_relaxation_rescues_the_corrector_loop():
     D7, _, _, p7 = pyoracle.solve(m, bcs, field_relaxation=0.7, **kw)
     assert p9["converged"] == 1 and p7["converged"] == 1
     assert np.linalg.norm(D9 - D7) / np.linalg.norm(D7) < 1e-6
+
+
+@pytest.mark.parametrize("model", [1, 2])
+def test_homogeneous_finite_deformation(model):
+    """A homogeneous deformation x = F X with stretch and shear (J = 1.188),
+    prescribed on every boundary over 20 increments, is reproduced exactly
+    by both total Lagrangian forms, and the stress everywhere is the
+    neoHookean Cauchy stress of F, sigma = (mu dev(J^-2/3 F F^T) +
+    K/2 (J^2 - 1) I) / J (neoHookeanElastic.C:275-303), restated here
+    independently."""
+    m = sg.box_mesh(6, 5, 4, 1.0, 0.9, 0.8, 0.2, 3)
+    F = np.array([[1.2, 0.1, 0.0], [0.0, 0.9, 0.05], [0.0, 0.0, 1.1]])
+    bcs = []
+    for p in range(6):
+        s, n = int(m["patch_start"][p]), int(m["patch_size"][p])
+        bcs.append((0, m["Cf"][s:s + n] @ (F - np.eye(3)).T, None))
+    mu, K = 1e6, 5e6
+    J = np.linalg.det(F)
+    bbar = J ** (-2.0 / 3.0) * F @ F.T
+    S = (mu * (bbar - np.trace(bbar) / 3 * np.eye(3)) + 0.5 * K * (J ** 2 - 1) * np.eye(3)) / J
+    expected = np.array([S[0, 0], S[0, 1], S[0, 2], S[1, 1], S[1, 2], S[2, 2]])
+    D, sig, _, p = pyoracle.solve(m, bcs, model=model, law=1, use_mu_K=1, mu=mu, K=K,
+                                  n_correctors=4000, n_increments=20, solution_tol=1e-10,
+                                  alternative_tol=1e-11, ls_boundary_delta=1)
+    assert p["converged"] == 1 and p["enforce_linear"] == 0
+    assert np.abs(D - m["C"] @ (F - np.eye(3)).T).max() < 1e-7
+    assert np.abs(sig - expected).max() < 1e-6 * np.abs(expected).max()
