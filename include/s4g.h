@@ -514,6 +514,17 @@ s4g_status s4g_foam_load_ramp(const s4g_foam_case* fc, double* end_time, int* co
  * increments, (endTime - startTime) / deltaT. */
 s4g_status s4g_foam_read_time(const char* control_dict, double* start_time, double* end_time,
                               double* delta_t);
+/* The model, law and controls of a case directory, from
+ * constant/solidProperties (solidModel and its <model>Coeffs, with the
+ * stabilisation sub-dictionary: solidModel.C:909-912,1138-1243,1305-1323),
+ * constant/mechanicalProperties (one linearElastic or neoHookeanElastic law,
+ * planeStress no) and system/fvSolution (the PCG solver of D, or DD for the
+ * incremental total Lagrangian model).  Entries that are not set keep the
+ * reference defaults (s4g_default_controls).  Anything not built -- another
+ * model, law or solver, plane stress, several laws, sigma0, predictor,
+ * solvePressureEqn -- is S4G_BAD_ARG, named in s4g_last_error. */
+s4g_status s4g_foam_read_controls(const char* case_dir, s4g_model* model, s4g_law* law,
+                                  s4g_lin_solver* lin, s4g_outer* outer);
 /* relaxationFactors of a system/fvSolution for one field ("D" or "DD"):
  * field_factor from fields { } (or the older flat form), equation_factor
  * from equations { }; 1 where none is set.  Field relaxation (the

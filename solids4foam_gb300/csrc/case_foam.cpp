@@ -972,6 +972,114 @@ s4g_status s4g_foam_read_relaxation(const char* fv_solution, const char* field,
   });
 }
 
+s4g_status s4g_foam_read_controls(const char* case_dir, s4g_model* model, s4g_law* law,
+                                  s4g_lin_solver* lin, s4g_outer* outer) {
+  if (!case_dir || !model || !law || !lin || !outer) return S4G_BAD_ARG;
+  return guarded([&] {
+    const std::string dir(case_dir);
+    auto readDict = [](const std::string& path) {
+      std::vector<Tok> t = payload(path);
+      Cursor c{t, 0, path};
+      return parseDict(c, false);
+    };
+    // a number: the last token of `key value;`, `key [dims] value;` or
+    // `key name [dims] value;` (a dimensionedScalar)
+    auto number = [](const Entry* e, const std::string& where) {
+      if (!e || e->isDict || e->val.empty()) fail(where + ": missing or bad entry");
+      return toDouble(e->val.back(), where + " " + e->key);
+    };
+    // constant/solidProperties: solidModel and <model>Coeffs (solidModel.C:909-912)
+    const std::string sp = dir + "/constant/solidProperties";
+    std::vector<Entry> props = readDict(sp);
+    const Entry* sm = find(props, "solidModel");
+    if (!sm || sm->val.size() != 1) fail(sp + ": no solidModel");
+    const std::string name = sm->val[0].s;
+    if (name == "linearGeometryTotalDisplacement") *model = S4G_LIN_GEOM_TOTAL_DISP;
+    else if (name == "nonLinearGeometryTotalLagrangian") *model = S4G_NONLIN_GEOM_TOTAL_LAG;
+    else if (name == "nonLinearGeometryTotalLagrangianTotalDisplacement")
+      *model = S4G_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP;
+    else fail(sp + ": solidModel " + name + " is not built");
+    s4g_default_controls(lin, outer);
+    if (const Entry* co = lookup(props, name + "Coeffs")) {
+      if (!co->isDict) fail(sp + ": " + name + "Coeffs must be a dictionary");
+      const std::string w = sp + ": " + name + "Coeffs";
+      if (const Entry* e = find(co->sub, "nCorrectors")) outer->n_correctors = (int)number(e, w);
+      if (const Entry* e = find(co->sub, "solutionTolerance")) outer->solution_tol = number(e, w);
+      if (const Entry* e = find(co->sub, "alternativeTolerance")) outer->alternative_tol = number(e, w);
+      if (const Entry* e = find(co->sub, "materialTolerance")) outer->material_tol = number(e, w);
+      if (const Entry* e = find(co->sub, "infoFrequency")) outer->info_frequency = (int)number(e, w);
+      if (const Entry* st = find(co->sub, "stabilisation")) {
+        if (!st->isDict) fail(w + ": stabilisation must be a dictionary");
+        const Entry* ty = find(st->sub, "type");
+        if (ty && (ty->val.size() != 1 || ty->val[0].s != "RhieChow"))
+          fail(w + ": stabilisation type " + (ty->val.empty() ? "" : ty->val[0].s) + " is not built");
+        if (const Entry* e = find(st->sub, "scaleFactor")) outer->stab_scale = number(e, w);
+      }
+      for (const char* k : {"predictor", "solvePressureEqn"})
+        if (const Entry* e = find(co->sub, k))
+          if (!e->val.empty() && (e->val[0].s == "yes" || e->val[0].s == "true" || e->val[0].s == "on"))
+            fail(w + ": " + k + " is not built");
+    }
+    // constant/mechanicalProperties: one law (linearElastic.C:62-89,
+    // neoHookeanElastic.C:50-79); planeStress must be no
+    const std::string mp = dir + "/constant/mechanicalProperties";
+    std::vector<Entry> mech = readDict(mp);
+    const Entry* ps = find(mech, "planeStress");
+    if (ps && !ps->val.empty() && (ps->val[0].s == "yes" || ps->val[0].s == "true" || ps->val[0].s == "on"))
+      fail(mp + ": planeStress yes is not built");
+    const Entry* laws = find(mech, "mechanical");
+    if (!laws || laws->isDict) fail(mp + ": no mechanical ( ... ) list");
+    // the list holds `name { ... }` sub-dictionaries: parse its tokens
+    std::vector<Tok> lt(laws->val.begin(), laws->val.end());
+    if (lt.size() < 2 || !lt.front().is('(') || !lt.back().is(')')) fail(mp + ": bad mechanical list");
+    std::vector<Tok> inner(lt.begin() + 1, lt.end() - 1);
+    Cursor lc{inner, 0, mp};
+    std::vector<Entry> list = parseDict(lc, false);
+    if (list.size() != 1 || !list[0].isDict)
+      fail(mp + ": " + std::to_string(list.size()) + " laws; one law is built");
+    const std::vector<Entry>& ld = list[0].sub;
+    const Entry* ty = find(ld, "type");
+    if (!ty || ty->val.size() != 1) fail(mp + ": the law has no type");
+    *law = s4g_law{};
+    if (ty->val[0].s == "linearElastic") law->type = S4G_LINEAR_ELASTIC;
+    else if (ty->val[0].s == "neoHookeanElastic") law->type = S4G_NEO_HOOKEAN;
+    else fail(mp + ": law type " + ty->val[0].s + " is not built");
+    const Entry *E = find(ld, "E"), *nu = find(ld, "nu"), *mu = find(ld, "mu"), *K = find(ld, "K");
+    if (E && nu && !(law->type == S4G_NEO_HOOKEAN && (mu || K))) {
+      law->E = number(E, mp);
+      law->nu = number(nu, mp);
+    } else if (mu && K && !(law->type == S4G_NEO_HOOKEAN && (E || nu))) {
+      law->use_mu_K = 1;
+      law->mu = number(mu, mp);
+      law->K = number(K, mp);
+    } else {
+      fail(mp + ": give E and nu, or mu and K");
+    }
+    if (const Entry* rho = find(ld, "rho")) law->rho = number(rho, mp);
+    if (find(ld, "sigma0")) fail(mp + ": sigma0 is not built");
+    // system/fvSolution: the solved field's solver (lduMatrix::solver::New)
+    const std::string fs = dir + "/system/fvSolution";
+    std::vector<Entry> sol = readDict(fs);
+    const char* field = *model == S4G_NONLIN_GEOM_TOTAL_LAG ? "DD" : "D";
+    const Entry* solvers = find(sol, "solvers");
+    const Entry* sd = solvers && solvers->isDict ? lookup(solvers->sub, field) : nullptr;
+    if (!sd || !sd->isDict) fail(fs + ": no solver for " + field);
+    const std::string w = fs + ": solver for " + field;
+    const Entry* sv = find(sd->sub, "solver");
+    if (!sv || sv->val.size() != 1 || sv->val[0].s != "PCG")
+      fail(w + ": solver " + (sv && !sv->val.empty() ? sv->val[0].s : std::string("?")) +
+           " is not built (PCG is)");
+    const Entry* pc = find(sd->sub, "preconditioner");
+    const std::string pname = pc && !pc->isDict && pc->val.size() == 1 ? pc->val[0].s : "";
+    if (pname == "DIC" || pname == "FDIC") lin->preconditioner = S4G_PRECOND_DIC;
+    else if (pname == "diagonal") lin->preconditioner = S4G_PRECOND_DIAGONAL;
+    else fail(w + ": preconditioner " + pname + " is not built (DIC, FDIC and diagonal are)");
+    if (const Entry* e = find(sd->sub, "tolerance")) lin->tolerance = number(e, w);
+    if (const Entry* e = find(sd->sub, "relTol")) lin->rel_tol = number(e, w);
+    if (const Entry* e = find(sd->sub, "maxIter")) lin->max_iter = (int)number(e, w);
+  });
+}
+
 s4g_status s4g_foam_load_ramp(const s4g_foam_case* m, double* end_time, int* constant_loads) {
   if (!m) return S4G_BAD_ARG;
   if (end_time) *end_time = m->rampEnd;

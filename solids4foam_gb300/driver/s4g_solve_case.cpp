@@ -8,10 +8,10 @@
 //                                             s4g_foam_apply_bcs, s4g_solver_set
 //   evolve()                                  s4g_solve, s4g_get_gradD
 //   after the loop                            s4g_point_interpolate, s4g_derived_fields
-// and prints one JSON line with the run's figures.  The material, model and
-// controls come from the command line (the reference reads them from
-// constant/mechanicalProperties, constant/solidProperties and
-// system/fvSolution).  A total Lagrangian case whose loads are series
+// and prints one JSON line with the run's figures.  The model, material and
+// controls come from the case (constant/solidProperties,
+// constant/mechanicalProperties, system/fvSolution: s4g_foam_read_controls),
+// as the reference reads them; command-line options override them.  A total Lagrangian case whose loads are series
 // (linear ramps from zero) runs one increment per time step of
 // system/controlDict unless --increments is given.  --plan-only stops after
 // the host-side mesh planning and needs no GPU.  --write writes pointD as an
@@ -33,6 +33,8 @@ namespace {
 void usage() {
   std::fprintf(stderr,
                "usage: s4g_solve_case CASE_DIR [options]\n"
+               "  (model, law and controls come from the case's constant/solidProperties,\n"
+               "   constant/mechanicalProperties and system/fvSolution; options override them)\n"
                "  --model linearGeometryTotalDisplacement | nonLinearGeometryTotalLagrangian |\n"
                "          nonLinearGeometryTotalLagrangianTotalDisplacement\n"
                "  --E E --nu NU            linearElastic (default 200e9, 0.3)\n"
@@ -85,7 +87,9 @@ int main(int argc, char** argv) {
     return argc < 2 ? 1 : 0;
   }
   const std::string caseDir = argv[1];
-  std::string modelName = "linearGeometryTotalDisplacement", writeTime;
+  std::string modelName, writeTime;
+  // the case's own model, law and controls when it has them; else defaults
+  s4g_model model = S4G_LIN_GEOM_TOTAL_DISP;
   s4g_law law{};
   law.type = S4G_LINEAR_ELASTIC;
   law.E = 200e9;
@@ -95,10 +99,14 @@ int main(int argc, char** argv) {
   s4g_lin_solver lin;
   s4g_outer outer;
   s4g_default_controls(&lin, &outer);
+  const bool fromCase = access((caseDir + "/constant/solidProperties").c_str(), R_OK) == 0;
+  if (fromCase)
+    check(s4g_foam_read_controls(caseDir.c_str(), &model, &law, &lin, &outer),
+          "reading the case's solidProperties, mechanicalProperties and fvSolution");
   s4g_mesh_opts mo{S4G_RENUMBER_TILED, 512, 0, 0, 0};
   s4g_precision precision = S4G_FP64;
   int increments = 1, device = 0;
-  bool planOnly = false, muK = false, incrementsGiven = false;
+  bool planOnly = false, muKGiven = false, eNuGiven = false, incrementsGiven = false;
   for (int i = 2; i < argc; ++i) {
     const std::string a = argv[i];
     auto val = [&]() -> const char* {
@@ -109,10 +117,10 @@ int main(int argc, char** argv) {
       return argv[++i];
     };
     if (a == "--model") modelName = val();
-    else if (a == "--E") law.E = std::atof(val());
-    else if (a == "--nu") law.nu = std::atof(val());
-    else if (a == "--mu") { law.mu = std::atof(val()); muK = true; }
-    else if (a == "--K") { law.K = std::atof(val()); muK = true; }
+    else if (a == "--E") { law.E = std::atof(val()); eNuGiven = true; }
+    else if (a == "--nu") { law.nu = std::atof(val()); eNuGiven = true; }
+    else if (a == "--mu") { law.mu = std::atof(val()); muKGiven = true; }
+    else if (a == "--K") { law.K = std::atof(val()); muKGiven = true; }
     else if (a == "--increments") { increments = std::atoi(val()); incrementsGiven = true; }
     else if (a == "--precision") {
       const std::string p = val();
@@ -148,17 +156,22 @@ int main(int argc, char** argv) {
     else if (a == "--write") writeTime = val();
     else { usage(); return 1; }
   }
-  s4g_model model;
-  if (modelName == "linearGeometryTotalDisplacement") model = S4G_LIN_GEOM_TOTAL_DISP;
-  else if (modelName == "nonLinearGeometryTotalLagrangian") model = S4G_NONLIN_GEOM_TOTAL_LAG;
-  else if (modelName == "nonLinearGeometryTotalLagrangianTotalDisplacement")
-    model = S4G_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP;
-  else { usage(); return 1; }
-  if (model != S4G_LIN_GEOM_TOTAL_DISP) {
+  static const char* const kModels[] = {"linearGeometryTotalDisplacement",
+                                        "nonLinearGeometryTotalLagrangian",
+                                        "nonLinearGeometryTotalLagrangianTotalDisplacement"};
+  if (!modelName.empty()) {
+    if (modelName == kModels[0]) model = S4G_LIN_GEOM_TOTAL_DISP;
+    else if (modelName == kModels[1]) model = S4G_NONLIN_GEOM_TOTAL_LAG;
+    else if (modelName == kModels[2]) model = S4G_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP;
+    else { usage(); return 1; }
+  }
+  modelName = kModels[(int)model];
+  if (muKGiven) law.use_mu_K = 1;
+  else if (eNuGiven) law.use_mu_K = 0;
+  if (!fromCase && model != S4G_LIN_GEOM_TOTAL_DISP) {
+    // no mechanicalProperties: the total Lagrangian models take neoHookeanElastic
     law.type = S4G_NEO_HOOKEAN;
-    law.use_mu_K = 1;
-  } else if (muK) {
-    law.use_mu_K = 1;
+    if (!eNuGiven) law.use_mu_K = 1;
   }
 
   // the case
@@ -213,10 +226,15 @@ int main(int argc, char** argv) {
   if (planOnly) {
     std::printf("{\"case\": \"%s\", \"cells\": %d, \"faces\": %d, \"internal_faces\": %d, "
                 "\"points\": %d, \"patches\": %d, \"parts\": %d, \"part_depth\": %d, "
-                "\"levels\": %d, \"load_ramp_end\": %g, \"increments\": %d}\n",
+                "\"levels\": %d, \"load_ramp_end\": %g, \"increments\": %d, \"model\": \"%s\", "
+                "\"law\": \"%s\", \"E\": %g, \"nu\": %g, \"mu\": %g, \"K\": %g, \"use_mu_K\": %d, "
+                "\"nCorrectors\": %d, \"tolerance\": %g, \"relTol\": %g, \"scaleFactor\": %g}\n",
                 caseDir.c_str(), desc.n_cells, desc.n_faces, desc.n_internal_faces, nPoints,
                 desc.n_patches, info.n_parts, info.part_depth, info.n_levels_global, rampEnd,
-                model == S4G_LIN_GEOM_TOTAL_DISP ? 1 : increments);
+                model == S4G_LIN_GEOM_TOTAL_DISP ? 1 : increments, modelName.c_str(),
+                law.type == S4G_LINEAR_ELASTIC ? "linearElastic" : "neoHookeanElastic", law.E,
+                law.nu, law.mu, law.K, law.use_mu_K, outer.n_correctors, lin.tolerance,
+                lin.rel_tol, outer.stab_scale);
     s4g_foam_free(fc);
     return 0;
   }

@@ -225,3 +225,37 @@ def read_relaxation(case_dir: str, field: str = "D"):
         os.path.join(case_dir, "system", "fvSolution").encode(), field.encode(), ct.byref(ff),
         ct.byref(ef)), "s4g_foam_read_relaxation")
     return ff.value, ef.value
+
+
+MODEL_NAMES = {_lib.LIN_GEOM_TOTAL_DISP: "linearGeometryTotalDisplacement",
+               _lib.NONLIN_GEOM_TOTAL_LAG: "nonLinearGeometryTotalLagrangian",
+               _lib.NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP:
+                   "nonLinearGeometryTotalLagrangianTotalDisplacement"}
+
+
+def read_controls(case_dir: str):
+    """The case's model, law and controls (constant/solidProperties,
+    constant/mechanicalProperties, system/fvSolution) as the keyword
+    arguments of SolidModel: dict(model=..., law=..., solver=..., outer=...).
+    Unset entries keep the reference defaults; anything not built raises."""
+    model, law = ct.c_int(), _lib.Law()
+    lin, out = _lib.LinSolver(), _lib.Outer()
+    _lib.check(_lib.lib().s4g_foam_read_controls(case_dir.encode(), ct.byref(model), ct.byref(law),
+                                                 ct.byref(lin), ct.byref(out)),
+               "s4g_foam_read_controls")
+    if law.type == _lib.LINEAR_ELASTIC:
+        lw = dict(type="linearElastic")
+    else:
+        lw = dict(type="neoHookeanElastic")
+    if law.use_mu_K:
+        lw.update(mu=law.mu, K=law.K)
+    else:
+        lw.update(E=law.E, nu=law.nu)
+    return dict(model=MODEL_NAMES[model.value], law=lw,
+                solver=dict(preconditioner="DIC" if lin.preconditioner == _lib.PRECOND_DIC
+                            else "diagonal",
+                            tolerance=lin.tolerance, relTol=lin.rel_tol, maxIter=lin.max_iter),
+                outer=dict(nCorrectors=out.n_correctors, solutionTolerance=out.solution_tol,
+                           alternativeTolerance=out.alternative_tol,
+                           materialTolerance=out.material_tol, infoFrequency=out.info_frequency,
+                           stabilisation=dict(type="RhieChow", scaleFactor=out.stab_scale)))

@@ -108,3 +108,24 @@ def test_relaxation_factors_are_refused(tmp_path):
     assert run(case, "--plan-only").returncode == 2
     fvs.write_text(head + "relaxationFactors { fields { p 0.3; } }\n")
     assert run(case, "--plan-only").returncode == 0
+
+
+def test_controls_come_from_the_case(tmp_path):
+    """Without options the driver takes model, law and controls from the
+    case's dictionaries; options override them."""
+    case = _ramp_case(tmp_path)
+    head = "FoamFile { version 2.0; format ascii; class dictionary; object x; }\n"
+    (tmp_path / "constant" / "solidProperties").write_text(
+        head + "solidModel nonLinearGeometryTotalLagrangianTotalDisplacement;\n"
+        "nonLinearGeometryTotalLagrangianTotalDisplacementCoeffs { nCorrectors 777; }\n")
+    (tmp_path / "constant" / "mechanicalProperties").write_text(
+        head + "planeStress no;\nmechanical ( r { type neoHookeanElastic; mu 2e6; K 3e7; } );\n")
+    (tmp_path / "system" / "fvSolution").write_text(
+        head + 'solvers { "D|DD" { solver PCG; preconditioner FDIC; tolerance 1e-8; relTol 0.2; } }\n')
+    out = json.loads(run(case, "--plan-only").stdout)
+    assert out["model"] == "nonLinearGeometryTotalLagrangianTotalDisplacement"
+    assert (out["law"], out["mu"], out["K"], out["use_mu_K"]) == ("neoHookeanElastic", 2e6, 3e7, 1)
+    assert (out["nCorrectors"], out["tolerance"], out["relTol"]) == (777, 1e-8, 0.2)
+    assert out["increments"] == 20                 # the traction ramp over 10 / 0.5
+    out = json.loads(run(case, "--plan-only", "--nCorrectors", "50", "--mu", "1e6").stdout)
+    assert (out["nCorrectors"], out["mu"]) == (50, 1e6)

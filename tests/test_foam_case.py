@@ -303,3 +303,81 @@ def test_other_load_series_are_rejected(tmp_path):
     with pytest.raises(_lib.S4GError, match="cannot open"):
         _series_case(tmp_path, """{ type solidTraction; pressure uniform 0;
             tractionSeries { file "$FOAM_CASE/constant/missing"; } }""")
+
+
+def _controls_case(tmp_path, solid=None, mech=None, fvs=None):
+    head = "FoamFile { version 2.0; format ascii; class dictionary; object x; }\n"
+    (tmp_path / "constant").mkdir(exist_ok=True)
+    (tmp_path / "system").mkdir(exist_ok=True)
+    (tmp_path / "constant" / "solidProperties").write_text(head + (solid or """
+solidModel     nonLinearGeometryTotalLagrangian;
+"nonLinearGeometryTotalLagrangianCoeffs|nonLinearGeometryUpdatedLagrangianCoeffs"
+{
+    nCorrectors             20000;
+    solutionTolerance       1e-08;
+    alternativeTolerance    1e-09;
+    infoFrequency           100;
+    stabilisation { type RhieChow; scaleFactor 0.2; }
+}
+"""))
+    (tmp_path / "constant" / "mechanicalProperties").write_text(head + (mech or """
+planeStress     no;
+mechanical
+(
+    rubber
+    {
+        type            neoHookeanElastic;
+        rho             rho [1 -3 0 0 0 0 0] 1000;
+        mu              mu [1 -1 -2 0 0 0 0] 3e+6;
+        K               K [1 -1 -2 0 0 0 0] 2e+7;
+    }
+);
+"""))
+    (tmp_path / "system" / "fvSolution").write_text(head + (fvs or """
+solvers
+{
+    "D|DD" { solver PCG; preconditioner FDIC; tolerance 1e-09; relTol 0.05; maxIter 500; }
+}
+"""))
+    return str(tmp_path)
+
+
+def test_case_controls(tmp_path):
+    """solidProperties (coefficients under a regular-expression key),
+    mechanicalProperties (dimensioned entries) and fvSolution map onto the
+    model, law, solver and outer-loop arguments; unset entries keep the
+    reference defaults."""
+    from solids4foam_gb300.foam_case import read_controls
+    c = read_controls(_controls_case(tmp_path))
+    assert c["model"] == "nonLinearGeometryTotalLagrangian"
+    assert c["law"] == dict(type="neoHookeanElastic", mu=3e6, K=2e7)
+    assert c["solver"] == dict(preconditioner="DIC", tolerance=1e-9, relTol=0.05, maxIter=500)
+    o = c["outer"]
+    assert (o["nCorrectors"], o["solutionTolerance"], o["alternativeTolerance"]) == (20000, 1e-8, 1e-9)
+    assert o["materialTolerance"] == 1e-5 and o["stabilisation"]["scaleFactor"] == 0.2
+    c = read_controls(_controls_case(tmp_path, solid="solidModel linearGeometryTotalDisplacement;\n",
+                                     mech="planeStress no; mechanical ( steel { type linearElastic; "
+                                          "E E [1 -1 -2 0 0 0 0] 200e+9; nu 0.3; } );\n"))
+    assert c["model"] == "linearGeometryTotalDisplacement"
+    assert c["law"] == dict(type="linearElastic", E=200e9, nu=0.3)
+    assert c["outer"]["nCorrectors"] == 10000 and c["outer"]["stabilisation"]["scaleFactor"] == 0.1
+
+
+@pytest.mark.parametrize("part,text,match", [
+    ("solid", "solidModel nonLinearGeometryUpdatedLagrangian;\n", "solidModel nonLinearGeometryUpdatedLagrangian is not built"),
+    ("mech", "planeStress yes; mechanical ( s { type linearElastic; E 1e9; nu 0.3; } );\n", "planeStress yes"),
+    ("mech", "planeStress no; mechanical ( a { type linearElastic; E 1e9; nu 0.3; } "
+             "b { type linearElastic; E 2e9; nu 0.3; } );\n", "2 laws; one law is built"),
+    ("mech", "planeStress no; mechanical ( s { type neoHookeanElastic; E 1e9; nu 0.3; mu 1; K 2; } );\n",
+     "give E and nu, or mu and K"),
+    ("mech", "planeStress no; mechanical ( s { type StVenantKirchhoffElastic; E 1e9; nu 0.3; } );\n",
+     "law type StVenantKirchhoffElastic is not built"),
+    ("fvs", "solvers { \"D|DD\" { solver GAMG; smoother GaussSeidel; tolerance 1e-9; relTol 0.1; } }\n",
+     "solver GAMG is not built"),
+    ("fvs", "solvers { \"D|DD\" { solver PCG; preconditioner GAMG; tolerance 1e-9; relTol 0.1; } }\n",
+     "preconditioner GAMG is not built"),
+])
+def test_case_controls_refusals(tmp_path, part, text, match):
+    from solids4foam_gb300.foam_case import read_controls
+    with pytest.raises(_lib.S4GError, match=match):
+        read_controls(_controls_case(tmp_path, **{part: text}))
