@@ -538,6 +538,21 @@ s4g_status s4g_foam_read_relaxation(const char* fv_solution, const char* field,
  * (uploaded from this case's s4g_mesh_desc). */
 s4g_status s4g_foam_apply_bcs(const s4g_foam_case* fc, s4g_mesh* mesh);
 void s4g_foam_free(s4g_foam_case* fc);
+/* Boundary values of D for writing results, Db [n_boundary_faces][3]:
+ * fixedDisplacement faces take the value read from the D file; every other
+ * face the cell value extrapolated with the cell gradient,
+ * D_P + (C_f - C_P) . gradD_P. */
+s4g_status s4g_foam_boundary_D(const s4g_foam_case* fc, const double* D, const double* gradD,
+                               double* Db);
+/* Writes <dir>/<name> as an ASCII volScalarField (width 1), volVectorField
+ * (3) or volSymmTensorField (6, XX XY XZ YY YZ ZZ), as the reference's time
+ * directories hold them: cell values [n_cells][width] and, per patch, a
+ * calculated value per face from boundary_values [n_boundary_faces][width]
+ * or, if that is NULL, the adjacent cell's value (empty patches: type
+ * empty).  The directory's last component names the time. */
+s4g_status s4g_foam_write_field(const s4g_foam_case* fc, const char* dir, const char* name,
+                                int width, const char* dimensions, const double* cell_values,
+                                const double* boundary_values);
 /* Writes an ASCII polyMesh (points, faces, owner, neighbour, boundary with
  * patch type "patch") into an existing directory; face f has the points
  * face_points[face_start[f] .. face_start[f+1]). */

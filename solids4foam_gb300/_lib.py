@@ -182,6 +182,9 @@ _SIGS = {
     "s4g_foam_read_controls": (ct.c_int, [ct.c_char_p, ct.POINTER(ct.c_int), ct.POINTER(Law),
                                           ct.POINTER(LinSolver), ct.POINTER(Outer)]),
     "s4g_foam_free": (None, [ct.c_void_p]),
+    "s4g_foam_boundary_D": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "s4g_foam_write_field": (ct.c_int, [ct.c_void_p, ct.c_char_p, ct.c_char_p, ct.c_int,
+                                        ct.c_char_p, ct.c_void_p, ct.c_void_p]),
     "s4g_foam_write_mesh": (ct.c_int, [ct.c_char_p, ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p,
                                        ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
                                        ct.c_void_p, ct.c_void_p, ct.c_void_p]),

@@ -1089,6 +1089,87 @@ s4g_status s4g_foam_load_ramp(const s4g_foam_case* m, double* end_time, int* con
 
 void s4g_foam_free(s4g_foam_case* m) { delete m; }
 
+s4g_status s4g_foam_boundary_D(const s4g_foam_case* m, const double* D, const double* gradD,
+                               double* Db) {
+  if (!m || !D || !gradD || !Db) return S4G_BAD_ARG;
+  for (size_t p = 0; p < m->patchName.size(); ++p) {
+    const s4g_foam_case::Bc* bc = p < m->bcs.size() && m->bcs[p].set ? &m->bcs[p] : nullptr;
+    for (int i = 0; i < m->patchSize[p]; ++i) {
+      const int f = m->patchStart[p] + i, b = f - m->nInt, c = m->owner[(size_t)f];
+      double* out = Db + 3 * (size_t)b;
+      if (bc && bc->type == S4G_FIXED_DISPLACEMENT) {
+        for (int k = 0; k < 3; ++k) out[k] = bc->vec3[3 * (size_t)i + k];
+        continue;
+      }
+      // D_P + (C_f - C_P) . gradD_P, gradD_ij = dD_j/dx_i
+      const double* g = gradD + 9 * (size_t)c;
+      double d[3];
+      for (int k = 0; k < 3; ++k) d[k] = m->Cf[3 * (size_t)f + k] - m->C[3 * (size_t)c + k];
+      for (int j = 0; j < 3; ++j)
+        out[j] = D[3 * (size_t)c + j] + d[0] * g[j] + d[1] * g[3 + j] + d[2] * g[6 + j];
+    }
+  }
+  return S4G_OK;
+}
+
+s4g_status s4g_foam_write_field(const s4g_foam_case* m, const char* dir, const char* name, int width,
+                                const char* dimensions, const double* cell_values,
+                                const double* boundary_values) {
+  if (!m || !dir || !name || !cell_values || (width != 1 && width != 3 && width != 6))
+    return S4G_BAD_ARG;
+  const char* cls = width == 1 ? "volScalarField" : width == 3 ? "volVectorField" : "volSymmTensorField";
+  const char* list = width == 1 ? "scalar" : width == 3 ? "vector" : "symmTensor";
+  std::string d(dir);
+  while (d.size() > 1 && d.back() == '/') d.pop_back();
+  const std::string time = d.substr(d.find_last_of('/') + 1);
+  const std::string path = d + "/" + name;
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) {
+    s4g::setLastError("cannot write " + path);
+    return S4G_BAD_ARG;
+  }
+  auto value = [&](const double* v) {
+    if (width == 1) {
+      std::fprintf(f, "%.12g\n", v[0]);
+    } else {
+      std::fputc('(', f);
+      for (int k = 0; k < width; ++k) std::fprintf(f, k ? " %.12g" : "%.12g", v[k]);
+      std::fputs(")\n", f);
+    }
+  };
+  std::fprintf(f,
+               "FoamFile\n{\n    version     2.0;\n    format      ascii;\n    class       %s;\n"
+               "    location    \"%s\";\n    object      %s;\n}\n"
+               "// Boundary values: %s.\n\n"
+               "dimensions      %s;\n\ninternalField   nonuniform List<%s>\n%d\n(\n",
+               cls, time.c_str(), name,
+               boundary_values ? "as given by the writer" : "those of the adjacent cells",
+               dimensions ? dimensions : "[0 0 0 0 0 0 0]", list, m->nCells);
+  for (int c = 0; c < m->nCells; ++c) value(cell_values + (size_t)width * c);
+  std::fputs(")\n;\n\nboundaryField\n{\n", f);
+  for (size_t p = 0; p < m->patchName.size(); ++p) {
+    std::fprintf(f, "    %s\n    {\n", m->patchName[p].c_str());
+    if (m->patchType[p] == "empty") {
+      std::fputs("        type            empty;\n    }\n", f);
+      continue;
+    }
+    std::fprintf(f, "        type            calculated;\n        value           nonuniform List<%s>\n%d\n(\n",
+                 list, m->patchSize[p]);
+    for (int i = 0; i < m->patchSize[p]; ++i) {
+      const int face = m->patchStart[p] + i;
+      value(boundary_values ? boundary_values + (size_t)width * (face - m->nInt)
+                            : cell_values + (size_t)width * m->owner[(size_t)face]);
+    }
+    std::fputs(")\n;\n    }\n", f);
+  }
+  std::fputs("}\n", f);
+  if (std::fclose(f) != 0) {
+    s4g::setLastError("cannot write " + path);
+    return S4G_BAD_ARG;
+  }
+  return S4G_OK;
+}
+
 s4g_status s4g_foam_write_mesh(const char* dir, int n_points, const double* points, int n_faces,
                                const int* face_start, const int* face_points, int n_int,
                                const int* owner, const int* neighbour, int n_patches,

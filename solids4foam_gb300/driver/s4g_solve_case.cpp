@@ -14,8 +14,8 @@
 // as the reference reads them; command-line options override them.  A total Lagrangian case whose loads are series
 // (linear ramps from zero) runs one increment per time step of
 // system/controlDict unless --increments is given.  --plan-only stops after
-// the host-side mesh planning and needs no GPU.  --write writes pointD as an
-// ASCII pointVectorField into <case>/<time>/pointD.
+// the host-side mesh planning and needs no GPU.  --write TIME writes D,
+// sigma, sigmaEq and pointD as ASCII fields into <case>/<TIME>/.
 
 #include "s4g.h"
 
@@ -286,10 +286,22 @@ int main(int argc, char** argv) {
               caseDir.c_str(), modelName.c_str(), n, model == S4G_LIN_GEOM_TOTAL_DISP ? 1 : increments,
               s4g_status_str(st), perf.converged,
               perf.n_correctors, perf.total_lin_iters, perf.solve_ms, maxD, maxPD, maxSeq);
-  if (!writeTime.empty() &&
-      !writePointField(caseDir, writeTime, pointD.data(), nPoints, fc, desc.n_patches)) {
-    std::fprintf(stderr, "s4g_solve_case: cannot write %s/%s/pointD\n", caseDir.c_str(), writeTime.c_str());
-    return 2;
+  if (!writeTime.empty()) {
+    // D, sigma, sigmaEq (solidModel::writeFields) and pointD in <case>/<time>
+    if (!writePointField(caseDir, writeTime, pointD.data(), nPoints, fc, desc.n_patches)) {
+      std::fprintf(stderr, "s4g_solve_case: cannot write %s/%s/pointD\n", caseDir.c_str(), writeTime.c_str());
+      return 2;
+    }
+    const std::string tdir = caseDir + "/" + writeTime;
+    std::vector<double> Db(3 * (size_t)(desc.n_faces - desc.n_internal_faces));
+    check(s4g_foam_boundary_D(fc, D.data(), gradD.data(), Db.data()), "s4g_foam_boundary_D");
+    check(s4g_foam_write_field(fc, tdir.c_str(), "D", 3, "[0 1 0 0 0 0 0]", D.data(), Db.data()),
+          "writing D");
+    check(s4g_foam_write_field(fc, tdir.c_str(), "sigma", 6, "[1 -1 -2 0 0 0 0]", sigma.data(), nullptr),
+          "writing sigma");
+    check(s4g_foam_write_field(fc, tdir.c_str(), "sigmaEq", 1, "[1 -1 -2 0 0 0 0]", sigmaEq.data(),
+                               nullptr),
+          "writing sigmaEq");
   }
   s4g_mesh_destroy(mesh);
   s4g_ctx_destroy(ctx);

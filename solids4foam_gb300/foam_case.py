@@ -259,3 +259,38 @@ def read_controls(case_dir: str):
                            alternativeTolerance=out.alternative_tol,
                            materialTolerance=out.material_tol, infoFrequency=out.info_frequency,
                            stabilisation=dict(type="RhieChow", scaleFactor=out.stab_scale)))
+
+
+def write_results(case_dir: str, time: str, D, sigma, gradD, polymesh: str = "constant/polyMesh",
+                  d_file: str = "0/D"):
+    """Writes D, sigma and sigmaEq into <case_dir>/<time>/ as ASCII vol
+    fields: cell values, and on the patches the prescribed displacement
+    (fixedDisplacement) or the gradient-extrapolated one for D, the adjacent
+    cell's value for sigma and sigmaEq."""
+    from .post import derived_fields
+    L = _lib.lib()
+    h = ct.c_void_p()
+    _lib.check(L.s4g_foam_read_mesh(os.path.join(case_dir, polymesh).encode(), ct.byref(h)),
+               "s4g_foam_read_mesh")
+    try:
+        _lib.check(L.s4g_foam_read_d(h, os.path.join(case_dir, d_file).encode()), "s4g_foam_read_d")
+        D = np.ascontiguousarray(D, np.float64)
+        sig = np.ascontiguousarray(sigma, np.float64)
+        G = np.ascontiguousarray(gradD, np.float64).reshape(-1, 9)
+        seq, _, _ = derived_fields(sig)
+        d = _lib.MeshDesc()
+        _lib.check(L.s4g_foam_mesh_desc(h, ct.byref(d), None), "s4g_foam_mesh_desc")
+        Db = np.zeros((d.n_faces - d.n_internal_faces, 3))
+        _lib.check(L.s4g_foam_boundary_D(h, D.ctypes.data, G.ctypes.data, Db.ctypes.data),
+                   "s4g_foam_boundary_D")
+        out = os.path.join(case_dir, time)
+        os.makedirs(out, exist_ok=True)
+        for name, width, dims, cells, bnd in (("D", 3, "[0 1 0 0 0 0 0]", D, Db),
+                                              ("sigma", 6, "[1 -1 -2 0 0 0 0]", sig, None),
+                                              ("sigmaEq", 1, "[1 -1 -2 0 0 0 0]", seq, None)):
+            _lib.check(L.s4g_foam_write_field(h, out.encode(), name.encode(), width, dims.encode(),
+                                              cells.ctypes.data,
+                                              None if bnd is None else bnd.ctypes.data),
+                       "s4g_foam_write_field")
+    finally:
+        L.s4g_foam_free(h)

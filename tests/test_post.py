@@ -96,3 +96,54 @@ def test_derived_fields():
     # uniaxial stress and pure shear
     s, _, _ = derived_fields(np.array([[7.0, 0, 0, 0, 0, 0], [0, 2.0, 0, 0, 0, 0]]))
     np.testing.assert_allclose(s, [7.0, 2.0 * np.sqrt(3.0)], rtol=1e-15)
+
+
+def _field_lists(path):
+    """(internalField rows, {patch: rows}) of an ASCII vol field written by
+    s4g_foam_write_field."""
+    import re
+    text = open(path).read()
+
+    def rows(block):
+        n, body = re.match(r"\s*(\d+)\s*\((.*)\)\s*$", block, re.S).groups()
+        vals = [list(map(float, r.strip("()").split())) for r in body.strip().splitlines()]
+        assert len(vals) == int(n)
+        return np.array(vals)
+
+    internal = re.search(r"internalField\s+nonuniform List<\w+>(.*?)\n;", text, re.S).group(1)
+    patches = {m.group(1): rows(m.group(2)) for m in re.finditer(
+        r"\n    (\w+)\n    \{\n        type            calculated;\n        value           "
+        r"nonuniform List<\w+>(.*?)\n;", text, re.S)}
+    return rows(internal), patches
+
+
+def test_written_fields(tmp_path):
+    """D, sigma and sigmaEq written into a time directory: cell values as
+    given; on the patches the prescribed displacement (fixedDisplacement)
+    or, elsewhere, the gradient-extrapolated value -- exact for a linear
+    field -- and the adjacent cell's stress."""
+    from solids4foam_gb300.foam_case import write_box_case, write_results
+    m = box_polymesh(4, 3, 3, 1.0, 0.9, 0.8, 0.2, 5)
+    write_box_case(str(tmp_path / "constant" / "polyMesh"), m)
+    (tmp_path / "0").mkdir()
+    free = "{ type solidTraction; traction uniform (0 0 0); pressure uniform 0; }"
+    (tmp_path / "0" / "D").write_text(
+        "FoamFile { version 2.0; format ascii; class volVectorField; object D; }\n"
+        f"boundaryField {{ xmin {free} xmax {free} ymin {free} ymax {free} zmax {free}\n"
+        "  zmin { type fixedDisplacement; value uniform (0 0 1e-3); } }\n")
+    D = A + m["C"] @ B.T
+    G = np.broadcast_to(B.T.reshape(9), (len(D), 9))
+    sig = np.random.default_rng(1).normal(size=(len(D), 6))
+    write_results(str(tmp_path), "1", D, sig, G)
+    cells, patches = _field_lists(str(tmp_path / "1" / "D"))
+    np.testing.assert_allclose(cells, D, rtol=1e-11, atol=1e-20)
+    for p, name in enumerate(m["patch_names"]):
+        s, n = int(m["patch_start"][p]), int(m["patch_size"][p])
+        want = (np.tile([0, 0, 1e-3], (n, 1)) if name == "zmin" else A + m["Cf"][s:s + n] @ B.T)
+        np.testing.assert_allclose(patches[name], want, rtol=1e-11, atol=1e-20)
+    cells, patches = _field_lists(str(tmp_path / "1" / "sigma"))
+    np.testing.assert_allclose(cells, sig, rtol=1e-11)
+    s, n = int(m["patch_start"][5]), int(m["patch_size"][5])
+    np.testing.assert_allclose(patches["zmax"], sig[m["owner"][s:s + n]], rtol=1e-11)
+    cells, _ = _field_lists(str(tmp_path / "1" / "sigmaEq"))
+    np.testing.assert_allclose(cells[:, 0], derived_fields(sig)[0], rtol=1e-11)
