@@ -1143,7 +1143,10 @@ s4g_status s4g_foam_write_field(const s4g_foam_case* m, const char* dir, const c
                "// Boundary values: %s.\n\n"
                "dimensions      %s;\n\ninternalField   nonuniform List<%s>\n%d\n(\n",
                cls, time.c_str(), name,
-               boundary_values ? "as given by the writer" : "those of the adjacent cells",
+               boundary_values ? "supplied with the field (for D from s4g_foam_boundary_D: the "
+                                 "prescribed value on fixedDisplacement patches, elsewhere the "
+                                 "cell value extrapolated with its gradient)"
+                               : "those of the adjacent cells",
                dimensions ? dimensions : "[0 0 0 0 0 0 0]", list, m->nCells);
   for (int c = 0; c < m->nCells; ++c) value(cell_values + (size_t)width * c);
   std::fputs(")\n;\n\nboundaryField\n{\n", f);
