@@ -66,6 +66,11 @@ struct FoamError {
 
 [[noreturn]] void fail(const std::string& msg) { throw FoamError{msg}; }
 
+// A uniform list `N{v}` is expanded item by item, so its size is bounded
+// (2^28 items) before anything is stored: a corrupt count must not take
+// the host's memory.
+constexpr long kMaxUniform = 1L << 28;
+
 // ------------------------------------------------------------- tokens ---
 
 struct Tok {
@@ -265,6 +270,7 @@ void parseList(Cursor& c, Item item) {
   if (isInteger(c.peek())) n = toLong(c.next(), c.where);
   if (c.peek().is('{')) {
     if (n < 0) fail(c.where + ": a uniform list needs a size");
+    if (n > kMaxUniform) fail(c.where + ": uniform list of " + std::to_string(n) + " items is too long");
     c.next();
     size_t at = c.p;
     for (long i = 0; i < n; ++i) {
@@ -418,6 +424,7 @@ void scanList(Scan& s, Item item) {
   if (s.peek() >= '0' && s.peek() <= '9') n = s.integer();
   if (s.peek() == '{') {
     if (n < 0) fail(s.where + ": a uniform list needs a size");
+    if (n > kMaxUniform) fail(s.where + ": uniform list of " + std::to_string(n) + " items is too long");
     ++s.p;
     const char* at = s.p;
     for (long i = 0; i < n; ++i) {

@@ -381,3 +381,36 @@ def test_case_controls_refusals(tmp_path, part, text, match):
     from solids4foam_gb300.foam_case import read_controls
     with pytest.raises(_lib.S4GError, match=match):
         read_controls(_controls_case(tmp_path, **{part: text}))
+
+
+def test_corrupt_case_files_are_errors(tmp_path):
+    """Truncated or corrupted case files (seeded) end in S4GError or in a
+    valid read, never in a crash; a uniform list with an absurd count is
+    refused before it is expanded."""
+    import random
+    import shutil
+    rng = random.Random(11)
+    files = ("constant/polyMesh/points", "constant/polyMesh/faces", "constant/polyMesh/owner",
+             "constant/polyMesh/neighbour", "constant/polyMesh/boundary", "0/D")
+    for k in range(120):
+        rel = files[k % len(files)]
+        d = tmp_path / f"c{k}"
+        shutil.copytree(PRISMS, d)
+        text = (d / rel).read_text()
+        if k % 2:
+            text = text[:rng.randrange(len(text))]
+        else:
+            chars = list(text)
+            for _ in range(rng.randint(1, 4)):
+                chars[rng.randrange(len(chars))] = rng.choice('(){};0123456789-e. \n"/*')
+            text = "".join(chars)
+        (d / rel).write_text(text)
+        try:
+            read_case(str(d))
+        except _lib.S4GError:
+            pass
+    d = tmp_path / "huge"
+    shutil.copytree(PRISMS, d)
+    (d / "constant" / "polyMesh" / "neighbour").write_text("2000000000{1}\n")
+    with pytest.raises(_lib.S4GError, match="too long"):
+        read_case(str(d))
