@@ -294,3 +294,40 @@ def write_results(case_dir: str, time: str, D, sigma, gradD, polymesh: str = "co
                        "s4g_foam_write_field")
     finally:
         L.s4g_foam_free(h)
+
+
+def read_time(case_dir: str):
+    """(startTime, endTime, deltaT) of system/controlDict."""
+    t0, t1, dt = ct.c_double(), ct.c_double(), ct.c_double()
+    _lib.check(_lib.lib().s4g_foam_read_time(
+        os.path.join(case_dir, "system", "controlDict").encode(), ct.byref(t0), ct.byref(t1),
+        ct.byref(dt)), "s4g_foam_read_time")
+    return t0.value, t1.value, dt.value
+
+
+def load_case(case_dir: str):
+    """Everything a solve of a meshed case needs, resolved as the C++ driver
+    resolves it: dict(mesh, bcs, model, law, solver, outer, n_increments).
+    The model, law and controls come from the case's dictionaries; a total
+    Lagrangian case whose loads ramp from zero runs one increment per
+    controlDict time step.  Raises for what is not built: relaxation
+    factors on the solved field, constant loads beside a ramp (total
+    Lagrangian), and everything the readers refuse."""
+    mesh, bcs = read_case(case_dir)
+    c = read_controls(case_dir)
+    tl = c["model"] != "linearGeometryTotalDisplacement"
+    if os.path.exists(os.path.join(case_dir, "system", "fvSolution")):
+        field = "DD" if c["model"] == "nonLinearGeometryTotalLagrangian" else "D"
+        ff, ef = read_relaxation(case_dir, field)
+        if ff != 1.0 or ef != 1.0:
+            raise ValueError(f"relaxationFactors for {field} (field {ff:g}, equation {ef:g}) "
+                             "are not built on the GPU path")
+    n_inc = 1
+    if tl and mesh.get("load_ramp_end"):
+        if mesh.get("constant_loads_beside_ramp"):
+            raise ValueError("constant loads beside load series are not built for the total "
+                             "Lagrangian models")
+        if os.path.exists(os.path.join(case_dir, "system", "controlDict")):
+            t0, t1, dt = read_time(case_dir)
+            n_inc = max(1, int(round((t1 - t0) / dt)))
+    return dict(mesh=mesh, bcs=bcs, n_increments=n_inc, **c)

@@ -147,6 +147,18 @@ class SolidModel:
             self.set_bc(names.index(name), *spec)
         self.set_controls(solver or {}, outer or {}, precision)
 
+    @classmethod
+    def from_case(cls, ctx: "Context", case_dir: str, **kw):
+        """A model of a meshed OpenFOAM case directory (foam_case.load_case):
+        returns (model, n_increments) for model.evolve(n_increments).
+        Keyword arguments (precision, renumber, part_size, ...) are passed
+        on to the constructor."""
+        from .foam_case import load_case
+        c = load_case(case_dir)
+        model = cls(ctx, c["mesh"], c["law"], c["bcs"], model=c["model"], solver=c["solver"],
+                    outer=c["outer"], **kw)
+        return model, c["n_increments"]
+
     def close(self):
         if self.h and self.ctx.h:
             self.L.s4g_mesh_destroy(self.h)

@@ -129,3 +129,26 @@ def test_controls_come_from_the_case(tmp_path):
     assert out["increments"] == 20                 # the traction ramp over 10 / 0.5
     out = json.loads(run(case, "--plan-only", "--nCorrectors", "50", "--mu", "1e6").stdout)
     assert (out["nCorrectors"], out["mu"]) == (50, 1e6)
+
+
+def test_python_load_case_matches_the_driver(tmp_path):
+    """foam_case.load_case resolves a case as the C++ driver does."""
+    from solids4foam_gb300.foam_case import load_case
+    case = _ramp_case(tmp_path)
+    head = "FoamFile { version 2.0; format ascii; class dictionary; object x; }\n"
+    (tmp_path / "constant" / "solidProperties").write_text(
+        head + "solidModel nonLinearGeometryTotalLagrangian;\n")
+    (tmp_path / "constant" / "mechanicalProperties").write_text(
+        head + "planeStress no;\nmechanical ( r { type neoHookeanElastic; mu 2e6; K 3e7; } );\n")
+    (tmp_path / "system" / "fvSolution").write_text(
+        head + 'solvers { "D|DD" { solver PCG; preconditioner DIC; tolerance 1e-8; relTol 0.2; } }\n')
+    c = load_case(case)
+    drv = json.loads(run(case, "--plan-only").stdout)
+    assert c["model"] == drv["model"] and c["n_increments"] == drv["increments"] == 20
+    assert c["law"] == dict(type="neoHookeanElastic", mu=2e6, K=3e7)
+    assert c["bcs"]["zmax"][0] == "solidTraction" and list(c["bcs"]["zmax"][1][0]) == [0, 0, -1e5]
+    (tmp_path / "system" / "fvSolution").write_text(
+        head + 'solvers { "D|DD" { solver PCG; preconditioner DIC; } }\n'
+        'relaxationFactors { fields { DD 0.8; } }\n')
+    with pytest.raises(ValueError, match="relaxationFactors for DD"):
+        load_case(case)
