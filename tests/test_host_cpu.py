@@ -136,7 +136,8 @@ def test_no_device_is_reported_without_gpu(built):
 
 def test_ctypes_structs_match_the_c_header(tmp_path):
     """Every ctypes mirror has the size and field offsets of its C struct
-    (compiled against include/s4g.h with the host C compiler)."""
+    (compiled against include/s4g.h with the host C compiler, as strict
+    C99)."""
     import ctypes as ct
     import shutil
     import subprocess
@@ -157,7 +158,9 @@ def test_ctypes_structs_match_the_c_header(tmp_path):
     src = tmp_path / "layout.c"
     src.write_text("\n".join(lines) + "\n")
     exe = tmp_path / "layout"
-    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    # the header is plain C: strict C99 with every warning an error
+    subprocess.run([cc, "-std=c99", "-pedantic", "-Wall", "-Wextra", "-Werror", "-I",
+                    os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
     got = {}
     for ln in out.splitlines():
