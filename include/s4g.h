@@ -437,6 +437,21 @@ s4g_status s4g_point_cells(int n_points, int n_faces, const int* face_start,
 s4g_status s4g_point_interpolate(int n_points, const double* points, const int* point_cell_start,
                                  const int* point_cells, int n_cells, const double* C,
                                  const double* D, const double* gradD, double* pointD);
+/* tractionBoundarySnGrad of the three models on the host, for a drop-in's
+ * own override (boundary evaluations outside evolve(); inside s4g_solve the
+ * same formula runs on the device): per face
+ *   g = ((t - n_c p) - n_c . sigma_b + impK n . gradD_b) / impK,
+ * with n_c = n for linear geometry (linGeomTotalDispSolid.C:235-271, whose
+ * n . (sigma_b - impK gradD_b) is the same expression) and for an enforced
+ * linear geometry, and n_c = Finv^T n / |Finv^T n| for the total Lagrangian
+ * forms (nonLinGeomTotalLagSolid.C:263-325,
+ * nonLinGeomTotalLagTotalDispSolid.C:284-328; gradD_b is then grad(DD) or
+ * grad(D)).  traction [n][3] and pressure [n] may be NULL (zero);
+ * normal [n][3]; sigma_b [n][6]; gradD_b, Finv_b [n][9] (Finv_b NULL:
+ * n_c = n); g_out [n][3]. */
+s4g_status s4g_traction_sngrad(int n_faces, const double* traction, const double* pressure,
+                               const double* normal, const double* sigma_b, const double* gradD_b,
+                               const double* Finv_b, double impK, double* g_out);
 /* solidModel::writeFields (solidModel.C:1936-1962): sigmaEq [n] =
  * sqrt(3/2 |dev sigma|^2); epsilon [n][6] = symm(gradD) and epsilonEq [n]
  * = sqrt(2/3 |dev epsilon|^2) (written by the reference for the

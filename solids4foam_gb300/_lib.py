@@ -163,6 +163,9 @@ _SIGS = {
                                          ct.c_void_p]),
     "s4g_derived_fields": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
                                       ct.c_void_p, ct.c_void_p]),
+    "s4g_traction_sngrad": (ct.c_int, [ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p,
+                                       ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_double,
+                                       ct.c_void_p]),
     "s4g_foam_read_mesh": (ct.c_int, [ct.c_char_p, ct.POINTER(ct.c_void_p)]),
     "s4g_foam_mesh_desc": (ct.c_int, [ct.c_void_p, ct.POINTER(MeshDesc), ct.POINTER(ct.c_int)]),
     "s4g_foam_mesh_points": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_void_p),

@@ -7,6 +7,7 @@
 //    extrapolated from the cell centre with the cell gradient,
 //        pointD_p = sum_c w_pc (D_c + (x_p - C_c) . gradD_c) / sum_c w_pc,
 //        w_pc = 1 / |x_p - C_c|;
+//  * tractionBoundarySnGrad, for boundary evaluations outside evolve();
 //  * the derived fields of solidModel::writeFields (solidModel.C:1936-1962):
 //    epsilon = symm(gradD), epsilonEq = sqrt(2/3 |dev epsilon|^2),
 //    sigmaEq = sqrt(3/2 |dev sigma|^2).
@@ -92,6 +93,35 @@ s4g_status s4g_point_interpolate(int n_points, const double* points, const int* 
     }
     // normalised where the weight sum exceeds OpenFOAM's ROOTVSMALL
     for (int j = 0; j < 3; ++j) pointD[3 * (size_t)p + j] = sumW > 1e-150 ? acc[j] / sumW : acc[j];
+  }
+  return S4G_OK;
+}
+
+s4g_status s4g_traction_sngrad(int n_faces, const double* traction, const double* pressure,
+                               const double* normal, const double* sigma_b, const double* gradD_b,
+                               const double* Finv_b, double impK, double* g_out) {
+  if (n_faces < 0 || !normal || !sigma_b || !gradD_b || !g_out || !(impK > 0))
+    return bad("s4g_traction_sngrad: bad arguments");
+  for (int f = 0; f < n_faces; ++f) {
+    const double* n = normal + 3 * (size_t)f;
+    const double* s = sigma_b + 6 * (size_t)f;
+    const double* G = gradD_b + 9 * (size_t)f;
+    double nc[3] = {n[0], n[1], n[2]};
+    if (Finv_b) {  // deformed normal Finv^T & n, normalised
+      const double* Fi = Finv_b + 9 * (size_t)f;
+      for (int j = 0; j < 3; ++j) nc[j] = n[0] * Fi[j] + n[1] * Fi[3 + j] + n[2] * Fi[6 + j];
+      const double m = std::sqrt(nc[0] * nc[0] + nc[1] * nc[1] + nc[2] * nc[2]);
+      if (!(m > 0)) return bad("s4g_traction_sngrad: degenerate deformed normal");
+      for (double& v : nc) v /= m;
+    }
+    const double S[3][3] = {{s[0], s[1], s[2]}, {s[1], s[3], s[4]}, {s[2], s[4], s[5]}};
+    const double p = pressure ? pressure[f] : 0.0;
+    for (int j = 0; j < 3; ++j) {
+      const double t = traction ? traction[3 * (size_t)f + j] : 0.0;
+      const double ncSig = nc[0] * S[0][j] + nc[1] * S[1][j] + nc[2] * S[2][j];
+      const double nG = n[0] * G[j] + n[1] * G[3 + j] + n[2] * G[6 + j];
+      g_out[3 * (size_t)f + j] = ((t - nc[j] * p) - ncSig + impK * nG) / impK;
+    }
   }
   return S4G_OK;
 }

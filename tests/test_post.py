@@ -147,3 +147,39 @@ def test_written_fields(tmp_path):
     np.testing.assert_allclose(patches["zmax"], sig[m["owner"][s:s + n]], rtol=1e-11)
     cells, _ = _field_lists(str(tmp_path / "1" / "sigmaEq"))
     np.testing.assert_allclose(cells[:, 0], derived_fields(sig)[0], rtol=1e-11)
+
+
+def test_traction_sngrad_on_the_host():
+    """s4g_traction_sngrad against the reference's formulas restated in
+    numpy: the linear form ((t - n p) - n.(sigma - impK gradD)) / impK and
+    the total Lagrangian form with the deformed normal Finv^T n."""
+    import ctypes as ct
+    from solids4foam_gb300 import _lib
+    rng = np.random.default_rng(3)
+    nf, impK = 7, 3.5e9
+    t = rng.normal(size=(nf, 3)) * 1e6
+    p = rng.normal(size=nf) * 1e5
+    n = rng.normal(size=(nf, 3))
+    n /= np.linalg.norm(n, axis=1)[:, None]
+    s6 = rng.normal(size=(nf, 6)) * 1e6
+    G = rng.normal(size=(nf, 3, 3)) * 1e-3
+    F = np.eye(3) + 0.1 * rng.normal(size=(nf, 3, 3))
+    Fi = np.linalg.inv(F)
+    S = np.array([[[a[0], a[1], a[2]], [a[1], a[3], a[4]], [a[2], a[4], a[5]]] for a in s6])
+
+    def call(Finv):
+        out = np.zeros((nf, 3))
+        args = [np.ascontiguousarray(a) for a in (t, p, n, s6, G.reshape(nf, 9))]
+        fi = None if Finv is None else np.ascontiguousarray(Finv.reshape(nf, 9))
+        assert _lib.lib().s4g_traction_sngrad(nf, *[a.ctypes.data for a in args],
+                                              None if fi is None else fi.ctypes.data,
+                                              ct.c_double(impK), out.ctypes.data) == _lib.OK
+        return out
+
+    lin = np.einsum("fi,fij->fj", n, S - impK * G)
+    np.testing.assert_allclose(call(None), ((t - n * p[:, None]) - lin) / impK, rtol=1e-12, atol=1e-18)
+    nc = np.einsum("fij,fi->fj", Fi, n)            # Finv^T & n
+    nc /= np.linalg.norm(nc, axis=1)[:, None]
+    tl = ((t - nc * p[:, None]) - np.einsum("fi,fij->fj", nc, S)
+          + impK * np.einsum("fi,fij->fj", n, G)) / impK
+    np.testing.assert_allclose(call(Fi), tl, rtol=1e-12, atol=1e-18)
