@@ -357,3 +357,45 @@ def test_homogeneous_finite_deformation(model):
     assert p["converged"] == 1 and p["enforce_linear"] == 0
     assert np.abs(D - m["C"] @ (F - np.eye(3)).T).max() < 1e-7
     assert np.abs(sig - expected).max() < 1e-6 * np.abs(expected).max()
+
+
+def test_pressurised_cylinder_readme_stresses(tmp_path):
+    """The reference's pressurisedCylinder case (tutorials/solids/
+    linearElasticity/pressurisedCylinder/README.md: r_i = 7 m, R_o =
+    18.625 m, E = 10 GPa, nu = 0.3, p = 10 MPa in its plot script, 30 cells
+    radially) against the analytical stresses that README gives,
+    sigma_r = p r_i^2/(R_o^2 - r_i^2) (1 - R_o^2/r^2) and sigma_theta with
+    (1 + R_o^2/r^2).  Those hold for plane stress and plane strain alike;
+    the full annulus here is in plane strain (exact displacement on the
+    outer wall and the end faces).  At the README's resolution the cell
+    stresses agree to 1% (L2), and halving the cells improves them."""
+    from solids4foam_gb300.foam_case import annulus_polymesh, read_case, write_polymesh
+    a, b, E, nu, p, h = 7.0, 18.625, 10e9, 0.3, 10e6, 0.5
+
+    def u_exact(X):
+        r = np.hypot(X[:, 0], X[:, 1])
+        ur = p * a ** 2 * (1 + nu) * ((1 - 2 * nu) * r + b ** 2 / r) / (E * (b ** 2 - a ** 2))
+        return np.stack([ur * X[:, 0] / r, ur * X[:, 1] / r, 0 * r], axis=1)
+
+    err = []
+    for nr, nt in ((15, 60), (30, 120)):
+        case = tmp_path / f"c{nr}"
+        write_polymesh(str(case / "constant" / "polyMesh"), **annulus_polymesh(nr, nt, 1, a, b, h))
+        m, _ = read_case(str(case), d_file=None)
+        bcs = []
+        for k in range(4):
+            s, n = int(m["patch_start"][k]), int(m["patch_size"][k])
+            bcs.append((1, None, np.full(n, p)) if k == 0 else (0, u_exact(m["Cf"][s:s + n]), None))
+        _, sig, _, pf = pyoracle.solve(m, bcs, E=E, nu=nu, n_correctors=20000, solution_tol=1e-9,
+                                       alternative_tol=1e-10)
+        assert pf["converged"] == 1
+        r = np.hypot(m["C"][:, 0], m["C"][:, 1])
+        c, s_ = m["C"][:, 0] / r, m["C"][:, 1] / r
+        sr = sig[:, 0] * c * c + 2 * sig[:, 1] * c * s_ + sig[:, 3] * s_ * s_
+        st = sig[:, 0] * s_ * s_ - 2 * sig[:, 1] * c * s_ + sig[:, 3] * c * c
+        k0 = p * a ** 2 / (b ** 2 - a ** 2)
+        er = np.linalg.norm(sr - k0 * (1 - b ** 2 / r ** 2)) / np.linalg.norm(k0 * (1 - b ** 2 / r ** 2))
+        et = np.linalg.norm(st - k0 * (1 + b ** 2 / r ** 2)) / np.linalg.norm(k0 * (1 + b ** 2 / r ** 2))
+        err.append((er, et))
+    assert err[1][0] < 0.01 and err[1][1] < 0.005
+    assert err[1][0] < 0.5 * err[0][0] and err[1][1] < 0.5 * err[0][1]
