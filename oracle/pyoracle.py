@@ -56,7 +56,7 @@ class Settings(ct.Structure):
         ("ls_boundary_delta", ct.c_int), ("n_increments", ct.c_int),
         ("n_threads", ct.c_int), ("max_correctors_run", ct.c_int),
         ("dic_domain", ct.c_void_p), ("max_seconds", ct.c_double),
-        ("field_relaxation", ct.c_double),
+        ("empty_direction", ct.c_int), ("field_relaxation", ct.c_double),
     ]
 
 

@@ -178,10 +178,10 @@ struct Mesh {
   std::vector<int> cfStart, cfFace, cbStart, cbFace;
   std::vector<int> newOfCaller;  // caller cell -> solver cell
 
-  bool build(const orc_mesh_desc* d, const int* perm, int lsBoundaryDelta);
+  bool build(const orc_mesh_desc* d, const int* perm, int lsBoundaryDelta, int emptyDir = 0);
 };
 
-bool Mesh::build(const orc_mesh_desc* d, const int* perm, int lsBoundaryDelta) {
+bool Mesh::build(const orc_mesh_desc* d, const int* perm, int lsBoundaryDelta, int emptyDir) {
   nC = d->n_cells; nF = d->n_faces; nI = d->n_internal_faces; nB = nF - nI;
   if (nC <= 0 || nI < 0 || nB < 0) return false;
   std::vector<int> newOf(nC);
@@ -292,8 +292,17 @@ bool Mesh::build(const orc_mesh_desc* d, const int* perm, int lsBoundaryDelta) {
     }
     dd[c] = acc;
   }
+  // In a 2-D mesh dd has no component along the empty direction: as
+  // OpenFOAM's inv(symmTensorField) does, add 1 there, invert, and take the
+  // 1 away again, so the gradient has no derivative across it.
+  auto addEmpty = [emptyDir](S6 s, double v) {
+    if (emptyDir == 1) s.xx += v;
+    else if (emptyDir == 2) s.yy += v;
+    else if (emptyDir == 3) s.zz += v;
+    return s;
+  };
   std::vector<S6> invDd(nC);
-  for (int c = 0; c < nC; ++c) invDd[c] = invS(dd[c]);
+  for (int c = 0; c < nC; ++c) invDd[c] = addEmpty(invS(addEmpty(dd[c], 1.0)), -1.0);
   lsP.resize(nI); lsN.resize(nI); lsB.resize(nB);
   for (int f = 0; f < nI; ++f) {
     V3 dl = C[nei[f]] - C[own[f]];
@@ -777,6 +786,9 @@ struct Solver {
       double r2 = 0;
       maxIters = 0;
       for (int cmpt = 0; cmpt < 3; ++cmpt) {
+        // the empty direction's component is not solved (fvMatrix solves
+        // only the mesh's solution directions)
+        if (cmpt + 1 == s.empty_direction) continue;
         for (int c = 0; c < m.nC; ++c) {
           bc[c] = cmpt == 0 ? src[c].x : cmpt == 1 ? src[c].y : src[c].z;
           xc[c] = cmpt == 0 ? U[c].x : cmpt == 1 ? U[c].y : U[c].z;
@@ -950,7 +962,8 @@ int orc_solve(const orc_mesh_desc* md, const orc_bc* bcs, const orc_settings* s,
               double* gradD_out, orc_perf* perf) {
   if (!md || !bcs || !validSettings(s)) return 1;
   Mesh m;
-  if (!m.build(md, perm, s->ls_boundary_delta)) return 2;
+  if (s->empty_direction < 0 || s->empty_direction > 3) return 1;
+  if (!m.build(md, perm, s->ls_boundary_delta, s->empty_direction)) return 2;
   auto t0 = std::chrono::steady_clock::now();
   Solver sol(m, *s, bcs);
   sol.run();

@@ -74,6 +74,11 @@ typedef struct {
                              order): DIC restricted to each subdomain */
   double max_seconds;     /* >0: stop after the corrector that passes this wall
                              time (bounded timing samples) */
+  int empty_direction;    /* 2-D cases (empty patches, whose faces the caller
+                             leaves out of the mesh): 1, 2 or 3 for x, y or z;
+                             0: 3-D.  The leastSquares tensor is inverted with
+                             OpenFOAM's treatment of the empty direction and
+                             that displacement component is not solved */
   double field_relaxation; /* fvSolution relaxationFactors { fields { "D|DD" f; } }:
                              after each solve D == D.prevIter + f (D - D.prevIter),
                              cells and boundary faces (solidModel.C:837-841,
