@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define S4G_ABI_VERSION 3
+#define S4G_ABI_VERSION 4
 
 /* Status codes.  Reference convention for errors is FatalError (abort), see
  * src/solids4FoamModels/solidModels/solidModel/solidModel.C:1735-1742; a
@@ -134,6 +134,14 @@ typedef struct s4g_mesh_opts {
   int no_autotune;        /* 1: skip the kernel-variant autotuner of the
                              processor-local PCG (results are identical
                              either way; only the speed differs) */
+  int empty_direction;    /* 2-D cases: 1, 2 or 3 for an x, y or z empty
+                             direction, whose empty patches' faces the caller
+                             leaves out of the mesh description (they have no
+                             faces in OpenFOAM's discretisation either).  The
+                             leastSquares tensor is inverted as OpenFOAM's
+                             inv() does with an empty direction, and that
+                             displacement component is not solved (plane
+                             strain).  0: 3-D. */
 } s4g_mesh_opts;
 
 typedef struct s4g_mesh s4g_mesh;
@@ -568,14 +576,27 @@ s4g_status s4g_foam_boundary_D(const s4g_foam_case* fc, const double* D, const d
 s4g_status s4g_foam_write_field(const s4g_foam_case* fc, const char* dir, const char* name,
                                 int width, const char* dimensions, const double* cell_values,
                                 const double* boundary_values);
-/* Writes an ASCII polyMesh (points, faces, owner, neighbour, boundary with
- * patch type "patch") into an existing directory; face f has the points
- * face_points[face_start[f] .. face_start[f+1]). */
+/* Writes an ASCII polyMesh (points, faces, owner, neighbour, boundary) into
+ * an existing directory; face f has the points
+ * face_points[face_start[f] .. face_start[f+1]); patch_types (NULL, or a
+ * NULL entry: "patch") names each patch's type, e.g. "empty". */
 s4g_status s4g_foam_write_mesh(const char* polymesh_dir, int n_points, const double* points,
                                int n_faces, const int* face_start, const int* face_points,
                                int n_internal_faces, const int* owner, const int* neighbour,
                                int n_patches, const char* const* patch_names,
-                               const int* patch_start, const int* patch_size);
+                               const int* patch_start, const int* patch_size,
+                               const char* const* patch_types);
+/* 2-D cases: a polyMesh with `empty` patches is read without their faces
+ * (they have none in OpenFOAM's discretisation either); every s4g_foam_*
+ * patch index, the s4g_mesh_desc and the faces then refer to the mesh
+ * without them.  This is the empty direction (1, 2, 3: x, y, z) to pass as
+ * s4g_mesh_opts.empty_direction; 0 for a 3-D mesh.  The empty patches must
+ * be normal to an axis, one cell across. */
+int s4g_foam_empty_direction(const s4g_foam_case* fc);
+/* Writes <dir>/<name> as an ASCII pointVectorField (values [n_points][3],
+ * patches calculated, empty patches empty). */
+s4g_status s4g_foam_write_point_field(const s4g_foam_case* fc, const char* dir, const char* name,
+                                      const char* dimensions, const double* values);
 
 #ifdef __cplusplus
 }

@@ -45,7 +45,7 @@ class MeshDesc(ct.Structure):
 class MeshOpts(ct.Structure):
     _fields_ = [("renumber", ct.c_int), ("part_size", ct.c_int),
                 ("ls_boundary_delta", ct.c_int), ("dic_subdomains", ct.c_int),
-                ("no_autotune", ct.c_int)]
+                ("no_autotune", ct.c_int), ("empty_direction", ct.c_int)]
 
 
 class MeshInfo(ct.Structure):
@@ -190,7 +190,10 @@ _SIGS = {
                                         ct.c_char_p, ct.c_void_p, ct.c_void_p]),
     "s4g_foam_write_mesh": (ct.c_int, [ct.c_char_p, ct.c_int, ct.c_void_p, ct.c_int, ct.c_void_p,
                                        ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_int,
-                                       ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+                                       ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "s4g_foam_empty_direction": (ct.c_int, [ct.c_void_p]),
+    "s4g_foam_write_point_field": (ct.c_int, [ct.c_void_p, ct.c_char_p, ct.c_char_p, ct.c_char_p,
+                                              ct.c_void_p]),
 }
 
 _lib = None

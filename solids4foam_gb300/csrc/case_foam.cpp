@@ -9,7 +9,8 @@
 //   fixedDisplacement  value                       (fixedDisplacementFvPatchVectorField.C:156-186)
 //   solidTraction      traction, pressure,         (solidTractionFvPatchVectorField.C:58-209)
 //                      relaxationFactor
-// and rejects everything else by name.
+// and rejects everything else by name.  A polyMesh with `empty` patches is
+// read as a 2-D mesh without their faces (s4g_foam_empty_direction).
 //
 // Format handled: a FoamFile header dictionary (format ascii), C and C++
 // comments, dictionaries `key value;` and `key { ... }`, lists `N ( ... )`,
@@ -43,6 +44,11 @@ struct s4g_foam_case {
   std::vector<std::string> patchName, patchType;
   std::vector<std::vector<std::string>> patchGroups;  // inGroups
   std::vector<int> patchStart, patchSize;
+  // 2-D: the empty patches' faces are taken out of the mesh above (as they
+  // have no faces in OpenFOAM's discretisation); their names stay for the
+  // writers, and emptyDir (1, 2, 3: x, y, z; 0: 3-D) is their normal
+  std::vector<std::string> emptyPatches;
+  int emptyDir = 0;
   // D boundary conditions, per patch
   struct Bc {
     bool set = false;
@@ -455,6 +461,73 @@ std::vector<int> scanLabels(Scan& s) {
 
 // ----------------------------------------------------------- polyMesh ---
 
+// 2-D meshes: the faces of `empty` patches leave the mesh (the cell centres
+// and volumes are already those of the closed cells).  The empty patches
+// must be normal to x, y or z, and every cell must have two such faces
+// (one cell across the empty direction), as OpenFOAM requires.
+void takeOutEmptyPatches(s4g_foam_case& m, const std::string& where) {
+  std::vector<char> isEmpty(m.patchName.size(), 0);
+  bool any = false;
+  for (size_t p = 0; p < m.patchName.size(); ++p)
+    if (m.patchType[p] == "empty") isEmpty[p] = 1, any = true;
+  if (!any) return;
+  int dir = 0;
+  std::vector<int> perCell((size_t)m.nCells, 0);
+  for (size_t p = 0; p < m.patchName.size(); ++p) {
+    if (!isEmpty[p]) continue;
+    for (int i = 0; i < m.patchSize[p]; ++i) {
+      const int f = m.patchStart[p] + i;
+      const double* S = &m.Sf[3 * (size_t)f];
+      const double mS = std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+      int k = -1;
+      for (int a = 0; a < 3; ++a)
+        if (mS > 0 && std::fabs(std::fabs(S[a]) / mS - 1.0) < 1e-6) k = a + 1;
+      if (k < 0 || (dir && k != dir))
+        fail(where + ": empty patch " + m.patchName[p] + " is not normal to x, y or z");
+      dir = k;
+      perCell[(size_t)m.owner[(size_t)f]]++;
+    }
+  }
+  for (int c = 0; c < m.nCells; ++c)
+    if (perCell[(size_t)c] != 2)
+      fail(where + ": a 2-D mesh needs one cell across the empty direction (two empty faces per cell)");
+  // compact the faces, keeping the order of the others
+  std::vector<int> owner, faceStart{0}, facePoints, pStart, pSize;
+  std::vector<double> Cf, Sf;
+  std::vector<std::string> names, types;
+  std::vector<std::vector<std::string>> groups;
+  auto keep = [&](int f) {
+    owner.push_back(m.owner[(size_t)f]);
+    for (int k = 0; k < 3; ++k) {
+      Cf.push_back(m.Cf[3 * (size_t)f + k]);
+      Sf.push_back(m.Sf[3 * (size_t)f + k]);
+    }
+    facePoints.insert(facePoints.end(), m.facePoints.begin() + m.faceStart[(size_t)f],
+                      m.facePoints.begin() + m.faceStart[(size_t)f + 1]);
+    faceStart.push_back((int)facePoints.size());
+  };
+  for (int f = 0; f < m.nInt; ++f) keep(f);
+  for (size_t p = 0; p < m.patchName.size(); ++p) {
+    if (isEmpty[p]) {
+      m.emptyPatches.push_back(m.patchName[p]);
+      continue;
+    }
+    pStart.push_back((int)owner.size());
+    pSize.push_back(m.patchSize[p]);
+    names.push_back(m.patchName[p]);
+    types.push_back(m.patchType[p]);
+    groups.push_back(m.patchGroups[p]);
+    for (int i = 0; i < m.patchSize[p]; ++i) keep(m.patchStart[p] + i);
+  }
+  m.owner.swap(owner); m.Cf.swap(Cf); m.Sf.swap(Sf);
+  m.faceStart.swap(faceStart); m.facePoints.swap(facePoints);
+  m.patchStart.swap(pStart); m.patchSize.swap(pSize);
+  m.patchName.swap(names); m.patchType.swap(types); m.patchGroups.swap(groups);
+  m.nFaces = (int)m.owner.size();
+  m.bcs.assign(m.patchName.size(), s4g_foam_case::Bc{});
+  m.emptyDir = dir;
+}
+
 void readMesh(s4g_foam_case& m, const std::string& dir) {
   {  // points
     Scan s(dir + "/points");
@@ -571,6 +644,7 @@ void readMesh(s4g_foam_case& m, const std::string& dir) {
   if (!cellGeometry(m.nCells, m.nFaces, m.nInt, m.owner.data(), m.neighbour.data(), m.Cf.data(),
                     m.Sf.data(), m.C.data(), m.V.data()))
     fail(where + ": a cell has no faces or a volume that is not positive");
+  takeOutEmptyPatches(m, where);
   m.bcs.assign(m.patchName.size(), s4g_foam_case::Bc{});
 }
 
@@ -1172,6 +1246,43 @@ s4g_status s4g_foam_write_field(const s4g_foam_case* m, const char* dir, const c
     }
     std::fputs(")\n;\n    }\n", f);
   }
+  for (const std::string& e : m->emptyPatches)
+    std::fprintf(f, "    %s\n    {\n        type            empty;\n    }\n", e.c_str());
+  std::fputs("}\n", f);
+  if (std::fclose(f) != 0) {
+    s4g::setLastError("cannot write " + path);
+    return S4G_BAD_ARG;
+  }
+  return S4G_OK;
+}
+
+int s4g_foam_empty_direction(const s4g_foam_case* m) { return m ? m->emptyDir : 0; }
+
+s4g_status s4g_foam_write_point_field(const s4g_foam_case* m, const char* dir, const char* name,
+                                      const char* dimensions, const double* values) {
+  if (!m || !dir || !name || !values) return S4G_BAD_ARG;
+  std::string d(dir);
+  while (d.size() > 1 && d.back() == '/') d.pop_back();
+  const std::string time = d.substr(d.find_last_of('/') + 1);
+  const std::string path = d + "/" + name;
+  FILE* f = std::fopen(path.c_str(), "w");
+  if (!f) {
+    s4g::setLastError("cannot write " + path);
+    return S4G_BAD_ARG;
+  }
+  std::fprintf(f,
+               "FoamFile\n{\n    version     2.0;\n    format      ascii;\n"
+               "    class       pointVectorField;\n    location    \"%s\";\n    object      %s;\n}\n\n"
+               "dimensions      %s;\n\ninternalField   nonuniform List<vector>\n%d\n(\n",
+               time.c_str(), name, dimensions ? dimensions : "[0 1 0 0 0 0 0]", m->nPoints);
+  for (int i = 0; i < m->nPoints; ++i)
+    std::fprintf(f, "(%.12g %.12g %.12g)\n", values[3 * (size_t)i], values[3 * (size_t)i + 1],
+                 values[3 * (size_t)i + 2]);
+  std::fputs(")\n;\n\nboundaryField\n{\n", f);
+  for (const std::string& p : m->patchName)
+    std::fprintf(f, "    %s\n    {\n        type            calculated;\n    }\n", p.c_str());
+  for (const std::string& e : m->emptyPatches)
+    std::fprintf(f, "    %s\n    {\n        type            empty;\n    }\n", e.c_str());
   std::fputs("}\n", f);
   if (std::fclose(f) != 0) {
     s4g::setLastError("cannot write " + path);
@@ -1184,7 +1295,7 @@ s4g_status s4g_foam_write_mesh(const char* dir, int n_points, const double* poin
                                const int* face_start, const int* face_points, int n_int,
                                const int* owner, const int* neighbour, int n_patches,
                                const char* const* names, const int* patch_start,
-                               const int* patch_size) {
+                               const int* patch_size, const char* const* types) {
   if (!dir || n_points < 0 || n_faces < 0 || n_int < 0 || n_int > n_faces || n_patches < 0 ||
       !points || !face_start || !face_points || !owner || (n_int > 0 && !neighbour) ||
       (n_patches > 0 && (!names || !patch_start || !patch_size)))
@@ -1213,7 +1324,8 @@ s4g_status s4g_foam_write_mesh(const char* dir, int n_points, const double* poin
     return S4G_BAD_ARG;
   s = std::to_string(n_patches) + "\n(\n";
   for (int p = 0; p < n_patches; ++p)
-    s += std::string("    ") + names[p] + "\n    {\n        type            patch;\n        nFaces          " +
+    s += std::string("    ") + names[p] + "\n    {\n        type            " +
+         (types && types[p] ? types[p] : "patch") + ";\n        nFaces          " +
          std::to_string(patch_size[p]) + ";\n        startFace       " + std::to_string(patch_start[p]) +
          ";\n    }\n";
   s += ")\n";

@@ -18,6 +18,7 @@ constexpr unsigned kErrIndefinite = 4u;
 // Read-only view of the uploaded mesh (storage order), passed by value.
 struct MeshView {
   int nC, nI, nB, nParts, subdomains;
+  int emptyDir;        // 2-D: 1, 2, 3 for an x, y, z empty direction; 0: 3-D
   const int* rowptr; const int* col; const int* fidx;      // CSR, fidx ~f for neighbour side
   const int* fown; const int* fnei;                        // internal faces
   const double* fS; const double* fmagS; const double* fw; const double* fdelta;

@@ -271,6 +271,7 @@ struct Engine {
 
     mv.nC = nC; mv.nI = nI; mv.nB = nB; mv.nParts = hp.nParts;
     mv.subdomains = (o && o->dic_subdomains) ? 1 : 0;
+    mv.emptyDir = o ? o->empty_direction : 0;
     mv.rowGrid = std::max(1, std::min((nC + kRowBlock - 1) / kRowBlock,
                                       ctx->numSMs * kRowBlocksPerSM));
     mv.rowptr = dRow; mv.col = dCol; mv.fidx = dFidx; mv.fown = dFown; mv.fnei = dFnei;

@@ -115,7 +115,18 @@ __global__ void kGeomLs(MeshView mv, GeomOutputs out, const double* bd) {
     S6 wdd = {r * d.x * d.x, r * d.x * d.y, r * d.x * d.z, r * d.y * d.y, r * d.y * d.z, r * d.z * d.z};
     acc = acc + wdd;
   }
-  S6 inv = invS(acc);
+  S6 inv;
+  if (mv.emptyDir) {
+    // 2-D: dd has no component along the empty direction; as OpenFOAM's
+    // inv(symmTensorField) does, add 1 there, invert, take the 1 away
+    const double e[3] = {mv.emptyDir == 1 ? 1.0 : 0.0, mv.emptyDir == 2 ? 1.0 : 0.0,
+                         mv.emptyDir == 3 ? 1.0 : 0.0};
+    const S6 a = {acc.xx + e[0], acc.xy, acc.xz, acc.yy + e[1], acc.yz, acc.zz + e[2]};
+    inv = invS(a);
+    inv.xx -= e[0]; inv.yy -= e[1]; inv.zz -= e[2];
+  } else {
+    inv = invS(acc);
+  }
   stS(out.invDd, s, inv);
   // per CSR entry, oriented so that grad += lsv (x) (U_nb - U_P) on both sides
   for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e) {
@@ -491,6 +502,11 @@ kRhs(MeshView mv, Controls c, FieldPtrs f, T* __restrict__ x, T* __restrict__ r,
         sumA += a;
       }
     }
+    // 2-D: the empty direction's component is not solved (its residual is
+    // zero, so its PCG stops before the first iteration and D keeps 0 there)
+    if (mv.emptyDir == 1) R.x = 0.0;
+    else if (mv.emptyDir == 2) R.y = 0.0;
+    else if (mv.emptyDir == 3) R.z = 0.0;
     stVT(r, s, R);
     stVT(x, s, V3{0, 0, 0});
     const double xb[3] = {st->xbar[0], st->xbar[1], st->xbar[2]};

@@ -174,6 +174,10 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
       return S4G_BAD_ARG;
     }
 
+  if (o && (o->empty_direction < 0 || o->empty_direction > 3)) {
+    err = "empty_direction must be 0 (3-D) or 1, 2, 3 (x, y, z)";
+    return S4G_BAD_ARG;
+  }
   const int renumber = o ? (int)o->renumber : (int)S4G_RENUMBER_TILED;
   int partSize = (o && o->part_size > 0) ? o->part_size : 512;
   partSize = std::max(32, std::min(partSize, 1 << 16));

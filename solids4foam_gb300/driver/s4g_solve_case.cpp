@@ -57,28 +57,6 @@ void check(s4g_status st, const char* what) {
   if (st != S4G_OK) die(what, st);
 }
 
-bool writePointField(const std::string& dir, const std::string& time, const double* v, int n,
-                     const s4g_foam_case* fc, int nPatches) {
-  const std::string tdir = dir + "/" + time;
-  mkdir(tdir.c_str(), 0755);
-  FILE* f = std::fopen((tdir + "/pointD").c_str(), "w");
-  if (!f) return false;
-  std::fprintf(f,
-               "FoamFile\n{\n    version     2.0;\n    format      ascii;\n"
-               "    class       pointVectorField;\n    location    \"%s\";\n"
-               "    object      pointD;\n}\n\ndimensions      [0 1 0 0 0 0 0];\n\n"
-               "internalField   nonuniform List<vector>\n%d\n(\n",
-               time.c_str(), n);
-  for (int i = 0; i < n; ++i)
-    std::fprintf(f, "(%.17g %.17g %.17g)\n", v[3 * i], v[3 * i + 1], v[3 * i + 2]);
-  std::fprintf(f, ")\n;\n\nboundaryField\n{\n");
-  for (int p = 0; p < nPatches; ++p)
-    std::fprintf(f, "    %s\n    {\n        type            calculated;\n    }\n",
-                 s4g_foam_patch_name(fc, p));
-  std::fprintf(f, "}\n");
-  return std::fclose(f) == 0;
-}
-
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -180,6 +158,7 @@ int main(int argc, char** argv) {
   s4g_mesh_desc desc;
   int nPoints = 0;
   check(s4g_foam_mesh_desc(fc, &desc, &nPoints), "s4g_foam_mesh_desc");
+  mo.empty_direction = s4g_foam_empty_direction(fc);  // 2-D: the empty patches' direction
   s4g_mesh_info info;
   check(s4g_mesh_plan(&desc, &mo, nullptr, &info), "s4g_mesh_plan");
   // the boundary conditions (optional for --plan-only) and their load ramp
@@ -228,13 +207,14 @@ int main(int argc, char** argv) {
                 "\"points\": %d, \"patches\": %d, \"parts\": %d, \"part_depth\": %d, "
                 "\"levels\": %d, \"load_ramp_end\": %g, \"increments\": %d, \"model\": \"%s\", "
                 "\"law\": \"%s\", \"E\": %g, \"nu\": %g, \"mu\": %g, \"K\": %g, \"use_mu_K\": %d, "
-                "\"nCorrectors\": %d, \"tolerance\": %g, \"relTol\": %g, \"scaleFactor\": %g}\n",
+                "\"nCorrectors\": %d, \"tolerance\": %g, \"relTol\": %g, \"scaleFactor\": %g, "
+                "\"empty_direction\": %d}\n",
                 caseDir.c_str(), desc.n_cells, desc.n_faces, desc.n_internal_faces, nPoints,
                 desc.n_patches, info.n_parts, info.part_depth, info.n_levels_global, rampEnd,
                 model == S4G_LIN_GEOM_TOTAL_DISP ? 1 : increments, modelName.c_str(),
                 law.type == S4G_LINEAR_ELASTIC ? "linearElastic" : "neoHookeanElastic", law.E,
                 law.nu, law.mu, law.K, law.use_mu_K, outer.n_correctors, lin.tolerance,
-                lin.rel_tol, outer.stab_scale);
+                lin.rel_tol, outer.stab_scale, mo.empty_direction);
     s4g_foam_free(fc);
     return 0;
   }
@@ -288,11 +268,10 @@ int main(int argc, char** argv) {
               perf.n_correctors, perf.total_lin_iters, perf.solve_ms, maxD, maxPD, maxSeq);
   if (!writeTime.empty()) {
     // D, sigma, sigmaEq (solidModel::writeFields) and pointD in <case>/<time>
-    if (!writePointField(caseDir, writeTime, pointD.data(), nPoints, fc, desc.n_patches)) {
-      std::fprintf(stderr, "s4g_solve_case: cannot write %s/%s/pointD\n", caseDir.c_str(), writeTime.c_str());
-      return 2;
-    }
     const std::string tdir = caseDir + "/" + writeTime;
+    mkdir(tdir.c_str(), 0755);
+    check(s4g_foam_write_point_field(fc, tdir.c_str(), "pointD", "[0 1 0 0 0 0 0]", pointD.data()),
+          "writing pointD");
     std::vector<double> Db(3 * (size_t)(desc.n_faces - desc.n_internal_faces));
     check(s4g_foam_boundary_D(fc, D.data(), gradD.data(), Db.data()), "s4g_foam_boundary_D");
     check(s4g_foam_write_field(fc, tdir.c_str(), "D", 3, "[0 1 0 0 0 0 0]", D.data(), Db.data()),

@@ -53,6 +53,7 @@ def read_case(case_dir: str, d_file: str | None = "0/D", polymesh: str = "consta
         mesh["face_start"] = _arr(fs.value, nf + 1, np.int32)
         mesh["face_points"] = _arr(fp.value, int(mesh["face_start"][-1]), np.int32)
         mesh["patch_names"] = [L.s4g_foam_patch_name(h, p).decode() for p in range(npch)]
+        mesh["empty_direction"] = L.s4g_foam_empty_direction(h)
         mesh["patch_types"] = [L.s4g_foam_patch_type(h, p).decode() for p in range(npch)]
         bcs = None
         if d_file is not None:
@@ -78,20 +79,22 @@ def read_case(case_dir: str, d_file: str | None = "0/D", polymesh: str = "consta
 
 
 def write_polymesh(polymesh_dir: str, points, face_start, face_points, owner, neighbour,
-                   patch_names, patch_start, patch_size):
-    """Writes an ASCII polyMesh (all patches of type patch) into
-    polymesh_dir, which is created if needed."""
+                   patch_names, patch_start, patch_size, patch_types=None):
+    """Writes an ASCII polyMesh into polymesh_dir, which is created if
+    needed; patch_types (default all "patch") may name e.g. "empty"."""
     os.makedirs(polymesh_dir, exist_ok=True)
     keep = [np.ascontiguousarray(points, np.float64), np.ascontiguousarray(face_start, np.int32),
             np.ascontiguousarray(face_points, np.int32), np.ascontiguousarray(owner, np.int32),
             np.ascontiguousarray(neighbour, np.int32), np.ascontiguousarray(patch_start, np.int32),
             np.ascontiguousarray(patch_size, np.int32)]
     names = (ct.c_char_p * len(patch_names))(*[n.encode() for n in patch_names])
+    types = None if patch_types is None else (ct.c_char_p * len(patch_types))(
+        *[t.encode() for t in patch_types])
     pts, fs, fp, own, nei, ps, pz = keep
     _lib.check(_lib.lib().s4g_foam_write_mesh(
         polymesh_dir.encode(), pts.shape[0], pts.ctypes.data, fs.shape[0] - 1, fs.ctypes.data,
         fp.ctypes.data, nei.shape[0], own.ctypes.data, nei.ctypes.data, len(patch_names), names,
-        ps.ctypes.data, pz.ctypes.data), "s4g_foam_write_mesh")
+        ps.ctypes.data, pz.ctypes.data, types), "s4g_foam_write_mesh")
 
 
 def box_polymesh(nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=1):

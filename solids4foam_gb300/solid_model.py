@@ -124,7 +124,9 @@ class SolidModel:
                  "linearGeometryTotalDisplacement", solver: dict | None = None,
                  outer: dict | None = None, precision: str = "FP64", renumber: str = "tiled",
                  part_size: int = 512, ls_boundary_delta: int = 0, dic_subdomains: bool = False,
-                 autotune: bool = True):
+                 autotune: bool = True, empty_direction: int = 0):
+        """empty_direction: 1, 2 or 3 for a 2-D case whose empty patches'
+        faces the mesh leaves out (x, y or z empty; plane strain); 0: 3-D."""
         if model not in MODELS:
             raise ValueError(f"unknown solidModel {model!r}; valid: {list(MODELS)}")
         self.ctx = ctx
@@ -135,7 +137,7 @@ class SolidModel:
         keep = []
         d = _desc(mesh, keep)
         opts = _lib.MeshOpts(RENUMBER[renumber], part_size, ls_boundary_delta,
-                             1 if dic_subdomains else 0, 0 if autotune else 1)
+                             1 if dic_subdomains else 0, 0 if autotune else 1, empty_direction)
         h = ct.c_void_p()
         _lib.check(self.L.s4g_mesh_upload(ctx.h, ct.byref(d), ct.byref(opts), ct.byref(h)),
                    "s4g_mesh_upload")
@@ -155,6 +157,7 @@ class SolidModel:
         on to the constructor."""
         from .foam_case import load_case
         c = load_case(case_dir)
+        kw.setdefault("empty_direction", c["mesh"].get("empty_direction", 0))
         model = cls(ctx, c["mesh"], c["law"], c["bcs"], model=c["model"], solver=c["solver"],
                     outer=c["outer"], **kw)
         return model, c["n_increments"]

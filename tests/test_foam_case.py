@@ -202,7 +202,7 @@ def test_bad_arguments_are_errors_not_crashes(tmp_path):
                                  m["points"].ctypes.data, 6, m["face_start"].ctypes.data,
                                  m["face_points"].ctypes.data, 0, m["owner"].ctypes.data, None,
                                  6, names, m["patch_start"].ctypes.data,
-                                 m["patch_size"].ctypes.data) == _lib.BAD_ARG
+                                 m["patch_size"].ctypes.data, None) == _lib.BAD_ARG
 
 
 def test_d_entries_by_group_and_regex(tmp_path):
@@ -414,3 +414,34 @@ def test_corrupt_case_files_are_errors(tmp_path):
     (d / "constant" / "polyMesh" / "neighbour").write_text("2000000000{1}\n")
     with pytest.raises(_lib.S4GError, match="too long"):
         read_case(str(d))
+
+
+def test_two_d_case(tmp_path):
+    """A 2-D case (the cooksMembrane tutorial's set-up with frontAndBack of
+    type empty) reads into the mesh without the empty faces -- bit for bit
+    the mesh the 2-D tests build by hand -- with empty direction 3; the
+    empty patch needs no boundary condition, the writers list it as empty,
+    and the driver plans it as 2-D."""
+    import json
+    import subprocess
+    from cases2d import cooks_membrane, cooks_membrane_case
+    from solids4foam_gb300 import build as b
+    from solids4foam_gb300.foam_case import load_case, write_results
+    case = cooks_membrane_case(tmp_path / "case", 20)
+    c = load_case(case)
+    m = c["mesh"]
+    _, ref = cooks_membrane(tmp_path / "ref", 20)
+    for k in ("owner", "neighbour", "C", "V", "Cf", "Sf", "patch_start", "patch_size"):
+        assert np.array_equal(m[k], ref[k]), k
+    assert m["patch_names"] == ["left", "right", "topAndBottom"] and m["empty_direction"] == 3
+    assert sorted(c["bcs"]) == ["left", "right", "topAndBottom"]
+    assert c["model"] == "linearGeometryTotalDisplacement" and c["solver"]["maxIter"] == 200
+    n = len(m["V"])
+    write_results(case, "1", np.zeros((n, 3)), np.zeros((n, 6)), np.zeros((n, 9)))
+    text = (tmp_path / "case" / "1" / "D").read_text()
+    assert "frontAndBack\n    {\n        type            empty;" in text
+    out = json.loads(subprocess.run([b.build_driver(), case, "--plan-only"], capture_output=True,
+                                    text=True, check=True).stdout)
+    assert out["empty_direction"] == 3 and out["cells"] == 400
+    with pytest.raises(_lib.S4GError, match="not normal to x, y or z"):
+        read_case(cooks_membrane_case(tmp_path / "tilted", 4, rotate_deg=30.0))

@@ -10,6 +10,8 @@ from oracle import pyoracle
 import solids4foam_gb300 as sg
 from solids4foam_gb300.cases import oracle_bcs
 
+from cases2d import cooks_membrane
+
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -401,44 +403,6 @@ def test_pressurised_cylinder_readme_stresses(tmp_path):
     assert err[1][0] < 0.5 * err[0][0] and err[1][1] < 0.5 * err[0][1]
 
 
-def _cooks_membrane(tmp_path, n):
-    """Cook's membrane as the reference's cooksMembrane tutorial meshes it
-    (one blockMesh hex block, straight edges, n x n x 1, corners (0,0),
-    (48,44), (48,60), (0,44) mm, 1 mm thick), with the empty front and back
-    faces left out of the discretisation (2-D)."""
-    from solids4foam_gb300.foam_case import polymesh_from_cells, read_case, write_polymesh
-    V = np.array([[0, 0], [48, 44], [48, 60], [0, 44]], float) * 1e-3
-    pid = lambda i, j, k: i + (n + 1) * (j + (n + 1) * k)
-    pts = []
-    for z in (-0.5e-3, 0.5e-3):
-        for j in range(n + 1):
-            for i in range(n + 1):
-                s, t = i / n, j / n
-                P = (1 - s) * (1 - t) * V[0] + s * (1 - t) * V[1] + s * t * V[2] + (1 - s) * t * V[3]
-                pts.append([P[0], P[1], z])
-    cells = []
-    for j in range(n):
-        for i in range(n):
-            v = [pid(i, j, 0), pid(i + 1, j, 0), pid(i + 1, j + 1, 0), pid(i, j + 1, 0)]
-            w = [pid(i, j, 1), pid(i + 1, j, 1), pid(i + 1, j + 1, 1), pid(i, j + 1, 1)]
-            cells.append([v, w] + [[v[e], v[(e + 1) % 4], w[(e + 1) % 4], w[e]] for e in range(4)])
-
-    def patch_of(c):
-        if abs(abs(c[2]) - 0.5e-3) < 1e-12:
-            return 3                                   # frontAndBack (empty)
-        return 0 if abs(c[0]) < 1e-12 else 1 if abs(c[0] - 0.048) < 1e-12 else 2
-    case = tmp_path / f"cook{n}"
-    write_polymesh(str(case / "constant" / "polyMesh"),
-                   **polymesh_from_cells(np.array(pts), cells, patch_of,
-                                         ["left", "right", "topAndBottom", "frontAndBack"]))
-    m, _ = read_case(str(case), d_file=None)
-    nf = int(m["patch_start"][3])                      # frontAndBack is the last patch
-    m2 = dict(owner=m["owner"][:nf], neighbour=m["neighbour"], C=m["C"], V=m["V"],
-              Cf=m["Cf"][:nf], Sf=m["Sf"][:nf], patch_start=m["patch_start"][:3],
-              patch_size=m["patch_size"][:3])
-    return m, m2
-
-
 def test_cooks_membrane_against_the_reference(tmp_path):
     """The reference's cooksMembrane tutorial (README.md "Expected Results"):
     E = 70 MPa, nu = 0.3333, left edge fixed, 6.25 MPa shear on the right,
@@ -452,7 +416,7 @@ def test_cooks_membrane_against_the_reference(tmp_path):
     from solids4foam_gb300.post import point_displacement
     corner = {}
     for n in (20, 40):
-        m, m2 = _cooks_membrane(tmp_path, n)
+        m, m2 = cooks_membrane(tmp_path, n)
         nr = int(m2["patch_size"][1])
         bcs = [(0, None, None), (1, np.tile([0.0, 6.25e6, 0.0], (nr, 1)), None), (1, None, None)]
         D, _, G, p = pyoracle.solve(m2, bcs, E=70e6, nu=0.3333, n_correctors=5000,
