@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define S4G_ABI_VERSION 4
+#define S4G_ABI_VERSION 5
 
 /* Status codes.  Reference convention for errors is FatalError (abort), see
  * src/solids4FoamModels/solidModels/solidModel/solidModel.C:1735-1742; a
@@ -71,6 +71,11 @@ typedef struct s4g_ctx_opts {
                    PCG batches are then launched kernel by kernel */
   int no_graphs; /* 1: launch PCG batches kernel by kernel instead of
                    replaying captured CUDA graphs (same results) */
+  int spin_limit; /* polls a bounded device wait (the exact-DIC sweeps'
+                   wait for the parts they depend on) makes before it gives
+                   up: the kernel then sets an error bit, returns, and the
+                   call reports S4G_TIMEOUT with the context still usable.
+                   0: the default, 4,194,304 (seconds of waiting) */
 } s4g_ctx_opts;
 
 /* Kernel kinds of the per-kernel timers. */
@@ -142,6 +147,17 @@ typedef struct s4g_mesh_opts {
                              inv() does with an empty direction, and that
                              displacement component is not solved (plane
                              strain).  0: 3-D. */
+  const int* part_of_cell; /* optional [n_cells]: the caller's decomposition
+                             of the cells into DIC subdomains (the
+                             counterpart of decomposePar's cellDecomposition),
+                             subdomain ids 0..n-1, every id used; a
+                             subdomain must fit the preconditioner kernel's
+                             shared memory (about 2,000 cells).  Needs
+                             renumber = S4G_RENUMBER_NONE and
+                             dic_subdomains = 1: each subdomain's DIC then
+                             runs in the caller's cell order, as a decomposed
+                             run's processor does.  NULL: the library's
+                             parts.  Read during s4g_mesh_upload only. */
 } s4g_mesh_opts;
 
 typedef struct s4g_mesh s4g_mesh;
@@ -245,6 +261,15 @@ typedef struct s4g_outer {
   double material_tol;     /* materialTolerance */
   double stab_scale;       /* stabilisation { type RhieChow; scaleFactor; } */
   int info_frequency;      /* infoFrequency */
+  double field_relaxation; /* fvSolution relaxationFactors { fields { D (DD for
+                              the incremental TL model) f; } }: after each
+                              solve D == D.prevIter + f (D - D.prevIter) on
+                              the cells and the boundary faces (relaxField
+                              "fixed", solidModel.C:837-841); f in (0, 1],
+                              0 or 1: no relaxation */
+  int relaxation_method;   /* <model>Coeffs relaxationMethod: 0 fixed, 1
+                              Aitken (solidModel.C:842-896, field_relaxation
+                              then gives the first corrector's factor) */
 } s4g_outer;
 
 typedef enum s4g_precision {
@@ -258,7 +283,8 @@ s4g_status s4g_solver_set(s4g_mesh* mesh, const s4g_lin_solver* lin,
 
 /* Fills the reference defaults: PCG+DIC tol 1e-9 relTol 0.1 maxIter 1000;
  * nCorrectors 10000, solutionTolerance 1e-6, alternativeTolerance 1e-7,
- * materialTolerance 1e-5, RhieChow 0.1, infoFrequency 100. */
+ * materialTolerance 1e-5, RhieChow 0.1, infoFrequency 100, no field
+ * relaxation (1), relaxationMethod fixed. */
 void s4g_default_controls(s4g_lin_solver* lin, s4g_outer* outer);
 
 /* -------------------------------------------------------------- solve -- */
@@ -399,6 +425,8 @@ typedef struct s4g_request {
   s4g_precision precision;
   s4g_model model;
   int n_increments;
+  const double* bc_relaxation; /* [n_bc] relaxationFactor of each solidTraction
+                                  patch (s4g_bc_set_relaxation), or NULL: 1 */
 } s4g_request;
 
 typedef struct s4g_server_stats {
@@ -539,22 +567,24 @@ s4g_status s4g_foam_read_time(const char* control_dict, double* start_time, doub
                               double* delta_t);
 /* The model, law and controls of a case directory, from
  * constant/solidProperties (solidModel and its <model>Coeffs, with the
- * stabilisation sub-dictionary: solidModel.C:909-912,1138-1243,1305-1323),
- * constant/mechanicalProperties (one linearElastic or neoHookeanElastic law,
- * planeStress no) and system/fvSolution (the PCG solver of D, or DD for the
- * incremental total Lagrangian model).  Entries that are not set keep the
- * reference defaults (s4g_default_controls).  Anything not built -- another
- * model, law or solver, plane stress, several laws, sigma0, predictor,
- * solvePressureEqn -- is S4G_BAD_ARG, named in s4g_last_error. */
+ * stabilisation sub-dictionary and relaxationMethod:
+ * solidModel.C:909-912,1138-1243,1305-1323), constant/mechanicalProperties
+ * (one linearElastic or neoHookeanElastic law, planeStress no) and
+ * system/fvSolution (the PCG solver of D, or DD for the incremental total
+ * Lagrangian model, and that field's relaxationFactors field factor).
+ * Entries that are not set keep the reference defaults
+ * (s4g_default_controls).  Anything not built -- another model, law or
+ * solver, plane stress, several laws, sigma0, predictor, solvePressureEqn --
+ * is S4G_BAD_ARG, named in s4g_last_error. */
 s4g_status s4g_foam_read_controls(const char* case_dir, s4g_model* model, s4g_law* law,
                                   s4g_lin_solver* lin, s4g_outer* outer);
 /* relaxationFactors of a system/fvSolution for one field ("D" or "DD"):
  * field_factor from fields { } (or the older flat form), equation_factor
  * from equations { }; 1 where none is set.  Field relaxation (the
  * reference's "fixed" relaxField, D == D.prevIter + f (D - D.prevIter),
- * solidModel.C:837-841) and equation relaxation (fvMatrix::relax) are not
- * built on the device path, so a caller refuses a case that sets either
- * below 1. */
+ * solidModel.C:837-841) is built: s4g_foam_read_controls puts the factor in
+ * s4g_outer.field_relaxation.  Equation relaxation (fvMatrix::relax) is not
+ * built on the device path, so a caller refuses a case that sets it below 1. */
 s4g_status s4g_foam_read_relaxation(const char* fv_solution, const char* field,
                                     double* field_factor, double* equation_factor);
 /* s4g_bc_set and s4g_bc_set_relaxation on every patch of an uploaded mesh

@@ -344,12 +344,27 @@ void amul(const Mesh& m, const Ldu& A, const double* x, double* y, int nt) {
 struct Dic {
   std::vector<double> rD;
   std::vector<int> dom;  // subdomain of each cell
-  int nd = 1;
+  int nd = 1;            // thread subdomains: contiguous ranges of cells
+  int nthreads = 1;
+  bool callerDomains = false;
+  std::vector<int> domStart, domCells;  // caller subdomains: their cells, ascending
   void build(const Mesh& m, const Ldu& A, int nt, const std::vector<int>* domain = nullptr) {
-    nd = std::max(1, nt);
+    nthreads = std::max(1, nt);
+    nd = nthreads;
     dom.resize(m.nC);
     for (int c = 0; c < m.nC; ++c) dom[c] = (int)((long long)c * nd / m.nC);
-    if (domain) dom = *domain;
+    if (domain) {
+      dom = *domain;
+      callerDomains = true;
+      int n = 0;
+      for (int c = 0; c < m.nC; ++c) n = std::max(n, dom[c] + 1);
+      domStart.assign(n + 1, 0);
+      for (int c = 0; c < m.nC; ++c) domStart[dom[c] + 1]++;
+      for (int d = 0; d < n; ++d) domStart[d + 1] += domStart[d];
+      domCells.resize(m.nC);
+      std::vector<int> fill(domStart.begin(), domStart.end() - 1);
+      for (int c = 0; c < m.nC; ++c) domCells[fill[dom[c]]++] = c;
+    }
     rD = A.diag;
     // calcReciprocalD: rD[u] -= upper^2/rD[l] over faces in order
     for (int u = 0; u < m.nC; ++u)
@@ -361,39 +376,52 @@ struct Dic {
       }
     for (int c = 0; c < m.nC; ++c) rD[c] = 1.0 / rD[c];
   }
+  // The substitutions of one subdomain; the cells are visited in increasing
+  // (forward) and decreasing (backward) order, given as a list or a range.
+  template <class CellAt>
+  void sweep(const Mesh& m, const Ldu& A, const double* r, double* wv, int n, CellAt at) const {
+    for (int q = 0; q < n; ++q) {
+      const int u = at(q);
+      double v = rD[u] * r[u];
+      for (int e = m.cfStart[u]; e < m.cfStart[u + 1]; ++e) {
+        int f = m.cfFace[e];
+        if (m.nei[f] != u) continue;
+        int l = m.own[f];
+        if (dom[l] != dom[u]) continue;
+        v -= rD[u] * A.upper[f] * wv[l];
+      }
+      wv[u] = v;
+    }
+    for (int q = n - 1; q >= 0; --q) {
+      const int l = at(q);
+      double v = wv[l];
+      for (int e = m.cfStart[l + 1] - 1; e >= m.cfStart[l]; --e) {
+        int f = m.cfFace[e];
+        if (m.own[f] != l) continue;
+        int u = m.nei[f];
+        if (dom[u] != dom[l]) continue;
+        v -= rD[l] * A.upper[f] * wv[u];
+      }
+      wv[l] = v;
+    }
+  }
   void apply(const Mesh& m, const Ldu& A, const double* r, double* wv) const {
-    auto sweep = [&](int, int c0, int c1) {
-      for (int u = c0; u < c1; ++u) {
-        double v = rD[u] * r[u];
-        for (int e = m.cfStart[u]; e < m.cfStart[u + 1]; ++e) {
-          int f = m.cfFace[e];
-          if (m.nei[f] != u) continue;
-          int l = m.own[f];
-          if (dom[l] != dom[u]) continue;
-          v -= rD[u] * A.upper[f] * wv[l];
-        }
-        wv[u] = v;
+    if (callerDomains) {
+      // the subdomains are independent: in parallel, each in cell order
+      const int n = (int)domStart.size() - 1;
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads) if (nthreads > 1)
+      for (int d = 0; d < n; ++d) {
+        const int* cells = domCells.data() + domStart[d];
+        sweep(m, A, r, wv, domStart[d + 1] - domStart[d], [&](int q) { return cells[q]; });
       }
-      for (int l = c1 - 1; l >= c0; --l) {
-        double v = wv[l];
-        for (int e = m.cfStart[l + 1] - 1; e >= m.cfStart[l]; --e) {
-          int f = m.cfFace[e];
-          if (m.own[f] != l) continue;
-          int u = m.nei[f];
-          if (dom[u] != dom[l]) continue;
-          v -= rD[l] * A.upper[f] * wv[u];
-        }
-        wv[l] = v;
-      }
-    };
-    if (nd == 1) {
-      sweep(0, 0, m.nC);
+    } else if (nd == 1) {
+      sweep(m, A, r, wv, m.nC, [](int q) { return q; });
     } else {
 #pragma omp parallel for schedule(static, 1) num_threads(nd)
       for (int d = 0; d < nd; ++d) {
         int c0 = (int)(((long long)d * m.nC + nd - 1) / nd);
         int c1 = (int)(((long long)(d + 1) * m.nC + nd - 1) / nd);
-        sweep(d, c0, c1);
+        sweep(m, A, r, wv, c1 - c0, [&](int q) { return c0 + q; });
       }
     }
   }
@@ -551,7 +579,7 @@ struct Solver {
       if (s.dic_domain) {
         std::vector<int> dom(m.nC);
         for (int c = 0; c < m.nC; ++c) dom[m.newOfCaller[c]] = s.dic_domain[c];
-        dic.build(m, A, 1, &dom);
+        dic.build(m, A, nt, &dom);
       } else {
         dic.build(m, A, nt);
       }

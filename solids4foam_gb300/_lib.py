@@ -25,7 +25,7 @@ LIN_GEOM_TOTAL_DISP, NONLIN_GEOM_TOTAL_LAG, NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP = 0
 
 class CtxOpts(ct.Structure):
     _fields_ = [("device", ct.c_int), ("verbose", ct.c_int), ("profile", ct.c_int),
-                ("no_graphs", ct.c_int)]
+                ("no_graphs", ct.c_int), ("spin_limit", ct.c_int)]
 
 
 # kernel kinds of the per-kernel timers (S4G_K_*)
@@ -45,7 +45,8 @@ class MeshDesc(ct.Structure):
 class MeshOpts(ct.Structure):
     _fields_ = [("renumber", ct.c_int), ("part_size", ct.c_int),
                 ("ls_boundary_delta", ct.c_int), ("dic_subdomains", ct.c_int),
-                ("no_autotune", ct.c_int), ("empty_direction", ct.c_int)]
+                ("no_autotune", ct.c_int), ("empty_direction", ct.c_int),
+                ("part_of_cell", ct.c_void_p)]
 
 
 class MeshInfo(ct.Structure):
@@ -70,7 +71,8 @@ class LinSolver(ct.Structure):
 class Outer(ct.Structure):
     _fields_ = [("n_correctors", ct.c_int), ("solution_tol", ct.c_double),
                 ("alternative_tol", ct.c_double), ("material_tol", ct.c_double),
-                ("stab_scale", ct.c_double), ("info_frequency", ct.c_int)]
+                ("stab_scale", ct.c_double), ("info_frequency", ct.c_int),
+                ("field_relaxation", ct.c_double), ("relaxation_method", ct.c_int)]
 
 
 class ServerOpts(ct.Structure):
@@ -82,7 +84,8 @@ class Request(ct.Structure):
     _fields_ = [("mesh", ct.c_void_p), ("mesh_opts", MeshOpts), ("law", Law), ("n_bc", ct.c_int),
                 ("bc_patch", ct.c_void_p), ("bc_type", ct.c_void_p), ("bc_vec3", ct.c_void_p),
                 ("bc_pressure", ct.c_void_p), ("lin", LinSolver), ("outer", Outer),
-                ("precision", ct.c_int), ("model", ct.c_int), ("n_increments", ct.c_int)]
+                ("precision", ct.c_int), ("model", ct.c_int), ("n_increments", ct.c_int),
+                ("bc_relaxation", ct.c_void_p)]
 
 
 class ServerStats(ct.Structure):

@@ -1096,6 +1096,12 @@ s4g_status s4g_foam_read_controls(const char* case_dir, s4g_model* model, s4g_la
           fail(w + ": stabilisation type " + (ty->val.empty() ? "" : ty->val[0].s) + " is not built");
         if (const Entry* e = find(st->sub, "scaleFactor")) outer->stab_scale = number(e, w);
       }
+      if (const Entry* e = find(co->sub, "relaxationMethod")) {
+        const std::string m = e->val.size() == 1 ? e->val[0].s : "";
+        if (m == "fixed") outer->relaxation_method = 0;
+        else if (m == "Aitken") outer->relaxation_method = 1;
+        else fail(w + ": relaxationMethod " + m + " is unknown (fixed or Aitken)");
+      }
       for (const char* k : {"predictor", "solvePressureEqn"})
         if (const Entry* e = find(co->sub, k))
           if (!e->val.empty() && (e->val[0].s == "yes" || e->val[0].s == "true" || e->val[0].s == "on"))
@@ -1158,6 +1164,13 @@ s4g_status s4g_foam_read_controls(const char* case_dir, s4g_model* model, s4g_la
     if (const Entry* e = find(sd->sub, "tolerance")) lin->tolerance = number(e, w);
     if (const Entry* e = find(sd->sub, "relTol")) lin->rel_tol = number(e, w);
     if (const Entry* e = find(sd->sub, "maxIter")) lin->max_iter = (int)number(e, w);
+    // relaxationFactors { fields { D f; } } (solidModel.C:837-841 via D.relax());
+    // an equation factor is returned by s4g_foam_read_relaxation for the caller
+    double ff = 1.0, ef = 1.0;
+    if (s4g_foam_read_relaxation(fs.c_str(), field, &ff, &ef) != S4G_OK)
+      fail(fs + ": bad relaxationFactors");
+    if (!(ff > 0.0 && ff <= 1.0)) fail(fs + ": field relaxation factor must be in (0, 1]");
+    outer->field_relaxation = ff;
   });
 }
 

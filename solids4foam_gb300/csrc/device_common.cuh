@@ -8,7 +8,7 @@ namespace s4g {
 
 constexpr int kRowBlock = 256;        // threads per block of the row kernels
 constexpr int kSweepBlock = 128;      // threads per block of the DIC sweeps
-constexpr int kSpinLimit = 1 << 22;   // bounded waits: iterations before giving up
+constexpr int kSpinLimit = 1 << 22;   // bounded waits: default polls before giving up
 
 // status bits of DevState::status
 constexpr unsigned kErrTimeout = 1u;
@@ -38,6 +38,7 @@ struct MeshView {
   const int* lowCnt;   // lower entries per row
   int maxRows, maxHalo, maxEntries, maxLevels;
   int rowGrid;         // blocks of the grid-stride row kernels
+  int spinLimit;       // polls of a bounded wait before it gives up (kErrTimeout)
   // processor-local DIC tables (see HostPrep)
   const int* locEntStart; const int* locSrc; const uint16_t* locIdx;
   const int* locMetaStart; const uint32_t* locMeta;
@@ -68,6 +69,7 @@ struct Controls {
   int nCorr;
   double solTol, altTol, matTol;
   int precond;           // 0 DIC, 1 diagonal
+  double fieldRelax;     // relaxField "fixed" factor (1: none)
 };
 
 // Mutable solver state in device memory.  Scalars that steer the loops are

@@ -48,6 +48,7 @@ struct Ctx {
   int verbose = 0;
   int profile = 0;
   int noGraphs = 0;
+  int spinLimit = kSpinLimit;
   int numSMs = 0;
   cudaStream_t stream = nullptr;
 };
@@ -274,6 +275,7 @@ struct Engine {
     mv.emptyDir = o ? o->empty_direction : 0;
     mv.rowGrid = std::max(1, std::min((nC + kRowBlock - 1) / kRowBlock,
                                       ctx->numSMs * kRowBlocksPerSM));
+    mv.spinLimit = ctx->spinLimit;
     mv.rowptr = dRow; mv.col = dCol; mv.fidx = dFidx; mv.fown = dFown; mv.fnei = dFnei;
     mv.fS = geo.fS; mv.fmagS = geo.fmagS; mv.fw = geo.fw; mv.fdelta = geo.fdelta;
     mv.C = geo.C; mv.invDd = geo.invDd;
@@ -330,6 +332,7 @@ struct Engine {
     S4G_TRY(alloc(&f.Gb, 9 * (size_t)nB));
     S4G_TRY(alloc(&f.sigb, 6 * (size_t)nB));
     S4G_TRY(alloc(&f.g, 3 * (size_t)nB));
+    S4G_TRY(alloc(&f.Ubr, 3 * (size_t)nB));
     S4G_TRY(alloc(&f.flux, 6 * (size_t)nI));
     S4G_TRY(alloc(&pc.x, 3 * (size_t)nC));
     S4G_TRY(alloc(&pc.r, 3 * (size_t)nC));
@@ -504,6 +507,9 @@ struct Engine {
     c.nCorr = outer.n_correctors;
     c.solTol = outer.solution_tol; c.altTol = outer.alternative_tol; c.matTol = outer.material_tol;
     c.precond = lin.preconditioner == S4G_PRECOND_DIC ? 0 : 1;
+    // relaxationFactors { fields { D f; } }: 0 or 1 leave the field as solved
+    const double fr = outer.field_relaxation;
+    c.fieldRelax = (fr > 0.0 && fr < 1.0) ? fr : 1.0;
     return c;
   }
 
@@ -626,6 +632,7 @@ struct Engine {
     S4G_CUDA(z(f.D[0], 3 * nC)); S4G_CUDA(z(f.D[1], 3 * nC)); S4G_CUDA(z(f.D0, 3 * nC));
     S4G_CUDA(z(f.D0b, 3 * nB)); S4G_CUDA(z(f.G, 9 * nC)); S4G_CUDA(z(f.sig, 6 * nC));
     S4G_CUDA(z(f.Gb, 9 * nB)); S4G_CUDA(z(f.sigb, 6 * nB)); S4G_CUDA(z(f.g, 3 * nB));
+    S4G_CUDA(z(f.Ubr, 3 * nB));
     S4G_CUDA(z(pc.x, 3 * nC)); S4G_CUDA(z(pc.r, 3 * nC)); S4G_CUDA(z(pc.w, 3 * nC));
     S4G_CUDA(z(pc.p, 3 * nC)); S4G_CUDA(z(pc.q, 3 * nC));
     if (fp32Allocated)
@@ -672,6 +679,7 @@ struct Engine {
     S4G_TRY(regrow(f.Gb, 9 * nB * o, 9 * nB * n));
     S4G_TRY(regrow(f.sigb, 6 * nB * o, 6 * nB * n));
     S4G_TRY(regrow(f.g, 3 * nB * o, 3 * nB * n));
+    S4G_TRY(regrow(f.Ubr, 3 * nB * o, 3 * nB * n));
     S4G_TRY(regrow(f.flux, 6 * nI * o, 6 * nI * n));
     S4G_TRY(regrow(dBval, 3 * nB * o, 3 * nB * n));
     S4G_TRY(regrow(dBpress, nB * o, nB * n));
@@ -1241,6 +1249,8 @@ s4g_status s4g_ctx_create(s4g_ctx** out, const s4g_ctx_opts* opts) {
   c->c.verbose = opts ? opts->verbose : 0;
   c->c.profile = opts ? opts->profile : 0;
   c->c.noGraphs = opts ? opts->no_graphs : 0;
+  if (opts && opts->spin_limit < 0) return setErr(S4G_BAD_ARG, "spin_limit must be >= 0");
+  c->c.spinLimit = (opts && opts->spin_limit > 0) ? opts->spin_limit : s4g::kSpinLimit;
   if (cudaSetDevice(dev) != cudaSuccess) return setErr(S4G_CUDA_ERROR, "cudaSetDevice failed");
   cudaDeviceGetAttribute(&c->c.numSMs, cudaDevAttrMultiProcessorCount, dev);
   if (cudaStreamCreateWithFlags(&c->c.stream, cudaStreamNonBlocking) != cudaSuccess)
@@ -1376,6 +1386,8 @@ void s4g_default_controls(s4g_lin_solver* lin, s4g_outer* outer) {
     outer->material_tol = 1e-5;
     outer->stab_scale = 0.1;
     outer->info_frequency = 100;
+    outer->field_relaxation = 1.0;
+    outer->relaxation_method = 0;
   }
 }
 
@@ -1391,6 +1403,12 @@ s4g_status s4g_solver_set(s4g_mesh* mesh, const s4g_lin_solver* lin, const s4g_o
   if (outer) {
     if (outer->n_correctors < 1 || !(outer->stab_scale >= 0))
       return setErr(S4G_BAD_ARG, "invalid outer controls");
+    if (!(outer->field_relaxation >= 0.0 && outer->field_relaxation <= 1.0))
+      return setErr(S4G_BAD_ARG, "field_relaxation must be in (0, 1] (0: none)");
+    if (outer->relaxation_method != 0 && outer->relaxation_method != 1)
+      return setErr(S4G_BAD_ARG, "relaxation_method must be 0 (fixed) or 1 (Aitken)");
+    if (outer->relaxation_method == 1)
+      return setErr(S4G_NOT_BUILT, "relaxationMethod Aitken is not built on the device");
     mesh->e.outer = *outer;
   }
   if (precision != S4G_FP64 && precision != S4G_FP32_REFINE) return setErr(S4G_BAD_ARG, "unknown precision");

@@ -52,6 +52,8 @@ struct FieldPtrs {
   double* sigb;  // [nB][6]
   double* g;     // [nB][3] traction snGrad
   double* gPrev; // [nB][3] TL: the g of the corrector before the last update
+  double* Ubr;   // [nB][3] field relaxation: the boundary values of the solved
+                 // field after the last relaxation (D.prevIter on the boundary)
   // total Lagrangian extras
   double* GD;  double* GD0;  double* GDb; double* GD0b;  // total gradient and old time
   double* Finv; double* Finvb; double* J; double* Jb;
@@ -69,6 +71,7 @@ __host__ __device__ inline FieldPtrs caseFields(FieldPtrs f, int cs, int nC, int
   if (f.D0b) f.D0b += c * 3 * nB;
   f.G += c * 9 * nC; f.sig += c * 6 * nC;
   f.Gb += c * 9 * nB; f.sigb += c * 6 * nB; f.g += c * 3 * nB;
+  f.Ubr += c * 3 * nB;
   f.flux += c * 6 * nI;
   return f;
 }

@@ -219,10 +219,12 @@ __device__ __forceinline__ V3 boundaryValue(const MeshView& mv, const Controls& 
 }
 
 // --------------------------------------------------------- post-solve pass ---
-// D_new = D + x (the correction of the corrector; x in the PCG type).
+// D_new = D + x (the correction of the corrector; x in the PCG type).  With
+// a field relaxation factor f (relaxField "fixed", solidModel.C:837-841):
+// D_new = D.prevIter + f (D_solved - D.prevIter) = D + f x.
 template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
-kApplyX(MeshView mv, FieldPtrs f, const T* __restrict__ x, const DevState* st) {
+kApplyX(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, const DevState* st) {
   const int cs = blockIdx.y;
   f = caseFields(f, cs, mv.nC, mv.nB, mv.nI);
   x += (size_t)cs * 3 * mv.nC;
@@ -231,12 +233,20 @@ kApplyX(MeshView mv, FieldPtrs f, const T* __restrict__ x, const DevState* st) {
   const int dc = st->dcur;
   const double* Uold = f.D[dc];
   double* Unew = f.D[dc ^ 1];
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x)
-    stV(Unew, s, ldV(Uold, s) + ldVT(x, s));
+  const double fr = c.fieldRelax;
+  if (fr == 1.0)
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x)
+      stV(Unew, s, ldV(Uold, s) + ldVT(x, s));
+  else
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x)
+      stV(Unew, s, ldV(Uold, s) + fr * ldVT(x, s));
 }
 
 // mode 0 (constructor): gradient only, from the current field.
 // mode 1 (corrector): apply the correction x, gradient, law, boundary, g.
+// With field relaxation the boundary values are relaxed too (the forced
+// assignment of GeometricField::relax): Ub = Ub.prevIter + f (Ub_new -
+// Ub.prevIter), Ub.prevIter kept in f.Ubr (mode 0 stores the constructor's).
 // For the TL model the law needs the global J check first, so mode 1 stops
 // after the kinematics (F, F^-1, J) and kPostLawTL finishes the pass.
 
@@ -258,6 +268,7 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
   const bool apply = (mode == 1);
   // the corrected field D + x, written by kApplyX (mode 1), or D (mode 0)
   const double* U = f.D[apply ? dc ^ 1 : dc];
+  const bool relax = c.fieldRelax != 1.0;
   double red[6] = {0, 0, 0, 0, 0, 0};  // sum U
   double mx[3] = {0, 0, 0};            // max|x|, max|U-D0|, max|U|
   double minJ = 1e300, maxJ = -1e300;
@@ -271,6 +282,13 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
       acc = acc + outer(ldV(mv.lsv, e), ldV(U, mv.col[e]) - Up);
     for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
       V3 Ub = boundaryValue(mv, c, f, b, Up, Gold);
+      if (relax) {
+        if (apply) {
+          const V3 pb = ldV(f.Ubr, b);
+          Ub = pb + c.fieldRelax * (Ub - pb);
+        }
+        stV(f.Ubr, b, Ub);
+      }
       acc = acc + outer(ldV(mv.bls, b), Ub - Up);
     }
     const T9 G = acc;
@@ -282,7 +300,7 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
       if (mv.btype[b] == 1) {
         sg = ldV(f.g, b);
       } else {
-        V3 Ub = boundaryValue(mv, c, f, b, Up, Gold);
+        const V3 Ub = relax ? ldV(f.Ubr, b) : boundaryValue(mv, c, f, b, Up, Gold);
         sg = mv.bdelta[b] * (Ub - (Up + dotVT(ldV(mv.bk, b), Gold)));
       }
       T9 Gb = G + outer(n, sg - dotVT(n, G));
@@ -318,7 +336,8 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
     }
     if (apply) {
       // maxima of squared magnitudes; the square root is taken once at the end
-      V3 xs = ldVT(x, s);
+      // max|D - D.prevIter|: the correction, or its relaxed part
+      const V3 xs = relax ? Up - ldV(f.D[dc], s) : ldVT(x, s);
       mx[0] = fmax(mx[0], magSqr(xs));
       mx[1] = fmax(mx[1], c.tl == 1 ? magSqr(Up) : magSqr(Up - ldV(f.D0, s)));
       mx[2] = fmax(mx[2], magSqr(Up));
@@ -611,7 +630,7 @@ void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const
   const int grid = (mv.nC + kRowBlock - 1) / kRowBlock;
   TimeScope ts(tm, S4G_K_POST, s);
   const dim3 g(mv.rowGrid, nCases);
-  if (mode == 1) kApplyX<T><<<g, kRowBlock, 0, s>>>(mv, f, x, st);
+  if (mode == 1) kApplyX<T><<<g, kRowBlock, 0, s>>>(mv, c, f, x, st);
   kPost<T><<<g, kRowBlock, 0, s>>>(mv, c, f, x, st, partials, mode);
   if (c.tl && mode == 1) kPostLawTL<<<grid, kRowBlock, 0, s>>>(mv, c, f, st);
 }

@@ -39,8 +39,9 @@ constexpr int kSweepSmBlock = 64;
 
 // Poll with relaxed loads (an acquire load per poll would also invalidate the
 // SM's L1 each time), then one acquire fence once the flag is seen.
-__device__ __forceinline__ void waitPart(const unsigned* flag, unsigned epoch, unsigned* status) {
-  for (int it = 0; it < kSpinLimit; ++it) {
+__device__ __forceinline__ void waitPart(const unsigned* flag, unsigned epoch, unsigned* status,
+                                         int limit) {
+  for (int it = 0; it < limit; ++it) {
     if (ldRelaxed(flag) == epoch) {
       fenceAcqRel();
       return;
@@ -85,7 +86,7 @@ kSweepFactor(MeshView mv, const double* val, const double* diag, double* rD, uns
     const int pLo = mv.partStart[part];
     if (!mv.subdomains)
       for (int i = mv.upPtr[part] + threadIdx.x; i < mv.upPtr[part + 1]; i += blockDim.x)
-        waitPart(flags + mv.upIdx[i], epoch, &st->status);
+        waitPart(flags + mv.upIdx[i], epoch, &st->status, mv.spinLimit);
     __syncthreads();
     for (int lvl = mv.lvlOff[part]; lvl < mv.lvlOff[part + 1]; ++lvl) {
       for (int row = mv.lvlStart[lvl] + threadIdx.x; row < mv.lvlStart[lvl + 1]; row += blockDim.x) {
@@ -243,7 +244,7 @@ kSweepSm(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
       const int* dep = DIR == 0 ? mv.upIdx : mv.dnIdx;
       const int d0 = DIR == 0 ? mv.upPtr[part] : mv.dnPtr[part];
       const int d1 = DIR == 0 ? mv.upPtr[part + 1] : mv.dnPtr[part + 1];
-      for (int i = d0 + threadIdx.x; i < d1; i += NT) waitPart(flags + dep[i], epoch, &st->status);
+      for (int i = d0 + threadIdx.x; i < d1; i += NT) waitPart(flags + dep[i], epoch, &st->status, mv.spinLimit);
     }
     __syncthreads();
     {

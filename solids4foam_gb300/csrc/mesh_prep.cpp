@@ -182,6 +182,24 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
   int partSize = (o && o->part_size > 0) ? o->part_size : 512;
   partSize = std::max(32, std::min(partSize, 1 << 16));
   const bool subdomains = o && o->dic_subdomains;
+  // the caller's decomposition (decomposePar's cellDecomposition): ids
+  // 0..n-1, none empty; each subdomain's DIC runs in the caller's order
+  const int* callerParts = o ? o->part_of_cell : nullptr;
+  int nCallerParts = 0;
+  if (callerParts) {
+    if (renumber != S4G_RENUMBER_NONE || !subdomains) {
+      err = "part_of_cell needs renumber = S4G_RENUMBER_NONE and dic_subdomains = 1";
+      return S4G_BAD_ARG;
+    }
+    for (int c = 0; c < nC; ++c) {
+      if (callerParts[c] < 0 || callerParts[c] >= nC) { err = "part_of_cell id out of range"; return S4G_BAD_ARG; }
+      nCallerParts = std::max(nCallerParts, callerParts[c] + 1);
+    }
+    std::vector<int> cnt(nCallerParts, 0);
+    for (int c = 0; c < nC; ++c) cnt[callerParts[c]]++;
+    for (int p = 0; p < nCallerParts; ++p)
+      if (cnt[p] == 0) { err = "part_of_cell ids must be 0..n-1 with every id used"; return S4G_BAD_ARG; }
+  }
 
   hp.nC = nC; hp.nI = nI; hp.nB = nB;
   Adj adj = buildAdjacency(nC, nI, d->owner, d->neighbour);
@@ -262,6 +280,17 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
   if (renumber == S4G_RENUMBER_TILED) {
     topo = order;
     parts = tiles;
+  } else if (callerParts) {
+    // cells grouped by the caller's subdomain, each in solver order
+    std::vector<size_t> at(nCallerParts + 1, 0);
+    for (int c = 0; c < nC; ++c) at[callerParts[c] + 1]++;
+    for (int p = 0; p < nCallerParts; ++p) at[p + 1] += at[p];
+    for (int p = 0; p < nCallerParts; ++p) parts.push_back({at[p], at[p + 1]});
+    topo.resize(nC);
+    for (int i = 0; i < nC; ++i) {
+      const int c = order[i];
+      topo[at[callerParts[c]]++] = c;
+    }
   } else {
     topo = order;
     std::stable_sort(topo.begin(), topo.end(), [&](int x, int y) { return glev[x] < glev[y]; });

@@ -51,6 +51,8 @@ struct Request {
   std::vector<s4g_bc_type> bcType;
   std::vector<std::vector<double>> bcVec, bcPress;
   std::vector<char> bcHasVec, bcHasPress;
+  std::vector<double> bcRelax;      // solidTraction relaxationFactor per entry
+  std::vector<int> partOfCell;      // copy of mesh_opts.part_of_cell (may be empty)
   s4g_lin_solver lin{};
   s4g_outer outer{};
   s4g_precision precision = S4G_FP64;
@@ -112,12 +114,17 @@ s4g_status runOne(s4g_ctx* ctx, Request& r) {
   d.C = r.C.data(); d.V = r.V.data(); d.Cf = r.Cf.data(); d.Sf = r.Sf.data();
   d.n_patches = r.nPatches; d.patch_start = r.patchStart.data(); d.patch_size = r.patchSize.data();
   s4g_mesh* mesh = nullptr;
-  s4g_status st = s4g_mesh_upload(ctx, &d, &r.meshOpts, &mesh);
+  s4g_mesh_opts mo = r.meshOpts;
+  mo.part_of_cell = r.partOfCell.empty() ? nullptr : r.partOfCell.data();
+  s4g_status st = s4g_mesh_upload(ctx, &d, &mo, &mesh);
   if (st != S4G_OK) { r.error = s4g_last_error(); return st; }
   st = s4g_material_set(mesh, &r.law);
   for (size_t i = 0; st == S4G_OK && i < r.bcPatch.size(); ++i)
     st = s4g_bc_set(mesh, r.bcPatch[i], r.bcType[i], r.bcHasVec[i] ? r.bcVec[i].data() : nullptr,
                     r.bcHasPress[i] ? r.bcPress[i].data() : nullptr);
+  for (size_t i = 0; st == S4G_OK && i < r.bcPatch.size(); ++i)
+    if (r.bcType[i] == S4G_SOLID_TRACTION && r.bcRelax[i] != 1.0)
+      st = s4g_bc_set_relaxation(mesh, r.bcPatch[i], r.bcRelax[i]);
   if (st == S4G_OK) st = s4g_solver_set(mesh, &r.lin, &r.outer, r.precision);
   if (st == S4G_OK) {
     r.D.assign(3 * (size_t)r.nCells, 0.0);
@@ -254,6 +261,9 @@ s4g_status s4g_server_submit(s4g_server* sv, const s4g_request* rq, uint64_t* id
   r->patchStart.assign(d->patch_start, d->patch_start + d->n_patches);
   r->patchSize.assign(d->patch_size, d->patch_size + d->n_patches);
   r->meshOpts = rq->mesh_opts;
+  if (rq->mesh_opts.part_of_cell)
+    r->partOfCell.assign(rq->mesh_opts.part_of_cell, rq->mesh_opts.part_of_cell + d->n_cells);
+  r->meshOpts.part_of_cell = nullptr;  // the copy above is used at upload
   r->law = rq->law;
   for (int i = 0; i < rq->n_bc; ++i) {
     const int p = rq->bc_patch[i];
@@ -267,6 +277,9 @@ s4g_status s4g_server_submit(s4g_server* sv, const s4g_request* rq, uint64_t* id
     r->bcHasPress.push_back(pr != nullptr);
     r->bcVec.emplace_back(v ? std::vector<double>(v, v + 3 * sz) : std::vector<double>());
     r->bcPress.emplace_back(pr ? std::vector<double>(pr, pr + sz) : std::vector<double>());
+    const double rf = rq->bc_relaxation ? rq->bc_relaxation[i] : 1.0;
+    if (!(rf > 0.0 && rf <= 1.0)) { delete r; return S4G_BAD_ARG; }
+    r->bcRelax.push_back(rf);
   }
   r->lin = rq->lin; r->outer = rq->outer; r->precision = rq->precision;
   r->model = rq->model; r->nIncrements = rq->n_increments < 1 ? 1 : rq->n_increments;

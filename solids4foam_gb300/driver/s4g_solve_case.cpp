@@ -3,7 +3,7 @@
 // inside solids4Foam, through the same C ABI and without OpenFOAM:
 //   read constant/polyMesh and 0/D            s4g_foam_read_mesh, s4g_foam_read_d
 //   load series -> increments                 s4g_foam_load_ramp, s4g_foam_read_time
-//   refuse relaxationFactors below 1          s4g_foam_read_relaxation
+//   field relaxation; refuse equation factors s4g_foam_read_relaxation
 //   upload the mesh, set law, BCs, controls   s4g_mesh_upload, s4g_material_set,
 //                                             s4g_foam_apply_bcs, s4g_solver_set
 //   evolve()                                  s4g_solve, s4g_get_gradD
@@ -81,7 +81,7 @@ int main(int argc, char** argv) {
   if (fromCase)
     check(s4g_foam_read_controls(caseDir.c_str(), &model, &law, &lin, &outer),
           "reading the case's solidProperties, mechanicalProperties and fvSolution");
-  s4g_mesh_opts mo{S4G_RENUMBER_TILED, 512, 0, 0, 0};
+  s4g_mesh_opts mo{S4G_RENUMBER_TILED, 512, 0, 0, 0, 0, nullptr};
   s4g_precision precision = S4G_FP64;
   int increments = 1, device = 0;
   bool planOnly = false, muKGiven = false, eNuGiven = false, incrementsGiven = false;
@@ -168,39 +168,53 @@ int main(int argc, char** argv) {
   double rampEnd = 0;
   int constantLoads = 0;
   if (haveD) check(s4g_foam_load_ramp(fc, &rampEnd, &constantLoads), "s4g_foam_load_ramp");
-  if (model != S4G_LIN_GEOM_TOTAL_DISP && rampEnd > 0) {
-    if (constantLoads) {
+  if (rampEnd > 0) {
+    if (model != S4G_LIN_GEOM_TOTAL_DISP && constantLoads) {
       std::fprintf(stderr, "s4g_solve_case: constant loads beside load series are not built for the "
                            "total Lagrangian models (the increments would ramp them too)\n");
       return 2;
     }
+    // The series are applied up to their end value (load factor n/N over the
+    // increments), which is the reference's load at endTime only for a run
+    // from time 0 to the series' end: any other time window is refused.
     double t0 = 0, t1 = 0, dt = 0;
-    if (!incrementsGiven &&
-        s4g_foam_read_time((caseDir + "/system/controlDict").c_str(), &t0, &t1, &dt) == S4G_OK) {
-      increments = (int)std::lround((t1 - t0) / dt);
-      if (std::fabs(t1 - rampEnd) > 1e-9 * rampEnd)
-        std::fprintf(stderr, "s4g_solve_case: warning: endTime %g is not the load series' end %g\n", t1,
-                     rampEnd);
+    if (s4g_foam_read_time((caseDir + "/system/controlDict").c_str(), &t0, &t1, &dt) == S4G_OK) {
+      if (t0 != 0.0 || std::fabs(t1 - rampEnd) > 1e-9 * rampEnd) {
+        std::fprintf(stderr,
+                     "s4g_solve_case: the load series end at %g but the run goes from %g to %g; "
+                     "only a run from 0 to the series' end is built\n",
+                     rampEnd, t0, t1);
+        return 2;
+      }
+      if (model != S4G_LIN_GEOM_TOTAL_DISP && !incrementsGiven)
+        increments = (int)std::lround((t1 - t0) / dt);
     }
   }
   if (increments < 1) {
     std::fprintf(stderr, "s4g_solve_case: increments must be >= 1\n");
     return 1;
   }
-  // field and equation relaxation of the solved field are not built
+  // field relaxation of the solved field is built (s4g_outer.field_relaxation,
+  // read with the controls); equation relaxation is not
   const std::string fvSolution = caseDir + "/system/fvSolution";
   if (access(fvSolution.c_str(), R_OK) == 0) {
     const char* solved = model == S4G_NONLIN_GEOM_TOTAL_LAG ? "DD" : "D";
     double fieldFactor = 1, eqnFactor = 1;
     check(s4g_foam_read_relaxation(fvSolution.c_str(), solved, &fieldFactor, &eqnFactor),
           "reading system/fvSolution");
-    if (fieldFactor != 1.0 || eqnFactor != 1.0) {
+    if (eqnFactor != 1.0) {
       std::fprintf(stderr,
-                   "s4g_solve_case: relaxationFactors for %s (field %g, equation %g) are not built "
-                   "on the GPU path\n",
-                   solved, fieldFactor, eqnFactor);
+                   "s4g_solve_case: equation relaxationFactors for %s (%g) are not built on the "
+                   "GPU path\n",
+                   solved, eqnFactor);
       return 2;
     }
+    if (!(fieldFactor > 0.0 && fieldFactor <= 1.0)) {
+      std::fprintf(stderr, "s4g_solve_case: field relaxation factor %g of %s is not in (0, 1]\n",
+                   fieldFactor, solved);
+      return 2;
+    }
+    outer.field_relaxation = fieldFactor;
   }
   if (planOnly) {
     std::printf("{\"case\": \"%s\", \"cells\": %d, \"faces\": %d, \"internal_faces\": %d, "
@@ -208,19 +222,19 @@ int main(int argc, char** argv) {
                 "\"levels\": %d, \"load_ramp_end\": %g, \"increments\": %d, \"model\": \"%s\", "
                 "\"law\": \"%s\", \"E\": %g, \"nu\": %g, \"mu\": %g, \"K\": %g, \"use_mu_K\": %d, "
                 "\"nCorrectors\": %d, \"tolerance\": %g, \"relTol\": %g, \"scaleFactor\": %g, "
-                "\"empty_direction\": %d}\n",
+                "\"empty_direction\": %d, \"fieldRelaxation\": %g}\n",
                 caseDir.c_str(), desc.n_cells, desc.n_faces, desc.n_internal_faces, nPoints,
                 desc.n_patches, info.n_parts, info.part_depth, info.n_levels_global, rampEnd,
                 model == S4G_LIN_GEOM_TOTAL_DISP ? 1 : increments, modelName.c_str(),
                 law.type == S4G_LINEAR_ELASTIC ? "linearElastic" : "neoHookeanElastic", law.E,
                 law.nu, law.mu, law.K, law.use_mu_K, outer.n_correctors, lin.tolerance,
-                lin.rel_tol, outer.stab_scale, mo.empty_direction);
+                lin.rel_tol, outer.stab_scale, mo.empty_direction, outer.field_relaxation);
     s4g_foam_free(fc);
     return 0;
   }
 
   // the solve
-  s4g_ctx_opts co{device, 0, 0, 0};
+  s4g_ctx_opts co{device, 0, 0, 0, 0};
   s4g_ctx* ctx = nullptr;
   check(s4g_ctx_create(&ctx, &co), "s4g_ctx_create");
   s4g_mesh* mesh = nullptr;

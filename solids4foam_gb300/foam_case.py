@@ -221,8 +221,9 @@ def annulus_polymesh(nr, nt, nz, a, b, h):
 def read_relaxation(case_dir: str, field: str = "D"):
     """(field factor, equation factor) of system/fvSolution's
     relaxationFactors for the solved field ("D", or "DD" for the incremental
-    total Lagrangian model); 1.0 where none is set.  Neither is built on the
-    device path: a case that sets one below 1 must be refused."""
+    total Lagrangian model); 1.0 where none is set.  The field factor is
+    built (read_controls returns it as outer["fieldRelaxation"]); equation
+    relaxation is not, and a case that sets it below 1 must be refused."""
     ff, ef = ct.c_double(), ct.c_double()
     _lib.check(_lib.lib().s4g_foam_read_relaxation(
         os.path.join(case_dir, "system", "fvSolution").encode(), field.encode(), ct.byref(ff),
@@ -261,7 +262,9 @@ def read_controls(case_dir: str):
                 outer=dict(nCorrectors=out.n_correctors, solutionTolerance=out.solution_tol,
                            alternativeTolerance=out.alternative_tol,
                            materialTolerance=out.material_tol, infoFrequency=out.info_frequency,
-                           stabilisation=dict(type="RhieChow", scaleFactor=out.stab_scale)))
+                           stabilisation=dict(type="RhieChow", scaleFactor=out.stab_scale),
+                           fieldRelaxation=out.field_relaxation,
+                           relaxationMethod="fixed" if out.relaxation_method == 0 else "Aitken"))
 
 
 def write_results(case_dir: str, time: str, D, sigma, gradD, polymesh: str = "constant/polyMesh",
@@ -313,24 +316,32 @@ def load_case(case_dir: str):
     resolves it: dict(mesh, bcs, model, law, solver, outer, n_increments).
     The model, law and controls come from the case's dictionaries; a total
     Lagrangian case whose loads ramp from zero runs one increment per
-    controlDict time step.  Raises for what is not built: relaxation
-    factors on the solved field, constant loads beside a ramp (total
-    Lagrangian), and everything the readers refuse."""
+    controlDict time step.  Raises for what is not built: equation
+    relaxation of the solved field, constant loads beside a ramp (total
+    Lagrangian), load series whose end is not the controlDict endTime (or a
+    startTime other than 0), and everything the readers refuse."""
     mesh, bcs = read_case(case_dir)
     c = read_controls(case_dir)
     tl = c["model"] != "linearGeometryTotalDisplacement"
     if os.path.exists(os.path.join(case_dir, "system", "fvSolution")):
         field = "DD" if c["model"] == "nonLinearGeometryTotalLagrangian" else "D"
         ff, ef = read_relaxation(case_dir, field)
-        if ff != 1.0 or ef != 1.0:
-            raise ValueError(f"relaxationFactors for {field} (field {ff:g}, equation {ef:g}) "
-                             "are not built on the GPU path")
+        if ef != 1.0:
+            raise ValueError(f"equation relaxationFactors for {field} ({ef:g}) are not built on "
+                             "the GPU path")
     n_inc = 1
-    if tl and mesh.get("load_ramp_end"):
-        if mesh.get("constant_loads_beside_ramp"):
+    ramp = mesh.get("load_ramp_end")
+    if ramp:
+        if tl and mesh.get("constant_loads_beside_ramp"):
             raise ValueError("constant loads beside load series are not built for the total "
                              "Lagrangian models")
         if os.path.exists(os.path.join(case_dir, "system", "controlDict")):
             t0, t1, dt = read_time(case_dir)
-            n_inc = max(1, int(round((t1 - t0) / dt)))
+            # the series are applied up to their end value, which is the
+            # reference's load at endTime only when the two coincide
+            if t0 != 0.0 or abs(t1 - ramp) > 1e-9 * ramp:
+                raise ValueError(f"load series end at {ramp:g} but the run goes from {t0:g} to "
+                                 f"{t1:g}: only a run from 0 to the series' end is built")
+            if tl:
+                n_inc = max(1, int(round((t1 - t0) / dt)))
     return dict(mesh=mesh, bcs=bcs, n_increments=n_inc, **c)

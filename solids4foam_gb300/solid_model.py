@@ -42,10 +42,13 @@ class Context:
     """One GPU (s4g_ctx)."""
 
     def __init__(self, device: int = 0, verbose: bool = False, profile: bool = False,
-                 graphs: bool = True):
+                 graphs: bool = True, spin_limit: int = 0):
+        """spin_limit: polls a bounded device wait makes before it gives up
+        and the solve returns S4G_TIMEOUT (0: the library's default)."""
         self.L = _lib.lib()
         h = ct.c_void_p()
-        opts = _lib.CtxOpts(device, 1 if verbose else 0, 1 if profile else 0, 0 if graphs else 1)
+        opts = _lib.CtxOpts(device, 1 if verbose else 0, 1 if profile else 0, 0 if graphs else 1,
+                            int(spin_limit))
         _lib.check(self.L.s4g_ctx_create(ct.byref(h), ct.byref(opts)), "s4g_ctx_create")
         self.h = h
         self.models = weakref.WeakSet()
@@ -109,6 +112,13 @@ def _control_structs(L, solver: dict, outer: dict, precision: str = "FP64"):
     out.alternative_tol = outer.get("alternativeTolerance", out.alternative_tol)
     out.material_tol = outer.get("materialTolerance", out.material_tol)
     out.info_frequency = outer.get("infoFrequency", out.info_frequency)
+    # relaxationFactors { fields { D f; } } of fvSolution, and the
+    # <model>Coeffs relaxationMethod
+    out.field_relaxation = outer.get("fieldRelaxation", 1.0)
+    method = outer.get("relaxationMethod", "fixed")
+    if method not in ("fixed", "Aitken"):
+        raise ValueError(f"unknown relaxationMethod {method!r}")
+    out.relaxation_method = 0 if method == "fixed" else 1
     stab = outer.get("stabilisation", {"type": "RhieChow", "scaleFactor": 0.1})
     if stab.get("type", "RhieChow") != "RhieChow":
         raise ValueError("only RhieChow stabilisation is built")
@@ -124,9 +134,14 @@ class SolidModel:
                  "linearGeometryTotalDisplacement", solver: dict | None = None,
                  outer: dict | None = None, precision: str = "FP64", renumber: str = "tiled",
                  part_size: int = 512, ls_boundary_delta: int = 0, dic_subdomains: bool = False,
-                 autotune: bool = True, empty_direction: int = 0):
+                 autotune: bool = True, empty_direction: int = 0, parts=None):
         """empty_direction: 1, 2 or 3 for a 2-D case whose empty patches'
-        faces the mesh leaves out (x, y or z empty; plane strain); 0: 3-D."""
+        faces the mesh leaves out (x, y or z empty; plane strain); 0: 3-D.
+        parts: the caller's decomposition into DIC subdomains (cell ->
+        subdomain id, decomposePar's cellDecomposition); implies
+        renumber="none" and dic_subdomains=True.  outer may hold
+        fieldRelaxation (fvSolution relaxationFactors fields factor) and
+        relaxationMethod ("fixed")."""
         if model not in MODELS:
             raise ValueError(f"unknown solidModel {model!r}; valid: {list(MODELS)}")
         self.ctx = ctx
@@ -136,8 +151,13 @@ class SolidModel:
         self.n_cells = int(np.asarray(mesh["V"]).shape[0])
         keep = []
         d = _desc(mesh, keep)
+        if parts is not None:
+            parts = np.ascontiguousarray(parts, dtype=np.int32)
+            keep.append(parts)
+            renumber, dic_subdomains = "none", True
         opts = _lib.MeshOpts(RENUMBER[renumber], part_size, ls_boundary_delta,
-                             1 if dic_subdomains else 0, 0 if autotune else 1, empty_direction)
+                             1 if dic_subdomains else 0, 0 if autotune else 1, empty_direction,
+                             None if parts is None else parts.ctypes.data)
         h = ct.c_void_p()
         _lib.check(self.L.s4g_mesh_upload(ctx.h, ct.byref(d), ct.byref(opts), ct.byref(h)),
                    "s4g_mesh_upload")
@@ -300,12 +320,20 @@ class SolidModel:
         return w
 
 
-def plan(mesh, renumber: str = "tiled", part_size: int = 512, dic_subdomains: bool = False):
-    """Host-only DIC order and scheduling figures (no GPU): (perm, info)."""
+def plan(mesh, renumber: str = "tiled", part_size: int = 512, dic_subdomains: bool = False,
+         parts=None):
+    """Host-only DIC order and scheduling figures (no GPU): (perm, info).
+    parts: a caller decomposition, as for SolidModel (renumber and
+    dic_subdomains are then passed as given, so that the library's checks
+    on them can be seen)."""
     L = _lib.lib()
     keep = []
     d = _desc(mesh, keep)
-    opts = _lib.MeshOpts(RENUMBER[renumber], part_size, 0, 1 if dic_subdomains else 0)
+    if parts is not None:
+        parts = np.ascontiguousarray(parts, dtype=np.int32)
+        keep.append(parts)
+    opts = _lib.MeshOpts(RENUMBER[renumber], part_size, 0, 1 if dic_subdomains else 0, 0, 0,
+                         None if parts is None else parts.ctypes.data)
     n = d.n_cells
     perm = np.zeros(n, np.int32)
     inf = _lib.MeshInfo()
@@ -336,11 +364,13 @@ class Server:
     def submit(self, mesh, law: dict, bcs: dict, model: str = "linearGeometryTotalDisplacement",
                solver: dict | None = None, outer: dict | None = None, precision: str = "FP64",
                n_increments: int = 1, renumber: str = "tiled", part_size: int = 512,
-               dic_subdomains: bool = False):
+               dic_subdomains: bool = False, parts=None):
+        """bcs entries are (type, value, pressure[, relaxationFactor]);
+        parts as for SolidModel."""
         keep = []
         d = _desc(mesh, keep)
         names = list(mesh.get("patch_names", PATCHES))
-        patches, types, vecs, press = [], [], [], []
+        patches, types, vecs, press, relax = [], [], [], [], []
         for name, spec in bcs.items():
             i = names.index(name)
             size = int(np.asarray(mesh["patch_size"])[i])
@@ -348,8 +378,7 @@ class Server:
             types.append(BC_TYPES[spec[0]])
             v = spec[1] if len(spec) > 1 else None
             p = spec[2] if len(spec) > 2 else None
-            if len(spec) > 3 and spec[3] not in (None, 1.0):
-                raise ValueError("the solve server takes no traction relaxationFactor")
+            relax.append(1.0 if len(spec) < 4 or spec[3] is None else float(spec[3]))
             va = None if v is None else np.ascontiguousarray(
                 np.broadcast_to(np.asarray(v, np.float64), (size, 3)))
             pa = None if p is None else np.ascontiguousarray(
@@ -362,11 +391,17 @@ class Server:
         ta_ = (ct.c_int * max(nb, 1))(*types)
         va_ = (ct.c_void_p * max(nb, 1))(*vecs)
         pr_ = (ct.c_void_p * max(nb, 1))(*press)
+        rl_ = (ct.c_double * max(nb, 1))(*relax)
         lin, out, prec = _control_structs(self.L, solver or {}, outer or {}, precision)
         rq = _lib.Request()
         rq.mesh = ct.cast(ct.pointer(d), ct.c_void_p)
+        if parts is not None:
+            parts = np.ascontiguousarray(parts, dtype=np.int32)
+            keep.append(parts)
+            renumber, dic_subdomains = "none", True
         rq.mesh_opts = _lib.MeshOpts(RENUMBER[renumber], part_size, 0,
-                                     1 if dic_subdomains else 0, 0)
+                                     1 if dic_subdomains else 0, 0, 0,
+                                     None if parts is None else parts.ctypes.data)
         rq.law = _law_struct(law)
         rq.n_bc = nb
         rq.bc_patch = ct.cast(pa_, ct.c_void_p)
@@ -376,6 +411,7 @@ class Server:
         rq.lin, rq.outer, rq.precision = lin, out, prec
         rq.model = MODELS[model]
         rq.n_increments = int(n_increments)
+        rq.bc_relaxation = ct.cast(rl_, ct.c_void_p)
         rid = ct.c_uint64()
         _lib.check(self.L.s4g_server_submit(self.h, ct.byref(rq), ct.byref(rid)),
                    "s4g_server_submit")

@@ -91,23 +91,48 @@ def test_constant_load_beside_a_ramp_is_refused_for_tl(tmp_path):
     assert r.returncode == 2 and "constant loads beside load series" in r.stderr
 
 
-def test_relaxation_factors_are_refused(tmp_path):
-    """relaxationFactors of the solved field are not built on the device
-    path: a case that sets them is refused by name, in either fvSolution
-    form, and a factor for another field is ignored."""
+def test_relaxation_factors(tmp_path):
+    """Field relaxation of the solved field is built and read from the
+    case (in either fvSolution form; a factor for another field is
+    ignored); equation relaxation is not built and is refused by name."""
     case = _ramp_case(tmp_path)
     fvs = tmp_path / "system" / "fvSolution"
     head = "FoamFile { version 2.0; format ascii; class dictionary; object fvSolution; }\n"
     fvs.write_text(head + 'relaxationFactors { fields { "D|DD" 0.9; } equations { U 0.5; } }\n')
     r = run(case, "--plan-only")
-    assert r.returncode == 2 and "relaxationFactors for D (field 0.9, equation 1)" in r.stderr
+    assert r.returncode == 0, r.stderr
+    assert json.loads(r.stdout)["fieldRelaxation"] == 0.9
     fvs.write_text(head + "relaxationFactors { equations { DD 0.99; } }\n")
     r = run(case, "--plan-only", "--model", "nonLinearGeometryTotalLagrangian")
-    assert r.returncode == 2 and "relaxationFactors for DD (field 1, equation 0.99)" in r.stderr
+    assert r.returncode == 2 and "equation relaxationFactors for DD (0.99)" in r.stderr
     fvs.write_text(head + "relaxationFactors { D 0.7; }\n")          # the older flat form
-    assert run(case, "--plan-only").returncode == 2
+    assert json.loads(run(case, "--plan-only").stdout)["fieldRelaxation"] == 0.7
     fvs.write_text(head + "relaxationFactors { fields { p 0.3; } }\n")
-    assert run(case, "--plan-only").returncode == 0
+    assert json.loads(run(case, "--plan-only").stdout)["fieldRelaxation"] == 1
+
+
+def test_time_window_other_than_the_series_is_refused(tmp_path):
+    """Load series are applied up to their end value, which is the
+    reference's load at endTime only for a run from 0 to the series' end:
+    a run that stops before it, or starts later, is refused (exit 2), by
+    the driver and by foam_case.load_case alike."""
+    from solids4foam_gb300.foam_case import load_case
+    case = _ramp_case(tmp_path)
+    cd = tmp_path / "system" / "controlDict"
+    head = "FoamFile { version 2.0; format ascii; class dictionary; object controlDict; }\n"
+    (tmp_path / "system" / "fvSolution").write_text(
+        head + 'solvers { "D|DD" { solver PCG; preconditioner DIC; } }\n')
+    (tmp_path / "constant" / "solidProperties").write_text(
+        head + "solidModel linearGeometryTotalDisplacement;\n")
+    (tmp_path / "constant" / "mechanicalProperties").write_text(
+        head + "planeStress no;\nmechanical ( r { type linearElastic; E 2e11; nu 0.3; } );\n")
+    for window in ("startTime 0;\nendTime 5;\ndeltaT 0.5;\n", "startTime 2;\nendTime 10;\ndeltaT 0.5;\n"):
+        cd.write_text(head + window)
+        for model in ("linearGeometryTotalDisplacement", "nonLinearGeometryTotalLagrangian"):
+            r = run(case, "--plan-only", "--model", model)
+            assert r.returncode == 2 and "only a run from 0 to the series' end" in r.stderr
+        with pytest.raises(ValueError, match="only a run from 0 to the series' end"):
+            load_case(case)
 
 
 def test_controls_come_from_the_case(tmp_path):
@@ -150,5 +175,9 @@ def test_python_load_case_matches_the_driver(tmp_path):
     (tmp_path / "system" / "fvSolution").write_text(
         head + 'solvers { "D|DD" { solver PCG; preconditioner DIC; } }\n'
         'relaxationFactors { fields { DD 0.8; } }\n')
-    with pytest.raises(ValueError, match="relaxationFactors for DD"):
+    assert load_case(case)["outer"]["fieldRelaxation"] == 0.8
+    (tmp_path / "system" / "fvSolution").write_text(
+        head + 'solvers { "D|DD" { solver PCG; preconditioner DIC; } }\n'
+        'relaxationFactors { equations { DD 0.8; } }\n')
+    with pytest.raises(ValueError, match="equation relaxationFactors for DD"):
         load_case(case)

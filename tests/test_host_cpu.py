@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol(built):
     for n in names:
         assert hasattr(L, n), n
     assert set(names) == set(_lib.declared_symbols())
-    assert L.s4g_abi_version() == 4
+    assert L.s4g_abi_version() == 5
     assert L.s4g_status_str(_lib.NOT_CONVERGED) == b"NOT_CONVERGED"
 
 
@@ -251,7 +251,31 @@ def test_server_footprint_of_the_models(built):
     assert used["nonLinearGeometryTotalLagrangian"] > used["linearGeometryTotalDisplacement"] > 0
     assert (used["nonLinearGeometryTotalLagrangianTotalDisplacement"]
             == used["nonLinearGeometryTotalLagrangian"])
+    # a solidTraction relaxationFactor travels with the request; one outside
+    # (0, 1] is refused at submit
     srv = sg.Server(max_slots=1, dry_run=True)
-    with pytest.raises(ValueError, match="relaxationFactor"):
-        srv.submit(m, lin, {"zmax": ("solidTraction", [0, 0, -1e5], None, 0.5)})
+    rid = srv.submit(m, lin, {"zmax": ("solidTraction", [0, 0, -1e5], None, 0.5)})
+    assert srv.result(rid)[0] == _lib.OK
+    with pytest.raises(_lib.S4GError, match="BAD_ARG"):
+        srv.submit(m, lin, {"zmax": ("solidTraction", [0, 0, -1e5], None, 1.5)})
     srv.close()
+
+
+def test_caller_decomposition_plan(built):
+    """s4g_mesh_opts.part_of_cell: the caller's subdomains become the
+    processor-local DIC's parts (in the caller's cell order); it needs the
+    caller's numbering and the processor-local DIC, and ids must be dense."""
+    from oracle.box_mesh import block_parts
+    m = sg.box_mesh(16, 8, 8, 1.0, 1.0, 1.0, 0.2, 3)
+    parts = block_parts(16, 8, 8, 4)
+    perm, info = plan(m, renumber="none", dic_subdomains=True, parts=parts)
+    assert info["n_parts"] == 16 and np.array_equal(perm, np.arange(16 * 8 * 8))
+    # in-part levels of a 4^3 block in lexicographic order: i + j + k
+    assert info["max_local_levels"] == 10
+    for kw in (dict(renumber="tiled", dic_subdomains=True), dict(renumber="none")):
+        with pytest.raises(_lib.S4GError, match="part_of_cell"):
+            plan(m, parts=parts, **kw)
+    gap = parts.copy()
+    gap[gap == 3] = 2
+    with pytest.raises(_lib.S4GError, match="every id used"):
+        plan(m, renumber="none", dic_subdomains=True, parts=gap)

@@ -429,3 +429,35 @@ def test_cooks_membrane_against_the_reference(tmp_path):
         corner[n] = point_displacement(m, D, G)[k, 1].mean() * 1e3      # mm
     assert abs(corner[20] - 32.12) < 0.01 * 32.12
     assert corner[20] < corner[40] < 32.28 and abs(corner[40] - 32.24) < 0.005 * 32.24
+
+
+@pytest.mark.parametrize("args", [(3, 4, 5, 1.0, 2.0, 0.5, 0.2, 7), (10, 8, 6, 1.0, 1.0, 1.0, 0.3, 3),
+                                  (24, 20, 16, 1.0, 1.0, 1.0, 0.2, 1),
+                                  (17, 5, 9, 2.0, 0.2, 0.3, 0.0, 1)])
+def test_oracle_box_mesh_equals_the_library_generator(built, args):
+    """The oracle's own numpy box generator (oracle/box_mesh.py), which the
+    CPU baseline uses so that no product code computes its inputs, gives
+    the library generator's mesh bit for bit: addressing, points and the
+    primitiveMesh geometry."""
+    from oracle.box_mesh import box_mesh
+    a = box_mesh(*args, points=True)
+    b = sg.box_mesh(*args, points=True)
+    for k in ("owner", "neighbour", "C", "V", "Cf", "Sf", "patch_start", "patch_size", "points"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_caller_subdomain_dic_is_thread_count_independent():
+    """The processor-local DIC over a caller decomposition (dic_domain)
+    gives the same solve on one thread and on several: the subdomains are
+    independent and each is swept in cell order (only the OpenMP sums of
+    the dot products change their order)."""
+    from oracle.box_mesh import box_mesh, block_parts
+    m = box_mesh(12, 10, 8, 1.0, 1.0, 1.0, 0.2, 5)
+    dom = block_parts(12, 10, 8, 4)
+    bcs = [(1, None, None)] * 4 + [(0, None, None), (1, None, np.full(120, 1e6))]
+    out = [pyoracle.solve(m, bcs, dic_domain=dom, E=70e9, nu=0.33, n_threads=t, n_correctors=400)
+           for t in (1, 4)]
+    assert out[0][3]["n_correctors"] == out[1][3]["n_correctors"]
+    assert out[0][3]["converged"] == 1
+    rel = lambda a, b: np.linalg.norm(a - b) / np.linalg.norm(b)
+    assert rel(out[1][0], out[0][0]) < 1e-10 and rel(out[1][1], out[0][1]) < 1e-10
