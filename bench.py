@@ -1,25 +1,31 @@
 #!/usr/bin/env python
 """Benchmark of the segregated finite-volume solid solve on GB300.
 
-One step is one full solve of the benchmark case: the 128^3 jittered unit cube (2,097,152 hex cells, interior vertices jittered +-0.2 h,
-seed 1), linear elastic E = 70 GPa, nu = 0.33, bottom fixed, top pressure
-10 MPa, sides traction-free, linearGeometryTotalDisplacement with PCG+DIC
-(tol 1e-9, relTol 0.1) and outer tolerance 1e-6 / 2000 correctors -- run to
+One step is one full solve of the benchmark case: the 128^3 jittered unit
+cube (2,097,152 hex cells, interior vertices jittered +-0.2 h, seed 1),
+linear elastic E = 70 GPa, nu = 0.33, bottom fixed, top pressure 10 MPa,
+sides traction-free, linearGeometryTotalDisplacement with PCG+DIC (tol 1e-9,
+relTol 0.1) and outer tolerance 1e-6 / 2000 correctors -- run to
 convergence through the library's public API.  By default the inner solves
-run in FP32 with FP64 refinement and the DIC factor is processor-local over
-the library's cell parts (the preconditioner of a decomposed run); one plain
-FP64 solve of the same case is timed beside it.  Inputs are synthetic
-(generated from the seed), the working set (about 1.7 GB) is far larger than
-L2, so no L2 flush is needed between steps.
+run in FP32 with FP64 refinement, and the DIC is processor-local over
+8^3-cell blocks given as the caller's decomposition (the preconditioner of a
+decomposed run with 4096 processors); one plain FP64 solve of the same case
+is timed beside it.  Inputs are synthetic (generated from the seed); the
+working set (about 1.7 GB) is far larger than L2, so no L2 flush is needed
+between steps.  The timed steps run the production path (CUDA graphs, no
+per-kernel events); the per-kernel breakdown and the roofline come from one
+more solve with CUDA events on every launch.
 
   python bench.py [--gpus N --steps K --warmup W] [--impl reference]
-                  [--precision FP32_REFINE|FP64] [--n 128] [--dic decomposed|exact]
-                  [--no-fp64] [--no-cpu] [--e2e-steps 1]
+                  [--precision FP32_REFINE|FP64] [--n 128] [--dic blocks|library|exact]
+                  [--no-fp64] [--no-cpu] [--no-batched] [--no-served] [--e2e-steps 1]
 
---impl reference times the CPU FP64 oracle (the restatement of the
-reference's solve; the reference itself needs an OpenFOAM installation that
-is not available) on all host cores over a bounded sample of correctors of
-the same case and reports the same metric, scaled to a full solve.
+--impl reference runs one full FP64 CPU solve of the same case by the oracle
+(the restatement of the reference's solve; the reference itself needs an
+OpenFOAM installation that is not available) on all host cores, with the
+same DIC subdomains and inputs from the oracle's own mesh generator, and
+reports the same metric.  It leaves its result where a GPU arm run after it
+on the same machine finds it and reports its error against it.
 """
 from __future__ import annotations
 
@@ -29,6 +35,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -162,6 +169,25 @@ def build_case(n):
     return cube_case(n)
 
 
+def cache_path(n):
+    """Where the reference arm leaves its oracle result, for the GPU arm of
+    the same run on the same machine to measure its error against."""
+    d = os.environ.get("S4G_BENCH_CACHE") or os.path.join(tempfile.gettempdir(), "s4g_bench")
+    return os.path.join(d, f"oracle_cube{n}_seed1_jitter0.2_blocks8.npz")
+
+
+def oracle_case(n):
+    """The benchmark case built by the oracle's own code (oracle/box_mesh.py:
+    the same mesh, bit for bit, as the library's generator) with the same
+    8^3-block decomposition: nothing of the product computes the CPU
+    baseline's inputs."""
+    from oracle.box_mesh import block_parts, box_mesh
+    mesh = box_mesh(n, n, n, 1.0, 1.0, 1.0, 0.2, 1)
+    top = int(mesh["patch_size"][5])
+    bcs = [(1, None, None)] * 4 + [(0, None, None), (1, None, np.full(top, 10e6))]
+    return mesh, bcs, block_parts(n, n, n, 8)
+
+
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -188,53 +214,74 @@ def allmax(dist, x):
     return float(t.item())
 
 
-def cpu_sample(case, n_correctors_full, sample_s=20.0, threads=None):
-    """Times the CPU oracle on the first correctors of the case with all host
-    threads; returns (solves/s scaled to a full solve, details)."""
+def host_threads():
+    return len(os.sched_getaffinity(0)) or 1
+
+
+def cpu_sample(n, sample_s=20.0, threads=None):
+    """The CPU oracle on the first correctors of the benchmark case, all host
+    threads, the same decomposition as the GPU arm: (seconds per corrector,
+    details).  A bounded sample, for a quick figure beside the GPU line."""
     from oracle import pyoracle
-    from solids4foam_gb300.cases import oracle_bcs
-    threads = threads or len(os.sched_getaffinity(0)) or 1
-    bcs = oracle_bcs(case["mesh"], case["bcs"])
-    law = case["law"]
-    # the oracle stops after the corrector that passes sample_s of wall time
-    _, _, _, pm = pyoracle.solve(case["mesh"], bcs, E=law["E"], nu=law["nu"], n_threads=threads,
-                                 max_seconds=sample_s, n_correctors=2000)
-    per_corr = pm["seconds"] / pm["n_correctors"]
-    full = n_correctors_full or pm["n_correctors"]
-    est = per_corr * full
-    return 1.0 / est, {
+    threads = threads or host_threads()
+    mesh, bcs, parts = oracle_case(n)
+    _, _, _, pm = pyoracle.solve(mesh, bcs, dic_domain=parts, E=70e9, nu=0.33,
+                                 n_threads=threads, max_seconds=sample_s, n_correctors=2000)
+    return pm["seconds"] / pm["n_correctors"], {
         "cores": threads,
-        "sample": (f"first {pm['n_correctors']} correctors of the same case "
-                   f"({pm['seconds']:.1f} s, {pm['total_lin_iters']} PCG iterations, "
-                   f"DIC restricted to {threads} thread subdomains), scaled to {full} correctors"),
-        "seconds_per_corrector": per_corr,
-    }
+        "sample": (f"first {pm['n_correctors']} correctors of the same case ({pm['seconds']:.1f} s, "
+                   f"{pm['total_lin_iters']} PCG iterations, DIC over the same 8^3-cell blocks)")}
 
 
 def run_reference(args):
+    """The reference arm: one full FP64 CPU solve of the benchmark case by the
+    oracle (the restatement of the reference's solve; the reference needs an
+    OpenFOAM installation that is not available), on all host threads, with
+    the GPU arm's decomposition (DIC restricted to the same 8^3-cell
+    blocks).  Its inputs come from the oracle's own generator.  One solve
+    takes about 20 minutes, so one step is timed, whatever --steps asks; a
+    solve that passes --ref-max-s is reported as an estimate, marked so."""
     world, rank, local, dist = dist_init()
     if rank != 0:
         return
-    case = build_case(args.n)
-    full = args.full_correctors or FULL_SOLVE_CORRECTORS_128
-    vals = []
-    info = None
-    for i in range(args.warmup + args.steps):
-        v, info = cpu_sample(case, full, sample_s=args.cpu_sample_s)
-        if i >= args.warmup:
-            vals.append(v)
-    value = statistics.median(vals)
+    from oracle import pyoracle
+    threads = host_threads()
+    mesh, bcs, parts = oracle_case(args.n)
+    D, sig, _, pm = pyoracle.solve(mesh, bcs, dic_domain=parts, E=70e9, nu=0.33,
+                                   n_threads=threads, n_correctors=2000,
+                                   max_seconds=args.ref_max_s)
+    complete = pm["converged"] == 1 or pm["n_correctors"] >= 2000
+    if complete:
+        secs = pm["seconds"]
+        sample = (f"one full solve: {pm['n_correctors']} correctors, {pm['total_lin_iters']} PCG "
+                  f"iterations, converged {pm['converged']}, DIC over the same 8^3-cell blocks")
+    else:
+        secs = pm["seconds"] / pm["n_correctors"] * args.full_correctors
+        sample = (f"ESTIMATE: stopped after {pm['n_correctors']} correctors ({pm['seconds']:.0f} s), "
+                  f"scaled to {args.full_correctors} correctors")
+    try:
+        os.makedirs(os.path.dirname(cache_path(args.n)), exist_ok=True)
+        if complete:
+            np.savez(cache_path(args.n), D=D, sigma=sig, n_correctors=pm["n_correctors"],
+                     pcg=pm["total_lin_iters"], seconds=pm["seconds"], threads=threads)
+    except OSError:
+        pass
+    value = 1.0 / secs
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "solves/s",
-        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 / value, "higher_is_better": True, "scaling": "weak",
+        "n_gpus": 1, "steps": 1, "warmup": 0, "steps_requested": args.steps,
+        "ms_per_step": 1000.0 * secs, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"cube{args.n}_jittered_linear_elastic_pcg_dic",
-                   "cells": args.n ** 3, "model": "linearGeometryTotalDisplacement",
-                   "note": "CPU FP64 oracle (restatement of the reference solve); the "
-                           "reference itself needs OpenFOAM, which is not installed"},
-        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": info["cores"],
-                         "kind": "port", "sample": info["sample"]},
+        "config": {"workload": f"cube{args.n}_jittered_linear_elastic", "cells": args.n ** 3,
+                   "model": "linearGeometryTotalDisplacement", "precision": "FP64",
+                   "dic": "blocks8 (4096 subdomains at 128^3)", "complete_solve": complete,
+                   "same_config_as_gpu_arm": "same mesh, loads, controls and DIC subdomains; "
+                   "FP64 throughout (the GPU headline runs FP32+refine, its plain_fp64 leg FP64)",
+                   "note": "CPU FP64 oracle (restatement of the reference's solve; the reference "
+                           "itself needs OpenFOAM, which is not installed); inputs from the "
+                           "oracle's own mesh generator"},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": threads, "kind": "port",
+                         "sample": sample},
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -245,15 +292,52 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
-def run_batched(args, ctx):
+class Budget:
+    """Wall-clock guard of the optional legs, so that a run stays inside
+    the time it is given."""
+
+    def __init__(self, seconds):
+        self.t0 = time.perf_counter()
+        self.seconds = seconds
+
+    def left(self):
+        return self.seconds - (time.perf_counter() - self.t0)
+
+
+def oracle_check_small(args, threads):
+    """The headline case's form at 32^3 against the oracle in this process:
+    FP32+refine and plain FP64 on the GPU, the oracle with the same blocks.
+    Stands in for the 128^3 comparison when the reference arm's result is
+    not on this machine."""
+    import solids4foam_gb300 as sg
+    from oracle import pyoracle
+    mesh, bcs_o, parts = oracle_case(32)
+    Do, so, _, po = pyoracle.solve(mesh, bcs_o, dic_domain=parts, E=70e9, nu=0.33,
+                                   n_threads=threads, n_correctors=2000)
+    c = build_case(32)
+    ctx = sg.Context(0)
+    out = {"workload": "cube32 (same form, same 8^3 blocks)", "oracle_correctors": po["n_correctors"]}
+    for prec in ("FP32_REFINE", "FP64"):
+        m = sg.SolidModel(ctx, c["mesh"], c["law"], c["bcs"], solver=c["solver"], outer=c["outer"],
+                          precision=prec, parts=c["parts"])
+        D, sig, p = m.evolve()
+        m.close()
+        out[prec] = {"rel_l2_D": rel_l2(D, Do), "rel_l2_sigma": rel_l2(sig, so),
+                     "correctors": p["n_correctors"]}
+    ctx.close()
+    return out
+
+
+def run_batched(args, ctx, budget):
     """Batched load cases (one 64^3 mesh, 64 cases, FP32+refine, one
     s4g_solve_cases call) against plain FP64 single solves of the same cases
-    one after another; both with the processor-local DIC."""
+    one after another; both over the same 8^3-cell blocks.  Case 0 is also
+    checked against the oracle."""
     import solids4foam_gb300 as sg
     from solids4foam_gb300.cases import load_cases
     lc = load_cases(args.batch_n, args.batch_cases)
     cases = lc["cases"]
-    kw = dict(solver=lc["solver"], outer=lc["outer"], dic_subdomains=True)
+    kw = dict(solver=lc["solver"], outer=lc["outer"], parts=lc["parts"])
     model = sg.SolidModel(ctx, lc["mesh"], lc["law"], cases[0], precision="FP32_REFINE", **kw)
     model.evolve_cases(cases[:2])  # warm-up: tuning, FP32 copies
     t0 = time.perf_counter()
@@ -276,24 +360,43 @@ def run_batched(args, ctx):
     m64.close()
     fp64_rate = 1.0 / statistics.mean(t64)
     rate = len(cases) / wall
-    return {"workload": f"cube{args.batch_n}_x{len(cases)}_load_cases", "cases": len(cases),
-            "cells": int(lc["mesh"]["V"].shape[0]), "solves_per_s": rate,
-            "wall_s": wall, "device_s": dev_s,
-            "correctors_min_max": [min(p["n_correctors"] for p in perfs),
-                                   max(p["n_correctors"] for p in perfs)],
-            "all_converged": all(p["converged"] == 1 for p in perfs),
-            "plain_fp64_solves_per_s": fp64_rate, "plain_fp64_cases_timed": n64,
-            "speedup_vs_plain_fp64": rate / fp64_rate,
-            "max_rel_l2_D_vs_fp64": max(errD), "max_rel_l2_sigma_vs_fp64": max(errS)}
+    out = {"workload": f"cube{args.batch_n}_x{len(cases)}_load_cases", "cases": len(cases),
+           "cells": int(lc["mesh"]["V"].shape[0]), "dic": "blocks8", "solves_per_s": rate,
+           "wall_s": wall, "device_s": dev_s,
+           "correctors_min_max": [min(p["n_correctors"] for p in perfs),
+                                  max(p["n_correctors"] for p in perfs)],
+           "all_converged": all(p["converged"] == 1 for p in perfs),
+           "plain_fp64_solves_per_s": fp64_rate, "plain_fp64_cases_timed": n64,
+           "speedup_vs_plain_fp64": rate / fp64_rate,
+           "max_rel_l2_D_vs_fp64": max(errD), "max_rel_l2_sigma_vs_fp64": max(errS)}
+    if args.batch_oracle_cases > 0 and budget.left() > 400:
+        from oracle import pyoracle
+        from oracle.box_mesh import block_parts, box_mesh
+        n = args.batch_n
+        mo = box_mesh(n, n, n, 1.0, 1.0, 1.0, 0.2, 2)
+        top = int(mo["patch_size"][5])
+        errs = []
+        for c in range(min(args.batch_oracle_cases, len(cases))):
+            bo = [(1, None, None)] * 4 + [(0, None, None),
+                                          (1, np.tile(lc["loads"][c], (top, 1)), None)]
+            Do, so, _, po = pyoracle.solve(mo, bo, dic_domain=block_parts(n, n, n, 8), E=200e9,
+                                           nu=0.3, n_threads=host_threads(), n_correctors=2000)
+            errs.append((rel_l2(Db[c], Do), rel_l2(sb[c], so)))
+        out["oracle_cases_checked"] = len(errs)
+        out["max_rel_l2_D_vs_oracle"] = max(e[0] for e in errs)
+        out["max_rel_l2_sigma_vs_oracle"] = max(e[1] for e in errs)
+    return out
 
 
-def run_served(args):
-    """A Poisson stream of uneven solves (linear FP32+refine with the
-    processor-local DIC; a --serve-tl-fraction share of neoHookean total
-    Lagrangian requests, 0 by default) through the server, against the same
-    requests solved one after another in plain FP64."""
+def run_served(args, budget):
+    """The served stream of config form 4 (Poisson arrivals; 80% linear
+    elastic, 20% neoHookean total Lagrangian over 10 increments; jittered
+    boxes of 8^3-96^3 cells; FP32+refine over 8^3-cell blocks) through the
+    server, against the same requests solved one after another in plain
+    FP64.  Requests of up to --serve-oracle-cells cells are also checked
+    against the oracle."""
     import solids4foam_gb300 as sg
-    from solids4foam_gb300.cases import served_stream
+    from solids4foam_gb300.cases import oracle_bcs, served_stream
     stream = served_stream(args.serve_n, tl_fraction=args.serve_tl_fraction)
     srv = sg.Server(max_slots=args.serve_slots)
     t0 = time.perf_counter()
@@ -304,47 +407,81 @@ def run_served(args):
             time.sleep(wait)
         kw = dict(req)
         kw["precision"] = "FP32_REFINE"
-        if kw.get("model", "linearGeometryTotalDisplacement") == "linearGeometryTotalDisplacement":
-            kw["dic_subdomains"] = True
         ids.append(srv.submit(**kw))
     results = [srv.result(i) for i in ids]
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
-    # plain FP64, one request after another
-    ctx = sg.Context(0)
-    seq, errs = 0.0, []
-    for (arrival, req), res in zip(stream, results):
-        kw = dict(req)
-        n_inc = kw.pop("n_increments", 1)
-        if kw.get("model", "linearGeometryTotalDisplacement") == "linearGeometryTotalDisplacement":
-            kw["dic_subdomains"] = True  # the same preconditioner as the served run
-        m = sg.SolidModel(ctx, kw.pop("mesh"), kw.pop("law"), kw.pop("bcs"), precision="FP64", **kw)
-        t1 = time.perf_counter()
-        D, sig, perf = m.evolve(n_increments=n_inc)
-        seq += time.perf_counter() - t1
-        m.close()
-        errs.append(rel_l2(res[1], D))
-    ctx.close()
     n = len(stream)
-    return {"workload": f"stream{n}_poisson_boxes_8^3-40^3",
-            "neoHookean_fraction": args.serve_tl_fraction,
-            "requests": n, "slots": args.serve_slots, "solves_per_s": n / wall,
-            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
-            "all_ok": all(r[0] in (0, 3) for r in results),
-            "plain_fp64_sequential_solves_per_s": n / seq,
-            "speedup_vs_plain_fp64_sequential": (n / wall) / (n / seq),
-            "max_rel_l2_D_vs_fp64": max(errs)}
+    out = {"workload": f"stream{n}_poisson_boxes_8^3-96^3",
+           "neoHookean_fraction": args.serve_tl_fraction,
+           "neoHookean_requests": sum(1 for _, r in stream if "model" in r),
+           "requests": n, "slots": args.serve_slots, "solves_per_s": n / wall,
+           "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "mean_ms": st["mean_ms"],
+           "all_converged": all(r[0] == 0 for r in results),
+           "statuses": [int(r[0]) for r in results]}
+    # plain FP64, one request after another
+    if budget.left() > 2.5 * wall + 60:
+        ctx = sg.Context(0)
+        seq, errs = 0.0, []
+        for (arrival, req), res in zip(stream, results):
+            kw = dict(req)
+            n_inc = kw.pop("n_increments", 1)
+            m = sg.SolidModel(ctx, kw.pop("mesh"), kw.pop("law"), kw.pop("bcs"), precision="FP64",
+                              **kw)
+            t1 = time.perf_counter()
+            D, sig, perf = m.evolve(n_increments=n_inc)
+            seq += time.perf_counter() - t1
+            m.close()
+            errs.append(rel_l2(res[1], D))
+        ctx.close()
+        out.update({"plain_fp64_sequential_solves_per_s": n / seq,
+                    "speedup_vs_plain_fp64_sequential": (n / wall) / (n / seq),
+                    "max_rel_l2_D_vs_fp64": max(errs)})
+    else:
+        out["plain_fp64_sequential"] = "skipped: not enough of the run's time budget left"
+    if args.serve_oracle_cells > 0 and budget.left() > 120:
+        from oracle import pyoracle
+        errs = []
+        for (arrival, req), res in zip(stream, results):
+            m = req["mesh"]
+            if m["V"].shape[0] > args.serve_oracle_cells:
+                continue
+            law, o = req["law"], req["outer"]
+            kw = dict(n_correctors=o["nCorrectors"], field_relaxation=o["fieldRelaxation"],
+                      n_threads=host_threads(), dic_domain=req["parts"])
+            if law["type"] == "linearElastic":
+                kw.update(E=law["E"], nu=law["nu"])
+            else:
+                kw.update(model=1, law=1, use_mu_K=1, mu=law["mu"], K=law["K"],
+                          n_increments=req["n_increments"])
+            Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, req["bcs"]), **kw)
+            errs.append((rel_l2(res[1], Do), rel_l2(res[2], so)))
+        if errs:
+            out["oracle_requests_checked"] = len(errs)
+            out["max_rel_l2_D_vs_oracle"] = max(e[0] for e in errs)
+            out["max_rel_l2_sigma_vs_oracle"] = max(e[1] for e in errs)
+    return out
+
+
+def model_kwargs(case, args):
+    kw = dict(solver=case["solver"], outer=case["outer"], precision=args.precision)
+    if args.dic == "blocks":
+        kw["parts"] = case["parts"]
+    elif args.dic == "library":
+        kw["dic_subdomains"] = True
+    return kw
 
 
 def run_gb300(args):
     import solids4foam_gb300 as sg
+    budget = Budget(args.budget_s)
     world, rank, local, dist = dist_init()
     case = build_case(args.n)
     mesh = case["mesh"]
-    ctx = sg.Context(local, profile=True)
-    kw = dict(solver=case["solver"], outer=case["outer"], precision=args.precision,
-              dic_subdomains=(args.dic == "decomposed"))
+    kw = model_kwargs(case, args)
+    # the production path: CUDA graphs on, no per-kernel events
+    ctx = sg.Context(local)
     model = sg.SolidModel(ctx, mesh, case["law"], case["bcs"], **kw)
     for _ in range(args.warmup):
         model.evolve()
@@ -352,9 +489,11 @@ def run_gb300(args):
     sampler.start()
     barrier(dist)
     perfs = []
+    tw0 = time.perf_counter()
     for _ in range(args.steps):
         D, sig, perf = model.evolve()
         perfs.append(perf)
+    wall_steps = time.perf_counter() - tw0
     barrier(dist)
     clocks = sampler.stop()
     ms = [p["solve_ms"] for p in perfs]
@@ -367,6 +506,8 @@ def run_gb300(args):
                                                      "patch_start", "patch_size"))
     h2d += sum(np.asarray(v).nbytes for _, v, p in case["bcs"].values() if v is not None)
     h2d += sum(np.asarray(p).nbytes for _, v, p in case["bcs"].values() if p is not None)
+    if "parts" in kw:
+        h2d += kw["parts"].nbytes
     d2h = mesh["V"].shape[0] * 8 * (3 + 6)
     for _ in range(args.e2e_steps):
         barrier(dist)
@@ -377,17 +518,21 @@ def run_gb300(args):
         e2e_ms.append(1000.0 * (time.perf_counter() - t0))
     e2e_step = allmax(dist, statistics.mean(e2e_ms)) if e2e_ms else None
 
-    # roofline of the dominant kernel (CUDA events on the library's stream)
+    # per-kernel CUDA events of one more solve, launched kernel by kernel
+    ctxp = sg.Context(local, profile=True)
+    mp = sg.SolidModel(ctxp, mesh, case["law"], case["bcs"], **kw)
+    _, _, pp = mp.evolve()
     v = 8 if args.precision == "FP64" else 4
     nC, nI = mesh["V"].shape[0], mesh["neighbour"].shape[0]
     nB = mesh["owner"].shape[0] - nI
-    tot_ms = {k: sum(p["kernel_ms"][k] for p in perfs) for k in perfs[0]["kernel_ms"]}
-    tot_n = {k: sum(p["kernel_launches_by"][k] for p in perfs) for k in perfs[0]["kernel_ms"]}
+    tot_ms, tot_n = pp["kernel_ms"], pp["kernel_launches_by"]
     dom = max(tot_ms, key=lambda k: tot_ms[k])
     peak, peak_kind = peaks()
     avg_ms = tot_ms[dom] / max(1, tot_n[dom])
-    n_loc = model.info()["n_local_entries"]
-    split = perfs[0]["spmv_unroll"] == 0 and perfs[0]["part_threads"] > 0
+    n_loc = mp.info()["n_local_entries"]
+    split = pp["spmv_unroll"] == 0 and pp["part_threads"] > 0
+    mp.close()
+    ctxp.close()
     ab = algorithmic_bytes(dom, nC, nI, nB, v, n_loc, split)
     achieved = ab / (avg_ms * 1e-3) / 1e9 if ab else None
     workload = f"cube{args.n}_{args.precision.lower()}_{args.dic}"
@@ -403,26 +548,54 @@ def run_gb300(args):
 
     # plain FP64 solve of the same case, for the FP32+refine comparison
     fp64 = None
+    D64 = s64 = None
     if args.precision != "FP64" and not args.no_fp64:
         kw64 = dict(kw, precision="FP64")
         m64 = sg.SolidModel(ctx, mesh, case["law"], case["bcs"], **kw64)
         D64, s64, p64 = m64.evolve()
         m64.close()
-        relD = float(np.linalg.norm(D - D64) / np.linalg.norm(D64))
-        relS = float(np.linalg.norm(sig - s64) / np.linalg.norm(s64))
         fp64 = {"solves_per_s": 1000.0 / p64["solve_ms"], "ms_per_solve": p64["solve_ms"],
                 "n_correctors": p64["n_correctors"], "pcg_iterations": p64["total_lin_iters"],
                 "speedup_of_fp32_refine": p64["solve_ms"] / ms_step,
-                "rel_l2_D_fp32_vs_fp64": relD, "rel_l2_sigma_fp32_vs_fp64": relS}
+                "rel_l2_D_fp32_vs_fp64": rel_l2(D, D64), "rel_l2_sigma_fp32_vs_fp64": rel_l2(sig, s64)}
 
-    batched = run_batched(args, ctx) if (rank == 0 and not args.no_batched) else None
-    served = run_served(args) if (rank == 0 and not args.no_served) else None
+    # error against the FP64 oracle: the reference arm's full solve when it
+    # ran on this machine before this arm, else the same form at 32^3
+    parity = None
+    if rank == 0:
+        cp = cache_path(args.n)
+        if os.path.exists(cp):
+            ref = np.load(cp)
+            parity = {"against": "the reference arm's full oracle solve of this case",
+                      "oracle_correctors": int(ref["n_correctors"]),
+                      "rel_l2_D": rel_l2(D, ref["D"]), "rel_l2_sigma": rel_l2(sig, ref["sigma"])}
+            if D64 is not None:
+                parity["plain_fp64"] = {"rel_l2_D": rel_l2(D64, ref["D"]),
+                                        "rel_l2_sigma": rel_l2(s64, ref["sigma"])}
+        elif not args.no_cpu and budget.left() > 300:
+            parity = oracle_check_small(args, host_threads())
+
+    batched = (run_batched(args, ctx, budget)
+               if (rank == 0 and not args.no_batched and budget.left() > 300) else None)
+    served = (run_served(args, budget)
+              if (rank == 0 and not args.no_served and budget.left() > 300) else None)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cv, info = cpu_sample(case, perfs[0]["n_correctors"], sample_s=args.cpu_sample_s)
-        cpu = {"value": cv, "unit": "solves/s", "cores": info["cores"], "kind": "port",
-               "sample": info["sample"]}
+        cp = cache_path(args.n)
+        if os.path.exists(cp):
+            ref = np.load(cp)
+            cpu = {"value": 1.0 / float(ref["seconds"]), "unit": "solves/s",
+                   "cores": int(ref["threads"]), "kind": "port",
+                   "sample": f"the reference arm's full solve in this run ({int(ref['n_correctors'])} "
+                             f"correctors, DIC over the same 8^3-cell blocks)"}
+        else:
+            spc, info = cpu_sample(args.n, sample_s=args.cpu_sample_s)
+            cpu = {"value": 1.0 / (spc * perfs[0]["n_correctors"]), "unit": "solves/s",
+                   "cores": info["cores"], "kind": "port",
+                   "sample": info["sample"] + f", scaled to this solve's "
+                             f"{perfs[0]['n_correctors']} correctors (estimate)"}
+    ctx.close()
     if rank != 0:
         return
     p0 = perfs[0]
@@ -436,14 +609,16 @@ def run_gb300(args):
                    "model": "linearGeometryTotalDisplacement", "law": "linearElastic",
                    "solver": "PCG+DIC tol 1e-9 relTol 0.1", "outer": "solutionTolerance 1e-6, "
                    "nCorrectors 2000", "precision": args.precision, "dic": args.dic,
-                   "dic_subdomains": model.info()["n_parts"] if args.dic == "decomposed" else 1,
-                   "parallelism": f"replicas{world}",
+                   "dic_subdomains": int(model.info()["n_parts"]) if args.dic != "exact" else 1,
+                   "parallelism": f"replicas{world}", "path": "production (CUDA graphs, no "
+                   "per-kernel events); kernels/roofline from one profiled solve in this run",
                    "l2": "working set ~1.7 GB >> 129 MB L2 (no flush needed)",
                    "n_correctors": p0["n_correctors"], "converged": p0["converged"],
                    "autotuned": {"part_threads": p0["part_threads"],
                                  "spmv": ("split" if p0["spmv_unroll"] == 0 else
                                           f"fused, unroll {p0['spmv_unroll']}")},
-                   "pcg_iterations": p0["total_lin_iters"]},
+                   "pcg_iterations": p0["total_lin_iters"],
+                   "wall_s_of_timed_steps": wall_steps},
         "e2e": {"value": (world * 1000.0 / e2e_step) if e2e_step else None, "unit": "solves/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(sum(p["kernel_launches"] for p in perfs)),
@@ -452,12 +627,14 @@ def run_gb300(args):
                      "peak_source": peak_kind, "traffic": traffic,
                      "algorithmic_bytes_per_launch": ab, "avg_launch_us": avg_ms * 1000},
         "kernels": kernels,
+        "error_vs_oracle": parity,
         "plain_fp64": fp64,
         "batched": batched,
         "served": served,
         "cpu_baseline": cpu,
         "clocks": clocks,
     }
+    model.close()
     print(json.dumps(line), flush=True)
 
 
@@ -468,24 +645,35 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="FP32_REFINE", choices=["FP64", "FP32_REFINE"])
-    ap.add_argument("--dic", default="decomposed", choices=["exact", "decomposed"])
+    ap.add_argument("--dic", default="blocks", choices=["blocks", "library", "exact"],
+                    help="DIC subdomains: 8^3-cell blocks (a decomposed run's processors), "
+                         "the library's own parts, or the exact global DIC")
     ap.add_argument("--no-fp64", action="store_true",
                     help="skip the plain-FP64 comparison solve")
     ap.add_argument("--n", type=int, default=128)
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-sample-s", type=float, default=20.0)
-    ap.add_argument("--full-correctors", type=int, default=0)
+    ap.add_argument("--full-correctors", type=int, default=FULL_SOLVE_CORRECTORS_128)
+    ap.add_argument("--ref-max-s", type=float, default=1500.0,
+                    help="reference arm: wall time after which the CPU solve stops and is "
+                         "reported as an estimate")
+    ap.add_argument("--budget-s", type=float, default=1500.0,
+                    help="wall time the optional legs of the GPU arm may take in all")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched load cases")
     ap.add_argument("--batch-n", type=int, default=64)
     ap.add_argument("--batch-cases", type=int, default=64)
     ap.add_argument("--batch-fp64-cases", type=int, default=3,
                     help="plain FP64 single solves timed for the batched comparison")
+    ap.add_argument("--batch-oracle-cases", type=int, default=1,
+                    help="batched cases also checked against the oracle")
     ap.add_argument("--no-served", action="store_true", help="skip the served stream")
     ap.add_argument("--serve-n", type=int, default=24)
     ap.add_argument("--serve-slots", type=int, default=8)
-    ap.add_argument("--serve-tl-fraction", type=float, default=0.0,
+    ap.add_argument("--serve-tl-fraction", type=float, default=0.2,
                     help="share of neoHookean total Lagrangian requests in the stream")
+    ap.add_argument("--serve-oracle-cells", type=int, default=25000,
+                    help="served requests up to this many cells are checked against the oracle")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

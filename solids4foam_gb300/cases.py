@@ -38,6 +38,18 @@ def box_mesh(nx, ny, nz, lx=1.0, ly=1.0, lz=1.0, jitter=0.0, seed=1, points=Fals
     return m
 
 
+def block_parts(nx, ny, nz, bx=8, by=None, bz=None):
+    """A decomposition of an nx x ny x nz box into blocks of bx x by x bz
+    cells (the last block of an axis takes the remainder), numbered block i
+    fastest -- a decomposePar "simple" decomposition into regular blocks,
+    handed to the library as its DIC subdomains (SolidModel(parts=...))."""
+    by = by or bx
+    bz = bz or bx
+    nbx, nby = -(-nx // bx), -(-ny // by)
+    k, j, i = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    return ((i // bx) + nbx * ((j // by) + nby * (k // bz))).ravel().astype(np.int32)
+
+
 def patch_faces(mesh, name):
     p = PATCHES.index(name)
     s, n = int(mesh["patch_start"][p]), int(mesh["patch_size"][p])
@@ -59,10 +71,11 @@ def cantilever_case():
                 outer=dict(nCorrectors=2000, solutionTolerance=1e-6))
 
 
-def cube_case(n=128, seed=1, jitter=0.2):
+def cube_case(n=128, seed=1, jitter=0.2, block=8):
     """Unit cube n^3 with interior vertices jittered +-0.2 h (seeded),
     E = 70 GPa, nu = 0.33; bottom (z=0) fixed, top uniform pressure 10 MPa,
-    sides traction-free; PCG+DIC tol 1e-9 relTol 0.1; outer 1e-6, 2000."""
+    sides traction-free; PCG+DIC tol 1e-9 relTol 0.1; outer 1e-6, 2000.
+    "parts": the block decomposition (block^3 cells) of a decomposed run."""
     mesh = box_mesh(n, n, n, 1.0, 1.0, 1.0, jitter, seed)
     n_top = int(mesh["patch_size"][5])
     bcs = {
@@ -71,24 +84,34 @@ def cube_case(n=128, seed=1, jitter=0.2):
     }
     return dict(mesh=mesh, bcs=bcs, law=dict(type="linearElastic", E=70e9, nu=0.33),
                 solver=dict(tolerance=1e-9, relTol=0.1, maxIter=1000),
-                outer=dict(nCorrectors=2000, solutionTolerance=1e-6))
+                outer=dict(nCorrectors=2000, solutionTolerance=1e-6),
+                parts=block_parts(n, n, n, block))
 
 
 def oracle_bcs(mesh, bcs):
     """The same boundary conditions as (type, value, pressure, relaxation)
     per patch for the CPU oracle: 0 fixedDisplacement, 1 solidTraction;
-    unnamed patches are traction-free."""
+    unnamed patches are traction-free.  Uniform values (one vector or one
+    pressure) are expanded to every face of the patch, as SolidModel.set_bc
+    does."""
     out = []
-    for name in PATCHES:
+    names = list(mesh.get("patch_names", PATCHES))
+    for p_i, name in enumerate(names):
         if name in bcs:
             t, v, p, *rest = bcs[name]
-            out.append((0 if t == "fixedDisplacement" else 1, v, p, rest[0] if rest else 1.0))
+            n = int(mesh["patch_size"][p_i])
+            if v is not None:
+                v = np.ascontiguousarray(np.broadcast_to(np.asarray(v, np.float64), (n, 3)))
+            if p is not None:
+                p = np.ascontiguousarray(np.broadcast_to(np.asarray(p, np.float64), (n,)))
+            out.append((0 if t == "fixedDisplacement" else 1, v, p,
+                        rest[0] if rest and rest[0] is not None else 1.0))
         else:
             out.append((1, None, None))
     return out
 
 
-def load_cases(n=64, n_cases=64, mesh_seed=2, load_seed=3, jitter=0.2):
+def load_cases(n=64, n_cases=64, mesh_seed=2, load_seed=3, jitter=0.2, block=8):
     """Batched load cases on one mesh: the jittered unit cube n^3 (seeded),
     E = 200 GPa, nu = 0.3, bottom fixed, and per case a uniform top traction
     whose components are drawn i.i.d. N(0, 1 MPa) (seeded); sides
@@ -100,19 +123,25 @@ def load_cases(n=64, n_cases=64, mesh_seed=2, load_seed=3, jitter=0.2):
              for c in range(n_cases)]
     return dict(mesh=mesh, bcs=cases[0], law=dict(type="linearElastic", E=200e9, nu=0.3),
                 solver=dict(tolerance=1e-9, relTol=0.1, maxIter=1000),
-                outer=dict(nCorrectors=2000, solutionTolerance=1e-6), cases=cases)
+                outer=dict(nCorrectors=2000, solutionTolerance=1e-6), cases=cases,
+                parts=block_parts(n, n, n, block), loads=t)
 
 
-def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=40 ** 3, tl_fraction=0.2,
-                  rate_per_s=20.0, nu_max=0.4):
+def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=96 ** 3, tl_fraction=0.2,
+                  rate_per_s=20.0, nu_max=0.45, block=8):
     """A stream of solve requests with Poisson arrivals (rate_per_s, seeded):
     jittered boxes whose cell counts are log-uniform in [min_cells,
-    max_cells] with aspect ratios up to 2; a tl_fraction of them are
-    neoHookeanElastic nonLinearGeometryTotalLagrangian solves (mu uniform in
-    0.5-5 MPa, K/mu uniform in 10-50, traction ramped over 10 increments),
-    the rest linearElastic (E log-uniform 1-300 GPa, nu uniform in
-    0.2-nu_max; the segregated corrector loop stops converging near nu = 0.42
-    on these meshes, in the CPU oracle as well, so nu_max defaults to 0.4).
+    max_cells] with aspect ratios up to 2, bottom fixed, top traction.
+    A tl_fraction of them are neoHookeanElastic
+    nonLinearGeometryTotalLagrangian solves: mu uniform in 0.5-5 MPa, K/mu
+    uniform in 10-50, traction (0, 0.05 mu, -0.05 mu) ramped over 10
+    increments.  The rest are linearElastic: E log-uniform in 1-300 GPa, nu
+    uniform in 0.2-nu_max, traction N(0, 1 MPa) per component.  The
+    segregated corrector loop needs field relaxation (relaxationFactors
+    fields D / DD) for nu above about 0.38 and for the neoHookean requests
+    -- the reference's own loop behaves the same way -- so those requests
+    set 0.7, and the neoHookean ones allow 5000 correctors per increment.
+    Each request carries its block decomposition (block^3 cells).
     Returns a list of (arrival_s, request kwargs)."""
     rng = np.random.default_rng(seed)
     t = 0.0
@@ -126,6 +155,7 @@ def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=40 ** 3, tl
         ny = max(4, int(round(cells / (nx * nz))))
         mesh = box_mesh(nx, ny, nz, nx / nz, ny / nz, 1.0, 0.2, 100 + i)
         top = int(mesh["patch_size"][5])
+        parts = block_parts(nx, ny, nz, block)
         if rng.uniform() < tl_fraction:
             mu = rng.uniform(0.5e6, 5e6)
             K = mu * rng.uniform(10.0, 50.0)
@@ -134,7 +164,7 @@ def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=40 ** 3, tl
                        bcs={"zmin": ("fixedDisplacement", None, None),
                             "zmax": ("solidTraction", tr, None)},
                        model="nonLinearGeometryTotalLagrangian", n_increments=10,
-                       outer=dict(nCorrectors=200))
+                       outer=dict(nCorrectors=5000, fieldRelaxation=0.7), parts=parts)
         else:
             E = np.exp(rng.uniform(np.log(1e9), np.log(300e9)))
             nu = rng.uniform(0.2, nu_max)
@@ -142,6 +172,7 @@ def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=40 ** 3, tl
             req = dict(mesh=mesh, law=dict(type="linearElastic", E=E, nu=nu),
                        bcs={"zmin": ("fixedDisplacement", None, None),
                             "zmax": ("solidTraction", tr, None)},
-                       outer=dict(nCorrectors=2000))
+                       outer=dict(nCorrectors=4000, fieldRelaxation=0.7 if nu > 0.35 else 1.0),
+                       parts=parts)
         out.append((t, req))
     return out

@@ -1,0 +1,283 @@
+"""GPU tests of the device features beside the plain loop, each against the
+CPU oracle: field relaxation (relaxField "fixed"), a caller's decomposition
+into DIC subdomains on the benchmark's cube form at 32^3, batched load cases
+and served requests of the benchmark's streams, the bounded-wait timeout and
+the NaN stop (failure paths that fault nothing), and the total Lagrangian
+paths that only the oracle had run: the enforceLinear switch and fixed
+values carried across increments (rigid rotation).
+
+Bars, from the solve's specification: relative L2 error of D <= 1e-6 and
+of sigma <= 1e-5 against the FP64 oracle at the same settings.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import solids4foam_gb300 as sg
+from solids4foam_gb300 import _lib
+from solids4foam_gb300.cases import oracle_bcs
+from oracle import pyoracle
+from oracle.box_mesh import block_parts, box_mesh as oracle_box_mesh
+
+pytestmark = pytest.mark.gpu
+TOL_D, TOL_S = 1e-6, 1e-5
+THREADS = min(16, os.cpu_count() or 1)
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def test_field_relaxation_linear_matches_oracle(ctx):
+    """relaxationFactors { fields { D 0.7; } } on a jittered box at nu = 0.45
+    under a shear traction, where the unrelaxed loop runs away: cells and
+    boundary faces relaxed after each solve, as the oracle does."""
+    m = sg.box_mesh(10, 10, 10, 1.0, 1.0, 1.0, 0.2, 3)
+    t = np.tile([1e5, 0.0, -1e6], (int(m["patch_size"][5]), 1))
+    bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", t, None)}
+    outer = dict(nCorrectors=3000, fieldRelaxation=0.7)
+    model = sg.SolidModel(ctx, m, dict(type="linearElastic", E=200e9, nu=0.45), bcs, outer=outer)
+    D, sig, perf = model.evolve()
+    Do, so, Go, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=model.permutation(), E=200e9,
+                                    nu=0.45, n_correctors=3000, field_relaxation=0.7,
+                                    n_threads=THREADS)
+    assert po["converged"] == 1 and perf["converged"] == 1
+    assert abs(perf["n_correctors"] - po["n_correctors"]) <= 1
+    assert rel(D, Do) < TOL_D and rel(sig, so) < TOL_S
+    assert rel(model.gradD(), Go) < TOL_S
+    model.close()
+
+
+def test_field_relaxation_tl_matches_oracle(ctx):
+    """Field relaxation of DD in the incremental total Lagrangian model
+    (neoHookean, K/mu = 10, three traction increments): the relaxed
+    boundary values carry from one increment into the next."""
+    m = sg.box_mesh(6, 5, 5, 1.0, 0.8, 0.8, 0.15, 12)
+    t = np.tile([0.0, 5e4, -5e4], (int(m["patch_size"][5]), 1))
+    bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", t, None)}
+    law = dict(type="neoHookeanElastic", mu=1e6, K=1e7)
+    model = sg.SolidModel(ctx, m, law, bcs, model="nonLinearGeometryTotalLagrangian",
+                          outer=dict(nCorrectors=3000, fieldRelaxation=0.7))
+    D, sig, perf = model.evolve(n_increments=3)
+    Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=model.permutation(), model=1,
+                                   law=1, use_mu_K=1, mu=1e6, K=1e7, n_correctors=3000,
+                                   n_increments=3, field_relaxation=0.7, n_threads=THREADS)
+    assert po["converged"] == 1 and perf["converged"] == 1
+    assert abs(perf["n_correctors"] - po["n_correctors"]) <= 3
+    assert abs(perf["total_lin_iters"] - po["total_lin_iters"]) <= 0.005 * po["total_lin_iters"]
+    assert rel(D, Do) < TOL_D and rel(sig, so) < TOL_S
+    model.close()
+
+
+def cube32_case():
+    """The benchmark's cube form at 32^3: unit cube, interior vertices
+    jittered +-0.2 h (seed 1), E = 70 GPa, nu = 0.33, bottom fixed, top
+    pressure 10 MPa; the oracle builds the same mesh with its own generator."""
+    m = oracle_box_mesh(32, 32, 32, 1.0, 1.0, 1.0, 0.2, 1)
+    bcs = {"zmin": ("fixedDisplacement", None, None),
+           "zmax": ("solidTraction", None, np.full(int(m["patch_size"][5]), 10e6))}
+    return m, bcs
+
+
+@pytest.mark.parametrize("precision", ["FP64", "FP32_REFINE"])
+def test_caller_blocks_cube32_match_oracle(ctx, precision):
+    """The benchmark's decomposition -- 8^3-cell blocks given by the caller
+    (part_of_cell), each block's DIC in the caller's cell order -- on the
+    32^3 cube, against the oracle with the same subdomains (dic_domain) and
+    the mesh from the oracle's own generator.  Plain FP64 takes the
+    oracle's iteration counts; FP32 + refinement stays within the bars."""
+    m, bcs = cube32_case()
+    parts = block_parts(32, 32, 32, 8)
+    model = sg.SolidModel(ctx, m, dict(type="linearElastic", E=70e9, nu=0.33), bcs,
+                          outer=dict(nCorrectors=2000), precision=precision, parts=parts)
+    D, sig, perf = model.evolve()
+    assert np.array_equal(model.parts(), parts)
+    Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), dic_domain=parts, E=70e9, nu=0.33,
+                                   n_correctors=2000, n_threads=THREADS)
+    model.close()
+    assert po["converged"] == 1 and perf["converged"] == 1
+    assert rel(D, Do) < TOL_D and rel(sig, so) < TOL_S
+    if precision == "FP64":
+        assert abs(perf["n_correctors"] - po["n_correctors"]) <= 1
+        assert abs(perf["total_lin_iters"] - po["total_lin_iters"]) <= 0.005 * po["total_lin_iters"]
+
+
+def test_library_parts_cube32_match_oracle(ctx):
+    """The library's own decomposition (coordinate-bisection parts, BFS
+    order inside) on the 32^3 cube in plain FP64, against the oracle run in
+    the library's DIC order with the same subdomains."""
+    m, bcs = cube32_case()
+    model = sg.SolidModel(ctx, m, dict(type="linearElastic", E=70e9, nu=0.33), bcs,
+                          outer=dict(nCorrectors=2000), dic_subdomains=True)
+    D, sig, perf = model.evolve()
+    Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=model.permutation(),
+                                   dic_domain=model.parts(), E=70e9, nu=0.33,
+                                   n_correctors=2000, n_threads=THREADS)
+    model.close()
+    assert po["converged"] == 1 and perf["converged"] == 1
+    assert abs(perf["n_correctors"] - po["n_correctors"]) <= 1
+    assert rel(D, Do) < TOL_D and rel(sig, so) < TOL_S
+
+
+def test_load_cases_match_oracle(ctx):
+    """Batched load cases of the 64^3 benchmark form at 24^3 (E = 200 GPa,
+    nu = 0.3, top tractions N(0, 1 MPa) per component), FP32 + refinement
+    over 8^3 caller blocks: every case against its own oracle solve."""
+    n = 24
+    m = oracle_box_mesh(n, n, n, 1.0, 1.0, 1.0, 0.2, 2)
+    parts = block_parts(n, n, n, 8)
+    tr = np.random.default_rng(3).normal(0.0, 1e6, (4, 3))
+    cases = [{"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", tr[c], None)}
+             for c in range(4)]
+    model = sg.SolidModel(ctx, m, dict(type="linearElastic", E=200e9, nu=0.3), cases[0],
+                          outer=dict(nCorrectors=2000), precision="FP32_REFINE", parts=parts)
+    Db, sb, perfs = model.evolve_cases(cases)
+    model.close()
+    top = int(m["patch_size"][5])
+    for c in range(4):
+        bo = [(1, None, None)] * 4 + [(0, None, None), (1, np.tile(tr[c], (top, 1)), None)]
+        Do, so, _, po = pyoracle.solve(m, bo, dic_domain=parts, E=200e9, nu=0.3, n_correctors=2000,
+                                       n_threads=THREADS)
+        assert po["converged"] == 1 and perfs[c]["converged"] == 1
+        assert rel(Db[c], Do) < TOL_D and rel(sb[c], so) < TOL_S
+
+
+def test_served_requests_match_oracle():
+    """Requests of the served stream's kinds through the server at once --
+    linear at nu = 0.45 with field relaxation 0.7, and neoHookean total
+    Lagrangian with field relaxation over traction increments -- each
+    against its oracle solve (8^3 caller blocks, FP32 + refinement)."""
+    reqs = []
+    for i, (n, kind) in enumerate([(10, "lin"), (14, "lin"), (6, "tl"), (9, "lin")]):
+        m = oracle_box_mesh(n, n, n, 1.0, 1.0, 1.0, 0.2, 40 + i)
+        top = int(m["patch_size"][5])
+        parts = block_parts(n, n, n, 8)
+        if kind == "lin":
+            t = np.array([2e5, -1e5, -1e6])
+            kw = dict(law=dict(type="linearElastic", E=100e9, nu=0.45),
+                      outer=dict(nCorrectors=4000, fieldRelaxation=0.7))
+            okw = dict(E=100e9, nu=0.45, field_relaxation=0.7, n_correctors=4000)
+            ninc = 1
+        else:
+            t = np.array([0.0, 5e4, -5e4])
+            kw = dict(law=dict(type="neoHookeanElastic", mu=1e6, K=1e7),
+                      model="nonLinearGeometryTotalLagrangian", n_increments=3,
+                      outer=dict(nCorrectors=3000, fieldRelaxation=0.7))
+            okw = dict(model=1, law=1, use_mu_K=1, mu=1e6, K=1e7, n_increments=3,
+                       field_relaxation=0.7, n_correctors=3000)
+            ninc = 3
+        bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", t, None)}
+        reqs.append((m, bcs, parts, kw, okw, ninc))
+    srv = sg.Server(max_slots=4)
+    ids = [srv.submit(m, bcs=bcs, precision="FP32_REFINE", parts=parts, **kw)
+           for m, bcs, parts, kw, _, _ in reqs]
+    res = [srv.result(i) for i in ids]
+    srv.close()
+    for (m, bcs, parts, kw, okw, ninc), (st, D, sig, perf) in zip(reqs, res):
+        assert st == _lib.OK and perf["converged"] == 1
+        Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), dic_domain=parts, n_threads=THREADS,
+                                       **okw)
+        assert po["converged"] == 1
+        assert rel(D, Do) < TOL_D and rel(sig, so) < TOL_S
+
+
+def test_bounded_wait_times_out_and_the_context_stays_usable():
+    """A bounded device wait that runs out ends the call with S4G_TIMEOUT
+    and leaves the context usable.  The exact DIC's sweeps wait for the
+    parts they depend on; with a limit of one poll those waits give up (the
+    kernel records it, skips the wait and returns -- nothing hangs), and a
+    solve on the same context afterwards is clean."""
+    c = sg.Context(0, spin_limit=1)
+    m = sg.box_mesh(16, 16, 16, 1.0, 1.0, 1.0, 0.2, 4)
+    bcs = {"zmin": ("fixedDisplacement", None, None),
+           "zmax": ("solidTraction", None, np.full(256, 1e6))}
+    law = dict(type="linearElastic", E=70e9, nu=0.33)
+    model = sg.SolidModel(c, m, law, bcs, part_size=64)
+    with pytest.raises(sg.S4GError) as e:
+        model.evolve()
+    assert e.value.status == _lib.TIMEOUT
+    model.close()
+    # the processor-local DIC has no waits: a clean solve on the same context
+    model = sg.SolidModel(c, m, law, bcs, dic_subdomains=True, part_size=64)
+    D, sig, perf = model.evolve()
+    assert perf["converged"] == 1 and perf["device_status"] == 0 and np.isfinite(D).all()
+    model.close()
+    c.close()
+
+
+def test_non_finite_field_is_detected_on_the_device(ctx):
+    """A neoHookean total-displacement solve that blows up (K/mu = 10, ten
+    traction increments, no relaxation -- the oracle stops on NaN too)
+    ends with S4G_NAN_DETECTED, and the context solves cleanly afterwards."""
+    m = sg.box_mesh(8, 8, 8, 1.0, 1.0, 1.0, 0.2, 5)
+    t = np.tile(np.random.default_rng(5).normal(0, 1e5, 3), (int(m["patch_size"][5]), 1))
+    bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("solidTraction", t, None)}
+    _, _, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), model=2, law=1, use_mu_K=1, mu=1e6,
+                                 K=1e7, n_correctors=3000, n_increments=10)
+    assert po["nan_detected"] == 1
+    model = sg.SolidModel(ctx, m, dict(type="neoHookeanElastic", mu=1e6, K=1e7), bcs,
+                          model="nonLinearGeometryTotalLagrangianTotalDisplacement",
+                          outer=dict(nCorrectors=3000))
+    with pytest.raises(sg.S4GError) as e:
+        model.evolve(n_increments=10)
+    assert e.value.status == _lib.NAN_DETECTED
+    model.close()
+    bcs2 = {"zmin": ("fixedDisplacement", None, None),
+            "zmax": ("solidTraction", None, np.full(64, 1e6))}
+    model = sg.SolidModel(ctx, m, dict(type="linearElastic", E=70e9, nu=0.33), bcs2)
+    D, sig, perf = model.evolve()
+    assert perf["converged"] == 1 and np.isfinite(D).all()
+    model.close()
+
+
+def test_enforce_linear_switch_matches_oracle(ctx):
+    """checkEnforceLinear (nonLinGeomTotalLagSolid.C:203-207 via
+    solidModel.C:1894-1913): a box crushed to half its height in one
+    increment takes J below 0.01 somewhere, so linear geometry is enforced
+    for the rest of the increment, on the device as in the oracle."""
+    m = sg.box_mesh(6, 5, 5, 1.0, 0.8, 0.8, 0.15, 12)
+    z = np.tile([0.0, 0.0, -0.5], (int(m["patch_size"][5]), 1))
+    bcs = {"zmin": ("fixedDisplacement", None, None), "zmax": ("fixedDisplacement", z, None)}
+    law = dict(type="neoHookeanElastic", mu=1e6, K=1e7)
+    model = sg.SolidModel(ctx, m, law, bcs, model="nonLinearGeometryTotalLagrangian",
+                          outer=dict(nCorrectors=1000))
+    D, sig, perf = model.evolve(n_increments=1)
+    Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=model.permutation(), model=1,
+                                   law=1, use_mu_K=1, mu=1e6, K=1e7, n_correctors=1000)
+    model.close()
+    assert po["enforce_linear"] == 1 and perf["enforce_linear"] == 1
+    assert po["converged"] == 1 and perf["converged"] == 1
+    assert abs(perf["n_correctors"] - po["n_correctors"]) <= 1
+    assert rel(D, Do) < TOL_D and rel(sig, so) < TOL_S
+
+
+@pytest.mark.parametrize("model_name,model_id", [("nonLinearGeometryTotalLagrangian", 1),
+                                                 ("nonLinearGeometryTotalLagrangianTotalDisplacement", 2)])
+def test_rigid_rotation_matches_oracle(ctx, model_name, model_id):
+    """A rigid rotation of 90 degrees about z prescribed on every boundary
+    over 45 increments: the incremental form carries nonzero fixed values
+    from one increment into the next (D.oldTime on the boundary).  The
+    device recovers D = (R - I) C stress-free, as the oracle does."""
+    m = sg.box_mesh(6, 5, 4, 1.0, 0.9, 0.8, 0.2, 3)
+    th = np.radians(90.0)
+    R = np.array([[np.cos(th), -np.sin(th), 0.0], [np.sin(th), np.cos(th), 0.0], [0.0, 0.0, 1.0]])
+    names = ["xmin", "xmax", "ymin", "ymax", "zmin", "zmax"]
+    bcs = {}
+    for p in range(6):
+        s, n = int(m["patch_start"][p]), int(m["patch_size"][p])
+        bcs[names[p]] = ("fixedDisplacement", m["Cf"][s:s + n] @ (R - np.eye(3)).T, None)
+    law = dict(type="neoHookeanElastic", mu=1e6, K=5e6)
+    outer = dict(nCorrectors=4000, solutionTolerance=1e-10, alternativeTolerance=1e-11)
+    model = sg.SolidModel(ctx, m, law, bcs, model=model_name, outer=outer, ls_boundary_delta=1)
+    D, sig, perf = model.evolve(n_increments=45)
+    Do, so, _, po = pyoracle.solve(m, oracle_bcs(m, bcs), perm=model.permutation(), model=model_id,
+                                   law=1, use_mu_K=1, mu=1e6, K=5e6, n_correctors=4000,
+                                   n_increments=45, solution_tol=1e-10, alternative_tol=1e-11,
+                                   ls_boundary_delta=1)
+    model.close()
+    assert po["converged"] == 1 and perf["converged"] == 1 and perf["enforce_linear"] == 0
+    exact = m["C"] @ (R - np.eye(3)).T
+    assert np.abs(D - exact).max() < 1e-7 * np.abs(exact).max()
+    assert np.abs(sig).max() < 1.0                    # below 1e-6 mu
+    assert rel(D, Do) < TOL_D
