@@ -580,6 +580,7 @@ def run_gb300(args):
     served = (run_served(args, budget)
               if (rank == 0 and not args.no_served and budget.left() > 300) else None)
 
+    n_parts = int(model.info()["n_parts"])
     cpu = None
     if rank == 0 and not args.no_cpu:
         cp = cache_path(args.n)
@@ -609,7 +610,7 @@ def run_gb300(args):
                    "model": "linearGeometryTotalDisplacement", "law": "linearElastic",
                    "solver": "PCG+DIC tol 1e-9 relTol 0.1", "outer": "solutionTolerance 1e-6, "
                    "nCorrectors 2000", "precision": args.precision, "dic": args.dic,
-                   "dic_subdomains": int(model.info()["n_parts"]) if args.dic != "exact" else 1,
+                   "dic_subdomains": n_parts if args.dic != "exact" else 1,
                    "parallelism": f"replicas{world}", "path": "production (CUDA graphs, no "
                    "per-kernel events); kernels/roofline from one profiled solve in this run",
                    "l2": "working set ~1.7 GB >> 129 MB L2 (no flush needed)",

@@ -319,6 +319,10 @@ typedef struct s4g_perf {
    * CUDA-event time and number of launches that did work */
   double kernel_ms[S4G_K_KINDS];
   long long kernel_launches_by[S4G_K_KINDS];
+  int device_loop;            /* 1: the corrector loop ran device-resident (one
+                                 CUDA graph launch per increment, its loops
+                                 decided on the device); 0: driven from the host
+                                 (profile, verbose or no_graphs) */
 } s4g_perf;
 
 /* Runs the solid model's evolve() for n_increments load increments (1 for

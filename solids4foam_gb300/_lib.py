@@ -108,10 +108,12 @@ class Perf(ct.Structure):
         ("tune_us", ct.c_double * 6),
         ("kernel_ms", ct.c_double * len(KERNEL_KINDS)),
         ("kernel_launches_by", ct.c_longlong * len(KERNEL_KINDS)),
+        ("device_loop", ct.c_int),
     ]
 
     def as_dict(self):
-        d = {f[0]: getattr(self, f[0]) for f in self._fields_[:-2]}
+        d = {f[0]: getattr(self, f[0]) for f in self._fields_[:-3]}
+        d["device_loop"] = self.device_loop
         d["tune_us"] = list(self.tune_us)
         d["kernel_ms"] = dict(zip(KERNEL_KINDS, list(self.kernel_ms)))
         d["kernel_launches_by"] = dict(zip(KERNEL_KINDS, list(self.kernel_launches_by)))

@@ -140,7 +140,9 @@ def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=96 ** 3, tl
     segregated corrector loop needs field relaxation (relaxationFactors
     fields D / DD) for nu above about 0.38 and for the neoHookean requests
     -- the reference's own loop behaves the same way -- so those requests
-    set 0.7, and the neoHookean ones allow 5000 correctors per increment.
+    set 0.7; the neoHookean ones also relax the traction gradient
+    (solidTraction relaxationFactor 0.5), without which their increments
+    after the first drift away, and allow 5000 correctors per increment.
     Each request carries its block decomposition (block^3 cells).
     Returns a list of (arrival_s, request kwargs)."""
     rng = np.random.default_rng(seed)
@@ -162,7 +164,7 @@ def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=96 ** 3, tl
             tr = np.tile([0.0, 0.05 * mu, -0.05 * mu], (top, 1))
             req = dict(mesh=mesh, law=dict(type="neoHookeanElastic", mu=mu, K=K),
                        bcs={"zmin": ("fixedDisplacement", None, None),
-                            "zmax": ("solidTraction", tr, None)},
+                            "zmax": ("solidTraction", tr, None, 0.5)},
                        model="nonLinearGeometryTotalLagrangian", n_increments=10,
                        outer=dict(nCorrectors=5000, fieldRelaxation=0.7), parts=parts)
         else:

@@ -106,6 +106,9 @@ struct DevState {
   unsigned counter[16];
   // sweep control
   unsigned ticket[2], ctasDone[2], partsDone[2], epoch[2];
+  // device-resident loop (conditional graph nodes): iterations of the PCG
+  // loop of the corrector in progress and correctors of the graph launch
+  unsigned loopPcg, loopOuter;
 };
 
 // The dynamic shared-memory limit of a kernel is a process-wide attribute:

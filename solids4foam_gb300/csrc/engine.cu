@@ -180,11 +180,19 @@ struct Engine {
   std::map<long, PcgGraph> pcgGraphs;
   int generation = 0;
   bool graphsOk = true;
+  // The device-resident corrector loop: one graph per (value type, model,
+  // case count) whose conditional WHILE nodes run the correctors and, inside
+  // each, the PCG iterations, with the loop decisions taken on the device.
+  std::map<long, PcgGraph> loopGraphs;
+  bool loopGraphsOk = true;
+  bool ranOnDevice = false;  // the last solve's corrector loop ran device-resident
 
   void dropGraphs() {
-    for (auto& kv : pcgGraphs)
-      if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
-    pcgGraphs.clear();
+    for (auto* m : {&pcgGraphs, &loopGraphs}) {
+      for (auto& kv : *m)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+      m->clear();
+    }
   }
 
   ~Engine() {
@@ -748,6 +756,7 @@ struct Engine {
     S4G_CUDA(cudaEventCreate(&e0));
     S4G_CUDA(cudaEventCreate(&e1));
     nRun = C;
+    ranOnDevice = false;
     S4G_TRY(initFields(0));
     S4G_TRY(resetSweepState());
     S4G_TRY(setLive());
@@ -808,6 +817,7 @@ struct Engine {
           perf->kernel_ms[k] = timer.ms[k];
           perf->kernel_launches_by[k] = timer.count[k];
         }
+        perf->device_loop = ranOnDevice ? 1 : 0;
       }
       if (h.status & kErrNaN) ret = setErr(S4G_NAN_DETECTED, "non-finite value in a load case");
       else if (h.status & kErrIndefinite && ret == S4G_OK) ret = setErr(S4G_INDEFINITE, "PCG met p.Ap <= 0 in a load case");
@@ -925,6 +935,97 @@ struct Engine {
     return g.exec;
   }
 
+  // Adds a conditional WHILE node on h after the work captured so far on s;
+  // work captured later depends on it.  body: the node's body graph.
+  bool addWhile(cudaStream_t s, cudaGraphConditionalHandle h, cudaGraph_t* body) {
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    if (cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &nd) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusActive)
+      return false;
+    cudaGraphNodeParams np{};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, cg, deps, nullptr, nd, &np) != cudaSuccess) return false;
+    *body = np.conditional.phGraph_out[0];
+    return cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1,
+                                               cudaStreamSetCaptureDependencies) == cudaSuccess;
+  }
+
+  // Builds the device-resident corrector loop of evolve() (one increment):
+  //   loop count = 0; cond(correctors) = any case live
+  //   WHILE correctors: right-hand side; cond(pcg) = any component active
+  //                     WHILE pcg: one PCG iteration; cond(pcg)
+  //                     post-solve pass; cond(correctors)
+  // Each loop is also bounded on the device (nCorrectors + 4 correctors,
+  // maxIter + 4 PCG iterations per corrector).
+  template <typename T>
+  bool buildLoopGraph(cudaGraph_t g, const Controls& c, int tl, const PcgPtrs<T>& p, int grid) {
+    cudaStream_t s = ctx->stream;
+    const cudaStreamCaptureMode mode = cudaStreamCaptureModeThreadLocal;
+    cudaGraphConditionalHandle hOut, hPcg;
+    if (cudaGraphConditionalHandleCreate(&hOut, g, 0, cudaGraphCondAssignDefault) != cudaSuccess ||
+        cudaGraphConditionalHandleCreate(&hPcg, g, 0, cudaGraphCondAssignDefault) != cudaSuccess)
+      return false;
+    const unsigned outerLimit = (unsigned)c.nCorr + 4, pcgLimit = (unsigned)c.maxIter + 4;
+    cudaGraph_t outerBody = nullptr, pcgBody = nullptr, ended = nullptr;
+    bool ok;
+    if (cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, mode) != cudaSuccess) return false;
+    launchSetLoopCond(hOut, dState, nRun, 1, 1, outerLimit, s);
+    ok = addWhile(s, hOut, &outerBody);
+    ok = cudaStreamEndCapture(s, &ended) == cudaSuccess && ok;
+    if (!ok || cudaStreamBeginCaptureToGraph(s, outerBody, nullptr, nullptr, 0, mode) != cudaSuccess)
+      return false;
+    launchRhs<T>(mv, c, f, p.x, p.r, dState, dPartials, s, nullptr, nRun);
+    launchSetLoopCond(hPcg, dState, nRun, 0, 1, pcgLimit, s);
+    ok = addWhile(s, hPcg, &pcgBody);
+    launchPost<T>(mv, c, f, p.x, dState, dPartials, 1, s, nullptr, nRun);
+    launchSetLoopCond(hOut, dState, nRun, 1, 0, outerLimit, s);
+    ok = cudaStreamEndCapture(s, &ended) == cudaSuccess && ok;
+    if (!ok || cudaStreamBeginCaptureToGraph(s, pcgBody, nullptr, nullptr, 0, mode) != cudaSuccess)
+      return false;
+    long long dummy = 0;
+    if (mv.subdomains && c.precond == 0)
+      launchLocalIteration<T>(mv, c, p, dState, dPartials, tuning<T>(), s, &dummy, nullptr, nRun);
+    else
+      launchPcgIteration<T>(mv, c, p, dState, dPartials, grid, s, &dummy, nullptr);
+    launchSetLoopCond(hPcg, dState, nRun, 0, 0, pcgLimit, s);
+    ok = cudaStreamEndCapture(s, &ended) == cudaSuccess;
+    (void)tl;
+    return ok && cudaGetLastError() == cudaSuccess;
+  }
+
+  // The loop graph for the current state of the engine (built on first use);
+  // nullptr if it cannot be built, in which case the host drives the loop.
+  template <typename T>
+  cudaGraphExec_t loopGraph(const Controls& c, int tl, const PcgPtrs<T>& p, int grid) {
+    const long key = ((long)(sizeof(T)) << 40) | ((long)tl << 32) | ((long)nRun << 8);
+    PcgGraph& g = loopGraphs[key];
+    const LocalTuning& t = tuning<T>();
+    if (g.exec && g.generation == generation && g.ntIdx == t.ntIdx && g.uIdx == t.uIdx &&
+        g.grid == grid && std::memcmp(&g.c, &c, sizeof(Controls)) == 0)
+      return g.exec;
+    if (g.exec) { cudaGraphExecDestroy(g.exec); g.exec = nullptr; }
+    cudaGraph_t graph = nullptr;
+    bool ok = cudaGraphCreate(&graph, 0) == cudaSuccess && buildLoopGraph<T>(graph, c, tl, p, grid);
+    if (ok) ok = cudaGraphInstantiate(&g.exec, graph, 0) == cudaSuccess;
+    if (graph) cudaGraphDestroy(graph);
+    if (!ok) {
+      loopGraphsOk = false;
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g.exec = nullptr;
+      cudaGetLastError();
+      return nullptr;
+    }
+    g.generation = generation; g.ntIdx = t.ntIdx; g.uIdx = t.uIdx; g.grid = grid; g.c = c;
+    return g.exec;
+  }
+
   template <typename T>
   s4g_status pcgLoop(const Controls& c, const PcgPtrs<T>& p, int grid) {
     // Iterations are launched in growing batches; the launches after the
@@ -972,6 +1073,22 @@ struct Engine {
   template <typename T>
   s4g_status correctorLoop(Controls& c, int tl, const PcgPtrs<T>& p, int grid) {
     cudaStream_t s = ctx->stream;
+    if (!ctx->profile && !ctx->noGraphs && !ctx->verbose && loopGraphsOk) {
+      cudaGraphExec_t exec = loopGraph<T>(c, tl, p, grid);
+      if (exec) {
+        // one launch runs every corrector on the device; the host waits once
+        const int corr0 = hState->nCorrDone, it0 = hState->pcgIter;
+        S4G_CUDA(cudaGraphLaunch(exec, s));
+        S4G_CUDA(cudaGetLastError());
+        S4G_TRY(readState());
+        const bool local = mv.subdomains && c.precond == 0;
+        const long long perIt = local ? (tuning<T>().uIdx == 2 ? 3 : 2) : (c.precond == 0 ? 5 : 4);
+        launches += 1 + (long long)(hState->nCorrDone - corr0) * (tl ? 6 : 5) +
+                    (long long)(hState->pcgIter - it0) * (perIt + 1);
+        ranOnDevice = true;
+        return S4G_OK;
+      }
+    }
     for (;;) {
       launchRhs<T>(mv, c, f, p.x, p.r, dState, dPartials, s, tm(), nRun);
       launches += 2;
@@ -1017,6 +1134,7 @@ struct Engine {
       else S4G_TRY(tuneLocal<double>(ct, pc));
     }
     nRun = 1;
+    ranOnDevice = false;
     S4G_TRY(initFields(tl));
     S4G_TRY(resetSweepState());
     S4G_TRY(setLive());
@@ -1096,6 +1214,7 @@ struct Engine {
         perf->kernel_ms[k] = timer.ms[k];
         perf->kernel_launches_by[k] = timer.count[k];
       }
+      perf->device_loop = ranOnDevice ? 1 : 0;
     }
     if (hState->status & kErrTimeout) return setErr(S4G_TIMEOUT, "a bounded device wait gave up");
     if (hState->status & kErrNaN) return setErr(S4G_NAN_DETECTED, "non-finite value in the iteration");

@@ -98,6 +98,17 @@ void launchGather(int n, int width, const int* c2s, const double* in, double* ou
 void launchTlShift(const MeshView& mv, const Controls& c, const FieldPtrs& f, DevState* st,
                    cudaStream_t s);
 
+// Device-resident loops (CUDA graph conditional WHILE nodes): sets the
+// condition of a loop from the device state of the nRun cases.  which = 0:
+// the PCG loop of a corrector, continue while any case's pcgContinue (first
+// = 1 at the corrector's start resets the iteration count); which = 1: the
+// corrector loop, continue while any case is live.  Each loop is also
+// bounded by `limit` iterations, past which the cases stop with the
+// timeout bit set, so that a loop always ends; a case whose status has the
+// timeout or NaN bit stops at once.
+void launchSetLoopCond(cudaGraphConditionalHandle h, DevState* st, int nRun, int which, int first,
+                       unsigned limit, cudaStream_t s);
+
 // ---- PCG (kernels_pcg.cu) ----------------------------------------------------
 // PCG arrays in the value type T of the inner solve: double (plain FP64) or
 // float (FP32 inner solve of the mixed-precision path).
@@ -159,12 +170,12 @@ void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaS
 // grid[0] resident blocks; uIdx selects the fused SpMV with a plain (0) or
 // unrolled (1) entry loop, or the split p-update + SpMV (2).  All SpMV
 // variants compute bit-identical results.
-constexpr int kLocNumNT = 1, kLocNumU = 3;
+constexpr int kLocNumNT = 2, kLocNumU = 3;
 extern const int kLocVariantsNT[kLocNumNT];
 extern const int kLocVariantsU[kLocNumU];
 struct LocalTuning {
   int ntIdx = 0, uIdx = 0;
-  int grid[kLocNumNT] = {1};
+  int grid[kLocNumNT] = {1, 1};
 };
 // One fused PCG iteration (two kernels): [x, r update of the previous
 // iteration + residual test + processor-local DIC + w.r] and

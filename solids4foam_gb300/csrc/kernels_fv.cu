@@ -280,8 +280,11 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
     T9 acc = zeroT();
     for (int e = mv.rowptr[s]; e < mv.rowptr[s + 1]; ++e)
       acc = acc + outer(ldV(mv.lsv, e), ldV(U, mv.col[e]) - Up);
+    // relaxed: the boundary values come from the field as solved, then
+    // relax against their previous values (the cells were relaxed already)
+    const V3 UpSolved = (relax && apply) ? ldV(f.D[dc], s) + ldVT(x, s) : Up;
     for (int b = mv.browptr[s]; b < mv.browptr[s + 1]; ++b) {
-      V3 Ub = boundaryValue(mv, c, f, b, Up, Gold);
+      V3 Ub = boundaryValue(mv, c, f, b, UpSolved, Gold);
       if (relax) {
         if (apply) {
           const V3 pb = ldV(f.Ubr, b);
@@ -561,6 +564,32 @@ kRhs(MeshView mv, Controls c, FieldPtrs f, T* __restrict__ x, T* __restrict__ r,
   st->pcgContinue = (any && c.maxIter > 0) ? 1 : 0;
 }
 
+__global__ void kSetLoopCond(cudaGraphConditionalHandle h, DevState* st, int nRun, int which,
+                             int first, unsigned limit) {
+  unsigned* count = which == 0 ? &st[0].loopPcg : &st[0].loopOuter;
+  if (first) *count = 0;
+  else *count += 1;
+  int any = 0;
+  for (int cs = 0; cs < nRun; ++cs) {
+    // a case whose wait gave up or whose field is not finite stops here
+    if (st[cs].status & (kErrTimeout | kErrNaN)) {
+      st[cs].pcgContinue = 0;
+      if (which == 1) st[cs].caseLive = 0;
+      continue;
+    }
+    any |= which == 0 ? st[cs].pcgContinue : st[cs].caseLive;
+  }
+  if (any && *count >= limit) {
+    for (int cs = 0; cs < nRun; ++cs) {
+      st[cs].status |= kErrTimeout;
+      st[cs].pcgContinue = 0;
+      if (which == 1) st[cs].caseLive = 0;
+    }
+    any = 0;
+  }
+  cudaGraphSetConditional(h, any ? 1u : 0u);
+}
+
 __global__ void kGather(int n, int width, const int* c2s, const double* in, double* out) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= (long)n * width) return;
@@ -656,6 +685,11 @@ template void launchRhs<float>(const MeshView&, const Controls&, const FieldPtrs
 void launchGather(int n, int width, const int* c2s, const double* in, double* out, cudaStream_t s) {
   long tot = (long)n * width;
   kGather<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, width, c2s, in, out);
+}
+
+void launchSetLoopCond(cudaGraphConditionalHandle h, DevState* st, int nRun, int which, int first,
+                       unsigned limit, cudaStream_t s) {
+  kSetLoopCond<<<1, 1, 0, s>>>(h, st, nRun, which, first, limit);
 }
 
 void launchTlShift(const MeshView& mv, const Controls& c, const FieldPtrs& f, DevState* st,

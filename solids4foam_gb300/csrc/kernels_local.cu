@@ -25,11 +25,12 @@
 // differs.
 //
 // Variants.  The SpMV step runs fused with a plain or an unrolled entry
-// loop, or split into a p-update pass and an SpMV; the autotuner (engine)
-// times them on the mesh and keeps the fastest.  They sum in the same order
-// (same grid and block), so all variants give bit-identical results.
-// kLocPrecond runs with kLocBlock threads per part; its sums are per part
-// (fixed block tree) and then over the parts in index order.
+// loop, or split into a p-update pass and an SpMV; kLocPrecond runs with 128
+// or 256 threads per part.  The autotuner (engine) times them on the mesh
+// and keeps the fastest.  The SpMV variants sum in the same order (same grid
+// and block); kLocPrecond sums each part in a fixed order that does not
+// depend on its block size, then over the parts in index order.  So all
+// variants give bit-identical results.
 //
 // Part tables (HostPrep step 9): in-part entries per row, lower entries in
 // CSR order then upper entries in reverse CSR order, coefficient rD_row*a_e
@@ -46,13 +47,9 @@
 namespace s4g {
 namespace {
 
-// Threads per part: the streaming phase wants many loads in flight, the
-// level walk uses at most a level's rows (<= 48 for 8x8x8 parts).
-constexpr int kLocBlock = 64;
-
 template <typename T>
 struct LocSmem {
-  T* c; uint32_t* m; uint16_t* idx; T* w; int* lv;
+  T* c; uint32_t* m; uint16_t* idx; T* w; T* r; int* lv;
 };
 
 template <typename T>
@@ -62,49 +59,83 @@ __device__ __forceinline__ LocSmem<T> locSmem(const MeshView& mv, unsigned char*
   s.c = (T*)raw;                              // EL coefficients (EL % 8 == 0)
   s.m = (uint32_t*)(s.c + EL);                // ML row metadata (ML % 4 == 0)
   s.idx = (uint16_t*)(s.m + ML);              // EL local columns
-  s.w = (T*)(s.idx + EL);                     // 3P
-  s.lv = (int*)(s.w + 3 * P);                 // maxLevels + 1
+  s.w = (T*)(s.idx + EL);                     // 3P: the substitutions' vector
+  s.r = s.w + 3 * P;                          // 3P: the updated residual
+  s.lv = (int*)(s.r + 3 * P);                 // maxLevels + 1
   return s;
 }
 
-// v -= sum_j c_j w_idx(j) over n staged entries from j0, in entry order.  The
-// first four entries have their operands loaded before the multiply-adds.
+// The static data of one thread's row of a level (its metadata, entry
+// columns and coefficients), read before the barrier that ends the level
+// in progress, so that after it only the loads of the neighbours' values
+// and the multiply-add chain remain.
+constexpr int kLocPre = 4;
 template <typename T>
-__device__ __forceinline__ void locRow(const LocSmem<T>& sm, int j0, int n, T& v0, T& v1, T& v2) {
-  constexpr int U = 4;
-  T a[U], w0[U], w1[U], w2[U];
+struct LocRow {
+  int i, n, j0;
+  int q[kLocPre];
+  T a[kLocPre];
+};
+
+template <int DIR, int NT, typename T>
+__device__ __forceinline__ void locPre(const LocSmem<T>& sm, int l, LocRow<T>& row) {
+  row.i = sm.lv[l] + (int)threadIdx.x;
+  row.n = 0;
+  if (row.i >= sm.lv[l + 1]) { row.i = -1; return; }
+  const uint32_t m = sm.m[row.i];
+  const int nl = (m >> 16) & 0xff;
+  row.j0 = DIR == 0 ? (int)(m & 0xffff) : (int)(m & 0xffff) + nl;
+  row.n = DIR == 0 ? nl : (int)(m >> 24);
 #pragma unroll
-  for (int u = 0; u < U; ++u) {
-    if (u < n) {
-      const int q = sm.idx[j0 + u];
-      a[u] = sm.c[j0 + u];
-      w0[u] = sm.w[3 * q]; w1[u] = sm.w[3 * q + 1]; w2[u] = sm.w[3 * q + 2];
+  for (int u = 0; u < kLocPre; ++u)
+    if (u < row.n) { row.q[u] = sm.idx[row.j0 + u]; row.a[u] = sm.c[row.j0 + u]; }
+}
+
+// v -= sum_j c_j w_idx(j) over the row's entries, in entry order.
+template <typename T>
+__device__ __forceinline__ void locApply(const LocSmem<T>& sm, const LocRow<T>& row) {
+  const int i = row.i;
+  T v0 = sm.w[3 * i], v1 = sm.w[3 * i + 1], v2 = sm.w[3 * i + 2];
+#pragma unroll
+  for (int u = 0; u < kLocPre; ++u)
+    if (u < row.n) {
+      const int q = row.q[u];
+      const T a = row.a[u];
+      v0 -= a * sm.w[3 * q]; v1 -= a * sm.w[3 * q + 1]; v2 -= a * sm.w[3 * q + 2];
     }
-  }
-#pragma unroll
-  for (int u = 0; u < U; ++u)
-    if (u < n) { v0 -= a[u] * w0[u]; v1 -= a[u] * w1[u]; v2 -= a[u] * w2[u]; }
-  for (int j = j0 + U; j < j0 + n; ++j) {
+  for (int j = row.j0 + kLocPre; j < row.j0 + row.n; ++j) {
     const int q = sm.idx[j];
     const T c = sm.c[j];
     v0 -= c * sm.w[3 * q]; v1 -= c * sm.w[3 * q + 1]; v2 -= c * sm.w[3 * q + 2];
   }
+  sm.w[3 * i] = v0; sm.w[3 * i + 1] = v1; sm.w[3 * i + 2] = v2;
 }
 
-// One substitution (DIR 0 forward, 1 backward) over the part's levels:
-// the rows of a level in parallel, a barrier between levels.
+// One substitution (DIR 0 forward, 1 backward) over the part's levels: the
+// rows of a level in parallel, a barrier between levels, the next level's
+// static data in registers while the current level runs.
 template <int DIR, int NT, typename T>
 __device__ __forceinline__ void locSweep(const LocSmem<T>& sm, int nL) {
+  if (nL <= 0) return;
+  LocRow<T> nxt;
+  locPre<DIR, NT>(sm, DIR == 0 ? 0 : nL - 1, nxt);
   for (int s = 0; s < nL; ++s) {
     const int l = DIR == 0 ? s : nL - 1 - s;
-    for (int i = sm.lv[l] + threadIdx.x; i < sm.lv[l + 1]; i += NT) {
+    const LocRow<T> cur = nxt;
+    if (s + 1 < nL) locPre<DIR, NT>(sm, DIR == 0 ? l + 1 : l - 1, nxt);
+    if (cur.i >= 0) locApply(sm, cur);
+    // rows beyond the first NT of a wide level
+    for (int i = sm.lv[l] + (int)threadIdx.x + NT; i < sm.lv[l + 1]; i += NT) {
+      LocRow<T> row;
       const uint32_t m = sm.m[i];
       const int nl = (m >> 16) & 0xff;
-      const int j0 = DIR == 0 ? (int)(m & 0xffff) : (int)(m & 0xffff) + nl;
-      const int n = DIR == 0 ? nl : (int)(m >> 24);
-      T v0 = sm.w[3 * i], v1 = sm.w[3 * i + 1], v2 = sm.w[3 * i + 2];
-      locRow(sm, j0, n, v0, v1, v2);
-      sm.w[3 * i] = v0; sm.w[3 * i + 1] = v1; sm.w[3 * i + 2] = v2;
+      row.i = i;
+      row.j0 = DIR == 0 ? (int)(m & 0xffff) : (int)(m & 0xffff) + nl;
+      row.n = DIR == 0 ? nl : (int)(m >> 24);
+#pragma unroll
+      for (int u = 0; u < kLocPre; ++u)
+        if (u < row.n) { row.q[u] = sm.idx[row.j0 + u]; row.a[u] = sm.c[row.j0 + u]; }
+      locApply(sm, row);
     }
     __syncthreads();
   }
@@ -116,16 +147,26 @@ __global__ void kLocGather(int n, const int* src, const double* rDa, T* out) {
   if (i < n) out[i] = src[i] >= 0 ? (T)rDa[src[i]] : T(0);
 }
 
-// Resident blocks the register budget is set for: the shared memory of a
-// 512-row part (with the 1 KB each block reserves) allows eight blocks per
-// SM in FP32 and five in FP64.
-template <typename T, int NT>
+// Resident blocks the register budget is set for (NT threads, RPT rows per
+// thread in flight at once in the streaming phase).
+template <typename T, int NT, int RPT>
 constexpr int locMinBlocks() {
-  return sizeof(T) == 4 ? 8 : 5;
+  return sizeof(T) == 4 ? (NT == 128 ? 4 : 2) : (NT == 128 ? 3 : 2);
 }
 
-template <typename T, int NT>
-__global__ void __launch_bounds__(NT, (locMinBlocks<T, NT>()))
+// The processor-local preconditioner of one PCG iteration: the pending
+// update x += alpha p, r -= alpha q, w = rD r, the forward and backward
+// substitutions of each part inside one CTA, and the w.r and sum|r| sums.
+//
+// Streaming: each thread issues the loads of RPT rows at once (all the
+// part's rows in one round trip when NT * RPT covers the part), while the
+// part's tables arrive by 16-byte cp.async.  The updated residual and w go
+// to shared memory.  Sums: per part, in a fixed order independent of NT
+// and RPT (64 lanes over the rows, lane l summing rows l, l+64, ..., then a
+// fixed tree), one record per part; the last CTA sums the records in part
+// order.  Every variant therefore gives bit-identical results.
+template <typename T, int NT, int RPT>
+__global__ void __launch_bounds__(NT, (locMinBlocks<T, NT, RPT>()))
 kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partials) {
   p = casePcg(p, blockIdx.y, mv.nC);
   st += blockIdx.y;
@@ -133,7 +174,7 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
   if (!st->pcgContinue) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   const LocSmem<T> sm = locSmem<T>(mv, smraw);
-  __shared__ double red[32 * 6];
+  __shared__ double red[2 * 6];
   // the vectors never alias one another
   const T* __restrict__ pg = st->pbuf ? p.p2 : p.p;  // p of the pending iteration
   const T* __restrict__ qg = p.q;
@@ -145,28 +186,18 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
 #pragma unroll
   for (int k = 0; k < 3; ++k) { pend[k] = st->pending[k] != 0; al[k] = (T)st->alpha[k]; }
   const bool anyPend = pend[0] || pend[1] || pend[2];
-  // Part assignment.  FP64 (long parts): parts come from a ticket counter,
-  // so CTAs that finish early take more (no tail of CTAs with one part more
-  // than the others); the next ticket is taken while the current part runs,
-  // and the sums are recorded per part, so the result does not depend on
-  // which CTA ran which part.  FP32 (short parts, where the ticket traffic
-  // costs more than the tail): CTA b takes parts b, b+G, ..., and sums its
-  // parts in that order (G, the grid, is fixed for a mesh).
-  constexpr bool kTicket = sizeof(T) == 8;
+  // Parts come from a ticket counter: CTAs that finish early take more (no
+  // tail of CTAs with one part more than the others); the next ticket is
+  // taken while the current part runs.
   __shared__ int sTicket;
-  if (threadIdx.x == 0) sTicket = kTicket ? (int)atomicAdd(&st->locTicket, 1u) : (int)blockIdx.x;
+  if (threadIdx.x == 0) sTicket = (int)atomicAdd(&st->locTicket, 1u);
   __syncthreads();
-  Acc<T> wr[3], ar[3];  // w.r and sum|r|: of a part (tickets) or of the CTA's parts
   for (int part = sTicket; part < mv.nParts;) {
     const int4 dA = mv.locDesc[2 * part], dB = mv.locDesc[2 * part + 1];
     const int pLo = dA.x, nR = dA.y, eLo = dA.z, nE = dA.w;
     const int mLo = dB.x, nM = dB.y, l0 = dB.z, nL = dB.w;
     int nextTicket = 0;
-    if (threadIdx.x == 0)
-      nextTicket = kTicket ? (int)atomicAdd(&st->locTicket, 1u) : part + (int)gridDim.x;
-    if (kTicket)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) { wr[k] = Acc<T>(); ar[k] = Acc<T>(); }
+    if (threadIdx.x == 0) nextTicket = (int)atomicAdd(&st->locTicket, 1u);
     // static part tables in flight while the vectors stream
     {
       const int nc = nE * (int)sizeof(T) / 16;
@@ -180,19 +211,12 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
       for (int k = threadIdx.x; k < nm; k += NT) cpAsync16((char*)sm.m + 16 * k, gm + 16 * k);
     }
     for (int k = threadIdx.x; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
-    // pending update (x += alpha p, r -= alpha q); w starts as rD r.  RB
-    // rows per thread at a time, every load issued before any store.  In
-    // FP32 a thread keeps its rows' residual in registers for the dot
-    // products after the substitutions (rows t, t+NT, ..., at most kRegRows).
-    constexpr int RB = 2;
-    constexpr bool kRegR = sizeof(T) == 4;
-    constexpr int kRegRows = kRegR ? 8 : 1;
-    const bool regR = kRegR && nR <= kRegRows * NT;
-    T rKeep[kRegRows][3];
-    for (int i0 = threadIdx.x, jr = 0; i0 < nR; i0 += RB * NT, jr += RB) {
-      T rv[RB][3], qv[RB][3], pv[RB][3], xv[RB][3], rd[RB];
+    // pending update: RPT rows per thread with every load issued before
+    // any store; r and w = rD r into shared memory
+    for (int i0 = threadIdx.x; i0 < nR; i0 += RPT * NT) {
+      T rv[RPT][3], qv[RPT][3], pv[RPT][3], xv[RPT][3], rd[RPT];
 #pragma unroll
-      for (int h = 0; h < RB; ++h) {
+      for (int h = 0; h < RPT; ++h) {
         const int i = i0 + h * NT;
         if (i < nR) {
           const size_t g = 3 * (size_t)(pLo + i);
@@ -205,7 +229,7 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
         }
       }
 #pragma unroll
-      for (int h = 0; h < RB; ++h) {
+      for (int h = 0; h < RPT; ++h) {
         const int i = i0 + h * NT;
         if (i < nR) {
           const size_t g = 3 * (size_t)(pLo + i);
@@ -216,18 +240,10 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
               rv[h][k] -= al[k] * qv[h][k];
               rg[g + k] = rv[h][k];
             }
+            sm.r[3 * i + k] = rv[h][k];
             sm.w[3 * i + k] = rd[h] * rv[h][k];
           }
         }
-      }
-      if (kRegR) {
-#pragma unroll
-        for (int jj = 0; jj < kRegRows; ++jj)
-#pragma unroll
-          for (int h = 0; h < RB; ++h)
-            if (jj == jr + h)
-#pragma unroll
-              for (int k = 0; k < 3; ++k) rKeep[jj][k] = rv[h][k];
       }
     }
     cpAsyncWaitAll();
@@ -236,76 +252,36 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
     // backward substitution: w_l -= sum_{u>l in part} (rD_l a_lu) w_u
     locSweep<0, NT>(sm, nL);
     locSweep<1, NT>(sm, nL);
-    // w out; w.r and sum|r| accumulated by the threads of the streaming
-    // phase over the same rows, from the residual kept in registers (FP32)
-    // or re-read (each thread reads back what it wrote)
+    // w out
     T* __restrict__ wg = p.w + 3 * (size_t)pLo;
     for (int k = threadIdx.x; k < 3 * nR; k += NT) wg[k] = sm.w[k];
-    if (regR) {
+    // the part's w.r and sum|r|: 64 lanes over the rows, then a fixed tree
+    double d6[6] = {0, 0, 0, 0, 0, 0};
+    if (threadIdx.x < 64) {
+      Acc<T> wr[3], ar[3];
+      for (int i = threadIdx.x; i < nR; i += 64)
 #pragma unroll
-      for (int jj = 0; jj < kRegRows; ++jj) {
-        const int i = threadIdx.x + jj * NT;
-        if (i < nR)
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            wr[k].add(sm.w[3 * i + k] * rKeep[jj][k]);
-            ar[k].add(fabs(rKeep[jj][k]));
-          }
-      }
-    } else {
-      constexpr int U = 4;
-      for (int i0 = threadIdx.x; i0 < nR; i0 += U * NT) {
-        T rv[U][3];
-#pragma unroll
-        for (int h = 0; h < U; ++h) {
-          const int i = i0 + h * NT;
-          if (i < nR)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) rv[h][k] = rg[3 * (size_t)(pLo + i) + k];
+        for (int k = 0; k < 3; ++k) {
+          const T r = sm.r[3 * i + k];
+          wr[k].add(sm.w[3 * i + k] * r);
+          ar[k].add(fabs(r));
         }
-#pragma unroll
-        for (int h = 0; h < U; ++h) {
-          const int i = i0 + h * NT;
-          if (i < nR)
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-              wr[k].add(sm.w[3 * i + k] * rv[h][k]);
-              ar[k].add(fabs(rv[h][k]));
-            }
-        }
-      }
-    }
-    if (kTicket) {
-      // the part's record: a fixed block tree over the threads' sums
-      double d6[6];
 #pragma unroll
       for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
-      blockSum<6>(d6, red);  // ends with a barrier
-      if (threadIdx.x == 0) {
-        double* q = partials + 8 * (size_t)part;
-        for (int k = 0; k < 6; ++k) q[k] = d6[k];
-      }
     }
-    __syncthreads();  // the next part may reuse the shared memory
-    if (threadIdx.x == 0) sTicket = nextTicket;
+    sum64<6>(d6, red);  // ends with a barrier: the next part may reuse the shared memory
+    if (threadIdx.x == 0) {
+      double* q = partials + 8 * (size_t)part;
+      for (int k = 0; k < 6; ++k) q[k] = d6[k];
+      sTicket = nextTicket;
+    }
     __syncthreads();
     part = sTicket;
   }
-  if (!kTicket) {
-    // the CTA's record: a fixed block tree over the threads' sums
-    double d6[6];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
-    blockSum<6>(d6, red);
-    if (threadIdx.x == 0) {
-      double* q = partials + 8 * (size_t)blockIdx.x;
-      for (int k = 0; k < 6; ++k) q[k] = d6[k];
-    }
-  }
-  // the last CTA sums the records (parts or CTAs) in index order
+  // the last CTA sums the part records in part order
   if (!lastBlockDone(&st->counter[5], gridDim.x)) return;
   double S[6];
-  reduceRecords<6>(partials, 8, kTicket ? mv.nParts : (int)gridDim.x, S, (double*)smraw);
+  reduceRecords<6>(partials, 8, mv.nParts, S, (double*)smraw);
   if (threadIdx.x != 0) return;
   st->counter[5] = 0;
   st->locTicket = 0;
@@ -515,35 +491,45 @@ kLocSpmvSplit(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   st->pcgContinue = any;
 }
 
-template <typename T, int NT>
-void launchPrecondNT(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
-                     double* partials, int grid, cudaStream_t s, int nCases) {
-  kLocPrecond<T, NT><<<dim3(grid, nCases), NT, localSmemBytes<T>(mv), s>>>(mv, c, p, st, partials);
+template <typename T, int NT, int RPT>
+void launchPrecondV(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
+                    double* partials, int grid, cudaStream_t s, int nCases) {
+  kLocPrecond<T, NT, RPT><<<dim3(grid, nCases), NT, localSmemBytes<T>(mv), s>>>(mv, c, p, st,
+                                                                               partials);
 }
 
-template <typename T, int NT>
-cudaError_t prepareNT(const MeshView& mv, int* blocksPerSM) {
+template <typename T, int NT, int RPT>
+cudaError_t prepareV(const MeshView& mv, int* blocksPerSM) {
   const int sm = (int)localSmemBytes<T>(mv);
-  cudaError_t e = setMaxDynamicSmem(kLocPrecond<T, NT>);
+  cudaError_t e = setMaxDynamicSmem(kLocPrecond<T, NT, RPT>);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, NT>, NT, sm);
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, NT, RPT>, NT, sm);
 }
 
 }  // namespace
 
-const int kLocVariantsNT[kLocNumNT] = {64};
+// Preconditioner variants (threads per part, rows per thread in flight):
+// FP32 {128 x 4, 256 x 2}, FP64 {128 x 2, 256 x 1}.  perf.part_threads
+// reports the threads of the one in use.
+const int kLocVariantsNT[kLocNumNT] = {128, 256};
 const int kLocVariantsU[kLocNumU] = {1, 6, 0};
 
 template <typename T>
 size_t localSmemBytes(const MeshView& mv) {
   const size_t P = mv.maxRows, EL = mv.maxLocEntries, ML = mv.maxLocMeta;
-  const size_t tables = sizeof(T) * (EL + 3 * P) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
+  const size_t tables = sizeof(T) * (EL + 6 * P) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
   return std::max(tables, (size_t)256 * 6 * sizeof(double));  // final reduction scratch
 }
 
 template <typename T>
 cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM) {
-  return prepareNT<T, kLocBlock>(mv, &blocksPerSM[0]);
+  if constexpr (sizeof(T) == 4) {
+    cudaError_t e = prepareV<T, 128, 4>(mv, &blocksPerSM[0]);
+    return e != cudaSuccess ? e : prepareV<T, 256, 2>(mv, &blocksPerSM[1]);
+  } else {
+    cudaError_t e = prepareV<T, 128, 2>(mv, &blocksPerSM[0]);
+    return e != cudaSuccess ? e : prepareV<T, 256, 1>(mv, &blocksPerSM[1]);
+  }
 }
 
 template <typename T>
@@ -554,7 +540,13 @@ void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaS
 template <typename T>
 void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                         double* partials, const LocalTuning& t, cudaStream_t s, int nCases) {
-  launchPrecondNT<T, kLocBlock>(mv, c, p, st, partials, t.grid[0], s, nCases);
+  if constexpr (sizeof(T) == 4) {
+    if (t.ntIdx == 1) launchPrecondV<T, 256, 2>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    else launchPrecondV<T, 128, 4>(mv, c, p, st, partials, t.grid[0], s, nCases);
+  } else {
+    if (t.ntIdx == 1) launchPrecondV<T, 256, 1>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    else launchPrecondV<T, 128, 2>(mv, c, p, st, partials, t.grid[0], s, nCases);
+  }
 }
 
 template <typename T>

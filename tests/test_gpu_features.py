@@ -281,3 +281,50 @@ def test_rigid_rotation_matches_oracle(ctx, model_name, model_id):
     assert np.abs(D - exact).max() < 1e-7 * np.abs(exact).max()
     assert np.abs(sig).max() < 1.0                    # below 1e-6 mu
     assert rel(D, Do) < TOL_D
+
+
+@pytest.mark.parametrize("kind", ["tl", "cases", "exact"])
+def test_device_loop_is_bit_identical_to_the_host_loop(kind):
+    """The device-resident corrector loop (one CUDA graph whose conditional
+    WHILE nodes run the correctors and the PCG iterations, decided on the
+    device) computes exactly what the host-driven loop computes: same bits,
+    same corrector and iteration counts.  Total Lagrangian increments,
+    batched load cases and the exact DIC's sweeps."""
+    m = sg.box_mesh(10, 9, 8, 1.0, 0.9, 0.8, 0.2, 6)
+    top = int(m["patch_size"][5])
+    out = []
+    for graphs in (True, False):
+        c = sg.Context(0, graphs=graphs)
+        if kind == "tl":
+            bcs = {"zmin": ("fixedDisplacement", None, None),
+                   "zmax": ("solidTraction", np.tile([0.0, 5e4, -5e4], (top, 1)), None, 0.5)}
+            model = sg.SolidModel(c, m, dict(type="neoHookeanElastic", mu=1e6, K=1e7), bcs,
+                                  model="nonLinearGeometryTotalLagrangian",
+                                  outer=dict(nCorrectors=3000, fieldRelaxation=0.7),
+                                  precision="FP32_REFINE", parts=block_parts(10, 9, 8, 4))
+            D, sig, perf = model.evolve(n_increments=3)
+            res = [(D, sig, perf)]
+        elif kind == "cases":
+            tr = np.random.default_rng(9).normal(0.0, 1e6, (3, 3))
+            cases = [{"zmin": ("fixedDisplacement", None, None),
+                      "zmax": ("solidTraction", tr[k], None)} for k in range(3)]
+            model = sg.SolidModel(c, m, dict(type="linearElastic", E=200e9, nu=0.3), cases[0],
+                                  precision="FP32_REFINE", parts=block_parts(10, 9, 8, 4))
+            Db, sb, perfs = model.evolve_cases(cases)
+            res = [(Db[k], sb[k], perfs[k]) for k in range(3)]
+        else:
+            bcs = {"zmin": ("fixedDisplacement", None, None),
+                   "zmax": ("solidTraction", None, np.full(top, 1e6))}
+            model = sg.SolidModel(c, m, dict(type="linearElastic", E=70e9, nu=0.33), bcs,
+                                  part_size=64)
+            D, sig, perf = model.evolve()
+            res = [(D, sig, perf)]
+        model.close()
+        c.close()
+        out.append(res)
+    for (D1, s1, p1), (D2, s2, p2) in zip(out[0], out[1]):
+        assert p1["device_loop"] == 1 and p2["device_loop"] == 0
+        assert p1["converged"] == 1
+        assert np.array_equal(D1, D2) and np.array_equal(s1, s2)
+        assert p1["n_correctors"] == p2["n_correctors"]
+        assert p1["total_lin_iters"] == p2["total_lin_iters"]
