@@ -464,6 +464,63 @@ def run_served(args, budget):
     return out
 
 
+def run_mesh_batch(args, budget):
+    """Many meshes in one launch (config form 3b): --mbatch-n jittered boxes
+    of 10-48 cells per edge, aspect ratios 1-4, E and nu drawn per mesh,
+    FP32+refine over 8^3-cell blocks, all advanced by one s4g_solve_batch
+    call (one CUDA-graph launch).  Against plain FP64 single solves of the
+    first --mbatch-fp64 meshes one after another, and the smallest mesh
+    against the oracle."""
+    import solids4foam_gb300 as sg
+    from solids4foam_gb300.cases import mesh_batch, oracle_bcs
+    cases = mesh_batch(args.mbatch_n)
+    ctx = sg.Context(0)
+    models = [sg.SolidModel(ctx, c["mesh"], c["law"], c["bcs"], outer=c["outer"],
+                            precision="FP32_REFINE", parts=c["parts"]) for c in cases]
+    sg.solve_batch(models)  # warm-up: tuning, FP32 copies, graph set-up
+    t0 = time.perf_counter()
+    res = sg.solve_batch(models)
+    wall = time.perf_counter() - t0
+    for m in models:
+        m.close()
+    n = len(cases)
+    out = {"workload": f"batch{n}_boxes_10-48_per_edge", "meshes": n,
+           "cells": int(sum(c["mesh"]["V"].shape[0] for c in cases)),
+           "solves_per_s": n / wall, "wall_s": wall, "device_s": res[0][2]["solve_ms"] / 1e3,
+           "all_converged": all(r[2]["converged"] == 1 for r in res),
+           "correctors_min_max": [min(r[2]["n_correctors"] for r in res),
+                                  max(r[2]["n_correctors"] for r in res)]}
+    k = min(args.mbatch_fp64, n)
+    if k and budget.left() > 200:
+        seq, errs = 0.0, []
+        for i in range(k):
+            c = cases[i]
+            m = sg.SolidModel(ctx, c["mesh"], c["law"], c["bcs"], outer=c["outer"], precision="FP64",
+                              parts=c["parts"])
+            t1 = time.perf_counter()
+            D, sig, p = m.evolve()
+            seq += time.perf_counter() - t1
+            m.close()
+            errs.append(rel_l2(res[i][0], D))
+        out.update({"plain_fp64_sequential_solves_per_s": k / seq, "plain_fp64_meshes_timed": k,
+                    "speedup_vs_plain_fp64_sequential": (n / wall) / (k / seq),
+                    "max_rel_l2_D_vs_fp64": max(errs)})
+    if budget.left() > 120:
+        from oracle import pyoracle
+        i = min(range(n), key=lambda j: cases[j]["mesh"]["V"].shape[0])
+        c = cases[i]
+        Do, so, _, po = pyoracle.solve(c["mesh"], oracle_bcs(c["mesh"], c["bcs"]),
+                                       dic_domain=c["parts"], E=c["law"]["E"], nu=c["law"]["nu"],
+                                       n_correctors=c["outer"]["nCorrectors"],
+                                       field_relaxation=c["outer"]["fieldRelaxation"],
+                                       n_threads=host_threads())
+        out["oracle_mesh_checked"] = {"cells": int(c["mesh"]["V"].shape[0]),
+                                      "rel_l2_D": rel_l2(res[i][0], Do),
+                                      "rel_l2_sigma": rel_l2(res[i][1], so)}
+    ctx.close()
+    return out
+
+
 def model_kwargs(case, args):
     kw = dict(solver=case["solver"], outer=case["outer"], precision=args.precision)
     if args.dic == "blocks":
@@ -577,6 +634,8 @@ def run_gb300(args):
 
     batched = (run_batched(args, ctx, budget)
                if (rank == 0 and not args.no_batched and budget.left() > 300) else None)
+    mbatch = (run_mesh_batch(args, budget)
+              if (rank == 0 and not args.no_mbatch and budget.left() > 300) else None)
     served = (run_served(args, budget)
               if (rank == 0 and not args.no_served and budget.left() > 300) else None)
 
@@ -631,6 +690,7 @@ def run_gb300(args):
         "error_vs_oracle": parity,
         "plain_fp64": fp64,
         "batched": batched,
+        "mesh_batch": mbatch,
         "served": served,
         "cpu_baseline": cpu,
         "clocks": clocks,
@@ -668,6 +728,10 @@ def main():
                     help="plain FP64 single solves timed for the batched comparison")
     ap.add_argument("--batch-oracle-cases", type=int, default=1,
                     help="batched cases also checked against the oracle")
+    ap.add_argument("--no-mbatch", action="store_true", help="skip the many-mesh batch")
+    ap.add_argument("--mbatch-n", type=int, default=256)
+    ap.add_argument("--mbatch-fp64", type=int, default=16,
+                    help="meshes of the batch solved one by one in plain FP64 for the comparison")
     ap.add_argument("--no-served", action="store_true", help="skip the served stream")
     ap.add_argument("--serve-n", type=int, default=24)
     ap.add_argument("--serve-slots", type=int, default=8)

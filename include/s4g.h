@@ -353,6 +353,22 @@ s4g_status s4g_solve_cases(s4g_mesh* mesh, int n_cases, const double* bval,
                            const double* bpress, double* D_out,
                            double* sigma_out, s4g_perf* perf);
 
+/* Many meshes in one launch: the linearGeometryTotalDisplacement solve of
+ * each mesh, with its own material, boundary conditions, controls and
+ * precision as set on it, all advanced by one CUDA-graph launch in which
+ * every mesh's device-resident corrector loop is an independent branch.
+ * Replaces running solidModel::evolve (linGeomTotalDispSolid.C:111-232)
+ * once per case, one case after another (applications/solvers/solids4Foam/
+ * solids4Foam.C:36-81 runs one case per process).  Each mesh's result is
+ * bit-identical to its s4g_solve.  The meshes belong to one context, which
+ * must not set profile, verbose or no_graphs.  D_out[i] [n_cells_i][3],
+ * sigma_out[i] [n_cells_i][6] (either array, or an entry, may be NULL),
+ * perf [n_meshes] (solve_ms: the whole launch) may be NULL.  Returns
+ * S4G_NOT_CONVERGED if a mesh did not converge, another status if one
+ * failed. */
+s4g_status s4g_solve_batch(s4g_mesh* const* meshes, int n_meshes, double* const* D_out,
+                           double* const* sigma_out, s4g_perf* perf);
+
 /* Cell gradient of D from the last solve, [n_cells][9] row-major,
  * grad(D)_ij = dD_j/dx_i (the reference's gradD field). */
 s4g_status s4g_get_gradD(s4g_mesh* mesh, double* gradD_out);

@@ -9,8 +9,8 @@ from ._lib import S4GError, lib
 from .cases import box_mesh, cantilever_case, cube_case
 from .foam_case import read_case, read_relaxation
 from .post import derived_fields, point_displacement
-from .solid_model import Context, Server, SolidModel
+from .solid_model import Context, Server, SolidModel, solve_batch
 
 __all__ = ["S4GError", "lib", "box_mesh", "cantilever_case", "cube_case", "Context",
            "Server", "SolidModel", "read_case", "read_relaxation", "point_displacement",
-           "derived_fields", "_lib"]
+           "derived_fields", "solve_batch", "_lib"]

@@ -143,6 +143,7 @@ _SIGS = {
     "s4g_solve": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
                              ct.POINTER(Perf)]),
     "s4g_get_gradD": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
+    "s4g_solve_batch": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "s4g_op_matrix": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "s4g_server_create": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "s4g_server_submit": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.POINTER(ct.c_uint64)]),

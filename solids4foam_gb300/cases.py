@@ -178,3 +178,30 @@ def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=96 ** 3, tl
                        parts=parts)
         out.append((t, req))
     return out
+
+
+def mesh_batch(n_meshes=256, seed=4, block=8):
+    """Many independent meshes solved in one launch: jittered boxes with nx,
+    ny, nz uniform integers in [10, 48], physical extents with the longest
+    over the shortest side uniform in [1, 4], E log-uniform in 1-300 GPa,
+    nu uniform in 0.2-0.45 (field relaxation 0.7 above nu = 0.35, as the
+    served stream), bottom fixed and a top traction N(0, 1 MPa) per
+    component.  Each case carries its block decomposition.  Returns a list
+    of dict(mesh, law, bcs, outer, parts)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n_meshes):
+        nx, ny, nz = (int(v) for v in rng.integers(10, 49, 3))
+        ratio = rng.uniform(1.0, 4.0)
+        ext = np.array([1.0, rng.uniform(1.0, ratio), ratio])
+        rng.shuffle(ext)
+        mesh = box_mesh(nx, ny, nz, ext[0], ext[1], ext[2], 0.2, 1000 + i)
+        E = np.exp(rng.uniform(np.log(1e9), np.log(300e9)))
+        nu = rng.uniform(0.2, 0.45)
+        tr = rng.normal(0.0, 1e6, 3)
+        out.append(dict(mesh=mesh, law=dict(type="linearElastic", E=E, nu=nu),
+                        bcs={"zmin": ("fixedDisplacement", None, None),
+                             "zmax": ("solidTraction", tr, None)},
+                        outer=dict(nCorrectors=4000, fieldRelaxation=0.7 if nu > 0.35 else 1.0),
+                        parts=block_parts(nx, ny, nz, block)))
+    return out

@@ -1223,6 +1223,88 @@ struct Engine {
     return S4G_OK;
   }
 
+  // ------------------------------------------------------ many meshes ---
+  // s4g_solve_batch: each mesh of the batch prepares its solve on the
+  // context's stream (matrix, FP32 copies, tuning, initial fields and the
+  // constructor's gradient pass), captures its device-resident corrector
+  // loop as an independent branch of one shared graph, and after the one
+  // launch of that graph reads back its own state and fields.
+  s4g_status batchPrepare() {
+    if (!materialSet) return setErr(S4G_BAD_ARG, "material not set");
+    if (law.type != S4G_LINEAR_ELASTIC)
+      return setErr(S4G_BAD_ARG, "s4g_solve_batch runs the linearGeometryTotalDisplacement model "
+                                 "(linearElastic law)");
+    S4G_TRY(ensureMatrix());
+    const bool mixed = precision == S4G_FP32_REFINE;
+    if (mixed) S4G_TRY(ensureFp32());
+    if (mv.subdomains && lin.preconditioner == S4G_PRECOND_DIC) {
+      const Controls ct = controls(0);
+      if (mixed) S4G_TRY(tuneLocal<float>(ct, pc32));
+      else S4G_TRY(tuneLocal<double>(ct, pc));
+    }
+    nRun = 1;
+    ranOnDevice = false;
+    S4G_TRY(initFields(0));
+    S4G_TRY(resetSweepState());
+    S4G_TRY(setLive());
+    timer.reset();
+    batchLaunches0 = launches;
+    const Controls c = controls(0);
+    launchTractionInit(mv, c, f, ctx->stream);
+    launchPost<double>(mv, c, f, pc.x, dState, dPartials, 0, ctx->stream);
+    launches += 2;
+    S4G_CUDA(cudaGetLastError());
+    return S4G_OK;
+  }
+  bool batchCapture(cudaGraph_t g) {
+    const Controls c = controls(0);
+    return precision == S4G_FP32_REFINE ? buildLoopGraph<float>(g, c, 0, pc32, sweepGrid32)
+                                        : buildLoopGraph<double>(g, c, 0, pc, sweepGrid);
+  }
+  s4g_status batchFinish(double* Dout, double* sigOut, s4g_perf* perf, float ms) {
+    cudaStream_t s = ctx->stream;
+    S4G_TRY(readState());
+    ranOnDevice = true;
+    const bool local = mv.subdomains && lin.preconditioner == S4G_PRECOND_DIC;
+    const long long perIt = local ? (tuning32or64().uIdx == 2 ? 3 : 2)
+                                  : (lin.preconditioner == S4G_PRECOND_DIC ? 5 : 4);
+    launches += 1 + (long long)hState->nCorrDone * 5 + (long long)hState->pcgIter * (perIt + 1);
+    if (Dout) {
+      launchGather(hp.nC, 3, dC2s, f.D[hState->dcur], dOut, s);
+      S4G_CUDA(cudaMemcpyAsync(Dout, dOut, sizeof(double) * 3 * hp.nC, cudaMemcpyDeviceToHost, s));
+    }
+    if (sigOut) {
+      launchGather(hp.nC, 6, dC2s, f.sig, dOut + 3 * (size_t)hp.nC, s);
+      S4G_CUDA(cudaMemcpyAsync(sigOut, dOut + 3 * (size_t)hp.nC, sizeof(double) * 6 * hp.nC,
+                               cudaMemcpyDeviceToHost, s));
+    }
+    S4G_CUDA(cudaStreamSynchronize(s));
+    lastModel = S4G_LIN_GEOM_TOTAL_DISP;
+    if (perf) {
+      std::memset(perf, 0, sizeof(*perf));
+      perf->n_correctors = hState->nCorrDone;
+      perf->converged = hState->converged;
+      perf->total_lin_iters = hState->totalLinIters;
+      perf->last_max_lin_iters = hState->lastMaxIters;
+      perf->initial_residual = hState->initResMag;
+      perf->rel_residual = hState->relRes;
+      perf->solve_ms = ms;
+      perf->kernel_launches = launches - batchLaunches0;
+      perf->device_status = (int)hState->status;
+      const LocalTuning& lt = tuning32or64();
+      perf->part_threads = local ? kLocVariantsNT[lt.ntIdx] : 0;
+      perf->spmv_unroll = local ? kLocVariantsU[lt.uIdx] : 0;
+      perf->device_loop = 1;
+    }
+    if (hState->status & kErrTimeout) return setErr(S4G_TIMEOUT, "a bounded device wait gave up");
+    if (hState->status & kErrNaN) return setErr(S4G_NAN_DETECTED, "non-finite value in the iteration");
+    if (hState->status & kErrIndefinite) return setErr(S4G_INDEFINITE, "PCG met p.Ap <= 0");
+    if (!hState->converged) return S4G_NOT_CONVERGED;
+    return S4G_OK;
+  }
+  const LocalTuning& tuning32or64() const { return precision == S4G_FP32_REFINE ? tune32 : tune64; }
+  long long batchLaunches0 = 0;
+
   // ---------------------------------------------------------- operators ---
   // All copies go through the library's stream (non-blocking: it does not
   // order against the legacy default stream), then wait for it.
@@ -1569,6 +1651,63 @@ s4g_status s4g_solve_cases(s4g_mesh* mesh, int n_cases, const double* bval,
   if (cudaSetDevice(mesh->e.ctx->device) != cudaSuccess)
     return setErr(S4G_CUDA_ERROR, "cudaSetDevice failed");
   return mesh->e.solveCases(n_cases, bval, bpress, D_out, sigma_out, perf);
+}
+
+s4g_status s4g_solve_batch(s4g_mesh* const* meshes, int n_meshes, double* const* D_out,
+                           double* const* sigma_out, s4g_perf* perf) {
+  if (!meshes || n_meshes < 1) return setErr(S4G_BAD_ARG, "need at least one mesh");
+  s4g_ctx* owner = meshes[0] ? meshes[0]->owner : nullptr;
+  if (!owner) return setErr(S4G_BAD_ARG, "null mesh");
+  for (int i = 0; i < n_meshes; ++i) {
+    if (!meshes[i] || meshes[i]->owner != owner)
+      return setErr(S4G_BAD_ARG, "every mesh of a batch must belong to the same context");
+    for (int j = 0; j < i; ++j)
+      if (meshes[j] == meshes[i]) return setErr(S4G_BAD_ARG, "a mesh appears twice in the batch");
+  }
+  s4g::Ctx& cx = owner->c;
+  if (cx.profile || cx.noGraphs || cx.verbose)
+    return setErr(S4G_BAD_ARG, "s4g_solve_batch runs one CUDA graph: the context must not set "
+                               "profile, verbose or no_graphs");
+  if (cudaSetDevice(cx.device) != cudaSuccess) return setErr(S4G_CUDA_ERROR, "cudaSetDevice failed");
+  for (int i = 0; i < n_meshes; ++i) {
+    const s4g_status st = meshes[i]->e.batchPrepare();
+    if (st != S4G_OK) return st;
+  }
+  cudaGraph_t g = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return setErr(S4G_CUDA_ERROR, "cudaGraphCreate failed");
+  for (int i = 0; i < n_meshes; ++i)
+    if (!meshes[i]->e.batchCapture(g)) {
+      cudaGraphDestroy(g);
+      cudaGetLastError();
+      return setErr(S4G_CUDA_ERROR, "capturing a mesh's corrector loop into the batch graph failed");
+    }
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t ie = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  if (ie != cudaSuccess) return setErr(S4G_CUDA_ERROR, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  cudaEventRecord(e0, cx.stream);
+  cudaError_t le = cudaGraphLaunch(exec, cx.stream);
+  cudaEventRecord(e1, cx.stream);
+  cudaError_t se = cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaGraphExecDestroy(exec);
+  if (le != cudaSuccess || se != cudaSuccess)
+    return setErr(S4G_CUDA_ERROR, std::string("batch graph: ") + cudaGetErrorString(le != cudaSuccess ? le : se));
+  s4g_status ret = S4G_OK;
+  for (int i = 0; i < n_meshes; ++i) {
+    const s4g_status st = meshes[i]->e.batchFinish(D_out ? D_out[i] : nullptr,
+                                                   sigma_out ? sigma_out[i] : nullptr,
+                                                   perf ? perf + i : nullptr, ms);
+    if (st == S4G_NOT_CONVERGED) { if (ret == S4G_OK) ret = st; }
+    else if (st != S4G_OK) ret = st;
+  }
+  return ret;
 }
 
 s4g_status s4g_op_amul_dot_noalloc(s4g_mesh* mesh, int k, const double* x, double* y,

@@ -320,6 +320,26 @@ class SolidModel:
         return w
 
 
+def solve_batch(models):
+    """s4g_solve_batch: the linear-geometry solves of several models (one
+    context, one CUDA-graph launch for all).  Returns a list of (D, sigma,
+    perf) in the order of `models`."""
+    n = len(models)
+    if n == 0:
+        return []
+    L = models[0].L
+    hs = (ct.c_void_p * n)(*[m.h.value if isinstance(m.h, ct.c_void_p) else m.h for m in models])
+    Ds = [np.zeros((m.n_cells, 3)) for m in models]
+    Ss = [np.zeros((m.n_cells, 6)) for m in models]
+    dp = (ct.c_void_p * n)(*[d.ctypes.data for d in Ds])
+    sp = (ct.c_void_p * n)(*[x.ctypes.data for x in Ss])
+    perfs = (_lib.Perf * n)()
+    st = L.s4g_solve_batch(ct.cast(hs, ct.c_void_p), n, ct.cast(dp, ct.c_void_p),
+                           ct.cast(sp, ct.c_void_p), ct.cast(perfs, ct.c_void_p))
+    _lib.check(st, "s4g_solve_batch", allow=(_lib.OK, _lib.NOT_CONVERGED))
+    return [(Ds[i], Ss[i], perfs[i].as_dict()) for i in range(n)]
+
+
 def plan(mesh, renumber: str = "tiled", part_size: int = 512, dic_subdomains: bool = False,
          parts=None):
     """Host-only DIC order and scheduling figures (no GPU): (perm, info).

@@ -2,7 +2,7 @@
 bit for bit, the single solve of the same mesh with that case's boundary
 values -- same corrector and PCG iteration counts, same D and sigma -- and
 cases converge independently (a zero-load case and strong cases side by
-side)."""
+side).  Many meshes in one launch (s4g_solve_batch) likewise."""
 import numpy as np
 import pytest
 
@@ -67,3 +67,37 @@ def test_batch_needs_the_local_dic(ctx):
     with pytest.raises(_lib.S4GError, match="dic_subdomains"):
         model.evolve_cases(cases)
     model.close()
+
+
+def test_solve_batch_equals_single_solves_and_the_oracle():
+    """s4g_solve_batch: meshes of the many-mesh batch form (jittered boxes of
+    uneven sizes and aspect ratios, E and nu drawn per mesh, field
+    relaxation where nu is high) advanced by one CUDA-graph launch, each
+    mesh's device-resident loop a branch of it.  Every mesh's result is
+    bit-identical to its own s4g_solve, and one is checked against the
+    oracle."""
+    from oracle import pyoracle
+    from solids4foam_gb300.cases import mesh_batch, oracle_bcs
+    cases = mesh_batch(6, seed=11)
+    c0 = sg.Context(0)
+    models = [sg.SolidModel(c0, c["mesh"], c["law"], c["bcs"], outer=c["outer"],
+                            precision="FP32_REFINE", parts=c["parts"]) for c in cases]
+    res = sg.solve_batch(models)
+    for (D, sig, perf), m in zip(res, models):
+        assert perf["converged"] == 1 and perf["device_loop"] == 1
+        D1, s1, p1 = m.evolve()
+        assert np.array_equal(D, D1) and np.array_equal(sig, s1)
+        assert p1["n_correctors"] == perf["n_correctors"]
+        assert p1["total_lin_iters"] == perf["total_lin_iters"]
+    k = min(range(len(cases)), key=lambda i: cases[i]["mesh"]["V"].shape[0])
+    c = cases[k]
+    Do, so, _, po = pyoracle.solve(c["mesh"], oracle_bcs(c["mesh"], c["bcs"]), dic_domain=c["parts"],
+                                   E=c["law"]["E"], nu=c["law"]["nu"], n_correctors=4000,
+                                   field_relaxation=c["outer"]["fieldRelaxation"], n_threads=8)
+    assert po["converged"] == 1
+    D, sig, _ = res[k]
+    assert np.linalg.norm(D - Do) / np.linalg.norm(Do) < 1e-6
+    assert np.linalg.norm(sig - so) / np.linalg.norm(so) < 1e-5
+    for m in models:
+        m.close()
+    c0.close()
