@@ -538,7 +538,7 @@ def run_gb300(args):
     mesh = case["mesh"]
     kw = model_kwargs(case, args)
     # the production path: CUDA graphs on, no per-kernel events
-    ctx = sg.Context(local)
+    ctx = sg.Context(local, graphs=not args.no_graphs)
     model = sg.SolidModel(ctx, mesh, case["law"], case["bcs"], **kw)
     for _ in range(args.warmup):
         model.evolve()
@@ -720,6 +720,10 @@ def main():
                          "reported as an estimate")
     ap.add_argument("--budget-s", type=float, default=1500.0,
                     help="wall time the optional legs of the GPU arm may take in all")
+    ap.add_argument("--no-graphs", action="store_true",
+                    help="host-driven corrector loop, kernel by kernel (for profilers)")
+    ap.add_argument("--no-profiled-solve", action="store_true",
+                    help="skip the solve with per-kernel events (no kernels/roofline)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched load cases")
     ap.add_argument("--batch-n", type=int, default=64)

@@ -526,6 +526,7 @@ struct Engine {
     S4G_CUDA(cudaMemsetAsync(pc.flags[0], 0, sizeof(unsigned) * hp.nParts, s));
     S4G_CUDA(cudaMemsetAsync(pc.flags[1], 0, sizeof(unsigned) * hp.nParts, s));
     S4G_CUDA(cudaMemsetAsync(dState, 0, sizeof(DevState) * nRun, s));
+    std::memset(hState, 0, sizeof(DevState) * nRun);  // the host mirror starts alike
     DevState init{};
     init.epoch[0] = 1; init.epoch[1] = 1;
     for (int cs = 0; cs < nRun; ++cs)
