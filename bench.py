@@ -448,7 +448,9 @@ def run_served(args, budget):
             if m["V"].shape[0] > args.serve_oracle_cells:
                 continue
             law, o = req["law"], req["outer"]
-            kw = dict(n_correctors=o["nCorrectors"], field_relaxation=o["fieldRelaxation"],
+            kw = dict(n_correctors=o["nCorrectors"], field_relaxation=o.get("fieldRelaxation", 1.0),
+                      solution_tol=o.get("solutionTolerance", 1e-6),
+                      alternative_tol=o.get("alternativeTolerance", 1e-7),
                       n_threads=host_threads(), dic_domain=req["parts"])
             if law["type"] == "linearElastic":
                 kw.update(E=law["E"], nu=law["nu"])
@@ -512,7 +514,9 @@ def run_mesh_batch(args, budget):
         Do, so, _, po = pyoracle.solve(c["mesh"], oracle_bcs(c["mesh"], c["bcs"]),
                                        dic_domain=c["parts"], E=c["law"]["E"], nu=c["law"]["nu"],
                                        n_correctors=c["outer"]["nCorrectors"],
-                                       field_relaxation=c["outer"]["fieldRelaxation"],
+                                       field_relaxation=c["outer"].get("fieldRelaxation", 1.0),
+                                       solution_tol=c["outer"].get("solutionTolerance", 1e-6),
+                                       alternative_tol=c["outer"].get("alternativeTolerance", 1e-7),
                                        n_threads=host_threads())
         out["oracle_mesh_checked"] = {"cells": int(c["mesh"]["V"].shape[0]),
                                       "rel_l2_D": rel_l2(res[i][0], Do),

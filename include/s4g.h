@@ -369,6 +369,19 @@ s4g_status s4g_solve_cases(s4g_mesh* mesh, int n_cases, const double* bval,
 s4g_status s4g_solve_batch(s4g_mesh* const* meshes, int n_meshes, double* const* D_out,
                            double* const* sigma_out, s4g_perf* perf);
 
+/* The mesh's points for the device step after the loop: points
+ * [n_points][3] and the cells of every point as s4g_point_cells returns
+ * them (caller cell ids; point_cell_start [n_points + 1]).  Copied once. */
+s4g_status s4g_mesh_set_points(s4g_mesh* mesh, int n_points, const double* points,
+                               const int* point_cell_start, const int* point_cells);
+/* pointD [n_points][3] of the last solve, computed on the device from the D
+ * and gradD the solve left there (total D and gradD for the total
+ * Lagrangian models), as mechanical().interpolate(D, gradD, pointD) does
+ * after each evolve() (linGeomTotalDispSolid.C:212, mechanicalModel.C:
+ * 829-841, enhancedVolPointInterpolate.C:351-423); bit-identical to
+ * s4g_point_interpolate on the same fields. */
+s4g_status s4g_get_pointD(s4g_mesh* mesh, double* pointD_out);
+
 /* Cell gradient of D from the last solve, [n_cells][9] row-major,
  * grad(D)_ij = dD_j/dx_i (the reference's gradD field). */
 s4g_status s4g_get_gradD(s4g_mesh* mesh, double* gradD_out);

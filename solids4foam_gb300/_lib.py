@@ -144,6 +144,9 @@ _SIGS = {
                              ct.POINTER(Perf)]),
     "s4g_get_gradD": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "s4g_solve_batch": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
+    "s4g_mesh_set_points": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p,
+                                       ct.c_void_p]),
+    "s4g_get_pointD": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "s4g_op_matrix": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "s4g_server_create": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "s4g_server_submit": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.POINTER(ct.c_uint64)]),

@@ -1387,6 +1387,60 @@ struct Engine {
     return S4G_OK;
   }
 
+  // Points of the mesh for the device point interpolation (s4g_mesh_set_points).
+  int nPoints = -1;
+  double* dPts = nullptr;
+  int* dPcs = nullptr;
+  int* dPcc = nullptr;
+  double* dPointD = nullptr;
+
+  s4g_status setPoints(int nP, const double* pts, const int* pcs, const int* pcc) {
+    if (nP < 0 || (nP > 0 && (!pts || !pcs || !pcc)))
+      return setErr(S4G_BAD_ARG, "s4g_mesh_set_points: bad arguments");
+    if (nP > 0 && pcs[0] != 0) return setErr(S4G_BAD_ARG, "point_cell_start[0] must be 0");
+    for (int p = 0; p < nP; ++p)
+      if (pcs[p + 1] < pcs[p]) return setErr(S4G_BAD_ARG, "point_cell_start must not decrease");
+    const int nE = nP > 0 ? pcs[nP] : 0;
+    for (int k = 0; k < nE; ++k)
+      if (pcc[k] < 0 || pcc[k] >= hp.nC) return setErr(S4G_BAD_ARG, "point cell out of range");
+    S4G_CUDA(cudaStreamSynchronize(ctx->stream));
+    for (void* q : {(void*)dPts, (void*)dPcs, (void*)dPcc, (void*)dPointD})
+      if (q) {
+        cudaFree(q);
+        allocs.erase(std::find(allocs.begin(), allocs.end(), q));
+      }
+    dPts = nullptr; dPcs = nullptr; dPcc = nullptr; dPointD = nullptr;
+    S4G_TRY(alloc(&dPts, 3 * (size_t)nP));
+    S4G_TRY(alloc(&dPcs, (size_t)nP + 1));
+    S4G_TRY(alloc(&dPcc, (size_t)nE));
+    S4G_TRY(alloc(&dPointD, 3 * (size_t)nP));
+    cudaStream_t s = ctx->stream;
+    if (nP > 0) {
+      S4G_CUDA(cudaMemcpyAsync(dPts, pts, sizeof(double) * 3 * nP, cudaMemcpyHostToDevice, s));
+      S4G_CUDA(cudaMemcpyAsync(dPcs, pcs, sizeof(int) * (nP + 1), cudaMemcpyHostToDevice, s));
+      if (nE) S4G_CUDA(cudaMemcpyAsync(dPcc, pcc, sizeof(int) * nE, cudaMemcpyHostToDevice, s));
+    }
+    S4G_CUDA(cudaStreamSynchronize(s));
+    nPoints = nP;
+    return S4G_OK;
+  }
+
+  s4g_status getPointD(double* out) {
+    if (lastModel < 0) return setErr(S4G_BAD_ARG, "no solve has run");
+    if (nPoints < 0) return setErr(S4G_BAD_ARG, "no points: call s4g_mesh_set_points first");
+    if (!out) return setErr(S4G_BAD_ARG, "null output");
+    const bool tlm = lastModel != S4G_LIN_GEOM_TOTAL_DISP;
+    const double* U = tlm ? f.D0 : f.D[hState->dcur];
+    const double* G = tlm ? f.GD : f.G;
+    launchPointInterp(nPoints, dPts, dPcs, dPcc, dC2s, geo.C, U, G, dPointD, ctx->stream);
+    launches++;
+    S4G_CUDA(cudaGetLastError());
+    S4G_CUDA(cudaMemcpyAsync(out, dPointD, sizeof(double) * 3 * (size_t)nPoints,
+                             cudaMemcpyDeviceToHost, ctx->stream));
+    S4G_CUDA(cudaStreamSynchronize(ctx->stream));
+    return S4G_OK;
+  }
+
   s4g_status getGradD(double* out) {
     if (lastModel < 0) return setErr(S4G_BAD_ARG, "no solve has run");
     const double* src = lastModel != S4G_LIN_GEOM_TOTAL_DISP ? f.GD : f.G;
@@ -1628,6 +1682,21 @@ s4g_status s4g_solve(s4g_mesh* mesh, s4g_model model, int n_increments, double* 
 s4g_status s4g_get_gradD(s4g_mesh* mesh, double* gradD_out) {
   if (!mesh || !gradD_out) return setErr(S4G_BAD_ARG, "null argument");
   return mesh->e.getGradD(gradD_out);
+}
+
+s4g_status s4g_mesh_set_points(s4g_mesh* mesh, int n_points, const double* points,
+                               const int* point_cell_start, const int* point_cells) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  if (cudaSetDevice(mesh->e.ctx->device) != cudaSuccess)
+    return setErr(S4G_CUDA_ERROR, "cudaSetDevice failed");
+  return mesh->e.setPoints(n_points, points, point_cell_start, point_cells);
+}
+
+s4g_status s4g_get_pointD(s4g_mesh* mesh, double* pointD_out) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  if (cudaSetDevice(mesh->e.ctx->device) != cudaSuccess)
+    return setErr(S4G_CUDA_ERROR, "cudaSetDevice failed");
+  return mesh->e.getPointD(pointD_out);
 }
 
 s4g_status s4g_op_matrix(s4g_mesh* mesh, double* diag, double* upper) {

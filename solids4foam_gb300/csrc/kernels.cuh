@@ -92,6 +92,12 @@ template <typename T>
 void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, T* x, T* r,
                DevState* st, double* partials, cudaStream_t s, LaunchTimer* tm = nullptr,
                int nCases = 1);
+// pointD [nP][3] (caller point order) from the storage-order cell centres C,
+// field U and gradient G, over the points' cells pcc (caller cell ids,
+// CSR pcs); see kPointInterp.
+void launchPointInterp(int nP, const double* pts, const int* pcs, const int* pcc, const int* c2s,
+                       const double* C, const double* U, const double* G, double* out,
+                       cudaStream_t s);
 // out[c] = in[c2s[c]] for rows of `width` doubles.
 void launchGather(int n, int width, const int* c2s, const double* in, double* out, cudaStream_t s);
 // TL: new time step -- old-time fields take the converged values.

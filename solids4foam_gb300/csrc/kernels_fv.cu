@@ -590,6 +590,42 @@ __global__ void kSetLoopCond(cudaGraphConditionalHandle h, DevState* st, int nRu
   cudaGraphSetConditional(h, any ? 1u : 0u);
 }
 
+// pointD after the loop (enhancedVolPointInterpolate.C:351-423 via
+// mechanicalModel.C:829-841): per point the inverse-distance-weighted
+// average over its cells of D_c + (x_p - C_c) . gradD_c.  The operations are
+// rounded one by one (no fused multiply-add) in the order of the host step
+// s4g_point_interpolate, so both give the same bits.
+__global__ void kPointInterp(int nP, const double* __restrict__ pts, const int* __restrict__ pcs,
+                             const int* __restrict__ pcc, const int* __restrict__ c2s,
+                             const double* __restrict__ C, const double* __restrict__ U,
+                             const double* __restrict__ G, double* __restrict__ out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nP) return;
+  const double x0 = pts[3 * (size_t)p], x1 = pts[3 * (size_t)p + 1], x2 = pts[3 * (size_t)p + 2];
+  double a0 = 0, a1 = 0, a2 = 0, sumW = 0;
+  for (int k = pcs[p]; k < pcs[p + 1]; ++k) {
+    const size_t s = (size_t)c2s[pcc[k]];
+    const double d0 = __dsub_rn(x0, C[3 * s]), d1 = __dsub_rn(x1, C[3 * s + 1]),
+                 d2 = __dsub_rn(x2, C[3 * s + 2]);
+    const double m2 = __dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2));
+    const double w = __ddiv_rn(1.0, __dsqrt_rn(m2));
+    const double* g = G + 9 * s;
+    const double* u = U + 3 * s;
+    double e[3];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      e[j] = __dmul_rn(w, __dadd_rn(u[j], __dadd_rn(__dadd_rn(__dmul_rn(d0, g[j]), __dmul_rn(d1, g[3 + j])),
+                                                    __dmul_rn(d2, g[6 + j]))));
+    a0 = __dadd_rn(a0, e[0]); a1 = __dadd_rn(a1, e[1]); a2 = __dadd_rn(a2, e[2]);
+    sumW = __dadd_rn(sumW, w);
+  }
+  // normalised where the weight sum exceeds OpenFOAM's ROOTVSMALL
+  const bool nrm = sumW > 1e-150;
+  out[3 * (size_t)p] = nrm ? __ddiv_rn(a0, sumW) : a0;
+  out[3 * (size_t)p + 1] = nrm ? __ddiv_rn(a1, sumW) : a1;
+  out[3 * (size_t)p + 2] = nrm ? __ddiv_rn(a2, sumW) : a2;
+}
+
 __global__ void kGather(int n, int width, const int* c2s, const double* in, double* out) {
   long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= (long)n * width) return;
@@ -685,6 +721,12 @@ template void launchRhs<float>(const MeshView&, const Controls&, const FieldPtrs
 void launchGather(int n, int width, const int* c2s, const double* in, double* out, cudaStream_t s) {
   long tot = (long)n * width;
   kGather<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(n, width, c2s, in, out);
+}
+
+void launchPointInterp(int nP, const double* pts, const int* pcs, const int* pcc, const int* c2s,
+                       const double* C, const double* U, const double* G, double* out,
+                       cudaStream_t s) {
+  if (nP > 0) kPointInterp<<<(nP + 255) / 256, 256, 0, s>>>(nP, pts, pcs, pcc, c2s, C, U, G, out);
 }
 
 void launchSetLoopCond(cudaGraphConditionalHandle h, DevState* st, int nRun, int which, int first,

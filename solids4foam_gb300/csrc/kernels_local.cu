@@ -25,8 +25,9 @@
 // differs.
 //
 // Variants.  The SpMV step runs fused with a plain or an unrolled entry
-// loop, or split into a p-update pass and an SpMV; kLocPrecond runs with 128
-// or 256 threads per part.  The autotuner (engine) times them on the mesh
+// loop, or split into a p-update pass and an SpMV; kLocPrecond streams a
+// part's rows with 4 (FP32) or 2 (FP64) rows per thread in flight, or half
+// that.  The autotuner (engine) times them on the mesh
 // and keeps the fastest.  The SpMV variants sum in the same order (same grid
 // and block); kLocPrecond sums each part in a fixed order that does not
 // depend on its block size, then over the parts in index order.  So all
@@ -69,7 +70,7 @@ __device__ __forceinline__ LocSmem<T> locSmem(const MeshView& mv, unsigned char*
 // columns and coefficients), read before the barrier that ends the level
 // in progress, so that after it only the loads of the neighbours' values
 // and the multiply-add chain remain.
-constexpr int kLocPre = 4;
+constexpr int kLocPre = 3;
 template <typename T>
 struct LocRow {
   int i, n, j0;
@@ -77,9 +78,9 @@ struct LocRow {
   T a[kLocPre];
 };
 
-template <int DIR, int NT, typename T>
-__device__ __forceinline__ void locPre(const LocSmem<T>& sm, int l, LocRow<T>& row) {
-  row.i = sm.lv[l] + (int)threadIdx.x;
+template <int DIR, typename T>
+__device__ __forceinline__ void locPre(const LocSmem<T>& sm, int l, int off, LocRow<T>& row) {
+  row.i = sm.lv[l] + off;
   row.n = 0;
   if (row.i >= sm.lv[l + 1]) { row.i = -1; return; }
   const uint32_t m = sm.m[row.i];
@@ -111,33 +112,35 @@ __device__ __forceinline__ void locApply(const LocSmem<T>& sm, const LocRow<T>& 
   sm.w[3 * i] = v0; sm.w[3 * i + 1] = v1; sm.w[3 * i + 2] = v2;
 }
 
-// One substitution (DIR 0 forward, 1 backward) over the part's levels: the
-// rows of a level in parallel, a barrier between levels, the next level's
-// static data in registers while the current level runs.
-template <int DIR, int NT, typename T>
+// One substitution (DIR 0 forward, 1 backward) over the part's levels, by
+// one warp: the rows of a level in parallel (two per lane, more for a level
+// wider than 64 rows), a warp barrier between levels, and the next level's
+// static data in registers while the current level runs.  A level's rows
+// are few (at most 48 in an 8^3-cell part), so one warp walks them with
+// cheap __syncwarp barriers while the rest of the CTA waits.
+template <int DIR, typename T>
 __device__ __forceinline__ void locSweep(const LocSmem<T>& sm, int nL) {
   if (nL <= 0) return;
-  LocRow<T> nxt;
-  locPre<DIR, NT>(sm, DIR == 0 ? 0 : nL - 1, nxt);
+  const int lane = (int)threadIdx.x;
+  LocRow<T> n0, n1;
+  locPre<DIR>(sm, DIR == 0 ? 0 : nL - 1, lane, n0);
+  locPre<DIR>(sm, DIR == 0 ? 0 : nL - 1, lane + 32, n1);
   for (int s = 0; s < nL; ++s) {
     const int l = DIR == 0 ? s : nL - 1 - s;
-    const LocRow<T> cur = nxt;
-    if (s + 1 < nL) locPre<DIR, NT>(sm, DIR == 0 ? l + 1 : l - 1, nxt);
-    if (cur.i >= 0) locApply(sm, cur);
-    // rows beyond the first NT of a wide level
-    for (int i = sm.lv[l] + (int)threadIdx.x + NT; i < sm.lv[l + 1]; i += NT) {
+    const LocRow<T> c0 = n0, c1 = n1;
+    if (s + 1 < nL) {
+      locPre<DIR>(sm, DIR == 0 ? l + 1 : l - 1, lane, n0);
+      locPre<DIR>(sm, DIR == 0 ? l + 1 : l - 1, lane + 32, n1);
+    }
+    if (c0.i >= 0) locApply(sm, c0);
+    if (c1.i >= 0) locApply(sm, c1);
+    // rows beyond the first 64 of a wide level
+    for (int off = lane + 64; sm.lv[l] + off < sm.lv[l + 1]; off += 32) {
       LocRow<T> row;
-      const uint32_t m = sm.m[i];
-      const int nl = (m >> 16) & 0xff;
-      row.i = i;
-      row.j0 = DIR == 0 ? (int)(m & 0xffff) : (int)(m & 0xffff) + nl;
-      row.n = DIR == 0 ? nl : (int)(m >> 24);
-#pragma unroll
-      for (int u = 0; u < kLocPre; ++u)
-        if (u < row.n) { row.q[u] = sm.idx[row.j0 + u]; row.a[u] = sm.c[row.j0 + u]; }
+      locPre<DIR>(sm, l, off, row);
       locApply(sm, row);
     }
-    __syncthreads();
+    __syncwarp();
   }
 }
 
@@ -151,7 +154,7 @@ __global__ void kLocGather(int n, const int* src, const double* rDa, T* out) {
 // thread in flight at once in the streaming phase).
 template <typename T, int NT, int RPT>
 constexpr int locMinBlocks() {
-  return sizeof(T) == 4 ? (NT == 128 ? 4 : 2) : (NT == 128 ? 3 : 2);
+  return sizeof(T) == 4 ? (RPT >= 4 ? 4 : 5) : (RPT >= 2 ? 3 : 4);
 }
 
 // The processor-local preconditioner of one PCG iteration: the pending
@@ -250,8 +253,11 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
     __syncthreads();
     // forward substitution: w_u -= sum_{l<u in part} (rD_u a_ul) w_l, then
     // backward substitution: w_l -= sum_{u>l in part} (rD_l a_lu) w_u
-    locSweep<0, NT>(sm, nL);
-    locSweep<1, NT>(sm, nL);
+    if (threadIdx.x < 32) {
+      locSweep<0>(sm, nL);
+      locSweep<1>(sm, nL);
+    }
+    __syncthreads();
     // w out
     T* __restrict__ wg = p.w + 3 * (size_t)pLo;
     for (int k = threadIdx.x; k < 3 * nR; k += NT) wg[k] = sm.w[k];
@@ -503,15 +509,21 @@ cudaError_t prepareV(const MeshView& mv, int* blocksPerSM) {
   const int sm = (int)localSmemBytes<T>(mv);
   cudaError_t e = setMaxDynamicSmem(kLocPrecond<T, NT, RPT>);
   if (e != cudaSuccess) return e;
+  // as much of the SM's memory as shared memory as possible: parts per SM
+  // are bounded by their staged tables
+  e = cudaFuncSetAttribute(kLocPrecond<T, NT, RPT>,
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, NT, RPT>, NT, sm);
 }
 
 }  // namespace
 
-// Preconditioner variants (threads per part, rows per thread in flight):
-// FP32 {128 x 4, 256 x 2}, FP64 {128 x 2, 256 x 1}.  perf.part_threads
-// reports the threads of the one in use.
-const int kLocVariantsNT[kLocNumNT] = {128, 256};
+// Preconditioner variants (threads per part x rows per thread in flight at
+// once): FP32 {128 x 4, 128 x 2}, FP64 {128 x 2, 128 x 1}; the second of
+// each pair holds fewer registers, so more parts are resident per SM.
+// perf.part_threads reports the threads of the one in use.
+const int kLocVariantsNT[kLocNumNT] = {128, 128};
 const int kLocVariantsU[kLocNumU] = {1, 6, 0};
 
 template <typename T>
@@ -525,10 +537,10 @@ template <typename T>
 cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM) {
   if constexpr (sizeof(T) == 4) {
     cudaError_t e = prepareV<T, 128, 4>(mv, &blocksPerSM[0]);
-    return e != cudaSuccess ? e : prepareV<T, 256, 2>(mv, &blocksPerSM[1]);
+    return e != cudaSuccess ? e : prepareV<T, 128, 2>(mv, &blocksPerSM[1]);
   } else {
     cudaError_t e = prepareV<T, 128, 2>(mv, &blocksPerSM[0]);
-    return e != cudaSuccess ? e : prepareV<T, 256, 1>(mv, &blocksPerSM[1]);
+    return e != cudaSuccess ? e : prepareV<T, 128, 1>(mv, &blocksPerSM[1]);
   }
 }
 
@@ -541,10 +553,10 @@ template <typename T>
 void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                         double* partials, const LocalTuning& t, cudaStream_t s, int nCases) {
   if constexpr (sizeof(T) == 4) {
-    if (t.ntIdx == 1) launchPrecondV<T, 256, 2>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    if (t.ntIdx == 1) launchPrecondV<T, 128, 2>(mv, c, p, st, partials, t.grid[1], s, nCases);
     else launchPrecondV<T, 128, 4>(mv, c, p, st, partials, t.grid[0], s, nCases);
   } else {
-    if (t.ntIdx == 1) launchPrecondV<T, 256, 1>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    if (t.ntIdx == 1) launchPrecondV<T, 128, 1>(mv, c, p, st, partials, t.grid[1], s, nCases);
     else launchPrecondV<T, 128, 2>(mv, c, p, st, partials, t.grid[0], s, nCases);
   }
 }

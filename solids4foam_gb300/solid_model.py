@@ -268,6 +268,23 @@ class SolidModel:
         _lib.check(self.L.s4g_get_gradD(self.h, G.ctypes.data), "s4g_get_gradD")
         return G
 
+    def set_points(self, points, point_cell_start, point_cells):
+        """The mesh's points and the cells of each point (s4g_point_cells)
+        for point_displacement_device."""
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        pcs = np.ascontiguousarray(point_cell_start, dtype=np.int32)
+        pcc = np.ascontiguousarray(point_cells, dtype=np.int32)
+        _lib.check(self.L.s4g_mesh_set_points(self.h, int(pts.shape[0]), pts.ctypes.data,
+                                              pcs.ctypes.data, pcc.ctypes.data),
+                   "s4g_mesh_set_points")
+        self.n_points = int(pts.shape[0])
+
+    def point_displacement_device(self):
+        """pointD of the last solve, interpolated on the device (s4g_get_pointD)."""
+        out = np.zeros((self.n_points, 3))
+        _lib.check(self.L.s4g_get_pointD(self.h, out.ctypes.data), "s4g_get_pointD")
+        return out
+
     def permutation(self):
         perm = np.zeros(self.n_cells, np.int32)
         _lib.check(self.L.s4g_mesh_get_permutation(self.h, perm.ctypes.data),

@@ -92,8 +92,12 @@ def test_solve_batch_equals_single_solves_and_the_oracle():
     k = min(range(len(cases)), key=lambda i: cases[i]["mesh"]["V"].shape[0])
     c = cases[k]
     Do, so, _, po = pyoracle.solve(c["mesh"], oracle_bcs(c["mesh"], c["bcs"]), dic_domain=c["parts"],
-                                   E=c["law"]["E"], nu=c["law"]["nu"], n_correctors=4000,
-                                   field_relaxation=c["outer"]["fieldRelaxation"], n_threads=8)
+                                   E=c["law"]["E"], nu=c["law"]["nu"],
+                                   n_correctors=c["outer"]["nCorrectors"],
+                                   field_relaxation=c["outer"].get("fieldRelaxation", 1.0),
+                                   solution_tol=c["outer"].get("solutionTolerance", 1e-6),
+                                   alternative_tol=c["outer"].get("alternativeTolerance", 1e-7),
+                                   n_threads=8)
     assert po["converged"] == 1
     D, sig, _ = res[k]
     assert np.linalg.norm(D - Do) / np.linalg.norm(Do) < 1e-6

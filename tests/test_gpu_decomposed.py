@@ -81,7 +81,7 @@ def test_decomposed_ragged_parts(ctx):
 def test_autotuned_variants_are_bit_identical(ctx, precision):
     """The autotuner only picks among kernel variants whose sums run in the
     same order: the tuned and the untuned run give identical bits, whatever
-    preconditioner block size (128 or 256 threads per part) and SpMV form
+    preconditioner variant (rows per thread in flight) and SpMV form
     each picks."""
     m = sg.box_mesh(14, 12, 10, 1.0, 0.9, 0.7, 0.2, 21)
     bcs = {"zmin": ("fixedDisplacement", None, None),
@@ -92,7 +92,7 @@ def test_autotuned_variants_are_bit_identical(ctx, precision):
         model = sg.SolidModel(ctx, m, law, bcs, outer=dict(nCorrectors=2000), precision=precision,
                               part_size=128, dic_subdomains=True, autotune=tune)
         D, sig, perf = model.evolve()
-        assert perf["part_threads"] in (128, 256) and perf["spmv_unroll"] in (0, 1, 6)
+        assert perf["part_threads"] == 128 and perf["spmv_unroll"] in (0, 1, 6)
         out.append((D, sig, perf["total_lin_iters"], perf["n_correctors"]))
         model.close()
     assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
