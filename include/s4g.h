@@ -620,6 +620,15 @@ s4g_status s4g_foam_read_controls(const char* case_dir, s4g_model* model, s4g_la
  * built on the device path, so a caller refuses a case that sets it below 1. */
 s4g_status s4g_foam_read_relaxation(const char* fv_solution, const char* field,
                                     double* field_factor, double* equation_factor);
+/* The leastSquares boundary delta of a system/fvSchemes for the gradient of
+ * one field ("D" or "DD"): gradSchemes grad(<field>) (else default)
+ * leastSquares gives 0 (OpenFOAM's patch-normal delta), extendedLeastSquares
+ * <minDet> gives 1 (the full face-centre delta, as the reference's
+ * cooksMembrane tutorial selects, tutorials/solids/linearElasticity/
+ * cooksMembrane/system/fvSchemes) -- the value of
+ * s4g_mesh_opts.ls_boundary_delta.  Other schemes are S4G_BAD_ARG. */
+s4g_status s4g_foam_read_grad_scheme(const char* fv_schemes, const char* field,
+                                     int* ls_boundary_delta);
 /* s4g_bc_set and s4g_bc_set_relaxation on every patch of an uploaded mesh
  * (uploaded from this case's s4g_mesh_desc). */
 s4g_status s4g_foam_apply_bcs(const s4g_foam_case* fc, s4g_mesh* mesh);

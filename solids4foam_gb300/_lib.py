@@ -191,6 +191,7 @@ _SIGS = {
     "s4g_foam_read_time": (ct.c_int, [ct.c_char_p] + [ct.POINTER(ct.c_double)] * 3),
     "s4g_foam_read_relaxation": (ct.c_int, [ct.c_char_p, ct.c_char_p, ct.POINTER(ct.c_double),
                                             ct.POINTER(ct.c_double)]),
+    "s4g_foam_read_grad_scheme": (ct.c_int, [ct.c_char_p, ct.c_char_p, ct.POINTER(ct.c_int)]),
     "s4g_foam_read_controls": (ct.c_int, [ct.c_char_p, ct.POINTER(ct.c_int), ct.POINTER(Law),
                                           ct.POINTER(LinSolver), ct.POINTER(Outer)]),
     "s4g_foam_free": (None, [ct.c_void_p]),

@@ -23,6 +23,7 @@
 
 #include <algorithm>
 #include <cerrno>
+#include <cctype>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -119,9 +120,24 @@ std::vector<Tok> tokenize(const std::string& t, const std::string& where) {
       continue;
     }
     size_t b = i;
-    while (i < n && !isPunct(t[i]) && t[i] != '"' && !(t[i] == ' ' || t[i] == '\t' || t[i] == '\n' ||
-                                                          t[i] == '\r' || t[i] == '\f' || t[i] == '\v'))
-      ++i;
+    // a word that starts with a letter may hold balanced parentheses, as
+    // OpenFOAM's words do (grad(D), div((impK*grad(D))), laplacian(DD,D))
+    const bool named = std::isalpha((unsigned char)c) || c == '_';
+    for (;;) {
+      while (i < n && !isPunct(t[i]) && t[i] != '"' && !(t[i] == ' ' || t[i] == '\t' || t[i] == '\n' ||
+                                                            t[i] == '\r' || t[i] == '\f' || t[i] == '\v'))
+        ++i;
+      if (!(named && i < n && t[i] == '(')) break;
+      int depth = 0;
+      size_t j = i;
+      for (; j < n; ++j) {
+        if (t[j] == '(') ++depth;
+        else if (t[j] == ')' && --depth == 0) break;
+        else if (t[j] == ';' || t[j] == '{' || t[j] == '}' || t[j] == '\n') break;
+      }
+      if (j >= n || t[j] != ')') break;  // not a balanced group: the word ends here
+      i = j + 1;
+    }
     out.push_back({Tok::Word, t.substr(b, i - b)});
   }
   return out;
@@ -1050,6 +1066,31 @@ s4g_status s4g_foam_read_relaxation(const char* fv_solution, const char* field,
     }
     if (field_factor) *field_factor = ff;
     if (equation_factor) *equation_factor = ef;
+  });
+}
+
+s4g_status s4g_foam_read_grad_scheme(const char* fv_schemes, const char* field,
+                                     int* ls_boundary_delta) {
+  if (!fv_schemes || !field || !ls_boundary_delta) return S4G_BAD_ARG;
+  return guarded([&] {
+    std::vector<Tok> t = payload(fv_schemes);
+    Cursor c{t, 0, fv_schemes};
+    std::vector<Entry> d = parseDict(c, false);
+    const std::string w = std::string(fv_schemes) + ": gradSchemes";
+    const Entry* gs = find(d, "gradSchemes");
+    if (!gs || !gs->isDict) fail(w + " missing");
+    const std::string key = std::string("grad(") + field + ")";
+    const Entry* e = lookup(gs->sub, key);
+    if (!e || (e->val.size() == 1 && e->val[0].s == "none")) e = find(gs->sub, "default");
+    if (!e || e->isDict || e->val.empty() || e->val[0].s == "none") fail(w + ": no scheme for " + key);
+    const std::string name = e->val[0].s;
+    // leastSquares: OpenFOAM's patch delta, normal to the patch;
+    // extendedLeastSquares: the full face-centre delta on the boundary
+    // (with minDet the scheme's threshold for adding neighbours, which the
+    // hexahedral and prismatic meshes here never reach)
+    if (name == "leastSquares" && e->val.size() == 1) *ls_boundary_delta = 0;
+    else if (name == "extendedLeastSquares" && e->val.size() == 2) *ls_boundary_delta = 1;
+    else fail(w + ": " + key + " " + name + " is not built (leastSquares and extendedLeastSquares are)");
   });
 }
 

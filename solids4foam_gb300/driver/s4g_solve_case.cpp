@@ -85,6 +85,7 @@ int main(int argc, char** argv) {
   s4g_precision precision = S4G_FP64;
   int increments = 1, device = 0;
   bool planOnly = false, muKGiven = false, eNuGiven = false, incrementsGiven = false;
+  bool lsDeltaGiven = false;
   for (int i = 2; i < argc; ++i) {
     const std::string a = argv[i];
     auto val = [&]() -> const char* {
@@ -128,7 +129,7 @@ int main(int argc, char** argv) {
     }
     else if (a == "--part-size") mo.part_size = std::atoi(val());
     else if (a == "--dic-subdomains") mo.dic_subdomains = 1;
-    else if (a == "--ls-full-delta") mo.ls_boundary_delta = 1;
+    else if (a == "--ls-full-delta") { mo.ls_boundary_delta = 1; lsDeltaGiven = true; }
     else if (a == "--device") device = std::atoi(val());
     else if (a == "--plan-only") planOnly = true;
     else if (a == "--write") writeTime = val();
@@ -159,6 +160,12 @@ int main(int argc, char** argv) {
   int nPoints = 0;
   check(s4g_foam_mesh_desc(fc, &desc, &nPoints), "s4g_foam_mesh_desc");
   mo.empty_direction = s4g_foam_empty_direction(fc);  // 2-D: the empty patches' direction
+  // the leastSquares boundary delta of the case's gradSchemes (unless given)
+  const std::string fvSchemes = caseDir + "/system/fvSchemes";
+  if (!lsDeltaGiven && access(fvSchemes.c_str(), R_OK) == 0)
+    check(s4g_foam_read_grad_scheme(fvSchemes.c_str(), model == S4G_NONLIN_GEOM_TOTAL_LAG ? "DD" : "D",
+                                    &mo.ls_boundary_delta),
+          "reading system/fvSchemes");
   s4g_mesh_info info;
   check(s4g_mesh_plan(&desc, &mo, nullptr, &info), "s4g_mesh_plan");
   // the boundary conditions (optional for --plan-only) and their load ramp
@@ -222,13 +229,14 @@ int main(int argc, char** argv) {
                 "\"levels\": %d, \"load_ramp_end\": %g, \"increments\": %d, \"model\": \"%s\", "
                 "\"law\": \"%s\", \"E\": %g, \"nu\": %g, \"mu\": %g, \"K\": %g, \"use_mu_K\": %d, "
                 "\"nCorrectors\": %d, \"tolerance\": %g, \"relTol\": %g, \"scaleFactor\": %g, "
-                "\"empty_direction\": %d, \"fieldRelaxation\": %g}\n",
+                "\"empty_direction\": %d, \"fieldRelaxation\": %g, \"ls_boundary_delta\": %d}\n",
                 caseDir.c_str(), desc.n_cells, desc.n_faces, desc.n_internal_faces, nPoints,
                 desc.n_patches, info.n_parts, info.part_depth, info.n_levels_global, rampEnd,
                 model == S4G_LIN_GEOM_TOTAL_DISP ? 1 : increments, modelName.c_str(),
                 law.type == S4G_LINEAR_ELASTIC ? "linearElastic" : "neoHookeanElastic", law.E,
                 law.nu, law.mu, law.K, law.use_mu_K, outer.n_correctors, lin.tolerance,
-                lin.rel_tol, outer.stab_scale, mo.empty_direction, outer.field_relaxation);
+                lin.rel_tol, outer.stab_scale, mo.empty_direction, outer.field_relaxation,
+                mo.ls_boundary_delta);
     s4g_foam_free(fc);
     return 0;
   }

@@ -313,7 +313,8 @@ def read_time(case_dir: str):
 
 def load_case(case_dir: str):
     """Everything a solve of a meshed case needs, resolved as the C++ driver
-    resolves it: dict(mesh, bcs, model, law, solver, outer, n_increments).
+    resolves it: dict(mesh, bcs, model, law, solver, outer, n_increments,
+    ls_boundary_delta).
     The model, law and controls come from the case's dictionaries; a total
     Lagrangian case whose loads ramp from zero runs one increment per
     controlDict time step.  Raises for what is not built: equation
@@ -344,4 +345,13 @@ def load_case(case_dir: str):
                                  f"{t1:g}: only a run from 0 to the series' end is built")
             if tl:
                 n_inc = max(1, int(round((t1 - t0) / dt)))
-    return dict(mesh=mesh, bcs=bcs, n_increments=n_inc, **c)
+    # the leastSquares boundary delta the case's gradSchemes select
+    lsd = 0
+    fvs = os.path.join(case_dir, "system", "fvSchemes")
+    if os.path.exists(fvs):
+        field = "DD" if c["model"] == "nonLinearGeometryTotalLagrangian" else "D"
+        v = ct.c_int()
+        _lib.check(_lib.lib().s4g_foam_read_grad_scheme(fvs.encode(), field.encode(), ct.byref(v)),
+                   "s4g_foam_read_grad_scheme")
+        lsd = v.value
+    return dict(mesh=mesh, bcs=bcs, n_increments=n_inc, ls_boundary_delta=lsd, **c)

@@ -178,6 +178,7 @@ class SolidModel:
         from .foam_case import load_case
         c = load_case(case_dir)
         kw.setdefault("empty_direction", c["mesh"].get("empty_direction", 0))
+        kw.setdefault("ls_boundary_delta", c["ls_boundary_delta"])
         model = cls(ctx, c["mesh"], c["law"], c["bcs"], model=c["model"], solver=c["solver"],
                     outer=c["outer"], **kw)
         return model, c["n_increments"]

@@ -105,4 +105,8 @@ mechanical ( steel { type linearElastic; rho rho [1 -3 0 0 0 0 0] 1;
 solvers { D { solver PCG; preconditioner FDIC; tolerance 1e-09; relTol 0.1; maxIter 200; } }
 relaxationFactors { equations { } fields { } }
 """)
+    # the tutorial's gradient scheme (its system/fvSchemes, gradSchemes)
+    (case / "system" / "fvSchemes").write_text(head + """
+gradSchemes { default none; grad(D) extendedLeastSquares 0; }
+""")
     return str(case)

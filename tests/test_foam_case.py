@@ -443,5 +443,32 @@ def test_two_d_case(tmp_path):
     out = json.loads(subprocess.run([b.build_driver(), case, "--plan-only"], capture_output=True,
                                     text=True, check=True).stdout)
     assert out["empty_direction"] == 3 and out["cells"] == 400
+    # the tutorial's extendedLeastSquares selects the full boundary delta
+    assert c["ls_boundary_delta"] == 1 and out["ls_boundary_delta"] == 1
     with pytest.raises(_lib.S4GError, match="not normal to x, y or z"):
         read_case(cooks_membrane_case(tmp_path / "tilted", 4, rotate_deg=30.0))
+
+
+def test_grad_scheme(tmp_path):
+    """gradSchemes: leastSquares gives the patch-normal boundary delta (0),
+    extendedLeastSquares the full face-centre delta (1); grad(D) before
+    default; other schemes are refused by name."""
+    import ctypes as ct
+    head = "FoamFile { version 2.0; format ascii; class dictionary; object fvSchemes; }\n"
+    f = tmp_path / "fvSchemes"
+    L = _lib.lib()
+
+    def read(text, field="D"):
+        f.write_text(head + text)
+        v = ct.c_int(-1)
+        _lib.check(L.s4g_foam_read_grad_scheme(str(f).encode(), field.encode(), ct.byref(v)),
+                   "s4g_foam_read_grad_scheme")
+        return v.value
+    assert read("gradSchemes { default leastSquares; }") == 0
+    assert read("gradSchemes { default none; grad(D) extendedLeastSquares 0; }") == 1
+    assert read("gradSchemes { default extendedLeastSquares 0; grad(D) leastSquares; }") == 0
+    assert read("gradSchemes { default leastSquares; grad(D) extendedLeastSquares 0; }", "DD") == 0
+    with pytest.raises(_lib.S4GError, match="Gauss is not built"):
+        read("gradSchemes { default Gauss linear; }")
+    with pytest.raises(_lib.S4GError, match="no scheme"):
+        read("gradSchemes { default none; }")
