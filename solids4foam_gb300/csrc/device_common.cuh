@@ -44,6 +44,7 @@ struct MeshView {
   const int* locMetaStart; const uint32_t* locMeta;
   const int4* locDesc;   // [nParts][2] part descriptors
   int maxLocEntries, maxLocMeta;
+  int locSlots;          // 1: fixed-slot in-part tables (see HostPrep::locSlots)
   // batched load cases: a launch's blockIdx.y is the case; per-case data
   // lies caseRec doubles (reduction records) or one field size apart
   long caseRec;

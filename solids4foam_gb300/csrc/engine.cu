@@ -384,6 +384,7 @@ struct Engine {
       S4G_TRY(upload(&dDesc, hp.locDesc));
       mv.locDesc = reinterpret_cast<const int4*>(dDesc);
       mv.maxLocEntries = hp.maxLocEntries; mv.maxLocMeta = hp.maxLocMeta;
+      mv.locSlots = hp.locSlots ? 1 : 0;
       if (localSmemBytes<double>(mv) + 2048 > (size_t)maxSmem)
         return setErr(S4G_BAD_ARG, "a DIC part does not fit in shared memory; use a smaller part_size");
       int per[kLocNumNT];

@@ -60,8 +60,9 @@ __device__ __forceinline__ LocSmem<T> locSmem(const MeshView& mv, unsigned char*
   s.c = (T*)raw;                              // EL coefficients (EL % 8 == 0)
   s.m = (uint32_t*)(s.c + EL);                // ML row metadata (ML % 4 == 0)
   s.idx = (uint16_t*)(s.m + ML);              // EL local columns
-  s.w = (T*)(s.idx + EL);                     // 3P: the substitutions' vector
-  s.r = s.w + 3 * P;                          // 3P: the updated residual
+  s.w = (T*)(s.idx + EL);                     // 3P + 3: the substitutions' vector
+                                              // and the zero row P of the slots
+  s.r = s.w + 3 * P + 3;                      // 3P: the updated residual
   s.lv = (int*)(s.r + 3 * P);                 // maxLevels + 1
   return s;
 }
@@ -112,35 +113,136 @@ __device__ __forceinline__ void locApply(const LocSmem<T>& sm, const LocRow<T>& 
   sm.w[3 * i] = v0; sm.w[3 * i + 1] = v1; sm.w[3 * i + 2] = v2;
 }
 
-// One substitution (DIR 0 forward, 1 backward) over the part's levels, by
-// one warp: the rows of a level in parallel (two per lane, more for a level
-// wider than 64 rows), a warp barrier between levels, and the next level's
-// static data in registers while the current level runs.  A level's rows
-// are few (at most 48 in an 8^3-cell part), so one warp walks them with
-// cheap __syncwarp barriers while the rest of the CTA waits.
-template <int DIR, typename T>
+// Warps that walk a part's levels (the rest of the CTA waits at a barrier).
+constexpr int kLocWalkWarps = 2;
+
+// Barrier of the walking warps: a warp barrier for one warp, a named CTA
+// barrier (id 1) over the walking warps for more.
+template <int W>
+__device__ __forceinline__ void walkBarrier() {
+  if (W == 1) __syncwarp();
+  else asm volatile("bar.sync 1, %0;" ::"r"(32 * W) : "memory");
+}
+
+// One substitution (DIR 0 forward, 1 backward) over the part's levels, by W
+// warps: the rows of a level in parallel (two per thread, more for a level
+// wider than 64 W rows), a barrier of the walking warps between levels,
+// and the next level's static data in registers while the current level
+// runs.  A level's rows are few (at most 48 in an 8^3-cell part), so a
+// couple of warps walk them while the rest of the CTA waits.
+template <int DIR, int W, typename T>
 __device__ __forceinline__ void locSweep(const LocSmem<T>& sm, int nL) {
   if (nL <= 0) return;
+  constexpr int NW = 32 * W;
   const int lane = (int)threadIdx.x;
   LocRow<T> n0, n1;
   locPre<DIR>(sm, DIR == 0 ? 0 : nL - 1, lane, n0);
-  locPre<DIR>(sm, DIR == 0 ? 0 : nL - 1, lane + 32, n1);
+  locPre<DIR>(sm, DIR == 0 ? 0 : nL - 1, lane + NW, n1);
   for (int s = 0; s < nL; ++s) {
     const int l = DIR == 0 ? s : nL - 1 - s;
     const LocRow<T> c0 = n0, c1 = n1;
     if (s + 1 < nL) {
       locPre<DIR>(sm, DIR == 0 ? l + 1 : l - 1, lane, n0);
-      locPre<DIR>(sm, DIR == 0 ? l + 1 : l - 1, lane + 32, n1);
+      locPre<DIR>(sm, DIR == 0 ? l + 1 : l - 1, lane + NW, n1);
     }
     if (c0.i >= 0) locApply(sm, c0);
     if (c1.i >= 0) locApply(sm, c1);
-    // rows beyond the first 64 of a wide level
-    for (int off = lane + 64; sm.lv[l] + off < sm.lv[l + 1]; off += 32) {
+    // rows beyond the first 2 NW of a wide level
+    for (int off = lane + 2 * NW; sm.lv[l] + off < sm.lv[l + 1]; off += NW) {
       LocRow<T> row;
       locPre<DIR>(sm, l, off, row);
       locApply(sm, row);
     }
-    __syncwarp();
+    walkBarrier<W>();
+  }
+}
+
+// Fixed-slot tables (HostPrep::locSlots): row r's lower entries sit at
+// 6 r .. 6 r + 2 and its upper ones at 6 r + 3 .. 6 r + 5, padded with a zero
+// coefficient on the zero row, so a row's whole static data is two short
+// loads away from its index.
+template <typename T>
+struct SlotRow {
+  int i;
+  int q[3];
+  T a[3];
+};
+
+template <int DIR, typename T>
+__device__ __forceinline__ void slotPre(const LocSmem<T>& sm, int lo, int hi, int off,
+                                        SlotRow<T>& row) {
+  row.i = lo + off;
+  if (row.i >= hi) { row.i = -1; return; }
+  const int b = 6 * row.i + (DIR == 0 ? 0 : 3);
+#pragma unroll
+  for (int u = 0; u < 3; ++u) { row.q[u] = sm.idx[b + u]; row.a[u] = sm.c[b + u]; }
+}
+
+// v -= a_u w_q(u) for the three slots in order (a padded slot subtracts an
+// exact zero); OUT (the backward substitution, which leaves w final): w also
+// goes to global memory and into the thread's w.r and sum|r| sums.
+template <bool OUT, typename T>
+__device__ __forceinline__ void slotApply(const LocSmem<T>& sm, const SlotRow<T>& row,
+                                          T* __restrict__ wg, Acc<T> (&wr)[3], Acc<T> (&ar)[3]) {
+  const int i = row.i;
+  T v[3] = {sm.w[3 * i], sm.w[3 * i + 1], sm.w[3 * i + 2]};
+  T x[3][3];
+#pragma unroll
+  for (int u = 0; u < 3; ++u)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) x[u][k] = sm.w[3 * row.q[u] + k];
+#pragma unroll
+  for (int u = 0; u < 3; ++u)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) v[k] -= row.a[u] * x[u][k];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) sm.w[3 * i + k] = v[k];
+  if (OUT) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      wg[3 * i + k] = v[k];
+      const T r = sm.r[3 * i + k];
+      wr[k].add(v[k] * r);
+      ar[k].add(fabs(r));
+    }
+  }
+}
+
+// One substitution over the part's levels by W warps with the slot tables:
+// the level bounds two levels ahead and the next level's slots are in
+// registers before the current level's neighbour loads, so each level costs
+// one round of shared-memory loads, the multiply-adds and a barrier.
+template <int DIR, int W, bool OUT, typename T>
+__device__ __forceinline__ void slotSweep(const LocSmem<T>& sm, int nL, T* __restrict__ wg,
+                                          Acc<T> (&wr)[3], Acc<T> (&ar)[3]) {
+  if (nL <= 0) return;
+  constexpr int NW = 32 * W;
+  const int t = (int)threadIdx.x;
+  auto lvl = [&](int q) { return DIR == 0 ? q : nL - 1 - q; };
+  int lo = sm.lv[lvl(0)], hi = sm.lv[lvl(0) + 1];
+  int lo1 = 0, hi1 = 0;
+  if (nL > 1) { lo1 = sm.lv[lvl(1)]; hi1 = sm.lv[lvl(1) + 1]; }
+  SlotRow<T> n0, n1;
+  slotPre<DIR>(sm, lo, hi, t, n0);
+  slotPre<DIR>(sm, lo, hi, t + NW, n1);
+  for (int q = 0; q < nL; ++q) {
+    const SlotRow<T> c0 = n0, c1 = n1;
+    const int clo = lo, chi = hi;
+    lo = lo1; hi = hi1;
+    if (q + 2 < nL) { lo1 = sm.lv[lvl(q + 2)]; hi1 = sm.lv[lvl(q + 2) + 1]; }
+    if (q + 1 < nL) {
+      slotPre<DIR>(sm, lo, hi, t, n0);
+      slotPre<DIR>(sm, lo, hi, t + NW, n1);
+    }
+    if (c0.i >= 0) slotApply<OUT>(sm, c0, wg, wr, ar);
+    if (c1.i >= 0) slotApply<OUT>(sm, c1, wg, wr, ar);
+    // rows beyond the first 2 NW of a wide level
+    for (int off = t + 2 * NW; clo + off < chi; off += NW) {
+      SlotRow<T> row;
+      slotPre<DIR>(sm, clo, chi, off, row);
+      slotApply<OUT>(sm, row, wg, wr, ar);
+    }
+    walkBarrier<W>();
   }
 }
 
@@ -168,7 +270,7 @@ constexpr int locMinBlocks() {
 // and RPT (64 lanes over the rows, lane l summing rows l, l+64, ..., then a
 // fixed tree), one record per part; the last CTA sums the records in part
 // order.  Every variant therefore gives bit-identical results.
-template <typename T, int NT, int RPT>
+template <typename T, int NT, int RPT, bool SLOT>
 __global__ void __launch_bounds__(NT, (locMinBlocks<T, NT, RPT>()))
 kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partials) {
   p = casePcg(p, blockIdx.y, mv.nC);
@@ -190,17 +292,26 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
   for (int k = 0; k < 3; ++k) { pend[k] = st->pending[k] != 0; al[k] = (T)st->alpha[k]; }
   const bool anyPend = pend[0] || pend[1] || pend[2];
   // Parts come from a ticket counter: CTAs that finish early take more (no
-  // tail of CTAs with one part more than the others); the next ticket is
-  // taken while the current part runs.
+  // tail of CTAs with one part more than the others); the next ticket and
+  // its part's descriptor are fetched while the current part runs.
   __shared__ int sTicket;
-  if (threadIdx.x == 0) sTicket = (int)atomicAdd(&st->locTicket, 1u);
+  __shared__ int4 sDesc[2];
+  if (threadIdx.x == 0) {
+    const int t0 = (int)atomicAdd(&st->locTicket, 1u);
+    sTicket = t0;
+    if (t0 < mv.nParts) { sDesc[0] = mv.locDesc[2 * t0]; sDesc[1] = mv.locDesc[2 * t0 + 1]; }
+  }
   __syncthreads();
   for (int part = sTicket; part < mv.nParts;) {
-    const int4 dA = mv.locDesc[2 * part], dB = mv.locDesc[2 * part + 1];
+    const int4 dA = sDesc[0], dB = sDesc[1];
     const int pLo = dA.x, nR = dA.y, eLo = dA.z, nE = dA.w;
     const int mLo = dB.x, nM = dB.y, l0 = dB.z, nL = dB.w;
     int nextTicket = 0;
-    if (threadIdx.x == 0) nextTicket = (int)atomicAdd(&st->locTicket, 1u);
+    int4 nA = dA, nB = dB;
+    if (threadIdx.x == 0) {
+      nextTicket = (int)atomicAdd(&st->locTicket, 1u);
+      if (nextTicket < mv.nParts) { nA = mv.locDesc[2 * nextTicket]; nB = mv.locDesc[2 * nextTicket + 1]; }
+    }
     // static part tables in flight while the vectors stream
     {
       const int nc = nE * (int)sizeof(T) / 16;
@@ -214,6 +325,7 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
       for (int k = threadIdx.x; k < nm; k += NT) cpAsync16((char*)sm.m + 16 * k, gm + 16 * k);
     }
     for (int k = threadIdx.x; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
+    if (SLOT && threadIdx.x < 3) sm.w[3 * mv.maxRows + threadIdx.x] = T(0);  // the zero row
     // pending update: RPT rows per thread with every load issued before
     // any store; r and w = rD r into shared memory
     for (int i0 = threadIdx.x; i0 < nR; i0 += RPT * NT) {
@@ -253,33 +365,47 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
     __syncthreads();
     // forward substitution: w_u -= sum_{l<u in part} (rD_u a_ul) w_l, then
     // backward substitution: w_l -= sum_{u>l in part} (rD_l a_lu) w_u
-    if (threadIdx.x < 32) {
-      locSweep<0>(sm, nL);
-      locSweep<1>(sm, nL);
-    }
-    __syncthreads();
-    // w out
     T* __restrict__ wg = p.w + 3 * (size_t)pLo;
-    for (int k = threadIdx.x; k < 3 * nR; k += NT) wg[k] = sm.w[k];
-    // the part's w.r and sum|r|: 64 lanes over the rows, then a fixed tree
     double d6[6] = {0, 0, 0, 0, 0, 0};
-    if (threadIdx.x < 64) {
-      Acc<T> wr[3], ar[3];
-      for (int i = threadIdx.x; i < nR; i += 64)
+    if constexpr (SLOT) {
+      // the backward substitution also writes w out and sums w.r and |r|
+      // over each walking thread's rows, in a fixed order; then a fixed tree
+      if (threadIdx.x < 32 * kLocWalkWarps) {
+        Acc<T> wr[3], ar[3];
+        slotSweep<0, kLocWalkWarps, false>(sm, nL, wg, wr, ar);
+        slotSweep<1, kLocWalkWarps, true>(sm, nL, wg, wr, ar);
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          const T r = sm.r[3 * i + k];
-          wr[k].add(sm.w[3 * i + k] * r);
-          ar[k].add(fabs(r));
-        }
+        for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
+      }
+    } else {
+      if (threadIdx.x < 32 * kLocWalkWarps) {
+        locSweep<0, kLocWalkWarps>(sm, nL);
+        locSweep<1, kLocWalkWarps>(sm, nL);
+      }
+      __syncthreads();
+      // w out
+      for (int k = threadIdx.x; k < 3 * nR; k += NT) wg[k] = sm.w[k];
+      // the part's w.r and sum|r|: 64 lanes over the rows, then a fixed tree
+      if (threadIdx.x < 64) {
+        Acc<T> wr[3], ar[3];
+        for (int i = threadIdx.x; i < nR; i += 64)
 #pragma unroll
-      for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
+          for (int k = 0; k < 3; ++k) {
+            const T r = sm.r[3 * i + k];
+            wr[k].add(sm.w[3 * i + k] * r);
+            ar[k].add(fabs(r));
+          }
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
+      }
     }
     sum64<6>(d6, red);  // ends with a barrier: the next part may reuse the shared memory
     if (threadIdx.x == 0) {
       double* q = partials + 8 * (size_t)part;
       for (int k = 0; k < 6; ++k) q[k] = d6[k];
       sTicket = nextTicket;
+      sDesc[0] = nA;
+      sDesc[1] = nB;
     }
     __syncthreads();
     part = sTicket;
@@ -500,21 +626,32 @@ kLocSpmvSplit(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
 template <typename T, int NT, int RPT>
 void launchPrecondV(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                     double* partials, int grid, cudaStream_t s, int nCases) {
-  kLocPrecond<T, NT, RPT><<<dim3(grid, nCases), NT, localSmemBytes<T>(mv), s>>>(mv, c, p, st,
-                                                                               partials);
+  if (mv.locSlots)
+    kLocPrecond<T, NT, RPT, true><<<dim3(grid, nCases), NT, localSmemBytes<T>(mv), s>>>(
+        mv, c, p, st, partials);
+  else
+    kLocPrecond<T, NT, RPT, false><<<dim3(grid, nCases), NT, localSmemBytes<T>(mv), s>>>(
+        mv, c, p, st, partials);
+}
+
+template <typename T, int NT, int RPT, bool SLOT>
+cudaError_t prepareK(const MeshView& mv, int* blocksPerSM) {
+  const int sm = (int)localSmemBytes<T>(mv);
+  cudaError_t e = setMaxDynamicSmem(kLocPrecond<T, NT, RPT, SLOT>);
+  if (e != cudaSuccess) return e;
+  // as much of the SM's memory as shared memory as possible: parts per SM
+  // are bounded by their staged tables
+  e = cudaFuncSetAttribute(kLocPrecond<T, NT, RPT, SLOT>,
+                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, NT, RPT, SLOT>,
+                                                       NT, sm);
 }
 
 template <typename T, int NT, int RPT>
 cudaError_t prepareV(const MeshView& mv, int* blocksPerSM) {
-  const int sm = (int)localSmemBytes<T>(mv);
-  cudaError_t e = setMaxDynamicSmem(kLocPrecond<T, NT, RPT>);
-  if (e != cudaSuccess) return e;
-  // as much of the SM's memory as shared memory as possible: parts per SM
-  // are bounded by their staged tables
-  e = cudaFuncSetAttribute(kLocPrecond<T, NT, RPT>,
-                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, NT, RPT>, NT, sm);
+  return mv.locSlots ? prepareK<T, NT, RPT, true>(mv, blocksPerSM)
+                     : prepareK<T, NT, RPT, false>(mv, blocksPerSM);
 }
 
 }  // namespace
@@ -529,7 +666,7 @@ const int kLocVariantsU[kLocNumU] = {1, 6, 0};
 template <typename T>
 size_t localSmemBytes(const MeshView& mv) {
   const size_t P = mv.maxRows, EL = mv.maxLocEntries, ML = mv.maxLocMeta;
-  const size_t tables = sizeof(T) * (EL + 6 * P) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
+  const size_t tables = sizeof(T) * (EL + 6 * P + 3) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
   return std::max(tables, (size_t)256 * 6 * sizeof(double));  // final reduction scratch
 }
 

@@ -532,6 +532,48 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
       hp.maxLocEntries = std::max(hp.maxLocEntries, hp.locEntStart[p + 1] - hp.locEntStart[p]);
       hp.maxLocMeta = std::max(hp.maxLocMeta, hp.locMetaStart[p + 1] - hp.locMetaStart[p]);
     }
+    // Fixed slots: where every row has at most 3 lower and 3 upper in-part
+    // entries (hexahedral meshes in the orders built here), each row gets
+    // exactly 3 + 3 slots -- the same entries in the same order, padded with
+    // a zero coefficient on a zero row (local index maxRows) -- so that a
+    // level walk finds a row's entries at 6 r + (0 | 3) without metadata.
+    bool slots = true;
+    for (size_t k = 0; k < hp.locMeta.size() && slots; ++k)
+      if (((hp.locMeta[k] >> 16) & 0xff) > 3 || (hp.locMeta[k] >> 24) > 3) slots = false;
+    if (slots && hp.maxRows >= 65535) slots = false;
+    hp.locSlots = slots;
+    if (slots) {
+      std::vector<int> src, est(1, 0);
+      std::vector<uint16_t> idx;
+      hp.maxLocEntries = 0;
+      for (int p = 0; p < hp.nParts; ++p) {
+        const int lo = hp.partStart[p], hi = hp.partStart[p + 1];
+        const size_t e0 = src.size();
+        const int* gs = hp.locSrc.data() + hp.locEntStart[p];
+        const uint16_t* gi = hp.locIdx.data() + hp.locEntStart[p];
+        const uint32_t* gm = hp.locMeta.data() + hp.locMetaStart[p];
+        for (int r = 0; r < hi - lo; ++r) {
+          const int off = (int)(gm[r] & 0xffff), nl = (gm[r] >> 16) & 0xff, nu = gm[r] >> 24;
+          for (int u = 0; u < 3; ++u) {
+            src.push_back(u < nl ? gs[off + u] : -1);
+            idx.push_back(u < nl ? gi[off + u] : (uint16_t)hp.maxRows);
+          }
+          for (int u = 0; u < 3; ++u) {
+            src.push_back(u < nu ? gs[off + nl + u] : -1);
+            idx.push_back(u < nu ? gi[off + nl + u] : (uint16_t)hp.maxRows);
+          }
+        }
+        while ((src.size() - e0) % 8) { src.push_back(-1); idx.push_back((uint16_t)hp.maxRows); }
+        est.push_back((int)src.size());
+        hp.maxLocEntries = std::max(hp.maxLocEntries, est[p + 1] - est[p]);
+      }
+      hp.locSrc.swap(src);
+      hp.locIdx.swap(idx);
+      hp.locEntStart.swap(est);
+      hp.locMeta.clear();
+      hp.locMetaStart.assign(hp.nParts + 1, 0);
+      hp.maxLocMeta = 0;
+    }
     hp.locDesc.resize(8 * (size_t)hp.nParts);
     for (int p = 0; p < hp.nParts; ++p) {
       int* d8 = hp.locDesc.data() + 8 * (size_t)p;

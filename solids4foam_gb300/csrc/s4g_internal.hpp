@@ -59,6 +59,10 @@ struct HostPrep {
   // and {locMetaStart, metas, lvlOff, levels}
   std::vector<int> locDesc;  // [nParts][8]
   int maxLocEntries = 0, maxLocMeta = 0;
+  // fixed-slot tables (every row has 3 lower then 3 upper slots, padded
+  // with a zero coefficient on the zero row maxRows): locSrc/locIdx hold
+  // the slots, locMeta is empty
+  bool locSlots = false;
 };
 
 // Sets the calling thread's s4g_last_error message (the server reports a
