@@ -256,7 +256,7 @@ __global__ void kLocGather(int n, const int* src, const double* rDa, T* out) {
 // thread in flight at once in the streaming phase).
 template <typename T, int NT, int RPT>
 constexpr int locMinBlocks() {
-  return sizeof(T) == 4 ? (RPT >= 4 ? 4 : 5) : (RPT >= 2 ? 3 : 4);
+  return sizeof(T) == 4 ? 4 : (RPT >= 2 ? 3 : 4);
 }
 
 // The processor-local preconditioner of one PCG iteration: the pending
@@ -294,8 +294,8 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
   // Parts come from a ticket counter: CTAs that finish early take more (no
   // tail of CTAs with one part more than the others); the next ticket and
   // its part's descriptor are fetched while the current part runs.
-  __shared__ int sTicket;
-  __shared__ int4 sDesc[2];
+  __shared__ int sTicket, sNextTicket;
+  __shared__ int4 sDesc[2], sNextDesc[2];
   if (threadIdx.x == 0) {
     const int t0 = (int)atomicAdd(&st->locTicket, 1u);
     sTicket = t0;
@@ -306,11 +306,12 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
     const int4 dA = sDesc[0], dB = sDesc[1];
     const int pLo = dA.x, nR = dA.y, eLo = dA.z, nE = dA.w;
     const int mLo = dB.x, nM = dB.y, l0 = dB.z, nL = dB.w;
-    int nextTicket = 0;
-    int4 nA = dA, nB = dB;
+    // the next part's ticket and descriptor go straight to shared memory
+    // (nothing of them stays in registers across the part)
     if (threadIdx.x == 0) {
-      nextTicket = (int)atomicAdd(&st->locTicket, 1u);
-      if (nextTicket < mv.nParts) { nA = mv.locDesc[2 * nextTicket]; nB = mv.locDesc[2 * nextTicket + 1]; }
+      const int nt = (int)atomicAdd(&st->locTicket, 1u);
+      sNextTicket = nt;
+      if (nt < mv.nParts) { sNextDesc[0] = mv.locDesc[2 * nt]; sNextDesc[1] = mv.locDesc[2 * nt + 1]; }
     }
     // static part tables in flight while the vectors stream
     {
@@ -403,9 +404,9 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
     if (threadIdx.x == 0) {
       double* q = partials + 8 * (size_t)part;
       for (int k = 0; k < 6; ++k) q[k] = d6[k];
-      sTicket = nextTicket;
-      sDesc[0] = nA;
-      sDesc[1] = nB;
+      sTicket = sNextTicket;
+      sDesc[0] = sNextDesc[0];
+      sDesc[1] = sNextDesc[1];
     }
     __syncthreads();
     part = sTicket;
@@ -638,11 +639,6 @@ template <typename T, int NT, int RPT, bool SLOT>
 cudaError_t prepareK(const MeshView& mv, int* blocksPerSM) {
   const int sm = (int)localSmemBytes<T>(mv);
   cudaError_t e = setMaxDynamicSmem(kLocPrecond<T, NT, RPT, SLOT>);
-  if (e != cudaSuccess) return e;
-  // as much of the SM's memory as shared memory as possible: parts per SM
-  // are bounded by their staged tables
-  e = cudaFuncSetAttribute(kLocPrecond<T, NT, RPT, SLOT>,
-                           cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, NT, RPT, SLOT>,
                                                        NT, sm);
