@@ -48,6 +48,17 @@
 namespace s4g {
 namespace {
 
+// Bytes of one part's staged region (tables, w with its zero row, r, level
+// starts), or of the final reduction's scratch if that is larger; rounded
+// to 16 bytes so that regions can follow one another.
+template <typename T>
+__host__ __device__ inline size_t locRegionBytes(const MeshView& mv) {
+  const size_t P = mv.maxRows, EL = mv.maxLocEntries, ML = mv.maxLocMeta;
+  const size_t tables = sizeof(T) * (EL + 6 * P + 3) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
+  const size_t b = tables > (size_t)256 * 6 * sizeof(double) ? tables : (size_t)256 * 6 * sizeof(double);
+  return (b + 15) / 16 * 16;
+}
+
 template <typename T>
 struct LocSmem {
   T* c; uint32_t* m; uint16_t* idx; T* w; T* r; int* lv;
@@ -246,6 +257,133 @@ __device__ __forceinline__ void slotSweep(const LocSmem<T>& sm, int nL, T* __res
   }
 }
 
+// Two parts walked together by the same threads: per level, thread t takes
+// row t of part A's level and row t of part B's level (parts may have
+// different level counts), and both rows' loads are issued before either's
+// multiply-adds -- two independent latency chains per level instead of one.
+template <bool OUT, typename T>
+__device__ __forceinline__ void slotApplyAB(const LocSmem<T>& sa, const SlotRow<T>& ra,
+                                            T* __restrict__ wga, Acc<T> (&wra)[3], Acc<T> (&ara)[3],
+                                            const LocSmem<T>& sb, const SlotRow<T>& rb,
+                                            T* __restrict__ wgb, Acc<T> (&wrb)[3],
+                                            Acc<T> (&arb)[3]) {
+  const bool ha = ra.i >= 0, hb = rb.i >= 0;
+  T va[3], vb[3], xa[3][3], xb[3][3];
+  if (ha) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) va[k] = sa.w[3 * ra.i + k];
+#pragma unroll
+    for (int u = 0; u < 3; ++u)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) xa[u][k] = sa.w[3 * ra.q[u] + k];
+  }
+  if (hb) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) vb[k] = sb.w[3 * rb.i + k];
+#pragma unroll
+    for (int u = 0; u < 3; ++u)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) xb[u][k] = sb.w[3 * rb.q[u] + k];
+  }
+  if (ha) {
+#pragma unroll
+    for (int u = 0; u < 3; ++u)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) va[k] -= ra.a[u] * xa[u][k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) sa.w[3 * ra.i + k] = va[k];
+  }
+  if (hb) {
+#pragma unroll
+    for (int u = 0; u < 3; ++u)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) vb[k] -= rb.a[u] * xb[u][k];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) sb.w[3 * rb.i + k] = vb[k];
+  }
+  if (OUT) {
+    if (ha) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        wga[3 * ra.i + k] = va[k];
+        const T r = sa.r[3 * ra.i + k];
+        wra[k].add(va[k] * r);
+        ara[k].add(fabs(r));
+      }
+    }
+    if (hb) {
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        wgb[3 * rb.i + k] = vb[k];
+        const T r = sb.r[3 * rb.i + k];
+        wrb[k].add(vb[k] * r);
+        arb[k].add(fabs(r));
+      }
+    }
+  }
+}
+
+// The level bounds of one part during a pair walk, two levels ahead.
+struct LevelCursor {
+  int lo, hi, lo1, hi1;
+};
+
+template <int DIR, typename T>
+__device__ __forceinline__ void cursorInit(const LocSmem<T>& sm, int nL, LevelCursor& c) {
+  c.lo = c.hi = c.lo1 = c.hi1 = 0;
+  if (nL > 0) { const int l = DIR == 0 ? 0 : nL - 1; c.lo = sm.lv[l]; c.hi = sm.lv[l + 1]; }
+  if (nL > 1) { const int l = DIR == 0 ? 1 : nL - 2; c.lo1 = sm.lv[l]; c.hi1 = sm.lv[l + 1]; }
+}
+
+// Advance to level q + 1 (the bounds of q + 2 are loaded); empty past nL.
+template <int DIR, typename T>
+__device__ __forceinline__ void cursorStep(const LocSmem<T>& sm, int nL, int q, LevelCursor& c) {
+  c.lo = c.lo1; c.hi = c.hi1;
+  if (q + 2 < nL) {
+    const int l = DIR == 0 ? q + 2 : nL - 3 - q;
+    c.lo1 = sm.lv[l]; c.hi1 = sm.lv[l + 1];
+  } else {
+    c.lo1 = c.hi1 = 0;
+  }
+}
+
+template <int DIR, int W, bool OUT, typename T>
+__device__ __forceinline__ void slotSweepPair(const LocSmem<T>& sa, int nLa, T* __restrict__ wga,
+                                              Acc<T> (&wra)[3], Acc<T> (&ara)[3],
+                                              const LocSmem<T>& sb, int nLb, T* __restrict__ wgb,
+                                              Acc<T> (&wrb)[3], Acc<T> (&arb)[3]) {
+  constexpr int NW = 32 * W;
+  const int t = (int)threadIdx.x;
+  const int nL = nLa > nLb ? nLa : nLb;
+  LevelCursor ca, cb;
+  cursorInit<DIR>(sa, nLa, ca);
+  cursorInit<DIR>(sb, nLb, cb);
+  SlotRow<T> na, nb;
+  slotPre<DIR>(sa, ca.lo, ca.hi, t, na);
+  slotPre<DIR>(sb, cb.lo, cb.hi, t, nb);
+  for (int q = 0; q < nL; ++q) {
+    const SlotRow<T> cra = na, crb = nb;
+    const int aLo = ca.lo, aHi = ca.hi, bLo = cb.lo, bHi = cb.hi;
+    cursorStep<DIR>(sa, nLa, q, ca);
+    cursorStep<DIR>(sb, nLb, q, cb);
+    slotPre<DIR>(sa, ca.lo, ca.hi, t, na);
+    slotPre<DIR>(sb, cb.lo, cb.hi, t, nb);
+    slotApplyAB<OUT>(sa, cra, wga, wra, ara, sb, crb, wgb, wrb, arb);
+    // rows beyond the first NW of a wide level
+    for (int off = t + NW; aLo + off < aHi; off += NW) {
+      SlotRow<T> row;
+      slotPre<DIR>(sa, aLo, aHi, off, row);
+      slotApply<OUT>(sa, row, wga, wra, ara);
+    }
+    for (int off = t + NW; bLo + off < bHi; off += NW) {
+      SlotRow<T> row;
+      slotPre<DIR>(sb, bLo, bHi, off, row);
+      slotApply<OUT>(sb, row, wgb, wrb, arb);
+    }
+    walkBarrier<W>();
+  }
+}
+
 template <typename T>
 __global__ void kLocGather(int n, const int* src, const double* rDa, T* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -257,6 +395,105 @@ __global__ void kLocGather(int n, const int* src, const double* rDa, T* out) {
 template <typename T, int NT, int RPT>
 constexpr int locMinBlocks() {
   return sizeof(T) == 4 ? 4 : (RPT >= 2 ? 3 : 4);
+}
+
+// Staging of one part: its tables by 16-byte cp.async, its level starts,
+// the zero row (slot tables), and the pending update x += alpha p,
+// r -= alpha q with RPT rows per thread in flight (every load issued before
+// any store); r and w = rD r into shared memory.  The caller waits for the
+// cp.async group and synchronises.
+template <typename T, int NT, int RPT, bool SLOT>
+__device__ __forceinline__ void locStage(const MeshView& mv, const PcgPtrs<T>& p,
+                                         const LocSmem<T>& sm, const T* __restrict__ pg,
+                                         const bool (&pend)[3], const T (&al)[3], int4 dA,
+                                         int4 dB) {
+  const int pLo = dA.x, nR = dA.y, eLo = dA.z, nE = dA.w;
+  const int mLo = dB.x, nM = dB.y, l0 = dB.z, nL = dB.w;
+  const T* __restrict__ qg = p.q;
+  const T* __restrict__ rDg = p.rD;
+  T* __restrict__ xg = p.x;
+  T* __restrict__ rg = p.r;
+  // static part tables in flight while the vectors stream
+  {
+    const int nc = nE * (int)sizeof(T) / 16;
+    const char* g = (const char*)(p.lcoef + eLo);
+    for (int k = threadIdx.x; k < nc; k += NT) cpAsync16((char*)sm.c + 16 * k, g + 16 * k);
+    const int ni = nE * 2 / 16;
+    const char* gi = (const char*)(mv.locIdx + eLo);
+    for (int k = threadIdx.x; k < ni; k += NT) cpAsync16((char*)sm.idx + 16 * k, gi + 16 * k);
+    const int nm = nM * 4 / 16;
+    const char* gm = (const char*)(mv.locMeta + mLo);
+    for (int k = threadIdx.x; k < nm; k += NT) cpAsync16((char*)sm.m + 16 * k, gm + 16 * k);
+  }
+  for (int k = threadIdx.x; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
+  if (SLOT && threadIdx.x < 3) sm.w[3 * mv.maxRows + threadIdx.x] = T(0);  // the zero row
+  // pending update: RPT rows per thread with every load issued before
+  // any store; r and w = rD r into shared memory
+  for (int i0 = threadIdx.x; i0 < nR; i0 += RPT * NT) {
+    T rv[RPT][3], qv[RPT][3], pv[RPT][3], xv[RPT][3], rd[RPT];
+#pragma unroll
+    for (int h = 0; h < RPT; ++h) {
+      const int i = i0 + h * NT;
+      if (i < nR) {
+        const size_t g = 3 * (size_t)(pLo + i);
+        rd[h] = rDg[pLo + i];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          rv[h][k] = rg[g + k];
+          if (pend[k]) { qv[h][k] = qg[g + k]; pv[h][k] = pg[g + k]; xv[h][k] = xg[g + k]; }
+        }
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < RPT; ++h) {
+      const int i = i0 + h * NT;
+      if (i < nR) {
+        const size_t g = 3 * (size_t)(pLo + i);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          if (pend[k]) {
+            xg[g + k] = xv[h][k] + al[k] * pv[h][k];
+            rv[h][k] -= al[k] * qv[h][k];
+            rg[g + k] = rv[h][k];
+          }
+          sm.r[3 * i + k] = rv[h][k];
+          sm.w[3 * i + k] = rd[h] * rv[h][k];
+        }
+      }
+    }
+  }
+}
+
+// After every part: the last CTA sums the part records in part order and
+// decides, per component, the residual test of the pending iteration, beta
+// and wArA, and whether the loop goes on.
+__device__ __forceinline__ void locDecide(const MeshView& mv, const Controls& c, DevState* st,
+                                          double* partials, bool anyPend, unsigned char* smraw) {
+  if (!lastBlockDone(&st->counter[5], gridDim.x)) return;
+  double S[6];
+  reduceRecords<6>(partials, 8, mv.nParts, S, (double*)smraw);
+  if (threadIdx.x != 0) return;
+  st->counter[5] = 0;
+  st->locTicket = 0;
+  int any = 0;
+  for (int k = 0; k < 3; ++k) {
+    if (st->pending[k]) {
+      st->pending[k] = 0;
+      const double fr = S[3 + k] / st->normFactor[k];
+      st->finalRes[k] = fr;
+      st->nIter[k] += 1;
+      const bool conv = fr < c.tol || (c.relTol > 1e-20 && fr < c.relTol * st->initRes[k]);
+      if (!isfinite(fr)) atomicOr(&st->status, kErrNaN);
+      st->active[k] = (!conv && st->nIter[k] < c.maxIter && isfinite(fr)) ? 1 : 0;
+    }
+    if (st->active[k]) {
+      st->beta[k] = st->nIter[k] == 0 ? 0.0 : S[k] / st->wArA[k];
+      st->wArA[k] = S[k];
+    }
+    any |= st->active[k];
+  }
+  if (anyPend) st->pcgIter += 1;
+  st->pcgContinue = any;
 }
 
 // The processor-local preconditioner of one PCG iteration: the pending
@@ -282,10 +519,6 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
   __shared__ double red[2 * 6];
   // the vectors never alias one another
   const T* __restrict__ pg = st->pbuf ? p.p2 : p.p;  // p of the pending iteration
-  const T* __restrict__ qg = p.q;
-  const T* __restrict__ rDg = p.rD;
-  T* __restrict__ xg = p.x;
-  T* __restrict__ rg = p.r;
   bool pend[3];
   T al[3];
 #pragma unroll
@@ -304,8 +537,7 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
   __syncthreads();
   for (int part = sTicket; part < mv.nParts;) {
     const int4 dA = sDesc[0], dB = sDesc[1];
-    const int pLo = dA.x, nR = dA.y, eLo = dA.z, nE = dA.w;
-    const int mLo = dB.x, nM = dB.y, l0 = dB.z, nL = dB.w;
+    const int pLo = dA.x, nR = dA.y, nL = dB.w;
     // the next part's ticket and descriptor go straight to shared memory
     // (nothing of them stays in registers across the part)
     if (threadIdx.x == 0) {
@@ -313,55 +545,7 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
       sNextTicket = nt;
       if (nt < mv.nParts) { sNextDesc[0] = mv.locDesc[2 * nt]; sNextDesc[1] = mv.locDesc[2 * nt + 1]; }
     }
-    // static part tables in flight while the vectors stream
-    {
-      const int nc = nE * (int)sizeof(T) / 16;
-      const char* g = (const char*)(p.lcoef + eLo);
-      for (int k = threadIdx.x; k < nc; k += NT) cpAsync16((char*)sm.c + 16 * k, g + 16 * k);
-      const int ni = nE * 2 / 16;
-      const char* gi = (const char*)(mv.locIdx + eLo);
-      for (int k = threadIdx.x; k < ni; k += NT) cpAsync16((char*)sm.idx + 16 * k, gi + 16 * k);
-      const int nm = nM * 4 / 16;
-      const char* gm = (const char*)(mv.locMeta + mLo);
-      for (int k = threadIdx.x; k < nm; k += NT) cpAsync16((char*)sm.m + 16 * k, gm + 16 * k);
-    }
-    for (int k = threadIdx.x; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
-    if (SLOT && threadIdx.x < 3) sm.w[3 * mv.maxRows + threadIdx.x] = T(0);  // the zero row
-    // pending update: RPT rows per thread with every load issued before
-    // any store; r and w = rD r into shared memory
-    for (int i0 = threadIdx.x; i0 < nR; i0 += RPT * NT) {
-      T rv[RPT][3], qv[RPT][3], pv[RPT][3], xv[RPT][3], rd[RPT];
-#pragma unroll
-      for (int h = 0; h < RPT; ++h) {
-        const int i = i0 + h * NT;
-        if (i < nR) {
-          const size_t g = 3 * (size_t)(pLo + i);
-          rd[h] = rDg[pLo + i];
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            rv[h][k] = rg[g + k];
-            if (pend[k]) { qv[h][k] = qg[g + k]; pv[h][k] = pg[g + k]; xv[h][k] = xg[g + k]; }
-          }
-        }
-      }
-#pragma unroll
-      for (int h = 0; h < RPT; ++h) {
-        const int i = i0 + h * NT;
-        if (i < nR) {
-          const size_t g = 3 * (size_t)(pLo + i);
-#pragma unroll
-          for (int k = 0; k < 3; ++k) {
-            if (pend[k]) {
-              xg[g + k] = xv[h][k] + al[k] * pv[h][k];
-              rv[h][k] -= al[k] * qv[h][k];
-              rg[g + k] = rv[h][k];
-            }
-            sm.r[3 * i + k] = rv[h][k];
-            sm.w[3 * i + k] = rd[h] * rv[h][k];
-          }
-        }
-      }
-    }
+    locStage<T, NT, RPT, SLOT>(mv, p, sm, pg, pend, al, dA, dB);
     cpAsyncWaitAll();
     __syncthreads();
     // forward substitution: w_u -= sum_{l<u in part} (rD_u a_ul) w_l, then
@@ -411,32 +595,101 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
     __syncthreads();
     part = sTicket;
   }
-  // the last CTA sums the part records in part order
-  if (!lastBlockDone(&st->counter[5], gridDim.x)) return;
-  double S[6];
-  reduceRecords<6>(partials, 8, mv.nParts, S, (double*)smraw);
-  if (threadIdx.x != 0) return;
-  st->counter[5] = 0;
-  st->locTicket = 0;
-  int any = 0;
-  for (int k = 0; k < 3; ++k) {
-    if (st->pending[k]) {
-      st->pending[k] = 0;
-      const double fr = S[3 + k] / st->normFactor[k];
-      st->finalRes[k] = fr;
-      st->nIter[k] += 1;
-      const bool conv = fr < c.tol || (c.relTol > 1e-20 && fr < c.relTol * st->initRes[k]);
-      if (!isfinite(fr)) atomicOr(&st->status, kErrNaN);
-      st->active[k] = (!conv && st->nIter[k] < c.maxIter && isfinite(fr)) ? 1 : 0;
-    }
-    if (st->active[k]) {
-      st->beta[k] = st->nIter[k] == 0 ? 0.0 : S[k] / st->wArA[k];
-      st->wArA[k] = S[k];
-    }
-    any |= st->active[k];
+  locDecide(mv, c, st, partials, anyPend, smraw);
+}
+
+// The slot-table preconditioner with two parts per CTA at a time: both are
+// staged together and walked together (slotSweepPair), so each level's
+// latency serves two parts.  Per part the arithmetic and the order of its
+// sums are those of kLocPrecond, so the results are bit-identical to it.
+// Shared memory: two part regions of localSmemBytes (rounded to 16 bytes).
+// Resident blocks of the paired kernel: its two part regions bound it to
+// three CTAs per SM in FP32 and two in FP64, so registers are set for that.
+template <typename T>
+constexpr int pairMinBlocks() {
+  return sizeof(T) == 4 ? 3 : 2;
+}
+
+template <typename T, int NT, int RPT>
+__global__ void __launch_bounds__(NT, (pairMinBlocks<T>()))
+kLocPrecondPair(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partials) {
+  p = casePcg(p, blockIdx.y, mv.nC);
+  st += blockIdx.y;
+  partials += (size_t)blockIdx.y * mv.caseRec;
+  if (!st->pcgContinue) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  const size_t region = locRegionBytes<T>(mv);
+  const LocSmem<T> sa = locSmem<T>(mv, smraw);
+  const LocSmem<T> sb = locSmem<T>(mv, smraw + region);
+  __shared__ double red[2 * 12];
+  const T* __restrict__ pg = st->pbuf ? p.p2 : p.p;
+  bool pend[3];
+  T al[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) { pend[k] = st->pending[k] != 0; al[k] = (T)st->alpha[k]; }
+  const bool anyPend = pend[0] || pend[1] || pend[2];
+  // tickets two at a time; the next pair's descriptors come ahead
+  __shared__ int sTicket, sNextTicket;
+  __shared__ int4 sDesc[4], sNextDesc[4];
+  if (threadIdx.x == 0) {
+    const int t0 = (int)atomicAdd(&st->locTicket, 2u);
+    sTicket = t0;
+    for (int j = 0; j < 2; ++j)
+      if (t0 + j < mv.nParts) {
+        sDesc[2 * j] = mv.locDesc[2 * (t0 + j)];
+        sDesc[2 * j + 1] = mv.locDesc[2 * (t0 + j) + 1];
+      }
   }
-  if (anyPend) st->pcgIter += 1;
-  st->pcgContinue = any;
+  __syncthreads();
+  for (int part = sTicket; part < mv.nParts;) {
+    const bool two = part + 1 < mv.nParts;
+    const int4 aA = sDesc[0], aB = sDesc[1];
+    int4 bA = aA, bB = aB;
+    if (two) { bA = sDesc[2]; bB = sDesc[3]; }
+    if (threadIdx.x == 0) {
+      const int nt = (int)atomicAdd(&st->locTicket, 2u);
+      sNextTicket = nt;
+      for (int j = 0; j < 2; ++j)
+        if (nt + j < mv.nParts) {
+          sNextDesc[2 * j] = mv.locDesc[2 * (nt + j)];
+          sNextDesc[2 * j + 1] = mv.locDesc[2 * (nt + j) + 1];
+        }
+    }
+    locStage<T, NT, RPT, true>(mv, p, sa, pg, pend, al, aA, aB);
+    if (two) locStage<T, NT, RPT, true>(mv, p, sb, pg, pend, al, bA, bB);
+    cpAsyncWaitAll();
+    __syncthreads();
+    const int nLa = aB.w, nLb = two ? bB.w : 0;
+    T* __restrict__ wga = p.w + 3 * (size_t)aA.x;
+    T* __restrict__ wgb = p.w + 3 * (size_t)bA.x;
+    double d[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) d[k] = 0;
+    if (threadIdx.x < 32 * kLocWalkWarps) {
+      Acc<T> wra[3], ara[3], wrb[3], arb[3];
+      slotSweepPair<0, kLocWalkWarps, false>(sa, nLa, wga, wra, ara, sb, nLb, wgb, wrb, arb);
+      slotSweepPair<1, kLocWalkWarps, true>(sa, nLa, wga, wra, ara, sb, nLb, wgb, wrb, arb);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        d[k] = wra[k].value(); d[3 + k] = ara[k].value();
+        d[6 + k] = wrb[k].value(); d[9 + k] = arb[k].value();
+      }
+    }
+    sum64<12>(d, red);  // ends with a barrier: the next parts may reuse the shared memory
+    if (threadIdx.x == 0) {
+      double* q = partials + 8 * (size_t)part;
+      for (int k = 0; k < 6; ++k) q[k] = d[k];
+      if (two) {
+        q += 8;
+        for (int k = 0; k < 6; ++k) q[k] = d[6 + k];
+      }
+      sTicket = sNextTicket;
+      for (int j = 0; j < 4; ++j) sDesc[j] = sNextDesc[j];
+    }
+    __syncthreads();
+    part = sTicket;
+  }
+  locDecide(mv, c, st, partials, anyPend, smraw);
 }
 
 // p_new = w (first iteration) or w + beta p_old, the same expression for a
@@ -635,6 +888,18 @@ void launchPrecondV(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, 
         mv, c, p, st, partials);
 }
 
+template <typename T>
+size_t pairSmemBytes(const MeshView& mv) {
+  return 2 * locRegionBytes<T>(mv);
+}
+
+template <typename T, int NT, int RPT>
+void launchPrecondPair(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
+                       double* partials, int grid, cudaStream_t s, int nCases) {
+  kLocPrecondPair<T, NT, RPT><<<dim3(grid, nCases), NT, pairSmemBytes<T>(mv), s>>>(mv, c, p, st,
+                                                                                  partials);
+}
+
 template <typename T, int NT, int RPT, bool SLOT>
 cudaError_t prepareK(const MeshView& mv, int* blocksPerSM) {
   const int sm = (int)localSmemBytes<T>(mv);
@@ -650,31 +915,35 @@ cudaError_t prepareV(const MeshView& mv, int* blocksPerSM) {
                      : prepareK<T, NT, RPT, false>(mv, blocksPerSM);
 }
 
+template <typename T, int NT, int RPT>
+cudaError_t preparePair(const MeshView& mv, int* blocksPerSM) {
+  cudaError_t e = setMaxDynamicSmem(kLocPrecondPair<T, NT, RPT>);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecondPair<T, NT, RPT>, NT,
+                                                       (int)pairSmemBytes<T>(mv));
+}
+
 }  // namespace
 
-// Preconditioner variants (threads per part x rows per thread in flight at
-// once): FP32 {128 x 4, 128 x 2}, FP64 {128 x 2, 128 x 1}; the second of
-// each pair holds fewer registers, so more parts are resident per SM.
-// perf.part_threads reports the threads of the one in use.
+// Preconditioner variants.  Slot-table meshes: one part per CTA at a time
+// (0) or two walked together (1); other meshes: 4 (FP32) or 2 (FP64) rows
+// per thread in flight while streaming (0), or half that (1).  All give
+// bit-identical results.  perf.part_threads reports 128 threads per CTA.
 const int kLocVariantsNT[kLocNumNT] = {128, 128};
 const int kLocVariantsU[kLocNumU] = {1, 6, 0};
 
 template <typename T>
 size_t localSmemBytes(const MeshView& mv) {
-  const size_t P = mv.maxRows, EL = mv.maxLocEntries, ML = mv.maxLocMeta;
-  const size_t tables = sizeof(T) * (EL + 6 * P + 3) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
-  return std::max(tables, (size_t)256 * 6 * sizeof(double));  // final reduction scratch
+  return locRegionBytes<T>(mv);
 }
 
 template <typename T>
 cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM) {
-  if constexpr (sizeof(T) == 4) {
-    cudaError_t e = prepareV<T, 128, 4>(mv, &blocksPerSM[0]);
-    return e != cudaSuccess ? e : prepareV<T, 128, 2>(mv, &blocksPerSM[1]);
-  } else {
-    cudaError_t e = prepareV<T, 128, 2>(mv, &blocksPerSM[0]);
-    return e != cudaSuccess ? e : prepareV<T, 128, 1>(mv, &blocksPerSM[1]);
-  }
+  constexpr int R0 = sizeof(T) == 4 ? 4 : 2, R1 = sizeof(T) == 4 ? 2 : 1;
+  cudaError_t e = prepareV<T, 128, R0>(mv, &blocksPerSM[0]);
+  if (e != cudaSuccess) return e;
+  if (mv.locSlots) return preparePair<T, 128, R0>(mv, &blocksPerSM[1]);
+  return prepareV<T, 128, R1>(mv, &blocksPerSM[1]);
 }
 
 template <typename T>
@@ -685,12 +954,12 @@ void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaS
 template <typename T>
 void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                         double* partials, const LocalTuning& t, cudaStream_t s, int nCases) {
-  if constexpr (sizeof(T) == 4) {
-    if (t.ntIdx == 1) launchPrecondV<T, 128, 2>(mv, c, p, st, partials, t.grid[1], s, nCases);
-    else launchPrecondV<T, 128, 4>(mv, c, p, st, partials, t.grid[0], s, nCases);
+  constexpr int R0 = sizeof(T) == 4 ? 4 : 2, R1 = sizeof(T) == 4 ? 2 : 1;
+  if (t.ntIdx == 1) {
+    if (mv.locSlots) launchPrecondPair<T, 128, R0>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    else launchPrecondV<T, 128, R1>(mv, c, p, st, partials, t.grid[1], s, nCases);
   } else {
-    if (t.ntIdx == 1) launchPrecondV<T, 128, 1>(mv, c, p, st, partials, t.grid[1], s, nCases);
-    else launchPrecondV<T, 128, 2>(mv, c, p, st, partials, t.grid[0], s, nCases);
+    launchPrecondV<T, 128, R0>(mv, c, p, st, partials, t.grid[0], s, nCases);
   }
 }
 
