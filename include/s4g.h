@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define S4G_ABI_VERSION 5
+#define S4G_ABI_VERSION 6
 
 /* Status codes.  Reference convention for errors is FatalError (abort), see
  * src/solids4FoamModels/solidModels/solidModel/solidModel.C:1735-1742; a
@@ -171,6 +171,9 @@ typedef struct s4g_mesh_info {
   long long device_bytes; /* device memory held by this mesh */
   long long n_local_entries; /* processor-local DIC table entries (with padding);
                                 0 unless dic_subdomains */
+  int local_slots;        /* 1: the processor-local tables have fixed 3 + 3 slots per
+                             row (every row has at most three lower and three upper
+                             in-part neighbours); 0: generic tables */
 } s4g_mesh_info;
 
 /* Uploads the mesh once: validation, renumbering, cell-to-face CSR in the

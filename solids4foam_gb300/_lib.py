@@ -54,7 +54,7 @@ class MeshInfo(ct.Structure):
                 ("n_boundary_faces", ct.c_int), ("n_parts", ct.c_int),
                 ("part_depth", ct.c_int), ("max_local_levels", ct.c_int),
                 ("n_levels_global", ct.c_int), ("device_bytes", ct.c_longlong),
-                ("n_local_entries", ct.c_longlong)]
+                ("n_local_entries", ct.c_longlong), ("local_slots", ct.c_int)]
 
 
 class Law(ct.Structure):

@@ -48,6 +48,11 @@ struct MeshView {
   // batched load cases: a launch's blockIdx.y is the case; per-case data
   // lies caseRec doubles (reduction records) or one field size apart
   long caseRec;
+  // within a case's records: the group records of the processor-local
+  // preconditioner (8 doubles per group of 32 parts) start locGrpOff
+  // doubles in, followed by the groups' arrival counters (unsigned)
+  long locGrpOff;
+  int locGroups;
 };
 
 // Batched launches: the case's boundary values (bval [case][nB][3],

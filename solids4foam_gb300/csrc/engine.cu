@@ -353,8 +353,13 @@ struct Engine {
     S4G_TRY(alloc(&dState, 1));
     S4G_CUDA(cudaMallocHost((void**)&hState, sizeof(DevState)));
     const size_t rowBlocks = (nC + kRowBlock - 1) / kRowBlock;
-    mv.caseRec = (long)std::max(8 * rowBlocks, 8 * (size_t)hp.nParts);
+    // per case: block or part records, then the preconditioner's group
+    // records and group counters (zero between launches)
+    mv.locGroups = (hp.nParts + 31) / 32;
+    mv.locGrpOff = (long)std::max(8 * rowBlocks, 8 * (size_t)hp.nParts);
+    mv.caseRec = (mv.locGrpOff + 8 * (long)mv.locGroups + (mv.locGroups + 1) / 2 + 7) / 8 * 8;
     S4G_TRY(alloc(&dPartials, (size_t)mv.caseRec));
+    S4G_CUDA(cudaMemsetAsync(dPartials, 0, sizeof(double) * (size_t)mv.caseRec, s));
     S4G_TRY(alloc(&dOut, 9 * (size_t)nC));
     S4G_CUDA(cudaMemsetAsync(dState, 0, sizeof(DevState), s));
 
@@ -703,6 +708,7 @@ struct Engine {
     }
     S4G_TRY(regrow(dState, o, n));
     S4G_TRY(regrow(dPartials, (size_t)mv.caseRec * o, (size_t)mv.caseRec * n));
+    S4G_CUDA(cudaMemsetAsync(dPartials, 0, sizeof(double) * (size_t)mv.caseRec * n, ctx->stream));
     cudaFreeHost(hState);
     hState = nullptr;
     S4G_CUDA(cudaMallocHost((void**)&hState, sizeof(DevState) * n));
@@ -811,7 +817,7 @@ struct Engine {
         perf->kernel_launches = launches - launches0;
         perf->device_status = (int)h.status;
         const LocalTuning& lt = mixed ? tune32 : tune64;
-        perf->part_threads = kLocVariantsNT[lt.ntIdx];
+        perf->part_threads = localPartThreads(mv, lt.ntIdx);
         perf->spmv_unroll = kLocVariantsU[lt.uIdx];
         for (int k = 0; k < 6; ++k)
           perf->tune_us[k] = k < kLocNumNT + kLocNumU ? tuneUs[mixed ? 1 : 0][k] : 0.0;
@@ -1207,7 +1213,7 @@ struct Engine {
       perf->device_status = (int)hState->status;
       const bool local = mv.subdomains && lin.preconditioner == S4G_PRECOND_DIC;
       const LocalTuning& lt = mixed ? tune32 : tune64;
-      perf->part_threads = local ? kLocVariantsNT[lt.ntIdx] : 0;
+      perf->part_threads = local ? localPartThreads(mv, lt.ntIdx) : 0;
       perf->spmv_unroll = local ? kLocVariantsU[lt.uIdx] : 0;
       for (int k = 0; k < 6; ++k)
         perf->tune_us[k] = (local && k < kLocNumNT + kLocNumU) ? tuneUs[mixed ? 1 : 0][k] : 0.0;
@@ -1294,7 +1300,7 @@ struct Engine {
       perf->kernel_launches = launches - batchLaunches0;
       perf->device_status = (int)hState->status;
       const LocalTuning& lt = tuning32or64();
-      perf->part_threads = local ? kLocVariantsNT[lt.ntIdx] : 0;
+      perf->part_threads = local ? localPartThreads(mv, lt.ntIdx) : 0;
       perf->spmv_unroll = local ? kLocVariantsU[lt.uIdx] : 0;
       perf->device_loop = 1;
     }
@@ -1582,6 +1588,7 @@ s4g_status s4g_mesh_plan(const s4g_mesh_desc* desc, const s4g_mesh_opts* opts, i
     info->max_local_levels = hp.maxLocalLevels;
     info->n_levels_global = hp.globalLevels;
     info->n_local_entries = (long long)hp.locSrc.size();
+    info->local_slots = hp.locSlots ? 1 : 0;
   }
   return S4G_OK;
 }
@@ -1598,6 +1605,7 @@ s4g_status s4g_mesh_get_info(const s4g_mesh* mesh, s4g_mesh_info* info) {
   info->n_levels_global = hp.globalLevels;
   info->device_bytes = (long long)mesh->e.bytes;
   info->n_local_entries = (long long)hp.locSrc.size();
+  info->local_slots = hp.locSlots ? 1 : 0;
   return S4G_OK;
 }
 

@@ -178,6 +178,8 @@ void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaS
 // variants compute bit-identical results.
 constexpr int kLocNumNT = 2, kLocNumU = 3;
 extern const int kLocVariantsNT[kLocNumNT];
+// Threads per part of preconditioner variant `variant` on this mesh.
+int localPartThreads(const MeshView& mv, int variant);
 extern const int kLocVariantsU[kLocNumU];
 struct LocalTuning {
   int ntIdx = 0, uIdx = 0;

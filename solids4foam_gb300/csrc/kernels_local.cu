@@ -25,13 +25,14 @@
 // differs.
 //
 // Variants.  The SpMV step runs fused with a plain or an unrolled entry
-// loop, or split into a p-update pass and an SpMV; kLocPrecond streams a
-// part's rows with 4 (FP32) or 2 (FP64) rows per thread in flight, or half
-// that.  The autotuner (engine) times them on the mesh
-// and keeps the fastest.  The SpMV variants sum in the same order (same grid
-// and block); kLocPrecond sums each part in a fixed order that does not
-// depend on its block size, then over the parts in index order.  So all
-// variants give bit-identical results.
+// loop, or split into a p-update pass and an SpMV; the preconditioner runs
+// with 128 or 64 threads per part (generic tables) or with 2 or 4 (FP32),
+// 1 or 2 (FP64) rows per thread in flight (slot tables).  The autotuner
+// (engine) times them on the mesh and keeps the fastest.  The SpMV variants
+// sum in the same order (same grid and block); the preconditioner sums each
+// part in a fixed order that depends neither on its block size nor on its
+// grid, then the parts in groups of 32 in part order, then the groups in
+// group order.  So all variants give bit-identical results.
 //
 // Part tables (HostPrep step 9): in-part entries per row, lower entries in
 // CSR order then upper entries in reverse CSR order, coefficient rD_row*a_e
@@ -47,17 +48,6 @@
 
 namespace s4g {
 namespace {
-
-// Bytes of one part's staged region (tables, w with its zero row, r, level
-// starts), or of the final reduction's scratch if that is larger; rounded
-// to 16 bytes so that regions can follow one another.
-template <typename T>
-__host__ __device__ inline size_t locRegionBytes(const MeshView& mv) {
-  const size_t P = mv.maxRows, EL = mv.maxLocEntries, ML = mv.maxLocMeta;
-  const size_t tables = sizeof(T) * (EL + 6 * P + 3) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
-  const size_t b = tables > (size_t)256 * 6 * sizeof(double) ? tables : (size_t)256 * 6 * sizeof(double);
-  return (b + 15) / 16 * 16;
-}
 
 template <typename T>
 struct LocSmem {
@@ -75,6 +65,21 @@ __device__ __forceinline__ LocSmem<T> locSmem(const MeshView& mv, unsigned char*
                                               // and the zero row P of the slots
   s.r = s.w + 3 * P + 3;                      // 3P: the updated residual
   s.lv = (int*)(s.r + 3 * P);                 // maxLevels + 1
+  return s;
+}
+
+// Shared memory of the slot-table kernel: coefficients, columns, w with the
+// zero row, level starts (no row metadata, no residual copy).
+template <typename T>
+__device__ __forceinline__ LocSmem<T> slotSmem(const MeshView& mv, unsigned char* raw) {
+  LocSmem<T> s;
+  const int P = mv.maxRows, EL = mv.maxLocEntries;
+  s.c = (T*)raw;                              // EL coefficients (EL % 8 == 0)
+  s.m = nullptr;
+  s.idx = (uint16_t*)(s.c + EL);              // EL local columns
+  s.w = (T*)(s.idx + EL);                     // 3P + 3
+  s.r = nullptr;
+  s.lv = (int*)(s.w + 3 * P + 3);             // maxLevels + 1
   return s;
 }
 
@@ -190,11 +195,9 @@ __device__ __forceinline__ void slotPre(const LocSmem<T>& sm, int lo, int hi, in
 }
 
 // v -= a_u w_q(u) for the three slots in order (a padded slot subtracts an
-// exact zero); OUT (the backward substitution, which leaves w final): w also
-// goes to global memory and into the thread's w.r and sum|r| sums.
-template <bool OUT, typename T>
-__device__ __forceinline__ void slotApply(const LocSmem<T>& sm, const SlotRow<T>& row,
-                                          T* __restrict__ wg, Acc<T> (&wr)[3], Acc<T> (&ar)[3]) {
+// exact zero).
+template <typename T>
+__device__ __forceinline__ void slotApply(const LocSmem<T>& sm, const SlotRow<T>& row) {
   const int i = row.i;
   T v[3] = {sm.w[3 * i], sm.w[3 * i + 1], sm.w[3 * i + 2]};
   T x[3][3];
@@ -208,179 +211,37 @@ __device__ __forceinline__ void slotApply(const LocSmem<T>& sm, const SlotRow<T>
     for (int k = 0; k < 3; ++k) v[k] -= row.a[u] * x[u][k];
 #pragma unroll
   for (int k = 0; k < 3; ++k) sm.w[3 * i + k] = v[k];
-  if (OUT) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      wg[3 * i + k] = v[k];
-      const T r = sm.r[3 * i + k];
-      wr[k].add(v[k] * r);
-      ar[k].add(fabs(r));
-    }
-  }
 }
 
-// One substitution over the part's levels by W warps with the slot tables:
-// the level bounds two levels ahead and the next level's slots are in
-// registers before the current level's neighbour loads, so each level costs
-// one round of shared-memory loads, the multiply-adds and a barrier.
-template <int DIR, int W, bool OUT, typename T>
-__device__ __forceinline__ void slotSweep(const LocSmem<T>& sm, int nL, T* __restrict__ wg,
-                                          Acc<T> (&wr)[3], Acc<T> (&ar)[3]) {
+// One substitution (DIR 0 forward, 1 backward) of kLocPrecondSlots: all 64
+// threads, one row per thread with its slots in registers a level ahead
+// and the level bounds two levels ahead (rows past the first 64 of a wide
+// level are read at the level), so each level costs one round of
+// shared-memory loads, the multiply-adds and a CTA barrier.
+template <int DIR, typename T>
+__device__ __forceinline__ void slotWalk(const LocSmem<T>& sm, int nL) {
   if (nL <= 0) return;
-  constexpr int NW = 32 * W;
+  constexpr int NW = 64;
   const int t = (int)threadIdx.x;
   auto lvl = [&](int q) { return DIR == 0 ? q : nL - 1 - q; };
   int lo = sm.lv[lvl(0)], hi = sm.lv[lvl(0) + 1];
   int lo1 = 0, hi1 = 0;
   if (nL > 1) { lo1 = sm.lv[lvl(1)]; hi1 = sm.lv[lvl(1) + 1]; }
-  SlotRow<T> n0, n1;
+  SlotRow<T> n0;
   slotPre<DIR>(sm, lo, hi, t, n0);
-  slotPre<DIR>(sm, lo, hi, t + NW, n1);
   for (int q = 0; q < nL; ++q) {
-    const SlotRow<T> c0 = n0, c1 = n1;
+    const SlotRow<T> c0 = n0;
     const int clo = lo, chi = hi;
     lo = lo1; hi = hi1;
     if (q + 2 < nL) { lo1 = sm.lv[lvl(q + 2)]; hi1 = sm.lv[lvl(q + 2) + 1]; }
-    if (q + 1 < nL) {
-      slotPre<DIR>(sm, lo, hi, t, n0);
-      slotPre<DIR>(sm, lo, hi, t + NW, n1);
-    }
-    if (c0.i >= 0) slotApply<OUT>(sm, c0, wg, wr, ar);
-    if (c1.i >= 0) slotApply<OUT>(sm, c1, wg, wr, ar);
-    // rows beyond the first 2 NW of a wide level
-    for (int off = t + 2 * NW; clo + off < chi; off += NW) {
+    if (q + 1 < nL) slotPre<DIR>(sm, lo, hi, t, n0);
+    if (c0.i >= 0) slotApply(sm, c0);
+    for (int off = t + NW; clo + off < chi; off += NW) {
       SlotRow<T> row;
       slotPre<DIR>(sm, clo, chi, off, row);
-      slotApply<OUT>(sm, row, wg, wr, ar);
+      slotApply(sm, row);
     }
-    walkBarrier<W>();
-  }
-}
-
-// Two parts walked together by the same threads: per level, thread t takes
-// row t of part A's level and row t of part B's level (parts may have
-// different level counts), and both rows' loads are issued before either's
-// multiply-adds -- two independent latency chains per level instead of one.
-template <bool OUT, typename T>
-__device__ __forceinline__ void slotApplyAB(const LocSmem<T>& sa, const SlotRow<T>& ra,
-                                            T* __restrict__ wga, Acc<T> (&wra)[3], Acc<T> (&ara)[3],
-                                            const LocSmem<T>& sb, const SlotRow<T>& rb,
-                                            T* __restrict__ wgb, Acc<T> (&wrb)[3],
-                                            Acc<T> (&arb)[3]) {
-  const bool ha = ra.i >= 0, hb = rb.i >= 0;
-  T va[3], vb[3], xa[3][3], xb[3][3];
-  if (ha) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) va[k] = sa.w[3 * ra.i + k];
-#pragma unroll
-    for (int u = 0; u < 3; ++u)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) xa[u][k] = sa.w[3 * ra.q[u] + k];
-  }
-  if (hb) {
-#pragma unroll
-    for (int k = 0; k < 3; ++k) vb[k] = sb.w[3 * rb.i + k];
-#pragma unroll
-    for (int u = 0; u < 3; ++u)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) xb[u][k] = sb.w[3 * rb.q[u] + k];
-  }
-  if (ha) {
-#pragma unroll
-    for (int u = 0; u < 3; ++u)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) va[k] -= ra.a[u] * xa[u][k];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) sa.w[3 * ra.i + k] = va[k];
-  }
-  if (hb) {
-#pragma unroll
-    for (int u = 0; u < 3; ++u)
-#pragma unroll
-      for (int k = 0; k < 3; ++k) vb[k] -= rb.a[u] * xb[u][k];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) sb.w[3 * rb.i + k] = vb[k];
-  }
-  if (OUT) {
-    if (ha) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        wga[3 * ra.i + k] = va[k];
-        const T r = sa.r[3 * ra.i + k];
-        wra[k].add(va[k] * r);
-        ara[k].add(fabs(r));
-      }
-    }
-    if (hb) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        wgb[3 * rb.i + k] = vb[k];
-        const T r = sb.r[3 * rb.i + k];
-        wrb[k].add(vb[k] * r);
-        arb[k].add(fabs(r));
-      }
-    }
-  }
-}
-
-// The level bounds of one part during a pair walk, two levels ahead.
-struct LevelCursor {
-  int lo, hi, lo1, hi1;
-};
-
-template <int DIR, typename T>
-__device__ __forceinline__ void cursorInit(const LocSmem<T>& sm, int nL, LevelCursor& c) {
-  c.lo = c.hi = c.lo1 = c.hi1 = 0;
-  if (nL > 0) { const int l = DIR == 0 ? 0 : nL - 1; c.lo = sm.lv[l]; c.hi = sm.lv[l + 1]; }
-  if (nL > 1) { const int l = DIR == 0 ? 1 : nL - 2; c.lo1 = sm.lv[l]; c.hi1 = sm.lv[l + 1]; }
-}
-
-// Advance to level q + 1 (the bounds of q + 2 are loaded); empty past nL.
-template <int DIR, typename T>
-__device__ __forceinline__ void cursorStep(const LocSmem<T>& sm, int nL, int q, LevelCursor& c) {
-  c.lo = c.lo1; c.hi = c.hi1;
-  if (q + 2 < nL) {
-    const int l = DIR == 0 ? q + 2 : nL - 3 - q;
-    c.lo1 = sm.lv[l]; c.hi1 = sm.lv[l + 1];
-  } else {
-    c.lo1 = c.hi1 = 0;
-  }
-}
-
-template <int DIR, int W, bool OUT, typename T>
-__device__ __forceinline__ void slotSweepPair(const LocSmem<T>& sa, int nLa, T* __restrict__ wga,
-                                              Acc<T> (&wra)[3], Acc<T> (&ara)[3],
-                                              const LocSmem<T>& sb, int nLb, T* __restrict__ wgb,
-                                              Acc<T> (&wrb)[3], Acc<T> (&arb)[3]) {
-  constexpr int NW = 32 * W;
-  const int t = (int)threadIdx.x;
-  const int nL = nLa > nLb ? nLa : nLb;
-  LevelCursor ca, cb;
-  cursorInit<DIR>(sa, nLa, ca);
-  cursorInit<DIR>(sb, nLb, cb);
-  SlotRow<T> na, nb;
-  slotPre<DIR>(sa, ca.lo, ca.hi, t, na);
-  slotPre<DIR>(sb, cb.lo, cb.hi, t, nb);
-  for (int q = 0; q < nL; ++q) {
-    const SlotRow<T> cra = na, crb = nb;
-    const int aLo = ca.lo, aHi = ca.hi, bLo = cb.lo, bHi = cb.hi;
-    cursorStep<DIR>(sa, nLa, q, ca);
-    cursorStep<DIR>(sb, nLb, q, cb);
-    slotPre<DIR>(sa, ca.lo, ca.hi, t, na);
-    slotPre<DIR>(sb, cb.lo, cb.hi, t, nb);
-    slotApplyAB<OUT>(sa, cra, wga, wra, ara, sb, crb, wgb, wrb, arb);
-    // rows beyond the first NW of a wide level
-    for (int off = t + NW; aLo + off < aHi; off += NW) {
-      SlotRow<T> row;
-      slotPre<DIR>(sa, aLo, aHi, off, row);
-      slotApply<OUT>(sa, row, wga, wra, ara);
-    }
-    for (int off = t + NW; bLo + off < bHi; off += NW) {
-      SlotRow<T> row;
-      slotPre<DIR>(sb, bLo, bHi, off, row);
-      slotApply<OUT>(sb, row, wgb, wrb, arb);
-    }
-    walkBarrier<W>();
+    __syncthreads();
   }
 }
 
@@ -390,89 +251,70 @@ __global__ void kLocGather(int n, const int* src, const double* rDa, T* out) {
   if (i < n) out[i] = src[i] >= 0 ? (T)rDa[src[i]] : T(0);
 }
 
-// Resident blocks the register budget is set for (NT threads, RPT rows per
-// thread in flight at once in the streaming phase).
-template <typename T, int NT, int RPT>
-constexpr int locMinBlocks() {
-  return sizeof(T) == 4 ? 4 : (RPT >= 2 ? 3 : 4);
+// Part records in groups of kLocGroup parts: the CTA whose part completes a
+// group (the last to arrive on the group's counter) sums the group's records
+// in part order by a fixed shuffle tree, and the last CTA of the launch sums
+// the group records -- one round trip each instead of one CTA reading every
+// part record at the end of the launch.
+constexpr int kLocGroup = 32;
+
+__device__ __forceinline__ int locGroupSize(int g, int nParts) {
+  const int n = nParts - g * kLocGroup;
+  return n < kLocGroup ? n : kLocGroup;
 }
 
-// Staging of one part: its tables by 16-byte cp.async, its level starts,
-// the zero row (slot tables), and the pending update x += alpha p,
-// r -= alpha q with RPT rows per thread in flight (every load issued before
-// any store); r and w = rD r into shared memory.  The caller waits for the
-// cp.async group and synchronises.
-template <typename T, int NT, int RPT, bool SLOT>
-__device__ __forceinline__ void locStage(const MeshView& mv, const PcgPtrs<T>& p,
-                                         const LocSmem<T>& sm, const T* __restrict__ pg,
-                                         const bool (&pend)[3], const T (&al)[3], int4 dA,
-                                         int4 dB) {
-  const int pLo = dA.x, nR = dA.y, eLo = dA.z, nE = dA.w;
-  const int mLo = dB.x, nM = dB.y, l0 = dB.z, nL = dB.w;
-  const T* __restrict__ qg = p.q;
-  const T* __restrict__ rDg = p.rD;
-  T* __restrict__ xg = p.x;
-  T* __restrict__ rg = p.r;
-  // static part tables in flight while the vectors stream
-  {
-    const int nc = nE * (int)sizeof(T) / 16;
-    const char* g = (const char*)(p.lcoef + eLo);
-    for (int k = threadIdx.x; k < nc; k += NT) cpAsync16((char*)sm.c + 16 * k, g + 16 * k);
-    const int ni = nE * 2 / 16;
-    const char* gi = (const char*)(mv.locIdx + eLo);
-    for (int k = threadIdx.x; k < ni; k += NT) cpAsync16((char*)sm.idx + 16 * k, gi + 16 * k);
-    const int nm = nM * 4 / 16;
-    const char* gm = (const char*)(mv.locMeta + mLo);
-    for (int k = threadIdx.x; k < nm; k += NT) cpAsync16((char*)sm.m + 16 * k, gm + 16 * k);
-  }
-  for (int k = threadIdx.x; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
-  if (SLOT && threadIdx.x < 3) sm.w[3 * mv.maxRows + threadIdx.x] = T(0);  // the zero row
-  // pending update: RPT rows per thread with every load issued before
-  // any store; r and w = rD r into shared memory
-  for (int i0 = threadIdx.x; i0 < nR; i0 += RPT * NT) {
-    T rv[RPT][3], qv[RPT][3], pv[RPT][3], xv[RPT][3], rd[RPT];
+// Thread 0: the arrival of `part`'s record (written by this thread) on its
+// group's counter; true if it completes the group.
+__device__ __forceinline__ bool locArrive(unsigned* gcnt, int part, int nParts) {
+  __threadfence();
+  const int g = part / kLocGroup;
+  return atomicAdd(&gcnt[g], 1u) + 1u == (unsigned)locGroupSize(g, nParts);
+}
+
+// One warp: the record of group g (lane j holds part g*32 + j), and the
+// group's counter back to zero for the next launch.
+__device__ __forceinline__ void locGroupSum(const double* rec, double* grec, unsigned* gcnt, int g,
+                                            int nParts) {
+  const int lane = threadIdx.x & 31;
+  const int part = g * kLocGroup + lane;
+  __threadfence();
+  double v[6];
 #pragma unroll
-    for (int h = 0; h < RPT; ++h) {
-      const int i = i0 + h * NT;
-      if (i < nR) {
-        const size_t g = 3 * (size_t)(pLo + i);
-        rd[h] = rDg[pLo + i];
+  for (int k = 0; k < 6; ++k) v[k] = part < nParts ? __ldcg(rec + 8 * (size_t)part + k) : 0.0;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          rv[h][k] = rg[g + k];
-          if (pend[k]) { qv[h][k] = qg[g + k]; pv[h][k] = pg[g + k]; xv[h][k] = xg[g + k]; }
-        }
-      }
-    }
+  for (int k = 0; k < 6; ++k)
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  if (lane == 0) {
 #pragma unroll
-    for (int h = 0; h < RPT; ++h) {
-      const int i = i0 + h * NT;
-      if (i < nR) {
-        const size_t g = 3 * (size_t)(pLo + i);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          if (pend[k]) {
-            xg[g + k] = xv[h][k] + al[k] * pv[h][k];
-            rv[h][k] -= al[k] * qv[h][k];
-            rg[g + k] = rv[h][k];
-          }
-          sm.r[3 * i + k] = rv[h][k];
-          sm.w[3 * i + k] = rd[h] * rv[h][k];
-        }
-      }
-    }
+    for (int k = 0; k < 6; ++k) grec[8 * (size_t)g + k] = v[k];
+    gcnt[g] = 0;
   }
 }
 
-// After every part: the last CTA sums the part records in part order and
-// decides, per component, the residual test of the pending iteration, beta
-// and wArA, and whether the loop goes on.
-__device__ __forceinline__ void locDecide(const MeshView& mv, const Controls& c, DevState* st,
-                                          double* partials, bool anyPend, unsigned char* smraw) {
+// End of a preconditioner launch, after the CTA's last part: thread 0
+// reports that part on its group counter (warp 0 sums the group if that
+// completes it); the last CTA sums the group records in group order -- lane
+// v of 64 sums groups v, v + 64, ..., then a fixed tree -- and decides, per
+// component, the residual test of the pending iteration, beta and wArA, and
+// whether the loop goes on.  Block size >= 64.
+__device__ __forceinline__ void locFinish(const MeshView& mv, const Controls& c, DevState* st,
+                                          double* partials, int lastPart, bool anyPend,
+                                          double* red, int* sGroup) {
+  double* grec = partials + mv.locGrpOff;
+  unsigned* gcnt = reinterpret_cast<unsigned*>(grec + 8 * (size_t)mv.locGroups);
+  const int t = (int)threadIdx.x;
+  if (t == 0)
+    *sGroup = (lastPart >= 0 && locArrive(gcnt, lastPart, mv.nParts)) ? lastPart / kLocGroup : -1;
+  __syncthreads();
+  if (*sGroup >= 0 && t < 32) locGroupSum(partials, grec, gcnt, *sGroup, mv.nParts);
   if (!lastBlockDone(&st->counter[5], gridDim.x)) return;
-  double S[6];
-  reduceRecords<6>(partials, 8, mv.nParts, S, (double*)smraw);
-  if (threadIdx.x != 0) return;
+  double S[6] = {0, 0, 0, 0, 0, 0};
+  if (t < 64)
+    for (int g = t; g < mv.locGroups; g += 64)
+#pragma unroll
+      for (int k = 0; k < 6; ++k) S[k] += __ldcg(grec + 8 * (size_t)g + k);
+  sum64<6>(S, red);
+  if (t != 0) return;
   st->counter[5] = 0;
   st->locTicket = 0;
   int any = 0;
@@ -496,6 +338,15 @@ __device__ __forceinline__ void locDecide(const MeshView& mv, const Controls& c,
   st->pcgContinue = any;
 }
 
+// Resident blocks the register budget is set for (NT threads, RPT rows per
+// thread in flight at once in the streaming phase).  With 64 threads every
+// thread walks; FP32 parts (about 31 KB of shared memory at 8^3 cells) then
+// fit seven CTAs per SM, each walking its own part.
+template <typename T, int NT, int RPT>
+constexpr int locMinBlocks() {
+  return NT == 64 ? (sizeof(T) == 4 ? 7 : 4) : (sizeof(T) == 4 ? 4 : (RPT >= 2 ? 3 : 4));
+}
+
 // The processor-local preconditioner of one PCG iteration: the pending
 // update x += alpha p, r -= alpha q, w = rD r, the forward and backward
 // substitutions of each part inside one CTA, and the w.r and sum|r| sums.
@@ -505,9 +356,11 @@ __device__ __forceinline__ void locDecide(const MeshView& mv, const Controls& c,
 // part's tables arrive by 16-byte cp.async.  The updated residual and w go
 // to shared memory.  Sums: per part, in a fixed order independent of NT
 // and RPT (64 lanes over the rows, lane l summing rows l, l+64, ..., then a
-// fixed tree), one record per part; the last CTA sums the records in part
-// order.  Every variant therefore gives bit-identical results.
-template <typename T, int NT, int RPT, bool SLOT>
+// fixed tree), one record per part; the records are summed in groups of 32
+// parts and the group records in group order (locFinish).  Every variant
+// therefore gives bit-identical results.  Used for generic part tables;
+// hexahedral parts with slot tables go to kLocPrecondSlots.
+template <typename T, int NT, int RPT>
 __global__ void __launch_bounds__(NT, (locMinBlocks<T, NT, RPT>()))
 kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partials) {
   p = casePcg(p, blockIdx.y, mv.nC);
@@ -519,6 +372,10 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
   __shared__ double red[2 * 6];
   // the vectors never alias one another
   const T* __restrict__ pg = st->pbuf ? p.p2 : p.p;  // p of the pending iteration
+  const T* __restrict__ qg = p.q;
+  const T* __restrict__ rDg = p.rD;
+  T* __restrict__ xg = p.x;
+  T* __restrict__ rg = p.r;
   bool pend[3];
   T al[3];
 #pragma unroll
@@ -527,8 +384,11 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
   // Parts come from a ticket counter: CTAs that finish early take more (no
   // tail of CTAs with one part more than the others); the next ticket and
   // its part's descriptor are fetched while the current part runs.
-  __shared__ int sTicket, sNextTicket;
+  __shared__ int sTicket, sNextTicket, sGroup;
   __shared__ int4 sDesc[2], sNextDesc[2];
+  double* grec = partials + mv.locGrpOff;
+  unsigned* gcnt = reinterpret_cast<unsigned*>(grec + 8 * (size_t)mv.locGroups);
+  int prev = -1;
   if (threadIdx.x == 0) {
     const int t0 = (int)atomicAdd(&st->locTicket, 1u);
     sTicket = t0;
@@ -537,32 +397,73 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
   __syncthreads();
   for (int part = sTicket; part < mv.nParts;) {
     const int4 dA = sDesc[0], dB = sDesc[1];
-    const int pLo = dA.x, nR = dA.y, nL = dB.w;
+    const int pLo = dA.x, nR = dA.y, eLo = dA.z, nE = dA.w;
+    const int mLo = dB.x, nM = dB.y, l0 = dB.z, nL = dB.w;
     // the next part's ticket and descriptor go straight to shared memory
     // (nothing of them stays in registers across the part)
+    // and the previous part's record is reported on its group counter
+    bool done = false;
     if (threadIdx.x == 0) {
       const int nt = (int)atomicAdd(&st->locTicket, 1u);
+      if (prev >= 0) done = locArrive(gcnt, prev, mv.nParts);
       sNextTicket = nt;
       if (nt < mv.nParts) { sNextDesc[0] = mv.locDesc[2 * nt]; sNextDesc[1] = mv.locDesc[2 * nt + 1]; }
     }
-    locStage<T, NT, RPT, SLOT>(mv, p, sm, pg, pend, al, dA, dB);
+    // static part tables in flight while the vectors stream
+    {
+      const int nc = nE * (int)sizeof(T) / 16;
+      const char* g = (const char*)(p.lcoef + eLo);
+      for (int k = threadIdx.x; k < nc; k += NT) cpAsync16((char*)sm.c + 16 * k, g + 16 * k);
+      const int ni = nE * 2 / 16;
+      const char* gi = (const char*)(mv.locIdx + eLo);
+      for (int k = threadIdx.x; k < ni; k += NT) cpAsync16((char*)sm.idx + 16 * k, gi + 16 * k);
+      const int nm = nM * 4 / 16;
+      const char* gm = (const char*)(mv.locMeta + mLo);
+      for (int k = threadIdx.x; k < nm; k += NT) cpAsync16((char*)sm.m + 16 * k, gm + 16 * k);
+    }
+    for (int k = threadIdx.x; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
+    // pending update: RPT rows per thread with every load issued before
+    // any store; r and w = rD r into shared memory
+    for (int i0 = threadIdx.x; i0 < nR; i0 += RPT * NT) {
+      T rv[RPT][3], qv[RPT][3], pv[RPT][3], xv[RPT][3], rd[RPT];
+#pragma unroll
+      for (int h = 0; h < RPT; ++h) {
+        const int i = i0 + h * NT;
+        if (i < nR) {
+          const size_t g = 3 * (size_t)(pLo + i);
+          rd[h] = rDg[pLo + i];
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            rv[h][k] = rg[g + k];
+            if (pend[k]) { qv[h][k] = qg[g + k]; pv[h][k] = pg[g + k]; xv[h][k] = xg[g + k]; }
+          }
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < RPT; ++h) {
+        const int i = i0 + h * NT;
+        if (i < nR) {
+          const size_t g = 3 * (size_t)(pLo + i);
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            if (pend[k]) {
+              xg[g + k] = xv[h][k] + al[k] * pv[h][k];
+              rv[h][k] -= al[k] * qv[h][k];
+              rg[g + k] = rv[h][k];
+            }
+            sm.r[3 * i + k] = rv[h][k];
+            sm.w[3 * i + k] = rd[h] * rv[h][k];
+          }
+        }
+      }
+    }
     cpAsyncWaitAll();
     __syncthreads();
     // forward substitution: w_u -= sum_{l<u in part} (rD_u a_ul) w_l, then
     // backward substitution: w_l -= sum_{u>l in part} (rD_l a_lu) w_u
     T* __restrict__ wg = p.w + 3 * (size_t)pLo;
     double d6[6] = {0, 0, 0, 0, 0, 0};
-    if constexpr (SLOT) {
-      // the backward substitution also writes w out and sums w.r and |r|
-      // over each walking thread's rows, in a fixed order; then a fixed tree
-      if (threadIdx.x < 32 * kLocWalkWarps) {
-        Acc<T> wr[3], ar[3];
-        slotSweep<0, kLocWalkWarps, false>(sm, nL, wg, wr, ar);
-        slotSweep<1, kLocWalkWarps, true>(sm, nL, wg, wr, ar);
-#pragma unroll
-        for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
-      }
-    } else {
+    {
       if (threadIdx.x < 32 * kLocWalkWarps) {
         locSweep<0, kLocWalkWarps>(sm, nL);
         locSweep<1, kLocWalkWarps>(sm, nL);
@@ -584,6 +485,7 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
         for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
       }
     }
+    if (threadIdx.x == 0) sGroup = done ? prev / kLocGroup : -1;
     sum64<6>(d6, red);  // ends with a barrier: the next part may reuse the shared memory
     if (threadIdx.x == 0) {
       double* q = partials + 8 * (size_t)part;
@@ -593,103 +495,202 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
       sDesc[1] = sNextDesc[1];
     }
     __syncthreads();
+    if (sGroup >= 0 && threadIdx.x < 32) locGroupSum(partials, grec, gcnt, sGroup, mv.nParts);
+    prev = part;
     part = sTicket;
   }
-  locDecide(mv, c, st, partials, anyPend, smraw);
+  locFinish(mv, c, st, partials, prev, anyPend, red, &sGroup);
 }
 
-// The slot-table preconditioner with two parts per CTA at a time: both are
-// staged together and walked together (slotSweepPair), so each level's
-// latency serves two parts.  Per part the arithmetic and the order of its
-// sums are those of kLocPrecond, so the results are bit-identical to it.
-// Shared memory: two part regions of localSmemBytes (rounded to 16 bytes).
-// Resident blocks of the paired kernel: its two part regions bound it to
-// three CTAs per SM in FP32 and two in FP64, so registers are set for that.
-template <typename T>
-constexpr int pairMinBlocks() {
-  return sizeof(T) == 4 ? 3 : 2;
-}
-
-template <typename T, int NT, int RPT>
-__global__ void __launch_bounds__(NT, (pairMinBlocks<T>()))
-kLocPrecondPair(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partials) {
+// The slot-table preconditioner (hexahedral parts, HostPrep::locSlots): 64
+// threads per part, all of them walking.  Parts go to CTAs in a fixed
+// stride (CTA b takes b, b + G, ...); the next part's descriptor arrives by
+// cp.async with the current part's tables.  A thread keeps the updated
+// residual of its rows t, t + 64, ... (up to 8 rows) in registers, so the
+// shared memory holds only the tables and w, and eight FP32 parts (five
+// FP64) of 512 rows fit per SM.  After the walk w leaves in one coalesced
+// pass and each thread sums w.r and |r| over its rows in row order, then a
+// fixed tree: a part's record depends neither on the grid nor on RPT, so
+// every variant gives bit-identical results.
+template <typename T, int RPT>
+__global__ void __launch_bounds__(64, (sizeof(T) == 4 ? 8 : 5))
+kLocPrecondSlots(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partials) {
+  constexpr int NT = 64, KR = 8;
   p = casePcg(p, blockIdx.y, mv.nC);
   st += blockIdx.y;
   partials += (size_t)blockIdx.y * mv.caseRec;
   if (!st->pcgContinue) return;
   extern __shared__ __align__(16) unsigned char smraw[];
-  const size_t region = locRegionBytes<T>(mv);
-  const LocSmem<T> sa = locSmem<T>(mv, smraw);
-  const LocSmem<T> sb = locSmem<T>(mv, smraw + region);
-  __shared__ double red[2 * 12];
-  const T* __restrict__ pg = st->pbuf ? p.p2 : p.p;
+  const LocSmem<T> sm = slotSmem<T>(mv, smraw);
+  __shared__ double red[2 * 6];
+  __shared__ __align__(16) int4 sDesc[2][2];
+  __shared__ int sGroup;
+  double* grec = partials + mv.locGrpOff;
+  unsigned* gcnt = reinterpret_cast<unsigned*>(grec + 8 * (size_t)mv.locGroups);
+  // the vectors never alias one another
+  const T* __restrict__ pg = st->pbuf ? p.p2 : p.p;  // p of the pending iteration
+  const T* __restrict__ qg = p.q;
+  const T* __restrict__ rDg = p.rD;
+  T* __restrict__ xg = p.x;
+  T* __restrict__ rg = p.r;
   bool pend[3];
   T al[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) { pend[k] = st->pending[k] != 0; al[k] = (T)st->alpha[k]; }
   const bool anyPend = pend[0] || pend[1] || pend[2];
-  // tickets two at a time; the next pair's descriptors come ahead
-  __shared__ int sTicket, sNextTicket;
-  __shared__ int4 sDesc[4], sNextDesc[4];
-  if (threadIdx.x == 0) {
-    const int t0 = (int)atomicAdd(&st->locTicket, 2u);
-    sTicket = t0;
-    for (int j = 0; j < 2; ++j)
-      if (t0 + j < mv.nParts) {
-        sDesc[2 * j] = mv.locDesc[2 * (t0 + j)];
-        sDesc[2 * j + 1] = mv.locDesc[2 * (t0 + j) + 1];
-      }
+  const int t = (int)threadIdx.x;
+  const int nParts = mv.nParts;
+  if (t < 3) sm.w[3 * mv.maxRows + t] = T(0);  // the zero row of the padded slots
+  int part = (int)blockIdx.x;
+  if (t == 0 && part < nParts) {
+    cpAsync16(&sDesc[0][0], mv.locDesc + 2 * part);
+    cpAsync16(&sDesc[0][1], mv.locDesc + 2 * part + 1);
   }
+  cpAsyncWaitAll();
   __syncthreads();
-  for (int part = sTicket; part < mv.nParts;) {
-    const bool two = part + 1 < mv.nParts;
-    const int4 aA = sDesc[0], aB = sDesc[1];
-    int4 bA = aA, bB = aB;
-    if (two) { bA = sDesc[2]; bB = sDesc[3]; }
-    if (threadIdx.x == 0) {
-      const int nt = (int)atomicAdd(&st->locTicket, 2u);
-      sNextTicket = nt;
-      for (int j = 0; j < 2; ++j)
-        if (nt + j < mv.nParts) {
-          sNextDesc[2 * j] = mv.locDesc[2 * (nt + j)];
-          sNextDesc[2 * j + 1] = mv.locDesc[2 * (nt + j) + 1];
-        }
+  int prev = -1, buf = 0;
+  for (; part < nParts; part += (int)gridDim.x, buf ^= 1) {
+    const int4 dA = sDesc[buf][0], dB = sDesc[buf][1];
+    const int pLo = dA.x, nR = dA.y, eLo = dA.z, nE = dA.w;
+    const int l0 = dB.z, nL = dB.w;
+    const int next = part + (int)gridDim.x;
+    if (t == 0 && next < nParts) {
+      cpAsync16(&sDesc[buf ^ 1][0], mv.locDesc + 2 * next);
+      cpAsync16(&sDesc[buf ^ 1][1], mv.locDesc + 2 * next + 1);
     }
-    locStage<T, NT, RPT, true>(mv, p, sa, pg, pend, al, aA, aB);
-    if (two) locStage<T, NT, RPT, true>(mv, p, sb, pg, pend, al, bA, bB);
+    // static part tables in flight while the vectors stream
+    {
+      const int nc = nE * (int)sizeof(T) / 16;
+      const char* g = (const char*)(p.lcoef + eLo);
+      for (int k = t; k < nc; k += NT) cpAsync16((char*)sm.c + 16 * k, g + 16 * k);
+      const int ni = nE * 2 / 16;
+      const char* gi = (const char*)(mv.locIdx + eLo);
+      for (int k = t; k < ni; k += NT) cpAsync16((char*)sm.idx + 16 * k, gi + 16 * k);
+    }
+    for (int k = t; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
+    // pending update x += alpha p, r -= alpha q and w = rD r, RPT rows per
+    // thread with every load issued before any store.  Thread 0 reports the
+    // previous part's record on its group counter while the first loads are
+    // in flight.
+    bool done = false;
+    T rK[KR][3];
+    const bool regR = nR <= KR * NT;
+    if (regR) {
+#pragma unroll
+      for (int it = 0; it < KR / RPT; ++it) {
+        T qv[RPT][3], pv[RPT][3], xv[RPT][3], rd[RPT];
+#pragma unroll
+        for (int h = 0; h < RPT; ++h) {
+          const int j = it * RPT + h, i = t + j * NT;
+          if (i < nR) {
+            const size_t g = 3 * (size_t)(pLo + i);
+            rd[h] = rDg[pLo + i];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              rK[j][k] = rg[g + k];
+              if (pend[k]) { qv[h][k] = qg[g + k]; pv[h][k] = pg[g + k]; xv[h][k] = xg[g + k]; }
+            }
+          }
+        }
+        if (it == 0 && t == 0 && prev >= 0) done = locArrive(gcnt, prev, nParts);
+#pragma unroll
+        for (int h = 0; h < RPT; ++h) {
+          const int j = it * RPT + h, i = t + j * NT;
+          if (i < nR) {
+            const size_t g = 3 * (size_t)(pLo + i);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              if (pend[k]) {
+                xg[g + k] = xv[h][k] + al[k] * pv[h][k];
+                rK[j][k] -= al[k] * qv[h][k];
+                rg[g + k] = rK[j][k];
+              }
+              sm.w[3 * i + k] = rd[h] * rK[j][k];
+            }
+          }
+        }
+      }
+    } else {
+      if (t == 0 && prev >= 0) done = locArrive(gcnt, prev, nParts);
+      for (int i0 = t; i0 < nR; i0 += RPT * NT) {
+        T rv[RPT][3], qv[RPT][3], pv[RPT][3], xv[RPT][3], rd[RPT];
+#pragma unroll
+        for (int h = 0; h < RPT; ++h) {
+          const int i = i0 + h * NT;
+          if (i < nR) {
+            const size_t g = 3 * (size_t)(pLo + i);
+            rd[h] = rDg[pLo + i];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              rv[h][k] = rg[g + k];
+              if (pend[k]) { qv[h][k] = qg[g + k]; pv[h][k] = pg[g + k]; xv[h][k] = xg[g + k]; }
+            }
+          }
+        }
+#pragma unroll
+        for (int h = 0; h < RPT; ++h) {
+          const int i = i0 + h * NT;
+          if (i < nR) {
+            const size_t g = 3 * (size_t)(pLo + i);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+              if (pend[k]) {
+                xg[g + k] = xv[h][k] + al[k] * pv[h][k];
+                rv[h][k] -= al[k] * qv[h][k];
+                rg[g + k] = rv[h][k];
+              }
+              sm.w[3 * i + k] = rd[h] * rv[h][k];
+            }
+          }
+        }
+      }
+    }
     cpAsyncWaitAll();
     __syncthreads();
-    const int nLa = aB.w, nLb = two ? bB.w : 0;
-    T* __restrict__ wga = p.w + 3 * (size_t)aA.x;
-    T* __restrict__ wgb = p.w + 3 * (size_t)bA.x;
-    double d[12];
+    // forward then backward substitution (each level ends with a barrier of
+    // all 64 threads, so after the last one w is final for every thread)
+    slotWalk<0>(sm, nL);
+    slotWalk<1>(sm, nL);
+    // w out in one coalesced pass; w.r and sum|r| over the thread's rows
+    // t, t + 64, ... in row order
+    T* __restrict__ wg = p.w + 3 * (size_t)pLo;
+    for (int k = t; k < 3 * nR; k += NT) wg[k] = sm.w[k];
+    Acc<T> wr[3], ar[3];
+    if (regR) {
 #pragma unroll
-    for (int k = 0; k < 12; ++k) d[k] = 0;
-    if (threadIdx.x < 32 * kLocWalkWarps) {
-      Acc<T> wra[3], ara[3], wrb[3], arb[3];
-      slotSweepPair<0, kLocWalkWarps, false>(sa, nLa, wga, wra, ara, sb, nLb, wgb, wrb, arb);
-      slotSweepPair<1, kLocWalkWarps, true>(sa, nLa, wga, wra, ara, sb, nLb, wgb, wrb, arb);
+      for (int j = 0; j < KR; ++j) {
+        const int i = t + j * NT;
+        if (i < nR)
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        d[k] = wra[k].value(); d[3 + k] = ara[k].value();
-        d[6 + k] = wrb[k].value(); d[9 + k] = arb[k].value();
+          for (int k = 0; k < 3; ++k) {
+            wr[k].add(sm.w[3 * i + k] * rK[j][k]);
+            ar[k].add(fabs(rK[j][k]));
+          }
       }
+    } else {
+      // each thread reads back the residual rows it wrote itself
+      for (int i = t; i < nR; i += NT)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+          const T r = rg[3 * (size_t)(pLo + i) + k];
+          wr[k].add(sm.w[3 * i + k] * r);
+          ar[k].add(fabs(r));
+        }
     }
-    sum64<12>(d, red);  // ends with a barrier: the next parts may reuse the shared memory
-    if (threadIdx.x == 0) {
+    double d6[6];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { d6[k] = wr[k].value(); d6[3 + k] = ar[k].value(); }
+    if (t == 0) sGroup = done ? prev / kLocGroup : -1;
+    sum64<6>(d6, red);  // ends with a barrier: the next part may reuse the shared memory
+    if (t == 0) {
       double* q = partials + 8 * (size_t)part;
-      for (int k = 0; k < 6; ++k) q[k] = d[k];
-      if (two) {
-        q += 8;
-        for (int k = 0; k < 6; ++k) q[k] = d[6 + k];
-      }
-      sTicket = sNextTicket;
-      for (int j = 0; j < 4; ++j) sDesc[j] = sNextDesc[j];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) q[k] = d6[k];
     }
-    __syncthreads();
-    part = sTicket;
+    if (sGroup >= 0 && t < 32) locGroupSum(partials, grec, gcnt, sGroup, nParts);
+    prev = part;
   }
-  locDecide(mv, c, st, partials, anyPend, smraw);
+  locFinish(mv, c, st, partials, prev, anyPend, red, &sGroup);
 }
 
 // p_new = w (first iteration) or w + beta p_old, the same expression for a
@@ -877,73 +878,67 @@ kLocSpmvSplit(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   st->pcgContinue = any;
 }
 
-template <typename T, int NT, int RPT>
+// Generic tables: kLocPrecond with NT threads and RPT rows per thread in
+// flight; slot tables: kLocPrecondSlots (64 threads) with RPTS.
+template <typename T, int NT, int RPT, int RPTS>
 void launchPrecondV(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                     double* partials, int grid, cudaStream_t s, int nCases) {
   if (mv.locSlots)
-    kLocPrecond<T, NT, RPT, true><<<dim3(grid, nCases), NT, localSmemBytes<T>(mv), s>>>(
+    kLocPrecondSlots<T, RPTS><<<dim3(grid, nCases), 64, localSmemBytes<T>(mv), s>>>(
         mv, c, p, st, partials);
   else
-    kLocPrecond<T, NT, RPT, false><<<dim3(grid, nCases), NT, localSmemBytes<T>(mv), s>>>(
+    kLocPrecond<T, NT, RPT><<<dim3(grid, nCases), NT, localSmemBytes<T>(mv), s>>>(
         mv, c, p, st, partials);
 }
 
-template <typename T>
-size_t pairSmemBytes(const MeshView& mv) {
-  return 2 * locRegionBytes<T>(mv);
-}
-
-template <typename T, int NT, int RPT>
-void launchPrecondPair(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
-                       double* partials, int grid, cudaStream_t s, int nCases) {
-  kLocPrecondPair<T, NT, RPT><<<dim3(grid, nCases), NT, pairSmemBytes<T>(mv), s>>>(mv, c, p, st,
-                                                                                  partials);
-}
-
-template <typename T, int NT, int RPT, bool SLOT>
-cudaError_t prepareK(const MeshView& mv, int* blocksPerSM) {
-  const int sm = (int)localSmemBytes<T>(mv);
-  cudaError_t e = setMaxDynamicSmem(kLocPrecond<T, NT, RPT, SLOT>);
-  if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, NT, RPT, SLOT>,
-                                                       NT, sm);
-}
-
-template <typename T, int NT, int RPT>
+template <typename T, int NT, int RPT, int RPTS>
 cudaError_t prepareV(const MeshView& mv, int* blocksPerSM) {
-  return mv.locSlots ? prepareK<T, NT, RPT, true>(mv, blocksPerSM)
-                     : prepareK<T, NT, RPT, false>(mv, blocksPerSM);
-}
-
-template <typename T, int NT, int RPT>
-cudaError_t preparePair(const MeshView& mv, int* blocksPerSM) {
-  cudaError_t e = setMaxDynamicSmem(kLocPrecondPair<T, NT, RPT>);
+  const int sm = (int)localSmemBytes<T>(mv);
+  if (mv.locSlots) {
+    cudaError_t e = setMaxDynamicSmem(kLocPrecondSlots<T, RPTS>);
+    if (e != cudaSuccess) return e;
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecondSlots<T, RPTS>, 64,
+                                                         sm);
+  }
+  cudaError_t e = setMaxDynamicSmem(kLocPrecond<T, NT, RPT>);
   if (e != cudaSuccess) return e;
-  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecondPair<T, NT, RPT>, NT,
-                                                       (int)pairSmemBytes<T>(mv));
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocksPerSM, kLocPrecond<T, NT, RPT>,
+                                                       NT, sm);
 }
 
 }  // namespace
 
-// Preconditioner variants.  Slot-table meshes: one part per CTA at a time
-// (0) or two walked together (1); other meshes: 4 (FP32) or 2 (FP64) rows
-// per thread in flight while streaming (0), or half that (1).  All give
-// bit-identical results.  perf.part_threads reports 128 threads per CTA.
-const int kLocVariantsNT[kLocNumNT] = {128, 128};
+// Preconditioner variants (threads per part x rows per thread in flight at
+// once).  Generic tables: FP32 {128 x 4, 64 x 4}, FP64 {128 x 2, 64 x 2};
+// the second of each pair has all its threads walking and half the threads
+// per CTA, so more parts are walked at once per SM where shared memory
+// allows.  Slot tables: 64 threads with FP32 {2, 4} and FP64 {1, 2} rows in
+// flight (the first without register spills).  perf.part_threads reports the threads of the one in use.
+const int kLocVariantsNT[kLocNumNT] = {128, 64};
 const int kLocVariantsU[kLocNumU] = {1, 6, 0};
+
+int localPartThreads(const MeshView& mv, int variant) {
+  return mv.locSlots ? 64 : kLocVariantsNT[variant];
+}
 
 template <typename T>
 size_t localSmemBytes(const MeshView& mv) {
-  return locRegionBytes<T>(mv);
+  const size_t P = mv.maxRows, EL = mv.maxLocEntries, ML = mv.maxLocMeta;
+  if (mv.locSlots)  // coefficients, columns, w with its zero row, level starts
+    return sizeof(T) * (EL + 3 * P + 3) + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
+  const size_t tables = sizeof(T) * (EL + 6 * P + 3) + 4 * ML + 2 * EL + sizeof(int) * (mv.maxLevels + 1);
+  return std::max(tables, (size_t)256 * 6 * sizeof(double));  // final reduction scratch
 }
 
 template <typename T>
 cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM) {
-  constexpr int R0 = sizeof(T) == 4 ? 4 : 2, R1 = sizeof(T) == 4 ? 2 : 1;
-  cudaError_t e = prepareV<T, 128, R0>(mv, &blocksPerSM[0]);
-  if (e != cudaSuccess) return e;
-  if (mv.locSlots) return preparePair<T, 128, R0>(mv, &blocksPerSM[1]);
-  return prepareV<T, 128, R1>(mv, &blocksPerSM[1]);
+  if constexpr (sizeof(T) == 4) {
+    cudaError_t e = prepareV<T, 128, 4, 2>(mv, &blocksPerSM[0]);
+    return e != cudaSuccess ? e : prepareV<T, 64, 4, 4>(mv, &blocksPerSM[1]);
+  } else {
+    cudaError_t e = prepareV<T, 128, 2, 1>(mv, &blocksPerSM[0]);
+    return e != cudaSuccess ? e : prepareV<T, 64, 2, 2>(mv, &blocksPerSM[1]);
+  }
 }
 
 template <typename T>
@@ -954,12 +949,12 @@ void launchLocalGather(int n, const int* src, const double* rDa, T* lcoef, cudaS
 template <typename T>
 void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                         double* partials, const LocalTuning& t, cudaStream_t s, int nCases) {
-  constexpr int R0 = sizeof(T) == 4 ? 4 : 2, R1 = sizeof(T) == 4 ? 2 : 1;
-  if (t.ntIdx == 1) {
-    if (mv.locSlots) launchPrecondPair<T, 128, R0>(mv, c, p, st, partials, t.grid[1], s, nCases);
-    else launchPrecondV<T, 128, R1>(mv, c, p, st, partials, t.grid[1], s, nCases);
+  if constexpr (sizeof(T) == 4) {
+    if (t.ntIdx == 1) launchPrecondV<T, 64, 4, 4>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    else launchPrecondV<T, 128, 4, 2>(mv, c, p, st, partials, t.grid[0], s, nCases);
   } else {
-    launchPrecondV<T, 128, R0>(mv, c, p, st, partials, t.grid[0], s, nCases);
+    if (t.ntIdx == 1) launchPrecondV<T, 64, 2, 2>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    else launchPrecondV<T, 128, 2, 1>(mv, c, p, st, partials, t.grid[0], s, nCases);
   }
 }
 

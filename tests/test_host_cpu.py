@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol(built):
     for n in names:
         assert hasattr(L, n), n
     assert set(names) == set(_lib.declared_symbols())
-    assert L.s4g_abi_version() == 5
+    assert L.s4g_abi_version() == 6
     assert L.s4g_status_str(_lib.NOT_CONVERGED) == b"NOT_CONVERGED"
 
 
@@ -272,6 +272,15 @@ def test_caller_decomposition_plan(built):
     assert info["n_parts"] == 16 and np.array_equal(perm, np.arange(16 * 8 * 8))
     # in-part levels of a 4^3 block in lexicographic order: i + j + k
     assert info["max_local_levels"] == 10
+    # lexicographic blocks: at most three lower and three upper neighbours
+    # per row, so the fixed-slot tables; a shuffled cell order within the
+    # parts needs the generic tables
+    assert info["local_slots"] == 1
+    from oracle.pyoracle import renumber_mesh
+    shuffle = np.random.default_rng(1).permutation(16 * 8 * 8)
+    _, info2 = plan(renumber_mesh(m, shuffle), renumber="none", dic_subdomains=True,
+                    parts=parts[shuffle])
+    assert info2["n_parts"] == 16 and info2["local_slots"] == 0
     for kw in (dict(renumber="tiled", dic_subdomains=True), dict(renumber="none")):
         with pytest.raises(_lib.S4GError, match="part_of_cell"):
             plan(m, parts=parts, **kw)
