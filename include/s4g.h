@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define S4G_ABI_VERSION 6
+#define S4G_ABI_VERSION 7
 
 /* Status codes.  Reference convention for errors is FatalError (abort), see
  * src/solids4FoamModels/solidModels/solidModel/solidModel.C:1735-1742; a
@@ -271,8 +271,11 @@ typedef struct s4g_outer {
                               "fixed", solidModel.C:837-841); f in (0, 1],
                               0 or 1: no relaxation */
   int relaxation_method;   /* <model>Coeffs relaxationMethod: 0 fixed, 1
-                              Aitken (solidModel.C:842-896, field_relaxation
-                              then gives the first corrector's factor) */
+                              Aitken (solidModel.C:842-896): a factor per
+                              cell and boundary face, field_relaxation (or 1)
+                              at each increment's first corrector, then
+                              alpha (r_prev . dr) / (|dr|^2 + SMALL) bounded
+                              to [0, 2], r = D.prevIter - D; D -= alpha r */
 } s4g_outer;
 
 typedef enum s4g_precision {
@@ -315,9 +318,9 @@ typedef struct s4g_perf {
   int spmv_unroll;            /* processor-local PCG: SpMV form in use: entries
                                  unrolled in the fused p-update + SpMV (1 or
                                  6), or 0 for the split form */
-  double tune_us[6];          /* autotuner timings (us): the preconditioner,
-                                 then the SpMV step plain/unrolled/split;
-                                 the rest 0 */
+  double tune_us[6];          /* autotuner timings (us): the two
+                                 preconditioner variants, then the SpMV
+                                 step plain/unrolled/split; the rest 0 */
   /* per kernel kind (S4G_K_*), only with s4g_ctx_opts.profile: summed
    * CUDA-event time and number of launches that did work */
   double kernel_ms[S4G_K_KINDS];
@@ -336,6 +339,24 @@ typedef struct s4g_perf {
  * models named above, with tractionBoundarySnGrad evaluated on the device. */
 s4g_status s4g_solve(s4g_mesh* mesh, s4g_model model, int n_increments,
                      double* D_out, double* sigma_out, s4g_perf* perf);
+
+/* One time step: the solid model's evolve() as solids4Foam's time loop calls
+ * it once per step (applications/solvers/solids4Foam/solids4Foam.C:58 ->
+ * solidModel::evolve, solidModel.H:759), with the boundary values last set
+ * by s4g_bc_set taken as they are (load factor 1: the caller evaluates its
+ * load series, e.g. tractionSeries, at the step's time).  The step starts
+ * from the state the previous step of the same model left on the device:
+ * the linear model takes that step's D as D.oldTime; the total Lagrangian
+ * forms continue from their shifted old-time fields.  The first step, a step
+ * after s4g_state_reset, s4g_solve, s4g_solve_cases or s4g_solve_batch, or a
+ * step of another model starts from zero.  A sequence of steps with boundary
+ * values (n/N) b equals s4g_solve with N increments.  perf counts this
+ * step's correctors and PCG iterations. */
+s4g_status s4g_solve_step(s4g_mesh* mesh, s4g_model model, double* D_out, double* sigma_out,
+                          s4g_perf* perf);
+/* Forget the state s4g_solve_step continues from: the next step starts from
+ * zero. */
+s4g_status s4g_state_reset(s4g_mesh* mesh);
 
 /* Batched load cases: n_cases independent solves of the
  * linearGeometryTotalDisplacement model on this mesh, advanced together with
@@ -589,13 +610,30 @@ s4g_status s4g_foam_bc(const s4g_foam_case* fc, int patch, s4g_bc_type* type,
                        const double** vec3, const double** pressure,
                        double* relaxation_factor);
 /* Load series read by s4g_foam_read_d: tractionSeries, pressureSeries and
- * displacementSeries are accepted when they are linear ramps from zero at
- * time 0 (any other table is S4G_BAD_ARG).  Such a series is what the load
- * increments of s4g_solve apply (load factor n/N over n_increments), and
- * s4g_foam_bc returns its end value.  end_time: the ramps' common end time,
- * 0 if the case has none; constant_loads: 1 if a constant nonzero load sits
- * beside them (the increments would ramp it as well). */
+ * displacementSeries (interpolationTable files of (time value) pairs,
+ * linear interpolation; outOfBounds clamp, warn, error or repeat;
+ * solidTraction...C:105-193,357-369, fixedDisplacement...C:174-185).
+ * s4g_foam_bc returns a series' end value.  When every series is a linear
+ * ramp from zero at time 0 and they end together, the load increments of
+ * s4g_solve apply them (load factor n/N): end_time is that end, and
+ * constant_loads is 1 if a constant nonzero load sits beside them (the
+ * increments would ramp it as well).  Otherwise end_time is 0: a case with
+ * other tables is stepped in time (s4g_foam_apply_bcs_at, s4g_solve_step). */
 s4g_status s4g_foam_load_ramp(const s4g_foam_case* fc, double* end_time, int* constant_loads);
+/* kind: 0 no load series, 1 linear ramps from zero with a common end (see
+ * s4g_foam_load_ramp), 2 other tables. */
+s4g_status s4g_foam_series_kind(const s4g_foam_case* fc, int* kind);
+/* The condition of a patch at a time: the series evaluated at `time` as
+ * the reference's boundary conditions evaluate them at the time step's time
+ * (tractionSeries_(time) etc.), constant values as read.  vec3
+ * [patch_size][3] (value or traction) and pressure [patch_size] are the
+ * caller's buffers (either may be NULL).  A time outside a series with
+ * outOfBounds error is S4G_BAD_ARG. */
+s4g_status s4g_foam_bc_at(const s4g_foam_case* fc, int patch, double time, s4g_bc_type* type,
+                          double* vec3, double* pressure, double* relaxation_factor);
+/* s4g_bc_set and s4g_bc_set_relaxation on every patch with the conditions
+ * at `time` (s4g_foam_bc_at): the boundary values of one time step. */
+s4g_status s4g_foam_apply_bcs_at(const s4g_foam_case* fc, s4g_mesh* mesh, double time);
 /* startTime (default 0), endTime and deltaT of a system/controlDict: the
  * time steps the reference's loop takes, which a caller maps to load
  * increments, (endTime - startTime) / deltaT. */

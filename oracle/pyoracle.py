@@ -57,6 +57,7 @@ class Settings(ct.Structure):
         ("n_threads", ct.c_int), ("max_correctors_run", ct.c_int),
         ("dic_domain", ct.c_void_p), ("max_seconds", ct.c_double),
         ("empty_direction", ct.c_int), ("field_relaxation", ct.c_double),
+        ("relaxation_method", ct.c_int),
     ]
 
 

@@ -524,6 +524,11 @@ struct Solver {
   std::vector<T9> FL, FLb, FL0, FL0b;  // TL: law's F and F.oldTime
   std::vector<S6> sig0, sig0b;
   bool enforceLinear = false;
+  // Aitken relaxation (solidModel.C:842-896): aitkenAlpha and aitkenResidual,
+  // volScalarField 1 and volVectorField 0 at construction (calculated
+  // patches: cells and every boundary face)
+  std::vector<double> aitA, aitAb;
+  std::vector<V3> aitR, aitRb;
 
   Ldu A;
   Dic dic;
@@ -797,6 +802,37 @@ struct Solver {
     }
   }
 
+  // relaxField "Aitken" (solidModel.C:842-896) on the solved field:
+  // r = D.prevIter - D; at iCorr 0 alpha = the field's relaxation factor
+  // (1 without one), else alpha = alpha (r_prev . dr) / (|dr|^2 + SMALL),
+  // dr = r_prev - r, bounded to [0, 2]; then D -= alpha r.  GeometricField
+  // arithmetic gives every boundary face the same update from its own
+  // values; the -= leaves fixed-value (fixedDisplacement) faces as they are.
+  void aitken(int iCorr, const std::vector<V3>& prev, const std::vector<V3>& prevB) {
+    if (aitA.empty()) {
+      aitA.assign(m.nC, 1.0); aitAb.assign(m.nB, 1.0);
+      aitR.assign(m.nC, V3{0, 0, 0}); aitRb.assign(m.nB, V3{0, 0, 0});
+    }
+    const double a0 = (s.field_relaxation > 0 && s.field_relaxation != 1.0) ? s.field_relaxation : 1.0;
+    auto step = [&](double& a, V3& rPrev, V3& u, const V3& p, bool apply) {
+      const V3 r = p - u;
+      if (iCorr == 0) {
+        a = a0;
+      } else {
+        const V3 dr = rPrev - r;
+        const double num = rPrev.x * dr.x + rPrev.y * dr.y + rPrev.z * dr.z;
+        const double den = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z + SMALL;
+        a = a * num / den;
+        a = std::max(0.0, std::min(2.0, a));
+      }
+      rPrev = r;
+      if (apply) u = u - a * r;
+    };
+    for (int c = 0; c < m.nC; ++c) step(aitA[c], aitR[c], U[c], prev[c], true);
+    for (int b = 0; b < m.nB; ++b)
+      step(aitAb[b], aitRb[b], Ub[b], prevB[b], patchType(b) != ORC_FIXED_DISPLACEMENT);
+  }
+
   // One call of the model's evolve() for the current load factor.
   bool evolve(int& correctorsLeft) {
     int iCorr = 0;
@@ -836,7 +872,9 @@ struct Solver {
       // relaxation factor, D == D.prevIter + f (D - D.prevIter) on the cells
       // and, by the forced assignment, on every boundary face
       const double fr = s.field_relaxation;
-      if (fr > 0 && fr != 1.0) {
+      if (s.relaxation_method == 1) {
+        aitken(iCorr, prev, prevB);
+      } else if (fr > 0 && fr != 1.0) {
         for (int c = 0; c < m.nC; ++c) U[c] = prev[c] + fr * (U[c] - prev[c]);
         for (int b = 0; b < m.nB; ++b) Ub[b] = prevB[b] + fr * (Ub[b] - prevB[b]);
       }

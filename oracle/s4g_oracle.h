@@ -83,6 +83,11 @@ typedef struct {
                              after each solve D == D.prevIter + f (D - D.prevIter),
                              cells and boundary faces (solidModel.C:837-841,
                              GeometricField::relax); 0 or 1: none */
+  int relaxation_method;  /* 0 "fixed" (field_relaxation above); 1 "Aitken"
+                             (solidModel.C:842-896): a per-cell (and per
+                             boundary face) factor alpha, field_relaxation
+                             (or 1) at the first corrector of each
+                             increment */
 } orc_settings;
 
 typedef struct {

@@ -142,6 +142,9 @@ _SIGS = {
     "s4g_default_controls": (None, [ct.POINTER(LinSolver), ct.POINTER(Outer)]),
     "s4g_solve": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_int, ct.c_void_p, ct.c_void_p,
                              ct.POINTER(Perf)]),
+    "s4g_solve_step": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p,
+                                  ct.POINTER(Perf)]),
+    "s4g_state_reset": (ct.c_int, [ct.c_void_p]),
     "s4g_get_gradD": (ct.c_int, [ct.c_void_p, ct.c_void_p]),
     "s4g_solve_batch": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p, ct.c_void_p]),
     "s4g_mesh_set_points": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_void_p, ct.c_void_p,
@@ -189,6 +192,10 @@ _SIGS = {
     "s4g_foam_load_ramp": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_double),
                                       ct.POINTER(ct.c_int)]),
     "s4g_foam_read_time": (ct.c_int, [ct.c_char_p] + [ct.POINTER(ct.c_double)] * 3),
+    "s4g_foam_series_kind": (ct.c_int, [ct.c_void_p, ct.POINTER(ct.c_int)]),
+    "s4g_foam_bc_at": (ct.c_int, [ct.c_void_p, ct.c_int, ct.c_double, ct.POINTER(ct.c_int),
+                                  ct.c_void_p, ct.c_void_p, ct.POINTER(ct.c_double)]),
+    "s4g_foam_apply_bcs_at": (ct.c_int, [ct.c_void_p, ct.c_void_p, ct.c_double]),
     "s4g_foam_read_relaxation": (ct.c_int, [ct.c_char_p, ct.c_char_p, ct.POINTER(ct.c_double),
                                             ct.POINTER(ct.c_double)]),
     "s4g_foam_read_grad_scheme": (ct.c_int, [ct.c_char_p, ct.c_char_p, ct.POINTER(ct.c_int)]),

@@ -195,23 +195,30 @@ def served_stream(n_requests=24, seed=5, min_cells=8 ** 3, max_cells=96 ** 3, tl
     return out
 
 
-def mesh_batch(n_meshes=256, seed=4, block=8):
+def mesh_batch(n_meshes=256, seed=4, block=8, max_aspect=2.0, nu_max=0.4):
     """Many independent meshes solved in one launch: jittered boxes with nx,
-    ny, nz uniform integers in [10, 48], physical extents with the longest
-    over the shortest side uniform in [1, 4], E log-uniform in 1-300 GPa,
-    nu uniform in 0.2-0.45 (relaxed_outer, as the served stream), bottom fixed and a top traction N(0, 1 MPa) per
-    component.  Each case carries its block decomposition.  Returns a list
-    of dict(mesh, law, bcs, outer, parts)."""
+    ny, nz uniform integers in [10, 48] whose largest is at most max_aspect
+    times the smallest (redrawn otherwise), with near-cubic cells (physical
+    extents in proportion to the cell counts), E log-uniform in 1-300 GPa,
+    nu uniform in 0.2-nu_max (relaxed_outer, as the served stream), bottom
+    fixed and a top traction N(0, 1 MPa) per component.  The segregated
+    corrector loop -- the reference's algorithm, as the oracle restates it
+    -- runs away or needs more than 8000 correctors on slender boxes under
+    shear (4:1 at nu = 0.42, relaxed or not) and on cells of high aspect
+    ratio, hence the bounds.  Each case carries its block decomposition.
+    Returns a list of dict(mesh, law, bcs, outer, parts)."""
     rng = np.random.default_rng(seed)
     out = []
     for i in range(n_meshes):
-        nx, ny, nz = (int(v) for v in rng.integers(10, 49, 3))
-        ratio = rng.uniform(1.0, 4.0)
-        ext = np.array([1.0, rng.uniform(1.0, ratio), ratio])
-        rng.shuffle(ext)
-        mesh = box_mesh(nx, ny, nz, ext[0], ext[1], ext[2], 0.2, 1000 + i)
+        while True:
+            n = rng.integers(10, 49, 3)
+            if n.max() <= max_aspect * n.min():
+                break
+        nx, ny, nz = (int(v) for v in n)
+        L = float(n.max())
+        mesh = box_mesh(nx, ny, nz, nx / L, ny / L, nz / L, 0.2, 1000 + i)
         E = np.exp(rng.uniform(np.log(1e9), np.log(300e9)))
-        nu = rng.uniform(0.2, 0.45)
+        nu = rng.uniform(0.2, nu_max)
         tr = rng.normal(0.0, 1e6, 3)
         out.append(dict(mesh=mesh, law=dict(type="linearElastic", E=E, nu=nu),
                         bcs={"zmin": ("fixedDisplacement", None, None),

@@ -50,17 +50,29 @@ struct s4g_foam_case {
   // writers, and emptyDir (1, 2, 3: x, y, z; 0: 3-D) is their normal
   std::vector<std::string> emptyPatches;
   int emptyDir = 0;
+  // A load series: an interpolationTable, (time value) pairs with
+  // increasing times, linear between them; outside its range by its
+  // outOfBounds (clamp, OpenFOAM's default, and warn: the end values; error:
+  // refused; repeat: periodic).  Empty t: no series (a constant load).
+  struct Series {
+    int width = 0;
+    int bounds = 0;  // 0 clamp or warn, 1 error, 2 repeat
+    std::vector<double> t, v;
+    std::string name;
+  };
   // D boundary conditions, per patch
   struct Bc {
     bool set = false;
     s4g_bc_type type = S4G_SOLID_TRACTION;
-    std::vector<double> vec3, pressure;
+    std::vector<double> vec3, pressure;  // constant values, or a series' end value
     double relax = 1.0;
+    Series vecSeries, presSeries;        // traction or displacement; pressure
   };
   std::vector<Bc> bcs;
-  // load series read from the D file (linear ramps from zero)
-  double rampEnd = 0;              // their common end time; 0: none
+  // load series read from the D file
+  double rampEnd = 0;              // linear ramps from zero: their common end time; 0: none
   bool constantBesideRamp = false; // a constant nonzero load beside them
+  int seriesKind = 0;              // 0 none, 1 all linear ramps from zero, 2 other tables
 };
 
 namespace {
@@ -741,11 +753,11 @@ struct Ramp {
   std::vector<double> value;  // the value at the end, width 1 or 3
 };
 
-// A time series (interpolationTable, read from its file as a list of
-// (time value) pairs) that is a linear ramp from zero: value(0) = 0 and
-// every point on the line to the last one.  Such a series is what the
-// load increments apply (load factor n/N); any other is rejected.
-Ramp readRamp(const Entry& series, int width, const std::string& caseDir, const std::string& where) {
+// A load series (interpolationTable) read from its file; ramp says whether
+// it is a linear ramp from zero at time 0 -- what the load increments apply
+// (load factor n/N) -- with its end time and end value.
+s4g_foam_case::Series readSeries(const Entry& series, int width, const std::string& caseDir,
+                                 const std::string& where, bool* ramp, Ramp* r) {
   if (!series.isDict) fail(where + ": " + series.key + " must be a dictionary");
   const Entry* f = lookup(series.sub, "file");
   if (!f) f = lookup(series.sub, "fileName");
@@ -753,39 +765,75 @@ Ramp readRamp(const Entry& series, int width, const std::string& caseDir, const 
   if (const Entry* is = lookup(series.sub, "interpolationScheme"))
     if (!is->val.empty() && is->val[0].s != "linear")
       fail(where + ": " + series.key + ": interpolationScheme " + is->val[0].s + " is not built");
+  s4g_foam_case::Series out;
+  out.width = width;
+  out.name = where + ": " + series.key;
+  if (const Entry* ob = lookup(series.sub, "outOfBounds")) {
+    const std::string b = ob->val.empty() ? std::string() : ob->val[0].s;
+    if (b == "clamp" || b == "warn") out.bounds = 0;
+    else if (b == "error") out.bounds = 1;
+    else if (b == "repeat") out.bounds = 2;
+    else fail(where + ": " + series.key + ": outOfBounds " + b + " is unknown (clamp, warn, error, repeat)");
+  }
   const std::string file = expandCase(f->val[0].s, caseDir);
   std::vector<Tok> t = payload(file);
   Cursor c{t, 0, file};
-  std::vector<double> times, vals;
   parseList(c, [&](Cursor& cc) {
     cc.expect('(');
-    times.push_back(toDouble(cc.next(), cc.where));
+    out.t.push_back(toDouble(cc.next(), cc.where));
     if (width == 3) {
       P3 v = parseVector(cc);
-      vals.push_back(v.x); vals.push_back(v.y); vals.push_back(v.z);
+      out.v.push_back(v.x); out.v.push_back(v.y); out.v.push_back(v.z);
     } else {
-      vals.push_back(toDouble(cc.next(), cc.where));
+      out.v.push_back(toDouble(cc.next(), cc.where));
     }
     cc.expect(')');
   });
-  const size_t n = times.size();
+  const size_t n = out.t.size();
   if (n < 2) fail(file + ": a series needs at least two points");
-  Ramp r;
-  r.end = times[n - 1];
-  r.value.assign(vals.end() - width, vals.end());
+  for (size_t i = 1; i < n; ++i)
+    if (!(out.t[i] > out.t[i - 1])) fail(file + ": times must increase");
+  r->end = out.t[n - 1];
+  r->value.assign(out.v.end() - width, out.v.end());
   double scale = 0;
-  for (double v : r.value) scale = std::max(scale, std::fabs(v));
-  for (size_t i = 0; i < n; ++i) {
-    if (i > 0 && !(times[i] > times[i - 1])) fail(file + ": times must increase");
+  for (double v : r->value) scale = std::max(scale, std::fabs(v));
+  *ramp = out.t[0] == 0.0;
+  for (size_t i = 0; i < n && *ramp; ++i)
     for (int k = 0; k < width; ++k) {
-      const double expect = r.value[(size_t)k] * (times[i] / r.end);
-      if (std::fabs(vals[i * width + k] - expect) > 1e-12 * scale + (i == 0 ? 0.0 : 1e-300))
-        fail(where + ": " + series.key + " (" + file +
-             ") is not a linear ramp from zero at time 0; only such series are built");
+      const double expect = r->value[(size_t)k] * (out.t[i] / r->end);
+      if (std::fabs(out.v[i * width + k] - expect) > 1e-12 * scale + (i == 0 ? 0.0 : 1e-300))
+        *ramp = false;
     }
+  return out;
+}
+
+// The series at time x (linear interpolation between its points).
+void seriesAt(const s4g_foam_case::Series& s, double x, double* out) {
+  const size_t n = s.t.size();
+  const int w = s.width;
+  const double t0 = s.t[0], t1 = s.t[n - 1];
+  if (s.bounds == 2 && (x < t0 || x > t1)) {
+    const double span = t1 - t0;
+    x = t0 + std::fmod(x - t0, span);
+    if (x < t0) x += span;
+  } else if (s.bounds == 1 && (x < t0 || x > t1)) {
+    fail(s.name + ": time " + std::to_string(x) + " is outside the series (outOfBounds error)");
   }
-  if (times[0] != 0.0) fail(where + ": " + series.key + " must start at time 0");
-  return r;
+  if (x <= t0) {
+    for (int k = 0; k < w; ++k) out[k] = s.v[(size_t)k];
+    return;
+  }
+  if (x >= t1) {
+    for (int k = 0; k < w; ++k) out[k] = s.v[(n - 1) * w + k];
+    return;
+  }
+  const size_t hi = (size_t)(std::upper_bound(s.t.begin(), s.t.end(), x) - s.t.begin());
+  const size_t lo = hi - 1;
+  const double f = (x - s.t[lo]) / (s.t[hi] - s.t[lo]);
+  for (int k = 0; k < w; ++k) {
+    const double a = s.v[lo * w + k], b = s.v[hi * w + k];
+    out[k] = a + f * (b - a);
+  }
 }
 
 void readD(s4g_foam_case& m, const std::string& path) {
@@ -802,11 +850,22 @@ void readD(s4g_foam_case& m, const std::string& path) {
   }
   std::vector<s4g_foam_case::Bc> bcs(m.patchName.size());
   double rampEnd = 0;
-  bool anyRamp = false, anyConstantLoad = false;
-  auto ramped = [&](const Ramp& r, const std::string& where) {
-    if (anyRamp && r.end != rampEnd) fail(where + ": load series end at different times");
-    anyRamp = true;
-    rampEnd = r.end;
+  bool anyRamp = false, anyConstantLoad = false, anyTable = false, rampsDiffer = false;
+  // a series that is a linear ramp from zero, with the others' end time, is
+  // what the load increments apply; any other table is stepped in time
+  auto series = [&](const Entry& e, int width, const std::string& where,
+                    s4g_foam_case::Series& keep) {
+    bool ramp = false;
+    Ramp r;
+    keep = readSeries(e, width, caseDir, where, &ramp, &r);
+    if (ramp) {
+      if (anyRamp && r.end != rampEnd) rampsDiffer = true;
+      anyRamp = true;
+      rampEnd = r.end;
+    } else {
+      anyTable = true;
+    }
+    return r;
   };
   auto nonzero = [](const std::vector<double>& v) {
     for (double x : v)
@@ -840,8 +899,7 @@ void readD(s4g_foam_case& m, const std::string& path) {
     if (type == "fixedDisplacement") {
       bc.type = S4G_FIXED_DISPLACEMENT;
       if (const Entry* ds = find(e->sub, "displacementSeries")) {
-        Ramp r = readRamp(*ds, 3, caseDir, where);
-        ramped(r, where);
+        Ramp r = series(*ds, 3, where, bc.vecSeries);
         bc.vec3 = tile(r.value);
       } else {
         const Entry* v = find(e->sub, "value");
@@ -855,16 +913,15 @@ void readD(s4g_foam_case& m, const std::string& path) {
       for (const char* q : {"traction", "pressure"}) {
         const std::string k(q);
         const Entry* plain = find(e->sub, k);
-        const Entry* series = find(e->sub, k + "Series");
+        const Entry* ser = find(e->sub, k + "Series");
         const Entry* field = find(e->sub, k + "Field");
-        if ((plain != nullptr) + (series != nullptr) + (field != nullptr) > 1)
+        if ((plain != nullptr) + (ser != nullptr) + (field != nullptr) > 1)
           fail(where + ": only one of " + k + ", " + k + "Series or " + k + "Field can be specified");
         if (field) fail(where + ": " + k + "Field is not built");
         std::vector<double>& out = k == "traction" ? bc.vec3 : bc.pressure;
         const int width = k == "traction" ? 3 : 1;
-        if (series) {
-          Ramp r = readRamp(*series, width, caseDir, where);
-          ramped(r, where);
+        if (ser) {
+          Ramp r = series(*ser, width, where, k == "traction" ? bc.vecSeries : bc.presSeries);
           out = tile(r.value);
         } else {
           if (!plain) fail(where + ": solidTraction needs " + k);
@@ -882,8 +939,10 @@ void readD(s4g_foam_case& m, const std::string& path) {
     }
   }
   m.bcs = std::move(bcs);
-  m.rampEnd = anyRamp ? rampEnd : 0.0;
-  m.constantBesideRamp = anyRamp && anyConstantLoad;
+  // ramps that end at different times are stepped in time like tables
+  m.seriesKind = (anyTable || rampsDiffer) ? 2 : anyRamp ? 1 : 0;
+  m.rampEnd = m.seriesKind == 1 ? rampEnd : 0.0;
+  m.constantBesideRamp = m.seriesKind == 1 && anyConstantLoad;
 }
 
 // ------------------------------------------------------------- writer ---
@@ -1219,6 +1278,67 @@ s4g_status s4g_foam_load_ramp(const s4g_foam_case* m, double* end_time, int* con
   if (!m) return S4G_BAD_ARG;
   if (end_time) *end_time = m->rampEnd;
   if (constant_loads) *constant_loads = m->constantBesideRamp ? 1 : 0;
+  return S4G_OK;
+}
+
+s4g_status s4g_foam_series_kind(const s4g_foam_case* m, int* kind) {
+  if (!m || !kind) return S4G_BAD_ARG;
+  *kind = m->seriesKind;
+  return S4G_OK;
+}
+
+s4g_status s4g_foam_bc_at(const s4g_foam_case* m, int p, double time, s4g_bc_type* type,
+                          double* vec3, double* pressure, double* relaxation_factor) {
+  if (!m || p < 0 || p >= (int)m->bcs.size()) return S4G_BAD_ARG;
+  const s4g_foam_case::Bc& bc = m->bcs[(size_t)p];
+  if (!bc.set) {
+    s4g::setLastError("no D file has been read for this case");
+    return S4G_BAD_ARG;
+  }
+  return guarded([&] {
+    const size_t n = (size_t)m->patchSize[(size_t)p];
+    if (type) *type = bc.type;
+    if (relaxation_factor) *relaxation_factor = bc.relax;
+    if (vec3) {
+      if (bc.vecSeries.t.empty()) {
+        std::copy(bc.vec3.begin(), bc.vec3.end(), vec3);
+      } else {
+        double v[3];
+        seriesAt(bc.vecSeries, time, v);
+        for (size_t i = 0; i < n; ++i)
+          for (int k = 0; k < 3; ++k) vec3[3 * i + k] = v[k];
+      }
+    }
+    if (pressure && bc.type == S4G_SOLID_TRACTION) {
+      if (bc.presSeries.t.empty()) {
+        std::copy(bc.pressure.begin(), bc.pressure.end(), pressure);
+      } else {
+        double v;
+        seriesAt(bc.presSeries, time, &v);
+        for (size_t i = 0; i < n; ++i) pressure[i] = v;
+      }
+    }
+  });
+}
+
+s4g_status s4g_foam_apply_bcs_at(const s4g_foam_case* m, s4g_mesh* mesh, double time) {
+  if (!m || !mesh) return S4G_BAD_ARG;
+  std::vector<double> v, pr;
+  for (size_t p = 0; p < m->bcs.size(); ++p) {
+    const size_t n = (size_t)m->patchSize[p];
+    v.assign(3 * n, 0.0);
+    pr.assign(n, 0.0);
+    s4g_bc_type type;
+    double rf = 1.0;
+    s4g_status st = s4g_foam_bc_at(m, (int)p, time, &type, v.data(), pr.data(), &rf);
+    if (st != S4G_OK) return st;
+    st = s4g_bc_set(mesh, (int)p, type, v.data(), type == S4G_SOLID_TRACTION ? pr.data() : nullptr);
+    if (st != S4G_OK) return st;
+    if (type == S4G_SOLID_TRACTION) {
+      st = s4g_bc_set_relaxation(mesh, (int)p, rf);
+      if (st != S4G_OK) return st;
+    }
+  }
   return S4G_OK;
 }
 

@@ -76,6 +76,8 @@ struct Controls {
   double solTol, altTol, matTol;
   int precond;           // 0 DIC, 1 diagonal
   double fieldRelax;     // relaxField "fixed" factor (1: none)
+  int aitken;            // relaxField "Aitken" (fieldRelax is then 1)
+  double aitkenA0;       // Aitken: the factor of an increment's first corrector
 };
 
 // Mutable solver state in device memory.  Scalars that steer the loops are

@@ -152,6 +152,9 @@ struct Engine {
   double* dPartials = nullptr;
   double* dOut = nullptr;
   bool tlAllocated = false;
+  // s4g_solve_step: the fields hold a finished step of model kind stepTl
+  bool stepLive = false;
+  int stepTl = -1;
   // material / controls
   bool materialSet = false;
   s4g_law law{};
@@ -340,6 +343,7 @@ struct Engine {
     S4G_TRY(alloc(&f.Gb, 9 * (size_t)nB));
     S4G_TRY(alloc(&f.sigb, 6 * (size_t)nB));
     S4G_TRY(alloc(&f.g, 3 * (size_t)nB));
+    S4G_TRY(alloc(&f.gPrev, 3 * (size_t)nB));
     S4G_TRY(alloc(&f.Ubr, 3 * (size_t)nB));
     S4G_TRY(alloc(&f.flux, 6 * (size_t)nI));
     S4G_TRY(alloc(&pc.x, 3 * (size_t)nC));
@@ -425,8 +429,20 @@ struct Engine {
     S4G_TRY(alloc(&f.FL, 9 * nC)); S4G_TRY(alloc(&f.FL0, 9 * nC));
     S4G_TRY(alloc(&f.FLb, 9 * nB)); S4G_TRY(alloc(&f.FL0b, 9 * nB));
     S4G_TRY(alloc(&f.sig0, 6 * nC)); S4G_TRY(alloc(&f.sig0b, 6 * nB));
-    S4G_TRY(alloc(&f.gPrev, 3 * nB));
     tlAllocated = true;
+    return S4G_OK;
+  }
+
+  // Aitken relaxation: a factor and a residual per cell and boundary face
+  // and load case, allocated when a solve first selects it.  Their values
+  // before an increment's first corrector are never read.
+  s4g_status ensureAitken() {
+    if (outer.relaxation_method != 1 || f.aitA) return S4G_OK;
+    const size_t nCB = (size_t)hp.nC + hp.nB;
+    S4G_TRY(alloc(&f.aitA, nCB * caseCap));
+    S4G_TRY(alloc(&f.aitR, 3 * nCB * caseCap));
+    ++generation;  // captured graphs hold the field pointers
+    dropGraphs();
     return S4G_OK;
   }
 
@@ -524,6 +540,9 @@ struct Engine {
     // relaxationFactors { fields { D f; } }: 0 or 1 leave the field as solved
     const double fr = outer.field_relaxation;
     c.fieldRelax = (fr > 0.0 && fr < 1.0) ? fr : 1.0;
+    c.aitken = outer.relaxation_method == 1 ? 1 : 0;
+    c.aitkenA0 = c.fieldRelax;
+    if (c.aitken) c.fieldRelax = 1.0;
     return c;
   }
 
@@ -641,13 +660,14 @@ struct Engine {
 
   s4g_status initFields(int tl) {
     cudaStream_t s = ctx->stream;
+    stepLive = false;
     // per-case arrays of the nRun cases of this solve
     const size_t nC = hp.nC * (size_t)nRun, nB = hp.nB * (size_t)nRun;
     auto z = [&](double* p, size_t n) { return cudaMemsetAsync(p, 0, n * sizeof(double), s); };
     S4G_CUDA(z(f.D[0], 3 * nC)); S4G_CUDA(z(f.D[1], 3 * nC)); S4G_CUDA(z(f.D0, 3 * nC));
     S4G_CUDA(z(f.D0b, 3 * nB)); S4G_CUDA(z(f.G, 9 * nC)); S4G_CUDA(z(f.sig, 6 * nC));
     S4G_CUDA(z(f.Gb, 9 * nB)); S4G_CUDA(z(f.sigb, 6 * nB)); S4G_CUDA(z(f.g, 3 * nB));
-    S4G_CUDA(z(f.Ubr, 3 * nB));
+    S4G_CUDA(z(f.Ubr, 3 * nB)); S4G_CUDA(z(f.gPrev, 3 * nB));
     S4G_CUDA(z(pc.x, 3 * nC)); S4G_CUDA(z(pc.r, 3 * nC)); S4G_CUDA(z(pc.w, 3 * nC));
     S4G_CUDA(z(pc.p, 3 * nC)); S4G_CUDA(z(pc.q, 3 * nC));
     if (fp32Allocated)
@@ -656,7 +676,6 @@ struct Engine {
     if (tl) {
       S4G_CUDA(z(f.GD, 9 * nC)); S4G_CUDA(z(f.GD0, 9 * nC)); S4G_CUDA(z(f.GDb, 9 * nB));
       S4G_CUDA(z(f.GD0b, 9 * nB)); S4G_CUDA(z(f.sig0, 6 * nC)); S4G_CUDA(z(f.sig0b, 6 * nB));
-      S4G_CUDA(z(f.gPrev, 3 * nB));
       // F = I, F^-1 = I, J = 1 (nonLinGeomTotalLagSolid.C:57-93)
       std::vector<double> I9(9 * std::max(nC, nB), 0.0), one(std::max(nC, nB), 1.0);
       for (size_t i = 0; i < std::max(nC, nB); ++i) { I9[9 * i] = 1; I9[9 * i + 4] = 1; I9[9 * i + 8] = 1; }
@@ -695,6 +714,11 @@ struct Engine {
     S4G_TRY(regrow(f.sigb, 6 * nB * o, 6 * nB * n));
     S4G_TRY(regrow(f.g, 3 * nB * o, 3 * nB * n));
     S4G_TRY(regrow(f.Ubr, 3 * nB * o, 3 * nB * n));
+    S4G_TRY(regrow(f.gPrev, 3 * nB * o, 3 * nB * n));
+    if (f.aitA) {
+      S4G_TRY(regrow(f.aitA, (nC + nB) * o, (nC + nB) * n));
+      S4G_TRY(regrow(f.aitR, 3 * (nC + nB) * o, 3 * (nC + nB) * n));
+    }
     S4G_TRY(regrow(f.flux, 6 * nI * o, 6 * nI * n));
     S4G_TRY(regrow(dBval, 3 * nB * o, 3 * nB * n));
     S4G_TRY(regrow(dBpress, nB * o, nB * n));
@@ -714,6 +738,7 @@ struct Engine {
     S4G_CUDA(cudaMallocHost((void**)&hState, sizeof(DevState) * n));
     std::memset(hState, 0, sizeof(DevState) * n);
     caseCap = C;
+    stepLive = false;
     ++generation;  // captured graphs refer to the old buffers
     dropGraphs();
     return S4G_OK;
@@ -741,6 +766,7 @@ struct Engine {
     cudaStream_t s = ctx->stream;
     const long long launches0 = launches;
     S4G_TRY(ensureCases(C));
+    S4G_TRY(ensureAitken());
     S4G_TRY(ensureMatrix());
     const bool mixed = precision == S4G_FP32_REFINE;
     if (mixed) S4G_TRY(ensureFp32());
@@ -1115,7 +1141,12 @@ struct Engine {
     }
   }
 
-  s4g_status solve(s4g_model model, int nInc, double* Dout, double* sigOut, s4g_perf* perf) {
+  // step: one evolve() of a time step (s4g_solve_step) with the boundary
+  // values as set (load factor 1), from the state the previous step left;
+  // the first step, a step after s4g_state_reset or after a full solve, and
+  // a step of another model start from zero as s4g_solve does.
+  s4g_status solve(s4g_model model, int nInc, double* Dout, double* sigOut, s4g_perf* perf,
+                   bool step = false) {
     if (model != S4G_LIN_GEOM_TOTAL_DISP && model != S4G_NONLIN_GEOM_TOTAL_LAG &&
         model != S4G_NONLIN_GEOM_TOTAL_LAG_TOTAL_DISP)
       return setErr(S4G_BAD_ARG, "unknown model");
@@ -1126,10 +1157,13 @@ struct Engine {
     if (tl && law.type != S4G_NEO_HOOKEAN) return setErr(S4G_BAD_ARG, "the TL model needs a neoHookeanElastic law");
     if (!tl && law.type != S4G_LINEAR_ELASTIC) return setErr(S4G_BAD_ARG, "the linear-geometry model needs a linearElastic law");
     if (tl) S4G_TRY(allocTL());
-    if (!tl) nInc = 1;
+    S4G_TRY(ensureAitken());
+    if (!tl || step) nInc = 1;
     if (nInc < 1) return setErr(S4G_BAD_ARG, "n_increments must be >= 1");
     cudaStream_t s = ctx->stream;
     const long long launches0 = launches;
+    const bool cont = step && stepLive && stepTl == tl;
+    stepLive = false;
     S4G_TRY(ensureMatrix());
     const bool mixed = precision == S4G_FP32_REFINE;
     if (mixed) S4G_TRY(ensureFp32());
@@ -1143,8 +1177,22 @@ struct Engine {
     }
     nRun = 1;
     ranOnDevice = false;
-    S4G_TRY(initFields(tl));
-    S4G_TRY(resetSweepState());
+    const int corr0 = cont ? hState->nCorrDone : 0;
+    const long long lin0 = cont ? hState->totalLinIters : 0;
+    if (!cont) {
+      S4G_TRY(initFields(tl));
+      S4G_TRY(resetSweepState());
+    } else {
+      // a later time step: evolve() restarts iCorr (and enforceLinear); the
+      // linear model's D.oldTime is the last step's D (the TL forms shifted
+      // theirs at the end of the last step)
+      int zero = 0;
+      S4G_CUDA(cudaMemcpyAsync(&dState->iCorr, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+      S4G_CUDA(cudaMemcpyAsync(&dState->enforceLinear, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
+      if (!tl)
+        S4G_CUDA(cudaMemcpyAsync(f.D0, f.D[hState->dcur], sizeof(double) * 3 * hp.nC,
+                                 cudaMemcpyDeviceToDevice, s));
+    }
     S4G_TRY(setLive());
     timer.reset();
     S4G_CUDA(cudaEventRecord(e0, s));
@@ -1156,13 +1204,13 @@ struct Engine {
     };
     if (!tl) {
       launchTractionInit(mv, c, f, s);
-      launchPost<double>(mv, c, f, pc.x, dState, dPartials, 0, s);
-      launches += 2;
+      if (!cont) launchPost<double>(mv, c, f, pc.x, dState, dPartials, 0, s);
+      launches += cont ? 1 : 2;
       S4G_TRY(loop(0));
-      nCorrTotal = hState->nCorrDone;
+      nCorrTotal = hState->nCorrDone - corr0;
     } else {
       for (int n = 1; n <= nInc; ++n) {
-        c.loadFactor = (double)n / nInc;
+        c.loadFactor = step ? 1.0 : (double)n / nInc;
         // evolve(): enforceLinear = false; iCorr restarts
         int zero = 0;
         S4G_CUDA(cudaMemcpyAsync(&dState->enforceLinear, &zero, sizeof(int), cudaMemcpyHostToDevice, s));
@@ -1176,7 +1224,7 @@ struct Engine {
         if (hState->status & (kErrTimeout | kErrNaN)) break;
       }
       S4G_TRY(readState());
-      nCorrTotal = hState->nCorrDone;
+      nCorrTotal = hState->nCorrDone - corr0;
     }
     S4G_CUDA(cudaEventRecord(e1, s));
     S4G_CUDA(cudaEventSynchronize(e1));
@@ -1202,7 +1250,7 @@ struct Engine {
       std::memset(perf, 0, sizeof(*perf));
       perf->n_correctors = nCorrTotal;
       perf->converged = hState->converged;
-      perf->total_lin_iters = hState->totalLinIters;
+      perf->total_lin_iters = hState->totalLinIters - lin0;
       perf->last_max_lin_iters = hState->lastMaxIters;
       perf->initial_residual = hState->initResMag;
       perf->rel_residual = hState->relRes;
@@ -1227,6 +1275,9 @@ struct Engine {
     if (hState->status & kErrTimeout) return setErr(S4G_TIMEOUT, "a bounded device wait gave up");
     if (hState->status & kErrNaN) return setErr(S4G_NAN_DETECTED, "non-finite value in the iteration");
     if (hState->status & kErrIndefinite) return setErr(S4G_INDEFINITE, "PCG met p.Ap <= 0");
+    // a later step may continue from a step's state
+    stepLive = step;
+    stepTl = tl;
     if (!hState->converged) return S4G_NOT_CONVERGED;
     return S4G_OK;
   }
@@ -1242,6 +1293,7 @@ struct Engine {
     if (law.type != S4G_LINEAR_ELASTIC)
       return setErr(S4G_BAD_ARG, "s4g_solve_batch runs the linearGeometryTotalDisplacement model "
                                  "(linearElastic law)");
+    S4G_TRY(ensureAitken());
     S4G_TRY(ensureMatrix());
     const bool mixed = precision == S4G_FP32_REFINE;
     if (mixed) S4G_TRY(ensureFp32());
@@ -1672,8 +1724,6 @@ s4g_status s4g_solver_set(s4g_mesh* mesh, const s4g_lin_solver* lin, const s4g_o
       return setErr(S4G_BAD_ARG, "field_relaxation must be in (0, 1] (0: none)");
     if (outer->relaxation_method != 0 && outer->relaxation_method != 1)
       return setErr(S4G_BAD_ARG, "relaxation_method must be 0 (fixed) or 1 (Aitken)");
-    if (outer->relaxation_method == 1)
-      return setErr(S4G_NOT_BUILT, "relaxationMethod Aitken is not built on the device");
     mesh->e.outer = *outer;
   }
   if (precision != S4G_FP64 && precision != S4G_FP32_REFINE) return setErr(S4G_BAD_ARG, "unknown precision");
@@ -1686,6 +1736,19 @@ s4g_status s4g_solve(s4g_mesh* mesh, s4g_model model, int n_increments, double* 
   if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
   cudaSetDevice(mesh->e.ctx->device);
   return mesh->e.solve(model, n_increments, D_out, sigma_out, perf);
+}
+
+s4g_status s4g_solve_step(s4g_mesh* mesh, s4g_model model, double* D_out, double* sigma_out,
+                          s4g_perf* perf) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  cudaSetDevice(mesh->e.ctx->device);
+  return mesh->e.solve(model, 1, D_out, sigma_out, perf, true);
+}
+
+s4g_status s4g_state_reset(s4g_mesh* mesh) {
+  if (!mesh) return setErr(S4G_BAD_ARG, "null mesh");
+  mesh->e.stepLive = false;
+  return S4G_OK;
 }
 
 s4g_status s4g_get_gradD(s4g_mesh* mesh, double* gradD_out) {

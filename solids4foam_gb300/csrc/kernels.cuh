@@ -51,9 +51,11 @@ struct FieldPtrs {
   double* Gb;    // [nB][9]
   double* sigb;  // [nB][6]
   double* g;     // [nB][3] traction snGrad
-  double* gPrev; // [nB][3] TL: the g of the corrector before the last update
+  double* gPrev; // [nB][3] the g the last corrector used (before its update)
   double* Ubr;   // [nB][3] field relaxation: the boundary values of the solved
                  // field after the last relaxation (D.prevIter on the boundary)
+  double* aitA;  // [nC + nB] Aitken factor of each cell, then of each boundary face
+  double* aitR;  // [nC + nB][3] Aitken residual D.prevIter - D of the last corrector
   // total Lagrangian extras
   double* GD;  double* GD0;  double* GDb; double* GD0b;  // total gradient and old time
   double* Finv; double* Finvb; double* J; double* Jb;
@@ -71,7 +73,8 @@ __host__ __device__ inline FieldPtrs caseFields(FieldPtrs f, int cs, int nC, int
   if (f.D0b) f.D0b += c * 3 * nB;
   f.G += c * 9 * nC; f.sig += c * 6 * nC;
   f.Gb += c * 9 * nB; f.sigb += c * 6 * nB; f.g += c * 3 * nB;
-  f.Ubr += c * 3 * nB;
+  f.Ubr += c * 3 * nB; f.gPrev += c * 3 * nB;
+  if (f.aitA) { f.aitA += c * (nC + nB); f.aitR += c * 3 * (nC + nB); }
   f.flux += c * 6 * nI;
   return f;
 }

@@ -191,11 +191,9 @@ __device__ __forceinline__ V3 relaxG(const MeshView& mv, int b, V3 gNew, V3 gOld
   return rf == 1.0 ? gNew : rf * gNew + (1.0 - rf) * gOld;
 }
 
-// The first update of an increment.  The g it relaxes against is the one
-// the previous corrector used: g itself for the linear-geometry model
-// (zero at the start), gPrev for the TL model, whose last corrector of the
-// previous increment has already written the update it would have used
-// next.
+// The first update of an increment or time step.  The g it relaxes against
+// is the one the previous corrector used (gPrev, zero at the start): that
+// corrector has already written the update it would have used next.
 __global__ void kTractionInit(MeshView mv, Controls c, FieldPtrs f) {
   f = caseFields(f, blockIdx.y, mv.nC, mv.nB, mv.nI);
   caseView(mv, blockIdx.y);
@@ -204,7 +202,7 @@ __global__ void kTractionInit(MeshView mv, Controls c, FieldPtrs f) {
   T9 Fi;
   const T9* pF = nullptr;
   if (c.tl) { Fi = ldT(f.Finvb, b); pF = &Fi; }
-  const V3 gOld = c.tl ? ldV(f.gPrev, b) : ldV(f.g, b);
+  const V3 gOld = ldV(f.gPrev, b);
   stV(f.g, b, relaxG(mv, b, tractionSnGrad(mv, c, b, ldS(f.sigb, b), ldT(f.Gb, b), pF, 0), gOld));
 }
 
@@ -219,9 +217,41 @@ __device__ __forceinline__ V3 boundaryValue(const MeshView& mv, const Controls& 
 }
 
 // --------------------------------------------------------- post-solve pass ---
+// relaxField "Aitken" (solidModel.C:842-896) of one cell or boundary face:
+// r = D.prevIter - D (p the value before the solve, u the solved one); at
+// an increment's first corrector alpha = aitkenA0 (the field's relaxation
+// factor, else 1), later alpha = alpha (r_prev . dr) / (|dr|^2 + SMALL) with
+// dr = r_prev - r, bounded to [0, 2]; then D -= alpha r (apply false: a
+// fixed-value face, which the -= leaves as it is).  Explicitly rounded
+// operations, in the oracle's order.
+__device__ __forceinline__ V3 aitkenRelax(const Controls& c, bool first, double* a,
+                                          double* rPrev, V3 p, V3 u, bool apply) {
+  const V3 r{__dsub_rn(p.x, u.x), __dsub_rn(p.y, u.y), __dsub_rn(p.z, u.z)};
+  double al;
+  if (first) {
+    al = c.aitkenA0;
+  } else {
+    const V3 rp = ldV(rPrev, 0);
+    const V3 dr{__dsub_rn(rp.x, r.x), __dsub_rn(rp.y, r.y), __dsub_rn(rp.z, r.z)};
+    const double num = __dadd_rn(__dadd_rn(__dmul_rn(rp.x, dr.x), __dmul_rn(rp.y, dr.y)),
+                                 __dmul_rn(rp.z, dr.z));
+    const double den = __dadd_rn(__dadd_rn(__dadd_rn(__dmul_rn(dr.x, dr.x), __dmul_rn(dr.y, dr.y)),
+                                           __dmul_rn(dr.z, dr.z)),
+                                 1e-15);
+    al = __ddiv_rn(__dmul_rn(*a, num), den);
+    al = fmax(0.0, fmin(2.0, al));
+  }
+  *a = al;
+  stV(rPrev, 0, r);
+  if (!apply) return u;
+  return V3{__dsub_rn(u.x, __dmul_rn(al, r.x)), __dsub_rn(u.y, __dmul_rn(al, r.y)),
+            __dsub_rn(u.z, __dmul_rn(al, r.z))};
+}
+
 // D_new = D + x (the correction of the corrector; x in the PCG type).  With
 // a field relaxation factor f (relaxField "fixed", solidModel.C:837-841):
-// D_new = D.prevIter + f (D_solved - D.prevIter) = D + f x.
+// D_new = D.prevIter + f (D_solved - D.prevIter) = D + f x; with Aitken the
+// cell's own factor (aitkenRelax).
 template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
 kApplyX(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, const DevState* st) {
@@ -234,7 +264,14 @@ kApplyX(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, const Dev
   const double* Uold = f.D[dc];
   double* Unew = f.D[dc ^ 1];
   const double fr = c.fieldRelax;
-  if (fr == 1.0)
+  if (c.aitken) {
+    const bool first = st->iCorr == 0;
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x) {
+      const V3 uo = ldV(Uold, s);
+      const V3 us = uo + ldVT(x, s);
+      stV(Unew, s, aitkenRelax(c, first, f.aitA + s, f.aitR + 3 * (size_t)s, uo, us, true));
+    }
+  } else if (fr == 1.0)
     for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x)
       stV(Unew, s, ldV(Uold, s) + ldVT(x, s));
   else
@@ -268,7 +305,7 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
   const bool apply = (mode == 1);
   // the corrected field D + x, written by kApplyX (mode 1), or D (mode 0)
   const double* U = f.D[apply ? dc ^ 1 : dc];
-  const bool relax = c.fieldRelax != 1.0;
+  const bool relax = c.fieldRelax != 1.0 || c.aitken;
   double red[6] = {0, 0, 0, 0, 0, 0};  // sum U
   double mx[3] = {0, 0, 0};            // max|x|, max|U-D0|, max|U|
   double minJ = 1e300, maxJ = -1e300;
@@ -288,7 +325,11 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
       if (relax) {
         if (apply) {
           const V3 pb = ldV(f.Ubr, b);
-          Ub = pb + c.fieldRelax * (Ub - pb);
+          if (c.aitken)
+            Ub = aitkenRelax(c, st->iCorr == 0, f.aitA + mv.nC + b, f.aitR + 3 * ((size_t)mv.nC + b),
+                             pb, Ub, mv.btype[b] == 1);
+          else
+            Ub = pb + c.fieldRelax * (Ub - pb);
         }
         stV(f.Ubr, b, Ub);
       }
@@ -311,7 +352,10 @@ kPost(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, DevState* s
       if (!c.tl) {
         S6 sb = mode == 1 ? hooke(c, Gb) : ldS(f.sigb, b);
         if (mode == 1) stS(f.sigb, b, sb);
-        if (mv.btype[b] == 1) stV(f.g, b, relaxG(mv, b, tractionSnGrad(mv, c, b, sb, Gb, nullptr, 0), sg));
+        if (mv.btype[b] == 1) {
+          stV(f.gPrev, b, sg);
+          stV(f.g, b, relaxG(mv, b, tractionSnGrad(mv, c, b, sb, Gb, nullptr, 0), sg));
+        }
       }
     }
     if (!c.tl) {

@@ -271,24 +271,39 @@ __device__ __forceinline__ bool locArrive(unsigned* gcnt, int part, int nParts) 
   return atomicAdd(&gcnt[g], 1u) + 1u == (unsigned)locGroupSize(g, nParts);
 }
 
-// One warp: the record of group g (lane j holds part g*32 + j), and the
-// group's counter back to zero for the next launch.
+// One warp: the record (N values) of group g (lane j holds part g*32 + j),
+// and the group's counter back to zero for the next launch.
+template <int N = 6>
 __device__ __forceinline__ void locGroupSum(const double* rec, double* grec, unsigned* gcnt, int g,
                                             int nParts) {
   const int lane = threadIdx.x & 31;
   const int part = g * kLocGroup + lane;
   __threadfence();
-  double v[6];
+  double v[N];
 #pragma unroll
-  for (int k = 0; k < 6; ++k) v[k] = part < nParts ? __ldcg(rec + 8 * (size_t)part + k) : 0.0;
+  for (int k = 0; k < N; ++k) v[k] = part < nParts ? __ldcg(rec + 8 * (size_t)part + k) : 0.0;
 #pragma unroll
-  for (int k = 0; k < 6; ++k)
+  for (int k = 0; k < N; ++k)
     for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
   if (lane == 0) {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) grec[8 * (size_t)g + k] = v[k];
+    for (int k = 0; k < N; ++k) grec[8 * (size_t)g + k] = v[k];
     gcnt[g] = 0;
   }
+}
+
+// The last CTA: the sum of the group records in group order -- lane v of
+// 64 sums groups v, v + 64, ..., then a fixed tree.  Result in thread 0.
+template <int N>
+__device__ __forceinline__ void locGroupsTotal(const double* grec, int nGroups, double (&S)[N],
+                                               double* red) {
+#pragma unroll
+  for (int k = 0; k < N; ++k) S[k] = 0;
+  if (threadIdx.x < 64)
+    for (int g = threadIdx.x; g < nGroups; g += 64)
+#pragma unroll
+      for (int k = 0; k < N; ++k) S[k] += __ldcg(grec + 8 * (size_t)g + k);
+  sum64<N>(S, red);
 }
 
 // End of a preconditioner launch, after the CTA's last part: thread 0
@@ -308,12 +323,8 @@ __device__ __forceinline__ void locFinish(const MeshView& mv, const Controls& c,
   __syncthreads();
   if (*sGroup >= 0 && t < 32) locGroupSum(partials, grec, gcnt, *sGroup, mv.nParts);
   if (!lastBlockDone(&st->counter[5], gridDim.x)) return;
-  double S[6] = {0, 0, 0, 0, 0, 0};
-  if (t < 64)
-    for (int g = t; g < mv.locGroups; g += 64)
-#pragma unroll
-      for (int k = 0; k < 6; ++k) S[k] += __ldcg(grec + 8 * (size_t)g + k);
-  sum64<6>(S, red);
+  double S[6];
+  locGroupsTotal<6>(grec, mv.locGroups, S, red);
   if (t != 0) return;
   st->counter[5] = 0;
   st->locTicket = 0;
@@ -932,11 +943,12 @@ size_t localSmemBytes(const MeshView& mv) {
 
 template <typename T>
 cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM) {
+  cudaError_t e;
   if constexpr (sizeof(T) == 4) {
-    cudaError_t e = prepareV<T, 128, 4, 2>(mv, &blocksPerSM[0]);
+    e = prepareV<T, 128, 4, 2>(mv, &blocksPerSM[0]);
     return e != cudaSuccess ? e : prepareV<T, 64, 4, 4>(mv, &blocksPerSM[1]);
   } else {
-    cudaError_t e = prepareV<T, 128, 2, 1>(mv, &blocksPerSM[0]);
+    e = prepareV<T, 128, 2, 1>(mv, &blocksPerSM[0]);
     return e != cudaSuccess ? e : prepareV<T, 64, 2, 2>(mv, &blocksPerSM[1]);
   }
 }

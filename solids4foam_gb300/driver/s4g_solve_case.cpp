@@ -3,6 +3,8 @@
 // inside solids4Foam, through the same C ABI and without OpenFOAM:
 //   read constant/polyMesh and 0/D            s4g_foam_read_mesh, s4g_foam_read_d
 //   load series -> increments                 s4g_foam_load_ramp, s4g_foam_read_time
+//   or time steps (other load tables)         s4g_foam_series_kind, s4g_foam_apply_bcs_at,
+//                                             s4g_solve_step
 //   field relaxation; refuse equation factors s4g_foam_read_relaxation
 //   upload the mesh, set law, BCs, controls   s4g_mesh_upload, s4g_material_set,
 //                                             s4g_foam_apply_bcs, s4g_solver_set
@@ -13,12 +15,15 @@
 // constant/mechanicalProperties, system/fvSolution: s4g_foam_read_controls),
 // as the reference reads them; command-line options override them.  A total Lagrangian case whose loads are series
 // (linear ramps from zero) runs one increment per time step of
-// system/controlDict unless --increments is given.  --plan-only stops after
+// system/controlDict unless --increments is given; a case with other load
+// tables (or --time-steps) runs one evolve() per time step, its series
+// evaluated at the step's time, as solids4Foam's time loop does.  --plan-only stops after
 // the host-side mesh planning and needs no GPU.  --write TIME writes D,
 // sigma, sigmaEq and pointD as ASCII fields into <case>/<TIME>/.
 
 #include "s4g.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -40,6 +45,8 @@ void usage() {
                "  --E E --nu NU            linearElastic (default 200e9, 0.3)\n"
                "  --mu MU --K K            neoHookeanElastic (the total Lagrangian models)\n"
                "  --increments N           load increments of the total Lagrangian models (1)\n"
+               "  --time-steps             one evolve() per controlDict time step (the default\n"
+               "                           for load tables other than ramps from zero)\n"
                "  --precision FP64|FP32_REFINE\n"
                "  --preconditioner DIC|diagonal  --tolerance T  --relTol R  --maxIter N\n"
                "  --nCorrectors N  --solutionTolerance T  --alternativeTolerance T\n"
@@ -85,6 +92,7 @@ int main(int argc, char** argv) {
   s4g_precision precision = S4G_FP64;
   int increments = 1, device = 0;
   bool planOnly = false, muKGiven = false, eNuGiven = false, incrementsGiven = false;
+  bool timeStepsGiven = false;
   bool lsDeltaGiven = false;
   for (int i = 2; i < argc; ++i) {
     const std::string a = argv[i];
@@ -101,6 +109,7 @@ int main(int argc, char** argv) {
     else if (a == "--mu") { law.mu = std::atof(val()); muKGiven = true; }
     else if (a == "--K") { law.K = std::atof(val()); muKGiven = true; }
     else if (a == "--increments") { increments = std::atoi(val()); incrementsGiven = true; }
+    else if (a == "--time-steps") timeStepsGiven = true;
     else if (a == "--precision") {
       const std::string p = val();
       if (p == "FP64") precision = S4G_FP64;
@@ -174,7 +183,22 @@ int main(int argc, char** argv) {
   if (!planOnly || haveD) check(s4g_foam_read_d(fc, dFile.c_str()), "reading 0/D");
   double rampEnd = 0;
   int constantLoads = 0;
+  int seriesKind = 0;
   if (haveD) check(s4g_foam_load_ramp(fc, &rampEnd, &constantLoads), "s4g_foam_load_ramp");
+  if (haveD) check(s4g_foam_series_kind(fc, &seriesKind), "s4g_foam_series_kind");
+  // time steps: the loads of controlDict's time steps t0 + k dt, k = 1..N
+  std::vector<double> stepTimes;
+  if (seriesKind == 2 || timeStepsGiven) {
+    double t0 = 0, t1 = 0, dt = 0;
+    if (s4g_foam_read_time((caseDir + "/system/controlDict").c_str(), &t0, &t1, &dt) != S4G_OK) {
+      std::fprintf(stderr, "s4g_solve_case: load tables are stepped through system/controlDict's "
+                           "time steps, which cannot be read: %s\n", s4g_last_error());
+      return 2;
+    }
+    const long nSteps = std::max(1L, std::lround((t1 - t0) / dt));
+    for (long k = 1; k <= nSteps; ++k) stepTimes.push_back(t0 + (double)k * dt);
+    rampEnd = 0;
+  }
   if (rampEnd > 0) {
     if (model != S4G_LIN_GEOM_TOTAL_DISP && constantLoads) {
       std::fprintf(stderr, "s4g_solve_case: constant loads beside load series are not built for the "
@@ -229,14 +253,15 @@ int main(int argc, char** argv) {
                 "\"levels\": %d, \"load_ramp_end\": %g, \"increments\": %d, \"model\": \"%s\", "
                 "\"law\": \"%s\", \"E\": %g, \"nu\": %g, \"mu\": %g, \"K\": %g, \"use_mu_K\": %d, "
                 "\"nCorrectors\": %d, \"tolerance\": %g, \"relTol\": %g, \"scaleFactor\": %g, "
-                "\"empty_direction\": %d, \"fieldRelaxation\": %g, \"ls_boundary_delta\": %d}\n",
+                "\"empty_direction\": %d, \"fieldRelaxation\": %g, \"ls_boundary_delta\": %d, "
+                "\"load_series\": %d, \"time_steps\": %d}\n",
                 caseDir.c_str(), desc.n_cells, desc.n_faces, desc.n_internal_faces, nPoints,
                 desc.n_patches, info.n_parts, info.part_depth, info.n_levels_global, rampEnd,
                 model == S4G_LIN_GEOM_TOTAL_DISP ? 1 : increments, modelName.c_str(),
                 law.type == S4G_LINEAR_ELASTIC ? "linearElastic" : "neoHookeanElastic", law.E,
                 law.nu, law.mu, law.K, law.use_mu_K, outer.n_correctors, lin.tolerance,
                 lin.rel_tol, outer.stab_scale, mo.empty_direction, outer.field_relaxation,
-                mo.ls_boundary_delta);
+                mo.ls_boundary_delta, seriesKind, (int)stepTimes.size());
     s4g_foam_free(fc);
     return 0;
   }
@@ -253,8 +278,30 @@ int main(int argc, char** argv) {
   const int n = desc.n_cells;
   std::vector<double> D(3 * (size_t)n), sigma(6 * (size_t)n), gradD(9 * (size_t)n);
   s4g_perf perf;
-  s4g_status st = s4g_solve(mesh, model, increments, D.data(), sigma.data(), &perf);
-  if (st != S4G_OK && st != S4G_NOT_CONVERGED) die("s4g_solve", st);
+  s4g_status st;
+  if (stepTimes.empty()) {
+    st = s4g_solve(mesh, model, increments, D.data(), sigma.data(), &perf);
+    if (st != S4G_OK && st != S4G_NOT_CONVERGED) die("s4g_solve", st);
+  } else {
+    // solids4Foam's time loop: the boundary conditions at the step's time,
+    // then one evolve()
+    int corr = 0;
+    long long pcg = 0;
+    double ms = 0;
+    for (double t : stepTimes) {
+      check(s4g_foam_apply_bcs_at(fc, mesh, t), "the boundary conditions at a time step");
+      st = s4g_solve_step(mesh, model, D.data(), sigma.data(), &perf);
+      if (st != S4G_OK && st != S4G_NOT_CONVERGED) die("s4g_solve_step", st);
+      if (st == S4G_NOT_CONVERGED)
+        std::fprintf(stderr, "time %g: Max iterations reached within momentum loop\n", t);
+      corr += perf.n_correctors;
+      pcg += perf.total_lin_iters;
+      ms += perf.solve_ms;
+    }
+    perf.n_correctors = corr;
+    perf.total_lin_iters = pcg;
+    perf.solve_ms = ms;
+  }
   if (st == S4G_NOT_CONVERGED) std::fprintf(stderr, "Max iterations reached within momentum loop\n");
   check(s4g_get_gradD(mesh, gradD.data()), "s4g_get_gradD");
 
@@ -281,12 +328,12 @@ int main(int argc, char** argv) {
   for (int p = 0; p < nPoints; ++p)
     maxPD = std::fmax(maxPD, std::sqrt(pointD[3 * p] * pointD[3 * p] + pointD[3 * p + 1] * pointD[3 * p + 1] +
                                        pointD[3 * p + 2] * pointD[3 * p + 2]));
-  std::printf("{\"case\": \"%s\", \"model\": \"%s\", \"cells\": %d, \"increments\": %d, \"status\": \"%s\", "
+  std::printf("{\"case\": \"%s\", \"model\": \"%s\", \"cells\": %d, \"increments\": %d, \"time_steps\": %d, \"status\": \"%s\", "
               "\"converged\": %d, \"correctors\": %d, \"pcg_iterations\": %lld, "
               "\"solve_ms\": %.3f, \"max_mag_D\": %.9g, \"max_mag_pointD\": %.9g, "
               "\"max_sigmaEq\": %.9g}\n",
               caseDir.c_str(), modelName.c_str(), n, model == S4G_LIN_GEOM_TOTAL_DISP ? 1 : increments,
-              s4g_status_str(st), perf.converged,
+              (int)stepTimes.size(), s4g_status_str(st), perf.converged,
               perf.n_correctors, perf.total_lin_iters, perf.solve_ms, maxD, maxPD, maxSeq);
   if (!writeTime.empty()) {
     // D, sigma, sigmaEq (solidModel::writeFields) and pointD in <case>/<time>

@@ -73,7 +73,43 @@ def read_case(case_dir: str, d_file: str | None = "0/D", polymesh: str = "consta
                        "s4g_foam_load_ramp")
             mesh["load_ramp_end"] = end.value or None
             mesh["constant_loads_beside_ramp"] = bool(mixed.value)
+            kind = ct.c_int()
+            _lib.check(L.s4g_foam_series_kind(h, ct.byref(kind)), "s4g_foam_series_kind")
+            mesh["load_series"] = kind.value
         return mesh, bcs
+    finally:
+        L.s4g_foam_free(h)
+
+
+def bcs_at(case_dir: str, times, d_file: str = "0/D", polymesh: str = "constant/polyMesh"):
+    """The D boundary conditions at each of `times` (s4g_foam_bc_at): the
+    load series evaluated at the time, as the reference's conditions
+    evaluate them at a time step, constant values as read.  One bcs dict
+    per time, in read_case's form."""
+    L = _lib.lib()
+    h = ct.c_void_p()
+    _lib.check(L.s4g_foam_read_mesh(os.path.join(case_dir, polymesh).encode(), ct.byref(h)),
+               "s4g_foam_read_mesh")
+    try:
+        _lib.check(L.s4g_foam_read_d(h, os.path.join(case_dir, d_file).encode()), "s4g_foam_read_d")
+        d = _lib.MeshDesc()
+        npts = ct.c_int()
+        _lib.check(L.s4g_foam_mesh_desc(h, ct.byref(d), ct.byref(npts)), "s4g_foam_mesh_desc")
+        sizes = _arr(d.patch_size, d.n_patches, np.int32)
+        names = [L.s4g_foam_patch_name(h, p).decode() for p in range(d.n_patches)]
+        out = []
+        for t in times:
+            bcs = {}
+            for p, name in enumerate(names):
+                n = int(sizes[p])
+                vec, press = np.zeros((n, 3)), np.zeros(n)
+                ty, rf = ct.c_int(), ct.c_double()
+                _lib.check(L.s4g_foam_bc_at(h, p, float(t), ct.byref(ty), vec.ctypes.data,
+                                            press.ctypes.data, ct.byref(rf)), "s4g_foam_bc_at")
+                bcs[name] = (BC_NAMES[ty.value], vec,
+                             press if ty.value == _lib.SOLID_TRACTION else None, rf.value)
+            out.append(bcs)
+        return out
     finally:
         L.s4g_foam_free(h)
 
@@ -317,7 +353,9 @@ def load_case(case_dir: str):
     ls_boundary_delta).
     The model, law and controls come from the case's dictionaries; a total
     Lagrangian case whose loads ramp from zero runs one increment per
-    controlDict time step.  Raises for what is not built: equation
+    controlDict time step; a case with other load tables gets time_steps,
+    [(time, bcs at that time)] for SolidModel.run_time_steps (None
+    otherwise).  Raises for what is not built: equation
     relaxation of the solved field, constant loads beside a ramp (total
     Lagrangian), load series whose end is not the controlDict endTime (or a
     startTime other than 0), and everything the readers refuse."""
@@ -331,6 +369,18 @@ def load_case(case_dir: str):
             raise ValueError(f"equation relaxationFactors for {field} ({ef:g}) are not built on "
                              "the GPU path")
     n_inc = 1
+    steps = None
+    if mesh.get("load_series") == 2:
+        # tables other than ramps from zero: one s4g_solve_step per
+        # controlDict time step, the series evaluated at its time
+        cd = os.path.join(case_dir, "system", "controlDict")
+        if not os.path.exists(cd):
+            raise ValueError("load series that are not ramps from zero are stepped through "
+                             "system/controlDict's time steps, and the case has none")
+        t0, t1, dt = read_time(case_dir)
+        n = max(1, int(round((t1 - t0) / dt)))
+        times = [t0 + k * dt for k in range(1, n + 1)]
+        steps = list(zip(times, bcs_at(case_dir, times)))
     ramp = mesh.get("load_ramp_end")
     if ramp:
         if tl and mesh.get("constant_loads_beside_ramp"):
@@ -354,4 +404,5 @@ def load_case(case_dir: str):
         _lib.check(_lib.lib().s4g_foam_read_grad_scheme(fvs.encode(), field.encode(), ct.byref(v)),
                    "s4g_foam_read_grad_scheme")
         lsd = v.value
-    return dict(mesh=mesh, bcs=bcs, n_increments=n_inc, ls_boundary_delta=lsd, **c)
+    return dict(mesh=mesh, bcs=bcs, n_increments=n_inc, ls_boundary_delta=lsd, time_steps=steps,
+                **c)

@@ -141,7 +141,8 @@ class SolidModel:
         subdomain id, decomposePar's cellDecomposition); implies
         renumber="none" and dic_subdomains=True.  outer may hold
         fieldRelaxation (fvSolution relaxationFactors fields factor) and
-        relaxationMethod ("fixed")."""
+        relaxationMethod ("fixed" or "Aitken")."""
+        self.time_steps = None
         if model not in MODELS:
             raise ValueError(f"unknown solidModel {model!r}; valid: {list(MODELS)}")
         self.ctx = ctx
@@ -172,15 +173,18 @@ class SolidModel:
     @classmethod
     def from_case(cls, ctx: "Context", case_dir: str, **kw):
         """A model of a meshed OpenFOAM case directory (foam_case.load_case):
-        returns (model, n_increments) for model.evolve(n_increments).
-        Keyword arguments (precision, renumber, part_size, ...) are passed
-        on to the constructor."""
+        returns (model, n_increments) for model.evolve(n_increments).  A
+        case with load tables other than ramps from zero keeps its time
+        steps in model.time_steps (for model.run_time_steps()).  Keyword
+        arguments (precision, renumber, part_size, ...) are passed on to the
+        constructor."""
         from .foam_case import load_case
         c = load_case(case_dir)
         kw.setdefault("empty_direction", c["mesh"].get("empty_direction", 0))
         kw.setdefault("ls_boundary_delta", c["ls_boundary_delta"])
         model = cls(ctx, c["mesh"], c["law"], c["bcs"], model=c["model"], solver=c["solver"],
                     outer=c["outer"], **kw)
+        model.time_steps = c["time_steps"]
         return model, c["n_increments"]
 
     def close(self):
@@ -232,6 +236,43 @@ class SolidModel:
                               sig.ctypes.data, ct.byref(perf))
         _lib.check(st, "s4g_solve", allow=(_lib.OK, _lib.NOT_CONVERGED))
         return D, sig, perf.as_dict()
+
+    def step(self, bcs: dict | None = None):
+        """One time step (s4g_solve_step): evolve() once with the boundary
+        values as they are, continuing from the previous step's state.
+        bcs (optional): {patch name: (type, value, pressure[, relaxation])}
+        set first, e.g. a load series evaluated at the step's time.
+        Returns (D [n,3], sigma [n,6], perf of this step)."""
+        if bcs:
+            names = list(self.mesh.get("patch_names", PATCHES))
+            for name, spec in bcs.items():
+                self.set_bc(names.index(name), spec[0], spec[1] if len(spec) > 1 else None,
+                            spec[2] if len(spec) > 2 else None,
+                            spec[3] if len(spec) > 3 else None)
+        D = np.zeros((self.n_cells, 3))
+        sig = np.zeros((self.n_cells, 6))
+        perf = _lib.Perf()
+        st = self.L.s4g_solve_step(self.h, MODELS[self.model], D.ctypes.data, sig.ctypes.data,
+                                   ct.byref(perf))
+        _lib.check(st, "s4g_solve_step", allow=(_lib.OK, _lib.NOT_CONVERGED))
+        return D, sig, perf.as_dict()
+
+    def run_time_steps(self, steps=None):
+        """Steps through [(time, bcs), ...] -- by default the case's own
+        time_steps (from_case) -- one s4g_solve_step each.  Returns (D,
+        sigma) of the last step and the perf of every step."""
+        steps = self.time_steps if steps is None else steps
+        if not steps:
+            raise ValueError("no time steps to run")
+        perfs = []
+        for _, bcs in steps:
+            D, sig, perf = self.step(bcs)
+            perfs.append(perf)
+        return D, sig, perfs
+
+    def reset_state(self):
+        """The next step starts from zero (s4g_state_reset)."""
+        _lib.check(self.L.s4g_state_reset(self.h), "s4g_state_reset")
 
     def evolve_cases(self, case_bcs: list):
         """Batched load cases (s4g_solve_cases): case_bcs is a list of

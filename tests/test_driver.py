@@ -85,6 +85,25 @@ def test_load_ramp_sets_the_increments(tmp_path):
     assert out["increments"] == 1
 
 
+def test_load_tables_run_time_steps(tmp_path):
+    """A load table that is not a ramp from zero (load, then unload) runs
+    one evolve() per controlDict time step (s4g_solve_step), its series
+    evaluated at each step's time; --time-steps asks the same of a ramp."""
+    case = _ramp_case(tmp_path)
+    (tmp_path / "constant" / "timeVsTraction").write_text(
+        "((0 (0 0 0)) (5 (0 0 -1e5)) (10 (0 0 -2e4)))")
+    for model in ("linearGeometryTotalDisplacement", "nonLinearGeometryTotalLagrangian"):
+        r = run(case, "--plan-only", "--model", model)
+        assert r.returncode == 0, r.stderr
+        out = json.loads(r.stdout)
+        assert out["load_series"] == 2 and out["time_steps"] == 20 and out["load_ramp_end"] == 0
+    (tmp_path / "constant" / "timeVsTraction").write_text("((0 (0 0 0)) (10 (0 0 -1e5)))")
+    out = json.loads(run(case, "--plan-only").stdout)
+    assert out["load_series"] == 1 and out["time_steps"] == 0
+    out = json.loads(run(case, "--plan-only", "--time-steps").stdout)
+    assert out["time_steps"] == 20
+
+
 def test_constant_load_beside_a_ramp_is_refused_for_tl(tmp_path):
     case = _ramp_case(tmp_path, xmin_traction="1e5 0 0")
     r = run(case, "--plan-only", "--model", "nonLinearGeometryTotalLagrangianTotalDisplacement")

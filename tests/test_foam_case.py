@@ -293,10 +293,44 @@ def test_load_series_that_ramp_from_zero(tmp_path):
     assert m["load_ramp_end"] is None
 
 
+def test_load_tables_are_evaluated_in_time(tmp_path):
+    """A load series that is not a ramp from zero (here a ramp to a plateau)
+    is read whole: read_case reports a table (load_series 2, no ramp end)
+    and gives its end value, and bcs_at evaluates it at the time steps'
+    times -- linear between points, the end values outside the table
+    (outOfBounds clamp, OpenFOAM's default), periodic with repeat, refused
+    with error."""
+    from solids4foam_gb300.foam_case import bcs_at
+    m, bcs = _series_case(tmp_path, """{ type solidTraction; pressure uniform 0;
+        tractionSeries { file "$FOAM_CASE/constant/bent"; } }""")
+    assert m["load_series"] == 2 and m["load_ramp_end"] is None
+    assert np.all(bcs["zmax"][1] == [1, 0, 0])
+    times = [0.0, 2.0, 5.0, 7.5, 12.0, -1.0]
+    got = [b["zmax"][1][0] for b in bcs_at(str(tmp_path), times)]
+    want = np.interp(times, [0, 5, 10], [0, 1, 1])
+    assert np.allclose(np.array(got)[:, 0], want, rtol=0, atol=1e-15)
+    assert all(np.all(b["zmax"][1] == b["zmax"][1][0]) for b in bcs_at(str(tmp_path), times))
+    # the other patches keep their constant values
+    assert all(np.all(b["xmin"][1] == 0) and b["zmin"][0] == "fixedDisplacement"
+               for b in bcs_at(str(tmp_path), times))
+    # ramps from zero with a common end stay the increments' ramp
+    m, _ = _series_case(tmp_path, """{ type solidTraction; pressure uniform 0;
+        tractionSeries { file "$FOAM_CASE/constant/timeVsTraction"; } }""")
+    assert m["load_series"] == 1 and m["load_ramp_end"] == 10.0
+    # outOfBounds repeat: periodic over the table's span
+    _series_case(tmp_path, """{ type solidTraction; pressure uniform 0;
+        tractionSeries { file "$FOAM_CASE/constant/bent"; outOfBounds repeat; } }""")
+    got = [b["zmax"][1][0, 0] for b in bcs_at(str(tmp_path), [12.5, 17.5, -7.5])]
+    assert np.allclose(got, [0.5, 1.0, 0.5], rtol=0, atol=1e-15)
+    # outOfBounds error
+    _series_case(tmp_path, """{ type solidTraction; pressure uniform 0;
+        tractionSeries { file "$FOAM_CASE/constant/bent"; outOfBounds error; } }""")
+    assert bcs_at(str(tmp_path), [10.0])[0]["zmax"][1][0, 0] == 1.0
+    with pytest.raises(_lib.S4GError, match="outside the series"):
+        bcs_at(str(tmp_path), [10.5])
+
+
 def test_other_load_series_are_rejected(tmp_path):
-    with pytest.raises(_lib.S4GError, match="not a linear ramp from zero"):
-        _series_case(tmp_path, """{ type solidTraction; pressure uniform 0;
-            tractionSeries { file "$FOAM_CASE/constant/bent"; } }""")
     with pytest.raises(_lib.S4GError, match="interpolationScheme step is not built"):
         _series_case(tmp_path, """{ type solidTraction; pressure uniform 0;
             tractionSeries { file "$FOAM_CASE/constant/timeVsTraction"; interpolationScheme step; } }""")

@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol(built):
     for n in names:
         assert hasattr(L, n), n
     assert set(names) == set(_lib.declared_symbols())
-    assert L.s4g_abi_version() == 6
+    assert L.s4g_abi_version() == 7
     assert L.s4g_status_str(_lib.NOT_CONVERGED) == b"NOT_CONVERGED"
 
 

@@ -334,6 +334,27 @@ def test_field_relaxation_rescues_the_corrector_loop():
     assert np.linalg.norm(D9 - D7) / np.linalg.norm(D7) < 1e-6
 
 
+def test_aitken_relaxation_keeps_the_fixed_point():
+    """relaxationMethod Aitken (solidModel.C:842-896), restated as written:
+    D -= alpha (D.prevIter - D), so alpha = 1 at the first corrector steps
+    twice the correction, and later factors come from the last two
+    residuals.  At nu = 0.3 it converges to the unrelaxed loop's fixed
+    point; the factors stay in [0, 2] by construction."""
+    m = sg.box_mesh(10, 10, 10, 1.0, 1.0, 1.0, 0.2, 3)
+    t = np.tile([0.0, 1e5, -1e5], (int(m["patch_size"][5]), 1))
+    bcs = [(1, None, None)] * 4 + [(0, None, None), (1, t, None)]
+    kw = dict(E=200e9, nu=0.3, n_correctors=4000, solution_tol=1e-10, alternative_tol=1e-10)
+    D0, _, _, p0 = pyoracle.solve(m, bcs, **kw)
+    for fr in (0.0, 0.7):
+        Da, _, _, pa = pyoracle.solve(m, bcs, relaxation_method=1, field_relaxation=fr, **kw)
+        assert p0["converged"] == 1 and pa["converged"] == 1
+        assert np.linalg.norm(Da - D0) / np.linalg.norm(D0) < 1e-7
+    # one corrector: alpha = 1 doubles the step of the unrelaxed first solve
+    D1, _, _, _ = pyoracle.solve(m, bcs, E=200e9, nu=0.3, n_correctors=1)
+    A1, _, _, _ = pyoracle.solve(m, bcs, E=200e9, nu=0.3, n_correctors=1, relaxation_method=1)
+    assert np.allclose(A1, 2.0 * D1, rtol=1e-12, atol=1e-20)
+
+
 @pytest.mark.parametrize("model", [1, 2])
 def test_homogeneous_finite_deformation(model):
     """A homogeneous deformation x = F X with stretch and shear (J = 1.188),
