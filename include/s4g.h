@@ -436,7 +436,9 @@ s4g_status s4g_op_precondition(s4g_mesh* mesh, int k, const double* r,
  * every mesh on the device, so calls that overlap in time on one device
  * race and must be ordered by the caller; the first call on a device does a
  * one-time set-up (a symbol-address lookup) and belongs before any stream
- * capture. */
+ * capture; the looked-up address is kept for the process, so the entry
+ * point must not be used after a cudaDeviceReset (or any destruction of the
+ * device's primary context) in the same process. */
 s4g_status s4g_op_amul_dot_noalloc(s4g_mesh* mesh, int k, const double* x,
                                    double* y, double* xAx);
 

@@ -43,6 +43,25 @@ def test_matches_allocating_entry_point_twice(ctx, k):
     model.close()
 
 
+def test_allocates_no_device_memory(ctx):
+    """The property the entry point exists for: a batch of calls leaves the
+    device's free memory exactly as it was (cudaMemGetInfo, read through
+    torch), while the allocating entry point is free to use the allocator."""
+    torch = pytest.importorskip("torch")
+    model = model_on(ctx, 12, 10, 9)
+    model.op_matrix()
+    x = np.random.default_rng(5).standard_normal((model.n_cells, 3))
+    model.op_amul_dot_noalloc(x)  # the one-time set-up of the device
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(50):
+        model.op_amul_dot_noalloc(x)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    model.close()
+    assert free1 == free0
+
+
 def test_needs_an_assembled_matrix(ctx):
     model = model_on(ctx, 5, 4, 4)
     with pytest.raises(_lib.S4GError, match="not assembled"):
