@@ -115,22 +115,24 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def algorithmic_bytes(kind, n_cells, n_faces, n_bfaces, v, n_loc=0, split=False):
+def algorithmic_bytes(kind, n_cells, n_faces, n_bfaces, v, n_loc=0, split=False, slots=False):
     """Minimal DRAM bytes of one launch of a kernel kind (k = 3 columns,
     v = value bytes, 4-byte indices); the formulas follow the solve's
     scope table: SpMV nnz(v+i) + 4(N+1) + 2Nvk; one DIC sweep
     nnz_L(v+i) + 4(N+1) + Nv + 2Nvk (+ Nvk for the backward w.r sums).
-    Fused processor-local iteration: loc_precond reads r, q, p, x and
-    writes r, x, w (7Nvk) plus rD (Nv), the in-part table (n_loc entries of
-    v + 2 bytes) and 4 bytes of row metadata per row; loc_spmv reads w and
-    p_old, writes p_new and q (4Nvk), plus the matrix nnz(v+i) + Nv + 4(N+1);
-    its split form (p-update pass, then SpMV on p_new) moves 5Nvk."""
+    Fused processor-local iteration: loc_precond reads r and q and writes r
+    and w (4Nvk) plus rD (Nv), the in-part table (n_loc entries of v + 2
+    bytes) and, with generic tables, 4 bytes of row metadata per row;
+    loc_spmv reads w, p_old and x, writes p_new, q and x (the pending
+    iteration's x += alpha p: 6Nvk), plus the matrix nnz(v+i) + Nv +
+    4(N+1); its split form (p-update pass with x, then SpMV on p_new) moves
+    7Nvk."""
     N, F, B, k = n_cells, n_faces, n_bfaces, 3
     nnz_l = F
     if kind == "loc_precond":
-        return 7 * N * v * k + N * v + n_loc * (v + 2) + 4 * N
+        return 4 * N * v * k + N * v + n_loc * (v + 2) + (0 if slots else 4 * N)
     if kind == "loc_spmv":
-        return (5 if split else 4) * N * v * k + 2 * F * (v + 4) + N * v + 4 * (N + 1)
+        return (7 if split else 6) * N * v * k + 2 * F * (v + 4) + N * v + 4 * (N + 1)
     if kind == "sweep_fwd":
         return nnz_l * (v + 4) + 4 * (N + 1) + N * v + 2 * N * v * k
     if kind == "sweep_bwd":
@@ -603,19 +605,20 @@ def run_gb300(args):
     peak, peak_kind = peaks()
     avg_ms = tot_ms[dom] / max(1, tot_n[dom])
     n_loc = mp.info()["n_local_entries"]
+    slots = bool(mp.info()["local_slots"])
     split = pp["spmv_unroll"] == 0 and pp["part_threads"] > 0
     mp.close()
     ctxp.close()
-    ab = algorithmic_bytes(dom, nC, nI, nB, v, n_loc, split)
+    ab = algorithmic_bytes(dom, nC, nI, nB, v, n_loc, split, slots)
     achieved = ab / (avg_ms * 1e-3) / 1e9 if ab else None
     workload = f"cube{args.n}_{args.precision.lower()}_{args.dic}"
     traffic = load_traffic(workload).get(dom)
     kernels = {k: {"launches": tot_n[k], "ms_total": round(tot_ms[k], 3),
                    "share": round(tot_ms[k] / max(1e-9, sum(tot_ms.values())), 4),
                    "avg_us": round(1000 * tot_ms[k] / max(1, tot_n[k]), 2),
-                   "gbs": (round(algorithmic_bytes(k, nC, nI, nB, v, n_loc, split) /
+                   "gbs": (round(algorithmic_bytes(k, nC, nI, nB, v, n_loc, split, slots) /
                                  (tot_ms[k] / max(1, tot_n[k]) * 1e-3) / 1e9, 1)
-                           if tot_n[k] and algorithmic_bytes(k, nC, nI, nB, v, n_loc, split)
+                           if tot_n[k] and algorithmic_bytes(k, nC, nI, nB, v, n_loc, split, slots)
                            else None)}
                for k in tot_ms if tot_n[k]}
 

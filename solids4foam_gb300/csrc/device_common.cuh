@@ -107,6 +107,9 @@ struct DevState {
   // r -= alpha q is pending per component; which p buffer is the newest
   int pending[3];
   int pbuf;
+  // x += alpha p of the pending iteration, not yet applied to x: the next
+  // SpMV pass applies it (it reads that p anyway), or kApplyX after the loop
+  int xPend[3];
   unsigned locTicket;    // next part of the processor-local preconditioner
   // error bits
   unsigned status;

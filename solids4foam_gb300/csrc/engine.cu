@@ -1018,7 +1018,7 @@ struct Engine {
     launchRhs<T>(mv, c, f, p.x, p.r, dState, dPartials, s, nullptr, nRun);
     launchSetLoopCond(hPcg, dState, nRun, 0, 1, pcgLimit, s);
     ok = addWhile(s, hPcg, &pcgBody);
-    launchPost<T>(mv, c, f, p.x, dState, dPartials, 1, s, nullptr, nRun);
+    launchPost<T>(mv, c, f, p.x, dState, dPartials, 1, s, nullptr, nRun, p.p, p.p2);
     launchSetLoopCond(hOut, dState, nRun, 1, 0, outerLimit, s);
     ok = cudaStreamEndCapture(s, &ended) == cudaSuccess && ok;
     if (!ok || cudaStreamBeginCaptureToGraph(s, pcgBody, nullptr, nullptr, 0, mode) != cudaSuccess)
@@ -1128,7 +1128,7 @@ struct Engine {
       launches += 2;
       S4G_TRY(readState());
       if (anyCase(&DevState::pcgContinue)) S4G_TRY(pcgLoop<T>(c, p, grid));
-      launchPost<T>(mv, c, f, p.x, dState, dPartials, 1, s, tm(), nRun);
+      launchPost<T>(mv, c, f, p.x, dState, dPartials, 1, s, tm(), nRun, p.p, p.p2);
       launches += tl ? 3 : 2;
       S4G_CUDA(cudaGetLastError());
       S4G_TRY(readState());

@@ -85,10 +85,13 @@ void launchTractionInit(const MeshView& mv, const Controls& c, const FieldPtrs& 
 // Post-solve pass: D += x, boundary values, leastSquares gradient, law,
 // boundary gradient/stress, next traction snGrad, convergence reductions.
 // mode 0: constructor pass (no correction, no stress); 1: corrector.
+// pA, pB: the fused PCG's two p buffers (a pending x += alpha p is applied
+// from the one DevState::pbuf names); null for the other PCG forms.
 template <typename T>
 void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const T* x,
                 DevState* st, double* partials, int mode, cudaStream_t s,
-                LaunchTimer* tm = nullptr, int nCases = 1);
+                LaunchTimer* tm = nullptr, int nCases = 1, const T* pA = nullptr,
+                const T* pB = nullptr);
 // RHS pass (FP64): R = div(sigma) + RhieChow + boundary terms, M*D_old for the
 // residual normalisation; zeroes x, sets r = R rounded to the PCG type.
 template <typename T>

@@ -251,15 +251,29 @@ __device__ __forceinline__ V3 aitkenRelax(const Controls& c, bool first, double*
 // D_new = D + x (the correction of the corrector; x in the PCG type).  With
 // a field relaxation factor f (relaxField "fixed", solidModel.C:837-841):
 // D_new = D.prevIter + f (D_solved - D.prevIter) = D + f x; with Aitken the
-// cell's own factor (aitkenRelax).
+// cell's own factor (aitkenRelax).  The processor-local PCG leaves the last
+// iteration's x += alpha p to the pass after the loop (DevState::xPend):
+// it is applied here first, the same operation as in the SpMV pass.
 template <typename T>
 __global__ void __launch_bounds__(kRowBlock)
-kApplyX(MeshView mv, Controls c, FieldPtrs f, const T* __restrict__ x, const DevState* st) {
+kApplyX(MeshView mv, Controls c, FieldPtrs f, T* __restrict__ x, const T* pA, const T* pB,
+        const DevState* st) {
   const int cs = blockIdx.y;
   f = caseFields(f, cs, mv.nC, mv.nB, mv.nI);
   x += (size_t)cs * 3 * mv.nC;
   st += cs;
   if (!st->caseLive) return;
+  if (st->xPend[0] | st->xPend[1] | st->xPend[2]) {
+    const T* __restrict__ pg = (st->pbuf ? pB : pA) + (size_t)cs * 3 * mv.nC;
+    bool xp[3];
+    T al[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) { xp[k] = st->xPend[k] != 0; al[k] = (T)st->alpha[k]; }
+    for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x)
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        if (xp[k]) x[3 * (size_t)s + k] = x[3 * (size_t)s + k] + al[k] * pg[3 * (size_t)s + k];
+  }
   const int dc = st->dcur;
   const double* Uold = f.D[dc];
   double* Unew = f.D[dc ^ 1];
@@ -601,6 +615,7 @@ kRhs(MeshView mv, Controls c, FieldPtrs f, T* __restrict__ x, T* __restrict__ r,
     st->finalRes[k] = st->initRes[k];
     st->nIter[k] = 0;
     st->pending[k] = 0;
+    st->xPend[k] = 0;
     st->active[k] = (st->initRes[k] < c.tol) ? 0 : 1;
     st->wArA[k] = 1e20;
     any |= st->active[k];
@@ -735,11 +750,11 @@ void launchTractionInit(const MeshView& mv, const Controls& c, const FieldPtrs& 
 template <typename T>
 void launchPost(const MeshView& mv, const Controls& c, const FieldPtrs& f, const T* x,
                 DevState* st, double* partials, int mode, cudaStream_t s, LaunchTimer* tm,
-                int nCases) {
+                int nCases, const T* pA, const T* pB) {
   const int grid = (mv.nC + kRowBlock - 1) / kRowBlock;
   TimeScope ts(tm, S4G_K_POST, s);
   const dim3 g(mv.rowGrid, nCases);
-  if (mode == 1) kApplyX<T><<<g, kRowBlock, 0, s>>>(mv, c, f, x, st);
+  if (mode == 1) kApplyX<T><<<g, kRowBlock, 0, s>>>(mv, c, f, const_cast<T*>(x), pA, pB, st);
   kPost<T><<<g, kRowBlock, 0, s>>>(mv, c, f, x, st, partials, mode);
   if (c.tl && mode == 1) kPostLawTL<<<grid, kRowBlock, 0, s>>>(mv, c, f, st);
 }
@@ -754,9 +769,11 @@ void launchRhs(const MeshView& mv, const Controls& c, const FieldPtrs& f, T* x, 
 }
 
 template void launchPost<double>(const MeshView&, const Controls&, const FieldPtrs&, const double*,
-                                 DevState*, double*, int, cudaStream_t, LaunchTimer*, int);
+                                 DevState*, double*, int, cudaStream_t, LaunchTimer*, int,
+                                 const double*, const double*);
 template void launchPost<float>(const MeshView&, const Controls&, const FieldPtrs&, const float*,
-                                DevState*, double*, int, cudaStream_t, LaunchTimer*, int);
+                                DevState*, double*, int, cudaStream_t, LaunchTimer*, int,
+                                const float*, const float*);
 template void launchRhs<double>(const MeshView&, const Controls&, const FieldPtrs&, double*, double*,
                                 DevState*, double*, cudaStream_t, LaunchTimer*, int);
 template void launchRhs<float>(const MeshView&, const Controls&, const FieldPtrs&, float*, float*,

@@ -382,10 +382,8 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
   const LocSmem<T> sm = locSmem<T>(mv, smraw);
   __shared__ double red[2 * 6];
   // the vectors never alias one another
-  const T* __restrict__ pg = st->pbuf ? p.p2 : p.p;  // p of the pending iteration
   const T* __restrict__ qg = p.q;
   const T* __restrict__ rDg = p.rD;
-  T* __restrict__ xg = p.x;
   T* __restrict__ rg = p.r;
   bool pend[3];
   T al[3];
@@ -433,10 +431,11 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
       for (int k = threadIdx.x; k < nm; k += NT) cpAsync16((char*)sm.m + 16 * k, gm + 16 * k);
     }
     for (int k = threadIdx.x; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
-    // pending update: RPT rows per thread with every load issued before
-    // any store; r and w = rD r into shared memory
+    // pending update r -= alpha q (x += alpha p is the SpMV pass's): RPT
+    // rows per thread with every load issued before any store; r and
+    // w = rD r into shared memory
     for (int i0 = threadIdx.x; i0 < nR; i0 += RPT * NT) {
-      T rv[RPT][3], qv[RPT][3], pv[RPT][3], xv[RPT][3], rd[RPT];
+      T rv[RPT][3], qv[RPT][3], rd[RPT];
 #pragma unroll
       for (int h = 0; h < RPT; ++h) {
         const int i = i0 + h * NT;
@@ -446,7 +445,7 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
 #pragma unroll
           for (int k = 0; k < 3; ++k) {
             rv[h][k] = rg[g + k];
-            if (pend[k]) { qv[h][k] = qg[g + k]; pv[h][k] = pg[g + k]; xv[h][k] = xg[g + k]; }
+            if (pend[k]) qv[h][k] = qg[g + k];
           }
         }
       }
@@ -458,7 +457,6 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
 #pragma unroll
           for (int k = 0; k < 3; ++k) {
             if (pend[k]) {
-              xg[g + k] = xv[h][k] + al[k] * pv[h][k];
               rv[h][k] -= al[k] * qv[h][k];
               rg[g + k] = rv[h][k];
             }
@@ -539,10 +537,8 @@ kLocPrecondSlots(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* pa
   double* grec = partials + mv.locGrpOff;
   unsigned* gcnt = reinterpret_cast<unsigned*>(grec + 8 * (size_t)mv.locGroups);
   // the vectors never alias one another
-  const T* __restrict__ pg = st->pbuf ? p.p2 : p.p;  // p of the pending iteration
   const T* __restrict__ qg = p.q;
   const T* __restrict__ rDg = p.rD;
-  T* __restrict__ xg = p.x;
   T* __restrict__ rg = p.r;
   bool pend[3];
   T al[3];
@@ -579,17 +575,17 @@ kLocPrecondSlots(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* pa
       for (int k = t; k < ni; k += NT) cpAsync16((char*)sm.idx + 16 * k, gi + 16 * k);
     }
     for (int k = t; k <= nL; k += NT) sm.lv[k] = mv.lvlStart[l0 + k] - pLo;
-    // pending update x += alpha p, r -= alpha q and w = rD r, RPT rows per
-    // thread with every load issued before any store.  Thread 0 reports the
-    // previous part's record on its group counter while the first loads are
-    // in flight.
+    // pending update r -= alpha q and w = rD r, RPT rows per thread with
+    // every load issued before any store (x += alpha p is the SpMV pass's).
+    // Thread 0 reports the previous part's record on its group counter
+    // while the first loads are in flight.
     bool done = false;
     T rK[KR][3];
     const bool regR = nR <= KR * NT;
     if (regR) {
 #pragma unroll
       for (int it = 0; it < KR / RPT; ++it) {
-        T qv[RPT][3], pv[RPT][3], xv[RPT][3], rd[RPT];
+        T qv[RPT][3], rd[RPT];
 #pragma unroll
         for (int h = 0; h < RPT; ++h) {
           const int j = it * RPT + h, i = t + j * NT;
@@ -599,7 +595,7 @@ kLocPrecondSlots(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* pa
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
               rK[j][k] = rg[g + k];
-              if (pend[k]) { qv[h][k] = qg[g + k]; pv[h][k] = pg[g + k]; xv[h][k] = xg[g + k]; }
+              if (pend[k]) qv[h][k] = qg[g + k];
             }
           }
         }
@@ -612,7 +608,6 @@ kLocPrecondSlots(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* pa
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
               if (pend[k]) {
-                xg[g + k] = xv[h][k] + al[k] * pv[h][k];
                 rK[j][k] -= al[k] * qv[h][k];
                 rg[g + k] = rK[j][k];
               }
@@ -624,7 +619,7 @@ kLocPrecondSlots(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* pa
     } else {
       if (t == 0 && prev >= 0) done = locArrive(gcnt, prev, nParts);
       for (int i0 = t; i0 < nR; i0 += RPT * NT) {
-        T rv[RPT][3], qv[RPT][3], pv[RPT][3], xv[RPT][3], rd[RPT];
+        T rv[RPT][3], qv[RPT][3], rd[RPT];
 #pragma unroll
         for (int h = 0; h < RPT; ++h) {
           const int i = i0 + h * NT;
@@ -634,7 +629,7 @@ kLocPrecondSlots(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* pa
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
               rv[h][k] = rg[g + k];
-              if (pend[k]) { qv[h][k] = qg[g + k]; pv[h][k] = pg[g + k]; xv[h][k] = xg[g + k]; }
+              if (pend[k]) qv[h][k] = qg[g + k];
             }
           }
         }
@@ -646,7 +641,6 @@ kLocPrecondSlots(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* pa
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
               if (pend[k]) {
-                xg[g + k] = xv[h][k] + al[k] * pv[h][k];
                 rv[h][k] -= al[k] * qv[h][k];
                 rg[g + k] = rv[h][k];
               }
@@ -729,15 +723,21 @@ kLocSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   const int* __restrict__ col = mv.col;
   const int* __restrict__ rp = mv.rowptr;
   T* __restrict__ qo = p.q;
-  bool act[3], first[3];
-  T b[3];
+  T* __restrict__ xg = p.x;
+  bool act[3], first[3], xp[3];
+  T b[3], al[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     act[k] = st->active[k] != 0; first[k] = st->nIter[k] == 0; b[k] = (T)st->beta[k];
+    xp[k] = st->xPend[k] != 0; al[k] = (T)st->alpha[k];
   }
   Acc<T> a0, a1, a2;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x) {
     const T dg = dia[s];
+    // the pending iteration's x += alpha p, from the p_old read here anyway
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      if (xp[k]) xg[3 * s + k] = xg[3 * s + k] + al[k] * po[3 * s + k];
     const T v0 = pNew(first[0], wv[3 * s], b[0], po[3 * s]);
     const T v1 = pNew(first[1], wv[3 * s + 1], b[1], po[3 * s + 1]);
     const T v2 = pNew(first[2], wv[3 * s + 2], b[2], po[3 * s + 2]);
@@ -787,6 +787,7 @@ kLocSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   st->counter[6] = 0;
   int any = 0;
   for (int k = 0; k < 3; ++k) {
+    st->xPend[k] = 0;  // applied by this pass
     if (!st->active[k]) continue;
     st->wApA[k] = sum[k];
     if (fabs(sum[k]) / st->normFactor[k] < 1e-300) {  // checkSingularity: stop this component
@@ -796,6 +797,7 @@ kLocSpmv(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
     if (sum[k] <= 0) atomicOr(&st->status, kErrIndefinite);
     st->alpha[k] = st->wArA[k] / sum[k];
     st->pending[k] = 1;
+    st->xPend[k] = 1;
     any = 1;
   }
   st->pbuf = pb ^ 1;
@@ -814,16 +816,21 @@ kLocPUpdate(MeshView mv, PcgPtrs<T> p, const DevState* st) {
   const T* __restrict__ po = pb ? p.p2 : p.p;
   T* __restrict__ pn = pb ? p.p : p.p2;
   const T* __restrict__ wv = p.w;
-  bool act[3], first[3];
-  T b[3];
+  T* __restrict__ xg = p.x;
+  bool act[3], first[3], xp[3];
+  T b[3], al[3];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     act[k] = st->active[k] != 0; first[k] = st->nIter[k] == 0; b[k] = (T)st->beta[k];
+    xp[k] = st->xPend[k] != 0; al[k] = (T)st->alpha[k];
   }
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < mv.nC; s += gridDim.x * blockDim.x)
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
+    for (int k = 0; k < 3; ++k) {
+      // the pending iteration's x += alpha p, from the p_old read here anyway
+      if (xp[k]) xg[3 * s + k] = xg[3 * s + k] + al[k] * po[3 * s + k];
       if (act[k]) pn[3 * s + k] = pNew(first[k], wv[3 * s + k], b[k], po[3 * s + k]);
+    }
 }
 
 // ... then q = A p_new with the p.q sums and the same decisions as kLocSpmv.
@@ -874,6 +881,7 @@ kLocSpmvSplit(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
   st->counter[6] = 0;
   int any = 0;
   for (int k = 0; k < 3; ++k) {
+    st->xPend[k] = 0;  // applied by this pass
     if (!st->active[k]) continue;
     st->wApA[k] = sum[k];
     if (fabs(sum[k]) / st->normFactor[k] < 1e-300) {  // checkSingularity: stop this component
@@ -883,6 +891,7 @@ kLocSpmvSplit(MeshView mv, PcgPtrs<T> p, DevState* st, double* partials) {
     if (sum[k] <= 0) atomicOr(&st->status, kErrIndefinite);
     st->alpha[k] = st->wArA[k] / sum[k];
     st->pending[k] = 1;
+    st->xPend[k] = 1;
     any = 1;
   }
   st->pbuf = pb ^ 1;
@@ -945,11 +954,11 @@ template <typename T>
 cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM) {
   cudaError_t e;
   if constexpr (sizeof(T) == 4) {
-    e = prepareV<T, 128, 4, 2>(mv, &blocksPerSM[0]);
-    return e != cudaSuccess ? e : prepareV<T, 64, 4, 4>(mv, &blocksPerSM[1]);
+    e = prepareV<T, 128, 4, 4>(mv, &blocksPerSM[0]);
+    return e != cudaSuccess ? e : prepareV<T, 64, 4, 8>(mv, &blocksPerSM[1]);
   } else {
-    e = prepareV<T, 128, 2, 1>(mv, &blocksPerSM[0]);
-    return e != cudaSuccess ? e : prepareV<T, 64, 2, 2>(mv, &blocksPerSM[1]);
+    e = prepareV<T, 128, 2, 2>(mv, &blocksPerSM[0]);
+    return e != cudaSuccess ? e : prepareV<T, 64, 2, 4>(mv, &blocksPerSM[1]);
   }
 }
 
@@ -962,11 +971,11 @@ template <typename T>
 void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                         double* partials, const LocalTuning& t, cudaStream_t s, int nCases) {
   if constexpr (sizeof(T) == 4) {
-    if (t.ntIdx == 1) launchPrecondV<T, 64, 4, 4>(mv, c, p, st, partials, t.grid[1], s, nCases);
-    else launchPrecondV<T, 128, 4, 2>(mv, c, p, st, partials, t.grid[0], s, nCases);
+    if (t.ntIdx == 1) launchPrecondV<T, 64, 4, 8>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    else launchPrecondV<T, 128, 4, 4>(mv, c, p, st, partials, t.grid[0], s, nCases);
   } else {
-    if (t.ntIdx == 1) launchPrecondV<T, 64, 2, 2>(mv, c, p, st, partials, t.grid[1], s, nCases);
-    else launchPrecondV<T, 128, 2, 1>(mv, c, p, st, partials, t.grid[0], s, nCases);
+    if (t.ntIdx == 1) launchPrecondV<T, 64, 2, 4>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    else launchPrecondV<T, 128, 2, 2>(mv, c, p, st, partials, t.grid[0], s, nCases);
   }
 }
 
