@@ -397,12 +397,20 @@ struct Engine {
       if (localSmemBytes<double>(mv) + 2048 > (size_t)maxSmem)
         return setErr(S4G_BAD_ARG, "a DIC part does not fit in shared memory; use a smaller part_size");
       int per[kLocNumNT];
+      // slot tables: the second variant is the first on the smallest grid
+      // that gives every CTA the same number of parts
+      auto grids = [&](LocalTuning& t, const int* per) {
+        for (int k = 0; k < kLocNumNT; ++k)
+          t.grid[k] = std::max(1, std::min(hp.nParts, std::max(1, per[k]) * ctx->numSMs));
+        if (mv.locSlots) {
+          const int waves = (hp.nParts + t.grid[0] - 1) / t.grid[0];
+          t.grid[1] = (hp.nParts + waves - 1) / waves;
+        }
+      };
       S4G_CUDA(localPrepare<double>(mv, per));
-      for (int k = 0; k < kLocNumNT; ++k)
-        tune64.grid[k] = std::max(1, std::min(hp.nParts, std::max(1, per[k]) * ctx->numSMs));
+      grids(tune64, per);
       S4G_CUDA(localPrepare<float>(mv, per));
-      for (int k = 0; k < kLocNumNT; ++k)
-        tune32.grid[k] = std::max(1, std::min(hp.nParts, std::max(1, per[k]) * ctx->numSMs));
+      grids(tune32, per);
       autotune = !(o && o->no_autotune);
       S4G_TRY(alloc(&pc.p2, 3 * (size_t)nC));
       double* lc;

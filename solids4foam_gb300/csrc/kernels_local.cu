@@ -932,8 +932,9 @@ cudaError_t prepareV(const MeshView& mv, int* blocksPerSM) {
 // once).  Generic tables: FP32 {128 x 4, 64 x 4}, FP64 {128 x 2, 64 x 2};
 // the second of each pair has all its threads walking and half the threads
 // per CTA, so more parts are walked at once per SM where shared memory
-// allows.  Slot tables: 64 threads with FP32 {2, 4} and FP64 {1, 2} rows in
-// flight (the first without register spills).  perf.part_threads reports the threads of the one in use.
+// allows.  Slot tables: 64 threads with 4 (FP32) or 2 (FP64) rows in
+// flight, on a grid of every resident CTA or on the smallest grid that
+// gives every CTA the same number of parts (no last wave of a few CTAs).  perf.part_threads reports the threads of the one in use.
 const int kLocVariantsNT[kLocNumNT] = {128, 64};
 const int kLocVariantsU[kLocNumU] = {1, 6, 0};
 
@@ -955,10 +956,10 @@ cudaError_t localPrepare(const MeshView& mv, int* blocksPerSM) {
   cudaError_t e;
   if constexpr (sizeof(T) == 4) {
     e = prepareV<T, 128, 4, 4>(mv, &blocksPerSM[0]);
-    return e != cudaSuccess ? e : prepareV<T, 64, 4, 8>(mv, &blocksPerSM[1]);
+    return e != cudaSuccess ? e : prepareV<T, 64, 4, 4>(mv, &blocksPerSM[1]);
   } else {
     e = prepareV<T, 128, 2, 2>(mv, &blocksPerSM[0]);
-    return e != cudaSuccess ? e : prepareV<T, 64, 2, 4>(mv, &blocksPerSM[1]);
+    return e != cudaSuccess ? e : prepareV<T, 64, 2, 2>(mv, &blocksPerSM[1]);
   }
 }
 
@@ -971,10 +972,10 @@ template <typename T>
 void launchLocalPrecond(const MeshView& mv, const Controls& c, const PcgPtrs<T>& p, DevState* st,
                         double* partials, const LocalTuning& t, cudaStream_t s, int nCases) {
   if constexpr (sizeof(T) == 4) {
-    if (t.ntIdx == 1) launchPrecondV<T, 64, 4, 8>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    if (t.ntIdx == 1) launchPrecondV<T, 64, 4, 4>(mv, c, p, st, partials, t.grid[1], s, nCases);
     else launchPrecondV<T, 128, 4, 4>(mv, c, p, st, partials, t.grid[0], s, nCases);
   } else {
-    if (t.ntIdx == 1) launchPrecondV<T, 64, 2, 4>(mv, c, p, st, partials, t.grid[1], s, nCases);
+    if (t.ntIdx == 1) launchPrecondV<T, 64, 2, 2>(mv, c, p, st, partials, t.grid[1], s, nCases);
     else launchPrecondV<T, 128, 2, 2>(mv, c, p, st, partials, t.grid[0], s, nCases);
   }
 }
