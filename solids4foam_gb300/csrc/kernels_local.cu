@@ -9,14 +9,18 @@
 // CTA from shared memory, and the PCG iteration (lduMatrix PCG, as in
 // kernels_pcg.cu) needs only two kernels:
 //
-//   kLocPrecond  x += alpha p, r -= alpha q for the components whose
-//                iteration is pending, sum|r| (the residual test of that
-//                iteration), then w = M^-1 r per part and the w.r sums; the
-//                last CTA decides convergence, beta and wArA.
-//   kLocSpmv     p_new = w + beta p_old and q = A p_new in one pass (a
-//                neighbour's p_new is recomputed from its w and p_old, so p
-//                is double-buffered), with the p.q sums; the last CTA decides
-//                alpha (and the singularity stop).
+//   kLocPrecondSlots / kLocPrecond
+//                r -= alpha q for the components whose iteration is
+//                pending, sum|r| (the residual test of that iteration),
+//                then w = M^-1 r per part and the w.r sums; the last CTA
+//                decides convergence, beta and wArA.
+//   kLocSpmv     the pending iteration's x += alpha p (from the p_old it
+//                reads anyway), p_new = w + beta p_old and q = A p_new in
+//                one pass (a neighbour's p_new is recomputed from its w and
+//                p_old, so p is double-buffered), with the p.q sums; the
+//                last CTA decides alpha (and the singularity stop).  The
+//                x update of a solve's last iteration is applied by kApplyX
+//                after the loop (DevState::xPend).
 //
 // The residual test of iteration n thus runs in the kernel that also
 // preconditions for iteration n+1; when the test stops a component, that
@@ -26,8 +30,9 @@
 //
 // Variants.  The SpMV step runs fused with a plain or an unrolled entry
 // loop, or split into a p-update pass and an SpMV; the preconditioner runs
-// with 128 or 64 threads per part (generic tables) or with 2 or 4 (FP32),
-// 1 or 2 (FP64) rows per thread in flight (slot tables).  The autotuner
+// with 128 or 64 threads per part (generic tables) or on two grids (slot
+// tables: every resident CTA, or the smallest grid that gives every CTA the
+// same number of parts).  The autotuner
 // (engine) times them on the mesh and keeps the fastest.  The SpMV variants
 // sum in the same order (same grid and block); the preconditioner sums each
 // part in a fixed order that depends neither on its block size nor on its
@@ -39,7 +44,8 @@
 // and the column's row index inside the part (16 bits); per-row metadata
 // (entry offset, lower and upper counts).  Both are padded per part so that
 // they are staged with 16-byte cp.async copies while the CTA streams the
-// x/r update.
+// residual update.  Hexahedral parts use fixed 3 + 3 slots per row instead
+// (HostPrep::locSlots, kLocPrecondSlots).
 
 #include <algorithm>
 
@@ -359,8 +365,8 @@ constexpr int locMinBlocks() {
 }
 
 // The processor-local preconditioner of one PCG iteration: the pending
-// update x += alpha p, r -= alpha q, w = rD r, the forward and backward
-// substitutions of each part inside one CTA, and the w.r and sum|r| sums.
+// update r -= alpha q, w = rD r, the forward and backward substitutions of
+// each part inside one CTA, and the w.r and sum|r| sums.
 //
 // Streaming: each thread issues the loads of RPT rows at once (all the
 // part's rows in one round trip when NT * RPT covers the part), while the
@@ -514,8 +520,9 @@ kLocPrecond(MeshView mv, Controls c, PcgPtrs<T> p, DevState* st, double* partial
 // The slot-table preconditioner (hexahedral parts, HostPrep::locSlots): 64
 // threads per part, all of them walking.  Parts go to CTAs in a fixed
 // stride (CTA b takes b, b + G, ...); the next part's descriptor arrives by
-// cp.async with the current part's tables.  A thread keeps the updated
-// residual of its rows t, t + 64, ... (up to 8 rows) in registers, so the
+// cp.async with the current part's tables.  It streams r, q and rD (RPT
+// rows per thread in flight), and a thread keeps the updated residual of its
+// rows t, t + 64, ... (up to 8 rows) in registers, so the
 // shared memory holds only the tables and w, and eight FP32 parts (five
 // FP64) of 512 rows fit per SM.  After the walk w leaves in one coalesced
 // pass and each thread sums w.r and |r| over its rows in row order, then a
