@@ -342,14 +342,25 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
   for (int s = 0; s < nC; ++s) hp.solverRank[s] = rank[hp.s2c[s]];
 
   // ---- 4. internal faces in storage orientation, sorted by (owner, neighbour)
+  // (a counting sort by the storage owner, then each owner's few faces by
+  // neighbour, in face order among equal pairs)
   std::vector<int> fidxOrder(nI);
-  std::iota(fidxOrder.begin(), fidxOrder.end(), 0);
   auto so = [&](int f) { return std::min(hp.c2s[d->owner[f]], hp.c2s[d->neighbour[f]]); };
   auto sn = [&](int f) { return std::max(hp.c2s[d->owner[f]], hp.c2s[d->neighbour[f]]); };
-  std::sort(fidxOrder.begin(), fidxOrder.end(), [&](int a, int b) {
-    int oa = so(a), ob = so(b);
-    return oa != ob ? oa < ob : sn(a) < sn(b);
-  });
+  {
+    std::vector<int> start(nC + 1, 0);
+    for (int f = 0; f < nI; ++f) ++start[so(f) + 1];
+    for (int s = 0; s < nC; ++s) start[s + 1] += start[s];
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int f = 0; f < nI; ++f) fidxOrder[fill[so(f)]++] = f;
+    for (int s = 0; s < nC; ++s)
+      for (int a = start[s] + 1; a < start[s + 1]; ++a) {
+        const int f = fidxOrder[a], key = sn(f);
+        int b = a;
+        for (; b > start[s] && sn(fidxOrder[b - 1]) > key; --b) fidxOrder[b] = fidxOrder[b - 1];
+        fidxOrder[b] = f;
+      }
+  }
   hp.fown.resize(nI); hp.fnei.resize(nI); hp.fcaller.resize(nI); hp.fflip.resize(nI);
   std::vector<int> fnew(nI);
   for (int k = 0; k < nI; ++k) {
@@ -504,6 +515,11 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
   hp.locSrc.clear(); hp.locIdx.clear(); hp.locMeta.clear();
   hp.maxLocEntries = 0; hp.maxLocMeta = 0;
   if (subdomains) {
+    hp.locSrc.reserve(2 * (size_t)nI + 8 * (size_t)hp.nParts);
+    hp.locIdx.reserve(2 * (size_t)nI + 8 * (size_t)hp.nParts);
+    hp.locMeta.reserve((size_t)nC + 4 * (size_t)hp.nParts);
+    hp.locEntStart.reserve((size_t)hp.nParts + 1);
+    hp.locMetaStart.reserve((size_t)hp.nParts + 1);
     for (int p = 0; p < hp.nParts; ++p) {
       const int lo = hp.partStart[p], hi = hp.partStart[p + 1];
       const size_t e0 = hp.locSrc.size();
@@ -545,6 +561,9 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
     if (slots) {
       std::vector<int> src, est(1, 0);
       std::vector<uint16_t> idx;
+      src.reserve(6 * (size_t)nC + 8 * (size_t)hp.nParts);
+      idx.reserve(6 * (size_t)nC + 8 * (size_t)hp.nParts);
+      est.reserve((size_t)hp.nParts + 1);
       hp.maxLocEntries = 0;
       for (int p = 0; p < hp.nParts; ++p) {
         const int lo = hp.partStart[p], hi = hp.partStart[p + 1];
