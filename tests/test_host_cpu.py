@@ -288,3 +288,17 @@ def test_caller_decomposition_plan(built):
     gap[gap == 3] = 2
     with pytest.raises(_lib.S4GError, match="every id used"):
         plan(m, renumber="none", dic_subdomains=True, parts=gap)
+
+
+def test_time_step_and_series_entry_points_check_their_arguments(built):
+    """s4g_solve_step, s4g_state_reset and the series entry points refuse
+    null handles with S4G_BAD_ARG (no device is touched)."""
+    L = _lib.lib()
+    perf = _lib.Perf()
+    assert L.s4g_solve_step(None, 0, None, None, ct.byref(perf)) == _lib.BAD_ARG
+    assert L.s4g_state_reset(None) == _lib.BAD_ARG
+    kind = ct.c_int()
+    assert L.s4g_foam_series_kind(None, ct.byref(kind)) == _lib.BAD_ARG
+    t = ct.c_int()
+    assert L.s4g_foam_bc_at(None, 0, 0.0, ct.byref(t), None, None, None) == _lib.BAD_ARG
+    assert L.s4g_foam_apply_bcs_at(None, None, 0.0) == _lib.BAD_ARG
