@@ -207,6 +207,14 @@ def barrier(dist):
         dist.barrier()
 
 
+def whole_job_rate(dist, world, step_ms):
+    """Replicas (weak scaling): every rank solves the same case, so the
+    job's solves/s is world solves per the slowest rank's mean step.
+    Returns (solves/s of the whole job, that step time in ms)."""
+    ms_step = allmax(dist, statistics.mean(step_ms))
+    return world * 1000.0 / ms_step, ms_step
+
+
 def allmax(dist, x):
     if not dist:
         return x
@@ -572,8 +580,7 @@ def run_gb300(args):
     barrier(dist)
     clocks = sampler.stop()
     ms = [p["solve_ms"] for p in perfs]
-    ms_step = allmax(dist, statistics.mean(ms))
-    value = world * 1000.0 / ms_step
+    value, ms_step = whole_job_rate(dist, world, ms)
 
     # end to end through the C ABI with host buffers: upload, solve, download
     e2e_ms = []
@@ -591,7 +598,7 @@ def run_gb300(args):
         m2.evolve()
         m2.close()
         e2e_ms.append(1000.0 * (time.perf_counter() - t0))
-    e2e_step = allmax(dist, statistics.mean(e2e_ms)) if e2e_ms else None
+    e2e_step = whole_job_rate(dist, world, e2e_ms)[1] if e2e_ms else None
 
     # per-kernel CUDA events of one more solve, launched kernel by kernel
     ctxp = sg.Context(local, profile=True)

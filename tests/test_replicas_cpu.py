@@ -1,0 +1,48 @@
+"""bench.py's multi-GPU form is replicas only: each rank solves the same
+case and the job's rate is world solves per the slowest rank's step.  The
+rank plumbing (process group, barrier, max over ranks) runs here as two
+gloo ranks on the CPU."""
+import os
+import socket
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.multiprocessing as mp  # noqa: E402
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _rank(rank, world, port, out):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), WORLD_SIZE=str(world),
+                      RANK=str(rank), LOCAL_RANK=str(rank))
+    import bench
+    w, r, local, dist = bench.dist_init()
+    assert (w, r, local) == (world, rank, rank) and dist is not None
+    # rank 1 is the slow replica: 200 ms steps against 100 and 120 ms
+    steps = [100.0, 120.0] if rank == 0 else [200.0, 200.0]
+    bench.barrier(dist)
+    value, ms = bench.whole_job_rate(dist, w, steps)
+    out[rank] = (value, ms)
+    dist.destroy_process_group()
+
+
+def test_two_replicas_report_the_slowest_rank():
+    world, port = 2, _free_port()
+    with mp.Manager() as mgr:
+        out = mgr.dict()
+        mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
+        res = dict(out)
+    for rank in range(world):
+        value, ms = res[rank]
+        assert ms == 200.0 and value == pytest.approx(2 * 1000.0 / 200.0)
+
+
+def test_one_process_is_its_own_job():
+    import bench
+    value, ms = bench.whole_job_rate(None, 1, [250.0, 250.0])
+    assert ms == 250.0 and value == 4.0
