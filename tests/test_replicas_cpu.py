@@ -17,7 +17,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _rank(rank, world, port, out):
+def _rank(rank, world, port, out_dir):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), WORLD_SIZE=str(world),
                       RANK=str(rank), LOCAL_RANK=str(rank))
     import bench
@@ -27,18 +27,16 @@ def _rank(rank, world, port, out):
     steps = [100.0, 120.0] if rank == 0 else [200.0, 200.0]
     bench.barrier(dist)
     value, ms = bench.whole_job_rate(dist, w, steps)
-    out[rank] = (value, ms)
+    with open(os.path.join(out_dir, f"rank{rank}"), "w") as f:
+        f.write(f"{value!r} {ms!r}")
     dist.destroy_process_group()
 
 
-def test_two_replicas_report_the_slowest_rank():
+def test_two_replicas_report_the_slowest_rank(tmp_path):
     world, port = 2, _free_port()
-    with mp.Manager() as mgr:
-        out = mgr.dict()
-        mp.spawn(_rank, args=(world, port, out), nprocs=world, join=True)
-        res = dict(out)
+    mp.spawn(_rank, args=(world, port, str(tmp_path)), nprocs=world, join=True)
     for rank in range(world):
-        value, ms = res[rank]
+        value, ms = (float(v) for v in (tmp_path / f"rank{rank}").read_text().split())
         assert ms == 200.0 and value == pytest.approx(2 * 1000.0 / 200.0)
 
 
