@@ -384,9 +384,13 @@ s4g_status prepareMesh(const s4g_mesh_desc* d, const s4g_mesh_opts* o, HostPrep&
       int c = hp.s2c[s];
       ent.clear();
       for (int e = adj.ptr[c]; e < adj.ptr[c + 1]; ++e) ent.push_back({adj.cell[e], adj.face[e]});
-      std::sort(ent.begin(), ent.end(), [&](const std::pair<int, int>& a, const std::pair<int, int>& b) {
-        return rank[a.first] < rank[b.first];
-      });
+      // a row's few neighbours by solver rank (distinct): insertion sort
+      for (size_t a = 1; a < ent.size(); ++a) {
+        const std::pair<int, int> v = ent[a];
+        size_t b = a;
+        for (; b > 0 && rank[ent[b - 1].first] > rank[v.first]; --b) ent[b] = ent[b - 1];
+        ent[b] = v;
+      }
       int k = hp.rowptr[s];
       for (auto& pr : ent) {
         int ns = hp.c2s[pr.first];
