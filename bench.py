@@ -150,6 +150,21 @@ def algorithmic_bytes(kind, n_cells, n_faces, n_bfaces, v, n_loc=0, split=False,
     return None
 
 
+def iteration_roofline(tot_ms, tot_n, n_cells, n_faces, n_bfaces, v, n_loc, split, slots, peak):
+    """The fused PCG iteration as a whole: the algorithmic bytes of its two
+    kernels (loc_precond, loc_spmv) over their summed average launch time,
+    or None when the solve did not run them."""
+    kinds = ("loc_precond", "loc_spmv")
+    if not all(tot_n.get(k) for k in kinds):
+        return None
+    nbytes = sum(algorithmic_bytes(k, n_cells, n_faces, n_bfaces, v, n_loc, split, slots)
+                 for k in kinds)
+    us = sum(1000.0 * tot_ms[k] / tot_n[k] for k in kinds)
+    achieved = nbytes / (us * 1e-6) / 1e9
+    return {"kernels": list(kinds), "algorithmic_bytes": nbytes, "us": us,
+            "achieved": achieved, "unit": "GB/s", "frac": achieved / peak if peak else None}
+
+
 def load_traffic(workload):
     """Per-launch DRAM traffic from the committed ncu summary, if it covers
     this workload: lines '<kind> <bytes_per_launch> <workload>'."""
@@ -713,7 +728,9 @@ def run_gb300(args):
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
                      "peak_source": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": ab, "avg_launch_us": avg_ms * 1000},
+                     "algorithmic_bytes_per_launch": ab, "avg_launch_us": avg_ms * 1000,
+                     "pcg_iteration": iteration_roofline(tot_ms, tot_n, nC, nI, nB, v, n_loc,
+                                                         split, slots, peak)},
         "kernels": kernels,
         "error_vs_oracle": parity,
         "plain_fp64": fp64,

@@ -1,7 +1,8 @@
-"""bench.py's multi-GPU form is replicas only: each rank solves the same
-case and the job's rate is world solves per the slowest rank's step.  The
-rank plumbing (process group, barrier, max over ranks) runs here as two
-gloo ranks on the CPU."""
+"""bench.py's host-side arithmetic on the CPU.  Its multi-GPU form is
+replicas only: each rank solves the same case and the job's rate is world
+solves per the slowest rank's step; the rank plumbing (process group,
+barrier, max over ranks) runs here as two gloo ranks.  And the roofline of
+the fused PCG iteration from per-kernel times."""
 import os
 import socket
 
@@ -44,3 +45,20 @@ def test_one_process_is_its_own_job():
     import bench
     value, ms = bench.whole_job_rate(None, 1, [250.0, 250.0])
     assert ms == 250.0 and value == 4.0
+
+
+def test_iteration_roofline_of_the_fused_pcg():
+    """bench.py's roofline of the fused PCG iteration: both kernels'
+    algorithmic bytes over their summed launch times (the 128^3 figures of
+    a solve: 121.6 us and 78.0 us per launch)."""
+    import bench
+    N, F, B = 2097152, 6242304, 98304
+    tot_n = {"loc_precond": 10, "loc_spmv": 10, "rhs": 1}
+    tot_ms = {"loc_precond": 1.216, "loc_spmv": 0.780, "rhs": 1.25}
+    it = bench.iteration_roofline(tot_ms, tot_n, N, F, B, 4, 6 * N, False, True, 6778.0)
+    b = (bench.algorithmic_bytes("loc_precond", N, F, B, 4, 6 * N, False, True)
+         + bench.algorithmic_bytes("loc_spmv", N, F, B, 4, 6 * N, False, True))
+    assert it["algorithmic_bytes"] == b and it["us"] == pytest.approx(199.6)
+    assert it["frac"] == pytest.approx(b / 199.6e-6 / 1e9 / 6778.0)
+    assert bench.iteration_roofline({"rhs": 1.0}, {"rhs": 1}, N, F, B, 4, 0, False, False,
+                                    6778.0) is None
